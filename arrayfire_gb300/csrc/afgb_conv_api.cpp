@@ -1,0 +1,444 @@
+// The six convolution entry points of the ArrayFire C API, with the
+// reference's argument checks, batch-kind inference, domain choice and dtype
+// dispatch (src/api/c/convolve.cpp), routed to this library's sm_103a
+// kernels.  No CPU fallback: every path below launches device code.
+#include <cstring>
+#include <string>
+
+#include "afgb_internal.hpp"
+#include "conv_direct.hpp"
+#include "nn_conv.hpp"
+
+namespace afgb {
+
+// src/api/c/convolve.cpp:77-97
+static int identify_batch_kind(int rank, const dim_t *sd, const dim_t *fd) {
+    dim_t sn = dim4_ndims(sd);
+    dim_t fn = dim4_ndims(fd);
+    if (sn == rank && fn == rank) return BATCH_NONE;
+    if (sn == rank && (fn > rank && fn <= 4)) return BATCH_RHS;
+    if ((sn > rank && sn <= 4) && fn == rank) return BATCH_LHS;
+    if ((sn > rank && sn <= 4) && (fn > rank && fn <= 4)) {
+        bool match = true, interleaved = true;
+        for (int i = rank; i < 4; ++i) {
+            match &= (sd[i] == fd[i]);
+            interleaved &= (sd[i] == 1 || fd[i] == 1 || sd[i] == fd[i]);
+        }
+        if (match) return BATCH_SAME;
+        return interleaved ? BATCH_DIFF : BATCH_UNSUPPORTED;
+    }
+    return BATCH_UNSUPPORTED;
+}
+
+// src/api/c/convolve.cpp:99-130 — true when the reference would take the
+// frequency-domain route
+static bool reference_picks_freq(int rank, const dim_t *sd, const dim_t *fd,
+                                 af_conv_domain domain) {
+    if (domain == AF_CONV_FREQ) return true;
+    if (domain != AF_CONV_AUTO) return false;
+    if (identify_batch_kind(rank, sd, fd) == BATCH_DIFF) return true;
+    dim_t kbatch = 1;
+    for (int i = 3; i >= rank; --i) kbatch *= fd[i];
+    if (kbatch >= 10) return true;
+    if (rank == 1 && fd[0] > 128) return true;
+    if (rank == 2) {
+        if (fd[0] > 17 || fd[1] > 17) return true;
+        if (fd[0] != fd[1] && fd[0] > 5) return true;
+    }
+    if (rank == 3 && (fd[0] > 5 || fd[1] > 5 || fd[2] > 5)) return true;
+    return false;
+}
+
+// filter sizes the spatial kernels accept: the same limits as the
+// reference CUDA backend (src/backend/cuda/kernel/convolve.hpp:149-157,
+// 242-266, 292-307), reported with the same error code
+static bool spatial_supported(int rank, const dim_t *fd) {
+    switch (rank) {
+        case 1: return fd[0] <= 129;
+        case 2: {
+            if (fd[0] * fd[1] > 17 * 17) return false;
+            bool small = fd[0] <= 5 && fd[1] <= 5;
+            bool square = fd[0] == fd[1] && fd[0] > 5 && fd[0] < 18;
+            return small || square;
+        }
+        case 3: return fd[0] * fd[1] * fd[2] <= 125;
+    }
+    return false;
+}
+
+static af_dtype acc_type(af_dtype t) {
+    switch (t) {
+        case f32: return f32;
+        case f64: return f64;
+        case c32: return c32;
+        case c64: return c64;
+        default: return f32;
+    }
+}
+
+// src/backend/cpu/convolve.cpp:38-58 (same rule in src/backend/cuda/convolve.cpp:28-50)
+static void conv_out_dims(dim_t *od, int rank, int kind, bool expand, const dim_t *sd,
+                          const dim_t *fd) {
+    if (expand) {
+        for (int d = 0; d < 4; ++d) {
+            if (kind == BATCH_NONE || kind == BATCH_RHS) od[d] = sd[d] + fd[d] - 1;
+            else od[d] = (d < rank) ? sd[d] + fd[d] - 1 : sd[d];
+        }
+    } else {
+        for (int d = 0; d < 4; ++d) od[d] = sd[d];
+        if (kind == BATCH_RHS)
+            for (int i = rank; i < 4; ++i) od[i] = fd[i];
+    }
+}
+
+// convolve() of src/api/c/convolve.cpp:132-215
+static af_err convolve_rank(af_array *out, const af_array signal, const af_array filter,
+                            af_conv_mode mode, int rank) {
+    Array *s = get_array(signal);
+    Array *f = get_array(filter);
+    if (dim4_ndims(f->dims) == 0 || dim4_ndims(s->dims) == 0) {
+        return af_retain_array(out, signal);
+    }
+    int kind = identify_batch_kind(rank, s->dims, f->dims);
+    AFGB_ARG_ASSERT(1, (kind != BATCH_UNSUPPORTED && kind != BATCH_DIFF));
+    const bool expand = mode == AF_CONV_EXPAND;
+    af_dtype st = s->type;
+    if (st == f16 || !dtype_valid(st)) AFGB_TYPE_ERROR(1, st);
+    if (!spatial_supported(rank, f->dims)) {
+        AFGB_THROW(AF_ERR_NOT_SUPPORTED,
+                   "CUDA N Dimensional Convolution doesn't support " + std::to_string(f->dims[0]) +
+                       "x" + std::to_string(f->dims[1]) + "x" + std::to_string(f->dims[2]) +
+                       " kernel");
+    }
+    Array filt = cast_array(*f, acc_type(st));
+    dim_t od[4];
+    conv_out_dims(od, rank, kind, expand, s->dims, f->dims);
+    Array o = *create_array(st, od);
+    launch_convolve_nd(*s, filt, o, kind, rank, expand);
+    *out = make_handle(&o);
+    return AF_SUCCESS;
+}
+
+static af_err convolve_domain(af_array *out, const af_array signal, const af_array filter,
+                              af_conv_mode mode, af_conv_domain domain, int rank) {
+    Array *s = get_array(signal);
+    Array *f = get_array(filter);
+    if (reference_picks_freq(rank, s->dims, f->dims, domain)) {
+        // The frequency-domain path (af_fft_convolve*) is not part of this
+        // library.  AUTO falls back to the spatial kernels when they accept
+        // the filter (floating results then differ from the reference's FFT
+        // result by rounding only); FREQ, DIFF batches and filters beyond the
+        // spatial limits are reported as not supported.
+        bool diff = identify_batch_kind(rank, s->dims, f->dims) == BATCH_DIFF;
+        if (domain == AF_CONV_FREQ || diff || !spatial_supported(rank, f->dims)) {
+            AFGB_THROW(AF_ERR_NOT_SUPPORTED,
+                       "frequency-domain convolution is not built in this library; "
+                       "use AF_CONV_SPATIAL with a supported filter size");
+        }
+    }
+    return convolve_rank(out, signal, filter, mode, rank);
+}
+
+// src/api/c/convolve.cpp:50-75 and :258-334
+static af_err convolve2_sep_impl(af_array *out, const af_array col_filter,
+                                 const af_array row_filter, const af_array signal,
+                                 af_conv_mode mode) {
+    Array *s = get_array(signal);
+    Array *cf = get_array(col_filter);
+    Array *rf = get_array(row_filter);
+    AFGB_ARG_ASSERT(1, (dim4_ndims(s->dims) >= 2));
+    const bool expand = mode == AF_CONV_EXPAND;
+    af_dtype st = s->type;
+    if (st == f16 || !dtype_valid(st)) AFGB_TYPE_ERROR(1, st);
+    af_dtype at = acc_type(st);
+    Array c = cast_array(*cf, at);
+    Array r = cast_array(*rf, at);
+    auto is_vector = [](const Array &a) {
+        int singular = 0, non_singular = 0;
+        for (int i = 0; i < 4; ++i) {
+            non_singular += (a.dims[i] != 0 && a.dims[i] != 1);
+            singular += (a.dims[i] == 1);
+        }
+        return singular == 3 && non_singular == 1;
+    };
+    if (c.elements() == 1 && r.elements() == 1) {
+        Array o = *create_array(st, s->dims);
+        launch_sep_scalar(*s, c, r, o);
+        *out = make_handle(&o);
+        return AF_SUCCESS;
+    }
+    AFGB_ARG_ASSERT(2, is_vector(c));
+    AFGB_ARG_ASSERT(3, is_vector(r));
+    if (c.elements() > 31 || r.elements() > 31) {
+        AFGB_THROW(AF_ERR_NOT_SUPPORTED, "CUDA convolution supports max kernel size of 31");
+    }
+    dim_t od[4] = {s->dims[0], s->dims[1], s->dims[2], s->dims[3]};
+    if (expand) {
+        od[0] += c.elements() - 1;
+        od[1] += r.elements() - 1;
+    }
+    Array o = *create_array(st, od);
+    launch_convolve2_sep(*s, c, r, o, expand);
+    *out = make_handle(&o);
+    return AF_SUCCESS;
+}
+
+// ---- NN: shared argument handling (src/api/c/convolve.cpp:344-392, 414-477)
+struct NNArgs {
+    dim_t stride[4], padding[4], dilation[4];
+};
+
+static NNArgs nn_args(unsigned stride_dims, const dim_t *strides, unsigned padding_dims,
+                      const dim_t *paddings, unsigned dilation_dims, const dim_t *dilations) {
+    NNArgs a;
+    if (stride_dims && !strides) AFGB_THROW(AF_ERR_ARG, "null strides");
+    if (padding_dims && !paddings) AFGB_THROW(AF_ERR_ARG, "null paddings");
+    if (dilation_dims && !dilations) AFGB_THROW(AF_ERR_ARG, "null dilations");
+    dim4_from(a.stride, stride_dims, strides);
+    dim4_from(a.padding, padding_dims, paddings);
+    dim4_from(a.dilation, dilation_dims, dilations);
+    dim_t sn = dim4_ndims(a.stride), pn = dim4_ndims(a.padding), dn = dim4_ndims(a.dilation);
+    AFGB_ARG_ASSERT(3, sn > 0 && sn <= 2);
+    AFGB_ARG_ASSERT(5, pn >= 0 && pn <= 2);
+    AFGB_ARG_ASSERT(7, dn > 0 && dn <= 2);
+    return a;
+}
+
+// the reference's getArray<T> type check (src/api/c/handle.hpp:50-57)
+static void require_type(const Array *a, af_dtype t) {
+    if (a->type != t) AFGB_THROW(AF_ERR_INTERNAL, "Invalid type for input array.");
+}
+
+static void nn_geometry(NNGeom &g, const Array *s, const Array *f, const NNArgs &a) {
+    std::memset(&g, 0, sizeof(g));
+    g.W = s->dims[0];
+    g.H = s->dims[1];
+    g.C = s->dims[2];
+    g.N = s->dims[3];
+    g.fw = f->dims[0];
+    g.fh = f->dims[1];
+    g.K = f->dims[3];
+    g.sx = a.stride[0];
+    g.sy = a.stride[1];
+    g.px = a.padding[0];
+    g.py = a.padding[1];
+    g.dx = a.dilation[0];
+    g.dy = a.dilation[1];
+    // src/backend/cpu/convolve.cpp:130-135 (C++ truncating division)
+    g.Wo = 1 + (g.W + 2 * g.px - (((g.fw - 1) * g.dx) + 1)) / g.sx;
+    g.Ho = 1 + (g.H + 2 * g.py - (((g.fh - 1) * g.dy) + 1)) / g.sy;
+    if (g.Wo < 0) g.Wo = 0;
+    if (g.Ho < 0) g.Ho = 0;
+}
+
+static af_err convolve2_nn_impl(af_array *out, const af_array signal, const af_array filter,
+                                unsigned stride_dims, const dim_t *strides, unsigned padding_dims,
+                                const dim_t *paddings, unsigned dilation_dims,
+                                const dim_t *dilations, afgb_precision prec,
+                                const af_array scales) {
+    Array *s = get_array(signal);
+    Array *f = get_array(filter);
+    NNArgs a = nn_args(stride_dims, strides, padding_dims, paddings, dilation_dims, dilations);
+    AFGB_DIM_ASSERT(1, s->dims[2] == f->dims[2]);
+    af_dtype t = s->type;
+    if (t != f32 && t != f64 && t != f16) AFGB_TYPE_ERROR(1, t);
+    require_type(f, t);
+    if (prec != AFGB_PRECISION_FP32 && t != f32) {
+        AFGB_THROW(AF_ERR_TYPE, "tensor-core precisions take f32 arrays");
+    }
+    NNGeom g;
+    nn_geometry(g, s, f, a);
+    dim_t od[4] = {g.Wo, g.Ho, g.K, g.N};
+    Array o = *create_array(t, od);
+    Array sd = s->is_linear() ? *s : make_dense(*s);
+    Array fd = f->is_linear() ? *f : make_dense(*f);
+    const Array *sc = nullptr;
+    Array scd;
+    if (scales) {
+        Array *sa = get_array(scales);
+        require_type(sa, f32);
+        AFGB_DIM_ASSERT(10, sa->elements() == g.K);
+        scd = sa->is_linear() ? *sa : make_dense(*sa);
+        sc = &scd;
+    }
+    nn_forward(g, sd, fd, o, prec, sc);
+    *out = make_handle(&o);
+    return AF_SUCCESS;
+}
+
+static af_err convolve2_grad_impl(af_array *out, const af_array incoming_gradient,
+                                  const af_array original_signal, const af_array original_filter,
+                                  const af_array convolved_output, unsigned stride_dims,
+                                  const dim_t *strides, unsigned padding_dims,
+                                  const dim_t *paddings, unsigned dilation_dims,
+                                  const dim_t *dilations, af_conv_gradient_type grad_type,
+                                  afgb_precision prec, bool real_bias) {
+    Array *gi = get_array(incoming_gradient);
+    Array *s = get_array(original_signal);
+    Array *f = get_array(original_filter);
+    Array *o = get_array(convolved_output);
+    bool same = true;
+    for (int i = 0; i < 4; ++i) same &= gi->dims[i] == o->dims[i];
+    AFGB_DIM_ASSERT(1, same);
+    AFGB_DIM_ASSERT(3, o->dims[2] == f->dims[3]);
+    AFGB_DIM_ASSERT(3, o->dims[3] == s->dims[3]);
+    AFGB_DIM_ASSERT(2, s->dims[2] == f->dims[2]);
+    NNArgs a = nn_args(stride_dims, strides, padding_dims, paddings, dilation_dims, dilations);
+    af_dtype t = o->type;
+    if (t != f32 && t != f64 && t != f16) AFGB_TYPE_ERROR(1, t);
+    require_type(gi, t);
+    require_type(s, t);
+    require_type(f, t);
+    if (prec != AFGB_PRECISION_FP32 && t != f32) {
+        AFGB_THROW(AF_ERR_TYPE, "tensor-core precisions take f32 arrays");
+    }
+    NNGeom g;
+    nn_geometry(g, s, f, a);
+    // the reference does not compare the gradient's spatial size with the
+    // forward geometry; a mismatch would index out of bounds here
+    AFGB_DIM_ASSERT(1, gi->dims[0] == g.Wo && gi->dims[1] == g.Ho);
+    Array gd = gi->is_linear() ? *gi : make_dense(*gi);
+    Array sd = s->is_linear() ? *s : make_dense(*s);
+    Array fd = f->is_linear() ? *f : make_dense(*f);
+    if (grad_type == AF_CONV_GRADIENT_FILTER) {
+        Array r = *create_array(t, f->dims);
+        nn_filter_grad(g, gd, sd, r, prec);
+        *out = make_handle(&r);
+    } else if (grad_type == AF_CONV_GRADIENT_BIAS && real_bias) {
+        dim_t bd[4] = {1, 1, g.K, 1};
+        Array r = *create_array(t, bd);
+        nn_bias_grad(g, gd, r);
+        *out = make_handle(&r);
+    } else {
+        Array r = *create_array(t, s->dims);
+        nn_data_grad(g, gd, fd, r, prec);
+        *out = make_handle(&r);
+    }
+    return AF_SUCCESS;
+}
+
+}  // namespace afgb
+
+using namespace afgb;
+
+extern "C" {
+
+af_err af_convolve1(af_array *out, const af_array signal, const af_array filter,
+                    const af_conv_mode mode, af_conv_domain domain) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    return convolve_domain(out, signal, filter, mode, domain, 1);
+    AFGB_CATCHALL
+}
+
+af_err af_convolve2(af_array *out, const af_array signal, const af_array filter,
+                    const af_conv_mode mode, af_conv_domain domain) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    Array *s = get_array(signal);
+    Array *f = get_array(filter);
+    if (dim4_ndims(s->dims) < 2 || dim4_ndims(f->dims) < 2) {
+        return af_convolve1(out, signal, filter, mode, domain);
+    }
+    return convolve_domain(out, signal, filter, mode, domain, 2);
+    AFGB_CATCHALL
+}
+
+af_err af_convolve3(af_array *out, const af_array signal, const af_array filter,
+                    const af_conv_mode mode, af_conv_domain domain) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    Array *s = get_array(signal);
+    Array *f = get_array(filter);
+    if (dim4_ndims(s->dims) < 3 || dim4_ndims(f->dims) < 3) {
+        return af_convolve2(out, signal, filter, mode, domain);
+    }
+    return convolve_domain(out, signal, filter, mode, domain, 3);
+    AFGB_CATCHALL
+}
+
+af_err af_convolve2_sep(af_array *out, const af_array col_filter, const af_array row_filter,
+                        const af_array signal, const af_conv_mode mode) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    return convolve2_sep_impl(out, col_filter, row_filter, signal, mode);
+    AFGB_CATCHALL
+}
+
+af_err af_convolve2_nn(af_array *out, const af_array signal, const af_array filter,
+                       const unsigned stride_dims, const dim_t *strides,
+                       const unsigned padding_dims, const dim_t *paddings,
+                       const unsigned dilation_dims, const dim_t *dilations) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    return convolve2_nn_impl(out, signal, filter, stride_dims, strides, padding_dims, paddings,
+                             dilation_dims, dilations, AFGB_PRECISION_FP32, nullptr);
+    AFGB_CATCHALL
+}
+
+af_err afgb_convolve2_nn_ex(af_array *out, const af_array signal, const af_array filter,
+                            const unsigned stride_dims, const dim_t *strides,
+                            const unsigned padding_dims, const dim_t *paddings,
+                            const unsigned dilation_dims, const dim_t *dilations,
+                            afgb_precision precision, const af_array out_channel_scales) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    if ((int)precision < 0 || (int)precision > 2) AFGB_THROW(AF_ERR_ARG, "unknown precision");
+    return convolve2_nn_impl(out, signal, filter, stride_dims, strides, padding_dims, paddings,
+                             dilation_dims, dilations, precision, out_channel_scales);
+    AFGB_CATCHALL
+}
+
+af_err af_convolve2_gradient_nn(af_array *out, const af_array incoming_gradient,
+                                const af_array original_signal, const af_array original_filter,
+                                const af_array convolved_output, const unsigned stride_dims,
+                                const dim_t *strides, const unsigned padding_dims,
+                                const dim_t *paddings, const unsigned dilation_dims,
+                                const dim_t *dilations, af_conv_gradient_type grad_type) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    return convolve2_grad_impl(out, incoming_gradient, original_signal, original_filter,
+                               convolved_output, stride_dims, strides, padding_dims, paddings,
+                               dilation_dims, dilations, grad_type, AFGB_PRECISION_FP32, false);
+    AFGB_CATCHALL
+}
+
+af_err afgb_convolve2_gradient_nn_ex(af_array *out, const af_array incoming_gradient,
+                                     const af_array original_signal,
+                                     const af_array original_filter,
+                                     const af_array convolved_output, const unsigned stride_dims,
+                                     const dim_t *strides, const unsigned padding_dims,
+                                     const dim_t *paddings, const unsigned dilation_dims,
+                                     const dim_t *dilations, af_conv_gradient_type grad_type,
+                                     afgb_precision precision) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    if ((int)precision < 0 || (int)precision > 2) AFGB_THROW(AF_ERR_ARG, "unknown precision");
+    return convolve2_grad_impl(out, incoming_gradient, original_signal, original_filter,
+                               convolved_output, stride_dims, strides, padding_dims, paddings,
+                               dilation_dims, dilations, grad_type, precision, true);
+    AFGB_CATCHALL
+}
+
+int afgb_identify_batch_kind(int rank, const dim_t *sdims, const dim_t *fdims) {
+    return identify_batch_kind(rank, sdims, fdims);
+}
+
+int afgb_conv_output_dims(dim_t *odims, int rank, int kind, int expand, const dim_t *sdims,
+                          const dim_t *fdims) {
+    conv_out_dims(odims, rank, kind, expand != 0, sdims, fdims);
+    return 0;
+}
+
+int afgb_nn_output_dims(dim_t *odims, const dim_t *sdims, const dim_t *fdims,
+                        const dim_t *stride, const dim_t *padding, const dim_t *dilation) {
+    dim_t Wo = 1 + (sdims[0] + 2 * padding[0] - (((fdims[0] - 1) * dilation[0]) + 1)) / stride[0];
+    dim_t Ho = 1 + (sdims[1] + 2 * padding[1] - (((fdims[1] - 1) * dilation[1]) + 1)) / stride[1];
+    odims[0] = Wo;
+    odims[1] = Ho;
+    odims[2] = fdims[3];
+    odims[3] = sdims[3];
+    return 0;
+}
+
+}  // extern "C"

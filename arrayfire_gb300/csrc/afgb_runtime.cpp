@@ -1,0 +1,581 @@
+// Runtime of libafgb300: error state, device memory, streams and the array
+// lifecycle exports (the af_array subset of include/af/array.h and
+// include/af/device.h that the convolution path needs).
+//
+// Design: one process, one GPU at a time.  Device memory comes from the
+// CUDA stream-ordered pool (cudaMallocAsync) with its release threshold
+// raised, so freed blocks stay cached for the next call — the role of the
+// reference's DefaultMemoryManager (src/backend/common/DefaultMemoryManager.cpp)
+// without its bookkeeping.  Work runs on one non-blocking stream per device,
+// or on a stream the caller installs (afgb_set_stream).
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "afgb_internal.hpp"
+
+namespace afgb {
+
+// ---------------------------------------------------------------- errors
+static thread_local std::string g_last_error;
+
+static bool print_errors() {
+    static int v = [] {
+        const char *e = std::getenv("AF_PRINT_ERRORS");
+        return (e && e[0] && e[0] != '0') ? 1 : 0;
+    }();
+    return v != 0;
+}
+
+[[noreturn]] void throw_err(af_err code, const char *file, int line, const std::string &msg) {
+    std::string full = msg + "\nIn " + file + ":" + std::to_string(line);
+    throw AfError(code, full);
+}
+
+void cuda_check(cudaError_t e, const char *what, const char *file, int line) {
+    if (e == cudaSuccess) return;
+    af_err code = (e == cudaErrorMemoryAllocation) ? AF_ERR_NO_MEM : AF_ERR_RUNTIME;
+    throw_err(code, file, line, std::string("CUDA error ") + cudaGetErrorName(e) + " (" +
+                                    cudaGetErrorString(e) + ") in " + what);
+}
+
+static bool synchronous_calls() {
+    // AF_SYNCHRONOUS_CALLS (src/backend/cuda/debug_cuda.hpp:64-72)
+    static int v = [] {
+        const char *e = std::getenv("AF_SYNCHRONOUS_CALLS");
+        return (e && e[0] == '1') ? 1 : 0;
+    }();
+    return v != 0;
+}
+
+void post_launch(const char *kernel_name) {
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw_err(AF_ERR_RUNTIME, __FILE__, __LINE__,
+                  std::string("kernel launch failed: ") + kernel_name + ": " +
+                      cudaGetErrorString(e));
+    }
+    if (synchronous_calls()) AFGB_CUDA(cudaStreamSynchronize(stream()));
+}
+
+af_err record_exception() {
+    af_err code = AF_ERR_UNKNOWN;
+    try {
+        throw;
+    } catch (const AfError &e) {
+        code = e.code;
+        g_last_error = e.what();
+    } catch (const std::bad_alloc &e) {
+        code = AF_ERR_NO_MEM;
+        g_last_error = std::string("host allocation failed: ") + e.what();
+    } catch (const std::exception &e) {
+        code = AF_ERR_INTERNAL;
+        g_last_error = e.what();
+    } catch (...) {
+        code = AF_ERR_UNKNOWN;
+        g_last_error = "unknown error";
+    }
+    if (print_errors()) std::fprintf(stderr, "[afgb300] %s\n", g_last_error.c_str());
+    return code;
+}
+
+// ---------------------------------------------------------------- dtypes
+size_t dtype_size(af_dtype t) {
+    switch (t) {
+        case f32: return 4;
+        case c32: return 8;
+        case f64: return 8;
+        case c64: return 16;
+        case b8: return 1;
+        case s32: return 4;
+        case u32: return 4;
+        case u8: return 1;
+        case s64: return 8;
+        case u64: return 8;
+        case s16: return 2;
+        case u16: return 2;
+        case f16: return 2;
+        case s8: return 1;
+    }
+    return 0;
+}
+bool dtype_valid(af_dtype t) { return (int)t >= 0 && (int)t <= (int)s8; }
+
+// ---------------------------------------------------------------- state
+namespace {
+struct DevState {
+    cudaStream_t own = nullptr;
+    bool pool_ready = false;
+    int sms = 0;
+};
+std::mutex g_mu;
+DevState g_dev[64];
+cudaStream_t g_user_stream = nullptr;
+bool g_user_stream_set = false;
+std::atomic<int> g_exact{0};
+std::atomic<int> g_fail_after{0};
+std::atomic<unsigned long long> g_launches{0};
+}  // namespace
+
+int device() {
+    int d = 0;
+    AFGB_CUDA(cudaGetDevice(&d));
+    if (d < 0 || d >= 64) AFGB_THROW(AF_ERR_DEVICE, "device ordinal out of range");
+    return d;
+}
+
+static DevState &dev_state(int d) {
+    DevState &s = g_dev[d];
+    if (!s.pool_ready) {
+        std::lock_guard<std::mutex> lk(g_mu);
+        if (!s.pool_ready) {
+            AFGB_CUDA(cudaStreamCreateWithFlags(&s.own, cudaStreamNonBlocking));
+            cudaMemPool_t pool;
+            AFGB_CUDA(cudaDeviceGetDefaultMemPool(&pool, d));
+            uint64_t thr = UINT64_MAX;
+            AFGB_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+            AFGB_CUDA(cudaDeviceGetAttribute(&s.sms, cudaDevAttrMultiProcessorCount, d));
+            s.pool_ready = true;
+        }
+    }
+    return s;
+}
+
+cudaStream_t stream() {
+    if (g_user_stream_set) return g_user_stream;
+    return dev_state(device()).own;
+}
+
+int num_sms() { return dev_state(device()).sms; }
+bool exact_fp() { return g_exact.load() != 0; }
+void count_launch(unsigned n) { g_launches += n; }
+
+// ---------------------------------------------------------------- memory
+void *alloc_device(size_t bytes) {
+    int fa = g_fail_after.load();
+    if (fa > 0) {
+        if (g_fail_after.fetch_sub(1) == 1) {
+            AFGB_THROW(AF_ERR_NO_MEM, "device allocation failed (injected)");
+        }
+    }
+    if (bytes == 0) bytes = 16;
+    void *p = nullptr;
+    cudaError_t e = cudaMallocAsync(&p, bytes, stream());
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        AFGB_THROW(AF_ERR_NO_MEM, "device allocation of " + std::to_string(bytes) +
+                                      " bytes failed: " + cudaGetErrorString(e));
+    }
+    return p;
+}
+
+void free_device(void *p) {
+    if (p) (void)cudaFreeAsync(p, stream());
+}
+
+Buffer::~Buffer() {
+    if (!ptr) return;
+    if (kind == BufKind::Pool) {
+        (void)cudaFreeAsync(ptr, stream());
+    } else if (kind == BufKind::Adopted) {
+        (void)cudaFree(ptr);
+    }
+}
+
+// ---------------------------------------------------------------- arrays
+dim_t dim4_ndims(const dim_t d[4]) {
+    dim_t num = d[0] * d[1] * d[2] * d[3];
+    if (num == 0) return 0;
+    if (num == 1) return 1;
+    if (d[3] != 1) return 4;
+    if (d[2] != 1) return 3;
+    if (d[1] != 1) return 2;
+    return 1;
+}
+
+void dim4_from(dim_t out[4], unsigned n, const dim_t *vals) {
+    for (unsigned i = 0; i < 4; ++i) out[i] = (n > i) ? vals[i] : 1;
+}
+
+dim_t Array::ndims() const { return dim4_ndims(dims); }
+
+bool Array::is_linear() const {
+    dim_t s = 1;
+    for (int i = 0; i < 4; ++i) {
+        if (dims[i] != 1 && strides[i] != s) return false;
+        s *= dims[i];
+    }
+    return true;
+}
+
+static void dense_strides(Array *a) {
+    a->strides[0] = 1;
+    for (int i = 1; i < 4; ++i) a->strides[i] = a->strides[i - 1] * a->dims[i - 1];
+}
+
+static const uint64_t kMagic = 0xAF6B300A11A5ull;
+struct Handle {
+    uint64_t magic = kMagic;
+    Array arr;
+};
+
+Array *get_array(const af_array a) {
+    if (!a) AFGB_THROW(AF_ERR_ARG, "Invalid (null) af_array handle");
+    Handle *h = static_cast<Handle *>(a);
+    if (h->magic != kMagic) AFGB_THROW(AF_ERR_ARG, "Invalid af_array handle");
+    return &h->arr;
+}
+
+af_array make_handle(Array *a) {
+    Handle *h = new Handle();
+    h->arr = *a;
+    return static_cast<af_array>(h);
+}
+
+Array *create_array(af_dtype t, const dim_t dims[4]) {
+    static thread_local Array scratch;
+    scratch = Array();
+    scratch.type = t;
+    for (int i = 0; i < 4; ++i) {
+        if (dims[i] < 0) AFGB_THROW(AF_ERR_SIZE, "negative dimension");
+        scratch.dims[i] = dims[i];
+    }
+    dense_strides(&scratch);
+    auto b = std::make_shared<Buffer>();
+    b->bytes = (size_t)scratch.elements() * dtype_size(t);
+    b->ptr = alloc_device(b->bytes);
+    b->kind = BufKind::Pool;
+    b->device = device();
+    scratch.buf = b;
+    return &scratch;
+}
+
+// ---------------------------------------------------------------- timing
+namespace {
+struct TimedLaunch {
+    std::string name;
+    cudaEvent_t a, b;
+};
+std::mutex g_tmu;
+std::atomic<int> g_timing{0};
+std::vector<TimedLaunch> g_timed;
+}  // namespace
+
+KernelTimer::KernelTimer(const char *n) : name(n) {
+    if (!g_timing.load()) return;
+    if (cudaEventCreate(&start) != cudaSuccess) {
+        start = nullptr;
+        return;
+    }
+    cudaEventRecord(start, stream());
+}
+
+KernelTimer::~KernelTimer() {
+    if (!start) return;
+    cudaEvent_t end;
+    if (cudaEventCreate(&end) != cudaSuccess) {
+        cudaEventDestroy(start);
+        return;
+    }
+    cudaEventRecord(end, stream());
+    std::lock_guard<std::mutex> lk(g_tmu);
+    g_timed.push_back(TimedLaunch{name, start, end});
+}
+
+}  // namespace afgb
+
+using namespace afgb;
+
+// ======================================================================
+// exported lifecycle API
+// ======================================================================
+extern "C" {
+
+af_err af_create_handle(af_array *arr, const unsigned ndims, const dim_t *const dims,
+                        const af_dtype type) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, arr != nullptr);
+    if (!dtype_valid(type)) AFGB_TYPE_ERROR(4, type);
+    AFGB_ARG_ASSERT(1, ndims <= 4);
+    dim_t d[4];
+    dim4_from(d, ndims, dims);
+    *arr = make_handle(create_array(type, d));
+    AFGB_CATCHALL
+}
+
+af_err af_create_array(af_array *arr, const void *const data, const unsigned ndims,
+                       const dim_t *const dims, const af_dtype type) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, arr != nullptr);
+    if (!dtype_valid(type)) AFGB_TYPE_ERROR(4, type);
+    AFGB_ARG_ASSERT(2, ndims <= 4);
+    dim_t d[4];
+    dim4_from(d, ndims, dims);
+    Array *a = create_array(type, d);
+    size_t bytes = (size_t)a->elements() * dtype_size(type);
+    if (bytes && data) {
+        AFGB_CUDA(cudaMemcpyAsync(a->data(), data, bytes, cudaMemcpyHostToDevice, stream()));
+    }
+    *arr = make_handle(a);
+    AFGB_CATCHALL
+}
+
+af_err af_device_array(af_array *arr, void *data, const unsigned ndims,
+                       const dim_t *const dims, const af_dtype type) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, arr != nullptr);
+    if (!dtype_valid(type)) AFGB_TYPE_ERROR(4, type);
+    AFGB_ARG_ASSERT(2, ndims <= 4);
+    Array a;
+    a.type = type;
+    dim4_from(a.dims, ndims, dims);
+    dense_strides(&a);
+    auto b = std::make_shared<Buffer>();
+    b->ptr = data;
+    b->bytes = (size_t)a.elements() * dtype_size(type);
+    b->kind = BufKind::Adopted;
+    b->device = device();
+    a.buf = b;
+    *arr = make_handle(&a);
+    AFGB_CATCHALL
+}
+
+af_err afgb_device_array_view(af_array *arr, void *data, const unsigned ndims,
+                              const dim_t *const dims, const dim_t *const strides,
+                              const af_dtype type) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, arr != nullptr);
+    if (!dtype_valid(type)) AFGB_TYPE_ERROR(5, type);
+    AFGB_ARG_ASSERT(2, ndims <= 4);
+    Array a;
+    a.type = type;
+    dim4_from(a.dims, ndims, dims);
+    if (strides) {
+        for (unsigned i = 0; i < 4; ++i) {
+            a.strides[i] = (i < ndims) ? strides[i] : (i == 0 ? 1 : a.strides[i - 1] * a.dims[i - 1]);
+        }
+    } else {
+        dense_strides(&a);
+    }
+    auto b = std::make_shared<Buffer>();
+    b->ptr = data;
+    b->kind = BufKind::View;
+    b->device = device();
+    a.buf = b;
+    *arr = make_handle(&a);
+    AFGB_CATCHALL
+}
+
+af_err af_get_data_ptr(void *data, const af_array arr) {
+    AFGB_TRY
+    Array *a = get_array(arr);
+    AFGB_ARG_ASSERT(0, data != nullptr);
+    size_t es = dtype_size(a->type);
+    if (a->elements() == 0) return AF_SUCCESS;
+    if (a->is_linear()) {
+        AFGB_CUDA(cudaMemcpyAsync(data, a->data(), (size_t)a->elements() * es,
+                                  cudaMemcpyDeviceToHost, stream()));
+    } else {
+        // strided view: one 2-D copy per (d2, d3) slice row set
+        char *dst = static_cast<char *>(data);
+        for (dim_t k3 = 0; k3 < a->dims[3]; ++k3)
+            for (dim_t k2 = 0; k2 < a->dims[2]; ++k2)
+                for (dim_t k1 = 0; k1 < a->dims[1]; ++k1) {
+                    const char *src = static_cast<const char *>(a->data()) +
+                                      (k1 * a->strides[1] + k2 * a->strides[2] +
+                                       k3 * a->strides[3]) * (dim_t)es;
+                    AFGB_CUDA(cudaMemcpy2DAsync(dst, es, src, a->strides[0] * es, es,
+                                                (size_t)a->dims[0], cudaMemcpyDeviceToHost,
+                                                stream()));
+                    dst += a->dims[0] * es;
+                }
+    }
+    AFGB_CUDA(cudaStreamSynchronize(stream()));
+    AFGB_CATCHALL
+}
+
+af_err af_get_device_ptr(void **ptr, const af_array arr) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, ptr != nullptr);
+    *ptr = get_array(arr)->data();
+    AFGB_CATCHALL
+}
+
+af_err af_release_array(af_array arr) {
+    AFGB_TRY
+    if (!arr) return AF_SUCCESS;
+    get_array(arr);
+    Handle *h = static_cast<Handle *>(arr);
+    h->magic = 0;
+    delete h;
+    AFGB_CATCHALL
+}
+
+af_err af_retain_array(af_array *out, const af_array in) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    *out = make_handle(get_array(in));
+    AFGB_CATCHALL
+}
+
+af_err af_get_elements(dim_t *elems, const af_array arr) {
+    AFGB_TRY
+    *elems = get_array(arr)->elements();
+    AFGB_CATCHALL
+}
+
+af_err af_get_type(af_dtype *type, const af_array arr) {
+    AFGB_TRY
+    *type = get_array(arr)->type;
+    AFGB_CATCHALL
+}
+
+af_err af_get_dims(dim_t *d0, dim_t *d1, dim_t *d2, dim_t *d3, const af_array arr) {
+    AFGB_TRY
+    Array *a = get_array(arr);
+    *d0 = a->dims[0];
+    *d1 = a->dims[1];
+    *d2 = a->dims[2];
+    *d3 = a->dims[3];
+    AFGB_CATCHALL
+}
+
+af_err af_get_numdims(unsigned *result, const af_array arr) {
+    AFGB_TRY
+    *result = (unsigned)get_array(arr)->ndims();
+    AFGB_CATCHALL
+}
+
+af_err af_get_strides(dim_t *s0, dim_t *s1, dim_t *s2, dim_t *s3, const af_array arr) {
+    AFGB_TRY
+    Array *a = get_array(arr);
+    *s0 = a->strides[0];
+    *s1 = a->strides[1];
+    *s2 = a->strides[2];
+    *s3 = a->strides[3];
+    AFGB_CATCHALL
+}
+
+af_err af_sync(const int dev) {
+    AFGB_TRY
+    if (dev >= 0) {
+        int cur = device();
+        if (dev != cur) AFGB_CUDA(cudaSetDevice(dev));
+        AFGB_CUDA(cudaStreamSynchronize(stream()));
+        if (dev != cur) AFGB_CUDA(cudaSetDevice(cur));
+    } else {
+        AFGB_CUDA(cudaStreamSynchronize(stream()));
+    }
+    AFGB_CATCHALL
+}
+
+af_err af_free_host(void *ptr) {
+    std::free(ptr);
+    return AF_SUCCESS;
+}
+
+void af_get_last_error(char **msg, dim_t *len) {
+    if (!msg) return;
+    const std::string &s = g_last_error;
+    char *m = static_cast<char *>(std::malloc(s.size() + 1));
+    if (!m) {
+        *msg = nullptr;
+        if (len) *len = 0;
+        return;
+    }
+    std::memcpy(m, s.c_str(), s.size() + 1);
+    *msg = m;
+    if (len) *len = (dim_t)s.size();
+    g_last_error.clear();
+}
+
+const char *af_err_to_string(const af_err err) {
+    switch (err) {
+        case AF_SUCCESS: return "Success";
+        case AF_ERR_NO_MEM: return "Device out of memory";
+        case AF_ERR_DRIVER: return "Driver not available or incompatible";
+        case AF_ERR_RUNTIME: return "Runtime error ";
+        case AF_ERR_INVALID_ARRAY: return "Invalid array";
+        case AF_ERR_ARG: return "Invalid input argument";
+        case AF_ERR_SIZE: return "Invalid input size";
+        case AF_ERR_TYPE: return "Function does not support this data type";
+        case AF_ERR_DIFF_TYPE: return "Input types are not the same";
+        case AF_ERR_BATCH: return "Invalid batch configuration";
+        case AF_ERR_DEVICE: return "Input does not belong to the current device.";
+        case AF_ERR_NOT_SUPPORTED: return "Function not supported";
+        case AF_ERR_NOT_CONFIGURED: return "Function not configured to build";
+        case AF_ERR_NONFREE: return "Function unavailable. ArrayFire compiled without Non-Free algorithms support";
+        case AF_ERR_NO_DBL: return "Double precision not supported for this device";
+        case AF_ERR_NO_GFX: return "Graphics functionality unavailable. ArrayFire compiled without Graphics support";
+        case AF_ERR_NO_HALF: return "Half precision floats not supported for this device";
+        case AF_ERR_LOAD_LIB: return "Failed to load dynamic library. ";
+        case AF_ERR_LOAD_SYM: return "Failed to load symbol";
+        case AF_ERR_ARR_BKND_MISMATCH: return "There was a mismatch between an array and the current backend";
+        case AF_ERR_INTERNAL: return "Internal error";
+        case AF_ERR_UNKNOWN: return "Unknown error";
+    }
+    return "Unknown error. Please open an issue and add this error code to the case in af_err_to_string.";
+}
+
+af_err afgb_set_stream(void *s) {
+    AFGB_TRY
+    g_user_stream = static_cast<cudaStream_t>(s);
+    g_user_stream_set = (s != nullptr);
+    AFGB_CATCHALL
+}
+
+af_err afgb_get_stream(void **s) {
+    AFGB_TRY
+    *s = static_cast<void *>(stream());
+    AFGB_CATCHALL
+}
+
+af_err afgb_set_exact_fp(int exact) {
+    g_exact.store(exact ? 1 : 0);
+    return AF_SUCCESS;
+}
+
+void afgb_debug_fail_alloc_after(int n) { g_fail_after.store(n > 0 ? n : 0); }
+
+unsigned long long afgb_kernel_launch_count(void) { return g_launches.load(); }
+
+void afgb_kernel_timing(int enable) {
+    g_timing.store(enable ? 1 : 0);
+    if (!enable) {
+        std::lock_guard<std::mutex> lk(g_tmu);
+        for (auto &t : g_timed) {
+            cudaEventDestroy(t.a);
+            cudaEventDestroy(t.b);
+        }
+        g_timed.clear();
+    }
+}
+
+af_err afgb_kernel_time(const char *name, unsigned long long *count, double *total_ms) {
+    AFGB_TRY
+    std::lock_guard<std::mutex> lk(g_tmu);
+    unsigned long long c = 0;
+    double tot = 0.0;
+    for (auto &t : g_timed) {
+        if (name && t.name != name) continue;
+        AFGB_CUDA(cudaEventSynchronize(t.b));
+        float ms = 0.f;
+        AFGB_CUDA(cudaEventElapsedTime(&ms, t.a, t.b));
+        tot += ms;
+        ++c;
+    }
+    if (count) *count = c;
+    if (total_ms) *total_ms = tot;
+    AFGB_CATCHALL
+}
+
+const char *afgb_version(void) { return "afgb300 0.1 (ArrayFire 3.10 convolution C ABI, sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,885 @@
+// Direct small-filter convolutions (af_convolve1/2/3, af_convolve2_sep) for
+// sm_103a.
+//
+// Reference behaviour: src/backend/cpu/kernel/convolve.hpp (the loop order
+// that defines the rounding) and src/backend/cuda/kernel/convolve*.cuh (the
+// reference's GPU kernels, which launch once per filter batch with the filter
+// in constant memory).  Design here:
+//   * one launch covers every batch slice (NONE/LHS/RHS/SAME) — the batch
+//     index comes from blockIdx.z, filters are read per slice;
+//   * the hot 2-D shapes (3x3, 5x5, 7x7 on f32 and 8-bit inputs) use a
+//     register-blocked tile kernel: a 64x64 output tile per CTA, the haloed
+//     input tile staged once in shared memory, each thread producing a 4x4
+//     block from 128-bit shared loads and taps held in registers;
+//   * the separable convolution is fused: column pass and row pass run in
+//     one CTA and the intermediate image never leaves shared memory (the
+//     reference writes a full-size temporary between two launches,
+//     src/backend/cuda/convolve.cpp:76-80);
+//   * every other dtype/shape uses a generic one-thread-per-output kernel
+//     with the same arithmetic.
+// The accumulation order is the reference's: taps of the outer dimension
+// outside, dim-0 taps inside, ascending, starting from zero.
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <type_traits>
+
+#include "conv_common.cuh"
+#include "conv_direct.hpp"
+
+namespace afgb {
+
+// ---------------------------------------------------------------------------
+// parameters
+// ---------------------------------------------------------------------------
+struct DirectParams {
+    const void *sig;
+    const void *filt;
+    void *out;
+    int rank;
+    int expand;
+    long long sd[4], ss[4];
+    long long od[4], os[4];
+    long long fd[4], fs[4];
+    long long in_step[4], out_step[4], filt_step[4];
+    long long batch[4];
+    long long nbatch;
+};
+
+struct BatchOff {
+    long long in, out, filt;
+};
+
+__device__ __forceinline__ BatchOff batch_offsets(const DirectParams &p, long long b) {
+    long long b1 = b % p.batch[1];
+    long long r = b / p.batch[1];
+    long long b2 = r % p.batch[2];
+    long long b3 = r / p.batch[2];
+    BatchOff o;
+    o.in = b1 * p.in_step[1] + b2 * p.in_step[2] + b3 * p.in_step[3];
+    o.out = b1 * p.out_step[1] + b2 * p.out_step[2] + b3 * p.out_step[3];
+    o.filt = b1 * p.filt_step[1] + b2 * p.filt_step[2] + b3 * p.filt_step[3];
+    return o;
+}
+
+// ---------------------------------------------------------------------------
+// generic kernel: one output per thread, any rank/dtype/stride
+// (one2one_{1,2,3}d, src/backend/cpu/kernel/convolve.hpp:19-130)
+// ---------------------------------------------------------------------------
+template <typename T, bool EXACT>
+__global__ void conv_generic_kernel(DirectParams p, long long slice) {
+    using A = typename AccOf<T>::type;
+    const T *sig = static_cast<const T *>(p.sig);
+    const A *filt = static_cast<const A *>(p.filt);
+    T *out = static_cast<T *>(p.out);
+    const long long total = slice * p.nbatch;
+    const long long f0 = p.fd[0];
+    const long long f1 = p.rank >= 2 ? p.fd[1] : 1;
+    const long long f2 = p.rank >= 3 ? p.fd[2] : 1;
+    const long long c0 = p.expand ? 0 : f0 / 2;
+    const long long c1 = p.expand ? 0 : f1 / 2;
+    const long long c2 = p.expand ? 0 : f2 / 2;
+    const long long o0 = p.od[0];
+    const long long o1 = p.rank >= 2 ? p.od[1] : 1;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        long long b = t / slice;
+        long long e = t - b * slice;
+        long long i = e % o0;
+        long long j = (e / o0) % o1;
+        long long k = e / (o0 * o1);
+        BatchOff bo = batch_offsets(p, b);
+        const T *in = sig + bo.in;
+        const A *w = filt + bo.filt;
+        A acc = acc_zero<A>();
+        for (long long wk = 0; wk < f2; ++wk) {
+            long long kIdx = k + c2 - wk;
+            bool kv = (p.rank < 3) || (kIdx >= 0 && kIdx < p.sd[2]);
+            for (long long wj = 0; wj < f1; ++wj) {
+                long long jIdx = j + c1 - wj;
+                bool jv = (p.rank < 2) || (jIdx >= 0 && jIdx < p.sd[1]);
+                for (long long wi = 0; wi < f0; ++wi) {
+                    long long iIdx = i + c0 - wi;
+                    T s{};
+                    if (kv && jv && iIdx >= 0 && iIdx < p.sd[0]) {
+                        long long off = iIdx * p.ss[0];
+                        if (p.rank >= 2) off += jIdx * p.ss[1];
+                        if (p.rank >= 3) off += kIdx * p.ss[2];
+                        s = in[off];
+                    }
+                    A fv = w[wi * p.fs[0] + (p.rank >= 2 ? wj * p.fs[1] : 0) +
+                             (p.rank >= 3 ? wk * p.fs[2] : 0)];
+                    acc = mac<EXACT>(acc, to_acc(s, A{}), fv);
+                }
+            }
+        }
+        long long ooff = bo.out + i * p.os[0];
+        if (p.rank >= 2) ooff += j * p.os[1];
+        if (p.rank >= 3) ooff += k * p.os[2];
+        out[ooff] = from_acc_any(acc, T{});
+    }
+}
+
+// ---------------------------------------------------------------------------
+// fast 2-D tile kernel
+// ---------------------------------------------------------------------------
+constexpr int T2_BX = 64;
+constexpr int T2_BY = 64;
+constexpr int T2_THREADS = 256;
+
+template <typename T>
+__device__ __forceinline__ float load_as_float(const T *p) {
+    return to_acc(__ldg(p), 0.0f);
+}
+template <>
+__device__ __forceinline__ float load_as_float<float>(const float *p) {
+    return __ldg(p);
+}
+
+template <typename T>
+__device__ __forceinline__ void store4(T *dst, const float *v, bool vec_ok) {
+    if (vec_ok) {
+        if constexpr (sizeof(T) == 4 && !IsInt<T>::value) {
+            *reinterpret_cast<float4 *>(dst) = make_float4(v[0], v[1], v[2], v[3]);
+            return;
+        } else if constexpr (sizeof(T) == 1) {
+            uint32_t w = (uint32_t)(uint8_t)from_acc<T>(v[0]) |
+                         ((uint32_t)(uint8_t)from_acc<T>(v[1]) << 8) |
+                         ((uint32_t)(uint8_t)from_acc<T>(v[2]) << 16) |
+                         ((uint32_t)(uint8_t)from_acc<T>(v[3]) << 24);
+            *reinterpret_cast<uint32_t *>(dst) = w;
+            return;
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c) dst[c] = from_acc_any(v[c], T{});
+}
+
+// T in {float, uint8_t, int8_t}; taps are float.  F0 x F1 filter.
+template <typename T, int F0, int F1, bool EXACT>
+__global__ void __launch_bounds__(T2_THREADS) conv2_tile_kernel(DirectParams p) {
+    constexpr int TW = T2_BX + F0 - 1;
+    constexpr int TH = T2_BY + F1 - 1;
+    constexpr int PITCH = ((TW + 3) / 4) * 4;
+    constexpr int WIN = 4 + F0 - 1;
+    constexpr int WIN4 = (WIN + 3) / 4;
+    __shared__ __align__(16) float tile[TH * PITCH];
+
+    const long long b = blockIdx.z;
+    BatchOff bo = batch_offsets(p, b);
+    const T *in = static_cast<const T *>(p.sig) + bo.in;
+    const float *w = static_cast<const float *>(p.filt) + bo.filt;
+    T *out = static_cast<T *>(p.out) + bo.out;
+
+    const long long i0 = (long long)blockIdx.x * T2_BX;
+    const long long j0 = (long long)blockIdx.y * T2_BY;
+    const int ci = p.expand ? 0 : F0 / 2;
+    const int cj = p.expand ? 0 : F1 / 2;
+    const long long ox = i0 + ci - (F0 - 1);
+    const long long oy = j0 + cj - (F1 - 1);
+    const long long sd0 = p.sd[0], sd1 = p.sd[1];
+    const long long ss0 = p.ss[0], ss1 = p.ss[1];
+
+    // stage the haloed input tile (zero outside the signal)
+    for (int idx = threadIdx.x; idx < TH * TW; idx += T2_THREADS) {
+        int r = idx / TW;
+        int c = idx - r * TW;
+        long long gx = ox + c, gy = oy + r;
+        float v = 0.0f;
+        if (gx >= 0 && gx < sd0 && gy >= 0 && gy < sd1) v = load_as_float<T>(in + gx * ss0 + gy * ss1);
+        tile[r * PITCH + c] = v;
+    }
+    float wr[F0 * F1];
+#pragma unroll
+    for (int fj = 0; fj < F1; ++fj)
+#pragma unroll
+        for (int fi = 0; fi < F0; ++fi) wr[fj * F0 + fi] = __ldg(w + fi * p.fs[0] + fj * p.fs[1]);
+    __syncthreads();
+
+    const int tx = threadIdx.x & 15;
+    const int ty = threadIdx.x >> 4;
+    float acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = 0.0f;
+
+    // walk input rows bottom-up so each output sees its dim-1 taps in
+    // ascending order (fj = rr + F1 - 1 - q), dim-0 taps ascending inside
+#pragma unroll
+    for (int q = 3 + F1 - 1; q >= 0; --q) {
+        float v[WIN4 * 4];
+        const float *row = tile + (4 * ty + q) * PITCH + 4 * tx;
+#pragma unroll
+        for (int u = 0; u < WIN4; ++u) {
+            float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
+            v[4 * u + 0] = t4.x;
+            v[4 * u + 1] = t4.y;
+            v[4 * u + 2] = t4.z;
+            v[4 * u + 3] = t4.w;
+        }
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+            const int fj = rr + F1 - 1 - q;
+            if (fj >= 0 && fj < F1) {
+#pragma unroll
+                for (int fi = 0; fi < F0; ++fi) {
+                    const float wv = wr[fj * F0 + fi];
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc)
+                        acc[rr][cc] = mac<EXACT>(acc[rr][cc], v[cc + F0 - 1 - fi], wv);
+                }
+            }
+        }
+    }
+
+    const long long od0 = p.od[0], od1 = p.od[1];
+    const long long x = i0 + 4 * tx;
+    const bool vec_ok = (x + 3 < od0) && (p.os[0] == 1) &&
+                        ((reinterpret_cast<uintptr_t>(out) % (4 * sizeof(T))) == 0) &&
+                        ((p.os[1] % 4) == 0) && ((x % 4) == 0);
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr) {
+        long long y = j0 + 4 * ty + rr;
+        if (y >= od1) break;
+        T *dst = out + y * p.os[1] + x * p.os[0];
+        if (vec_ok) {
+            store4<T>(dst, acc[rr], true);
+        } else {
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc)
+                if (x + cc < od0) dst[cc * p.os[0]] = from_acc_any(acc[rr][cc], T{});
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// fused separable kernel (f32 and 8-bit inputs)
+// ---------------------------------------------------------------------------
+constexpr int SP_BX = 64;
+constexpr int SP_BY = 64;
+constexpr int SP_THREADS = 256;
+
+struct SepParams {
+    const void *sig;
+    const float *cf;
+    const float *rf;
+    void *out;
+    int cflen, rflen;
+    int expand;
+    long long sd[4], ss[4];
+    long long od[4], os[4];
+    long long tw;  // width of the intermediate image (reference temp dims[0])
+};
+
+// tap as the reference's separable kernel sees it: converted to the input
+// type (src/backend/cpu/kernel/convolve.hpp:233), then back to float for the
+// exact integer arithmetic
+template <typename T>
+__device__ __forceinline__ float sep_tap(float f) {
+    if constexpr (IsInt<T>::value) return (float)from_acc<T>(f);
+    return f;
+}
+template <typename T>
+__device__ __forceinline__ float sep_round(float a) {
+    if constexpr (IsInt<T>::value) return (float)from_acc<T>(a);
+    return a;
+}
+
+// CFL/RFL: compile-time filter lengths (0 = runtime, bounded by 31)
+template <typename T, int CFL, int RFL, bool EXACT>
+__global__ void __launch_bounds__(SP_THREADS) sep_fused_kernel(SepParams p) {
+    constexpr int CMAX = CFL ? CFL : 31;
+    constexpr int RMAX = RFL ? RFL : 31;
+    const int cfl = CFL ? CFL : p.cflen;
+    const int rfl = RFL ? RFL : p.rflen;
+    const int TW = SP_BX + cfl - 1;
+    const int TH = SP_BY + rfl - 1;
+    const int PITCH = ((SP_BX + CMAX - 1 + 3) / 4) * 4;
+    extern __shared__ __align__(16) float smem[];
+    float *tile = smem;                           // TH x PITCH input values
+    float *temp = smem + (SP_BY + RMAX - 1) * PITCH;  // TH x SP_BX intermediate
+    __shared__ float ctap[32], rtap[32];
+
+    const long long b = blockIdx.z;
+    const long long b2 = b % p.sd[2];
+    const long long b3 = b / p.sd[2];
+    const T *in = static_cast<const T *>(p.sig) + b2 * p.ss[2] + b3 * p.ss[3];
+    T *out = static_cast<T *>(p.out) + b2 * p.os[2] + b3 * p.os[3];
+
+    const long long i0 = (long long)blockIdx.x * SP_BX;
+    const long long j0 = (long long)blockIdx.y * SP_BY;
+    const int cc0 = p.expand ? 0 : cfl / 2;
+    const int cr0 = p.expand ? 0 : rfl / 2;
+    const long long ox = i0 + cc0 - (cfl - 1);
+    const long long oy = j0 + cr0 - (rfl - 1);
+    const long long sd0 = p.sd[0], sd1 = p.sd[1];
+
+    if (threadIdx.x < 32) {
+        ctap[threadIdx.x] = threadIdx.x < cfl ? sep_tap<T>(p.cf[threadIdx.x]) : 0.0f;
+        rtap[threadIdx.x] = threadIdx.x < rfl ? sep_tap<T>(p.rf[threadIdx.x]) : 0.0f;
+    }
+    for (int idx = threadIdx.x; idx < TH * TW; idx += SP_THREADS) {
+        int r = idx / TW;
+        int c = idx - r * TW;
+        long long gx = ox + c, gy = oy + r;
+        float v = 0.0f;
+        if (gx >= 0 && gx < sd0 && gy >= 0 && gy < sd1)
+            v = load_as_float<T>(in + gx * p.ss[0] + gy * p.ss[1]);
+        tile[r * PITCH + c] = v;
+    }
+    __syncthreads();
+
+    // pass 1 (dim 0): temp[r][x] = IN( sum_f tile[r][x + cfl-1-f] * c[f] ),
+    // 8 consecutive x per work item; rows outside the signal are zero
+    // (isCJValid in the reference's second pass)
+    constexpr int W1 = 8 + CMAX - 1;
+    constexpr int W1V = (W1 + 3) / 4;
+    for (int it = threadIdx.x; it < TH * (SP_BX / 8); it += SP_THREADS) {
+        const int r = it / (SP_BX / 8);
+        const int g = it - r * (SP_BX / 8);
+        const long long gy = oy + r;
+        float a[8];
+#pragma unroll
+        for (int e = 0; e < 8; ++e) a[e] = 0.0f;
+        if (gy >= 0 && gy < sd1) {
+            float v[W1V * 4];
+            const float *row = tile + r * PITCH + 8 * g;
+#pragma unroll
+            for (int u = 0; u < W1V; ++u) {
+                if (4 * u < 8 + cfl - 1) {
+                    float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
+                    v[4 * u] = t4.x;
+                    v[4 * u + 1] = t4.y;
+                    v[4 * u + 2] = t4.z;
+                    v[4 * u + 3] = t4.w;
+                } else {
+                    v[4 * u] = v[4 * u + 1] = v[4 * u + 2] = v[4 * u + 3] = 0.0f;
+                }
+            }
+#pragma unroll
+            for (int f = 0; f < CMAX; ++f) {
+                if (f < cfl) {
+                    const float wv = ctap[f];
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) {
+                        // window index e + cfl-1-f, resolved at compile time
+                        // when CFL is fixed
+                        a[e] = mac<EXACT>(a[e], v[e + (CFL ? CFL - 1 - f : 0) +
+                                                   (CFL ? 0 : cfl - 1 - f)],
+                                          wv);
+                    }
+                }
+            }
+#pragma unroll
+            for (int e = 0; e < 8; ++e) a[e] = sep_round<T>(a[e]);
+        }
+        float *trow = temp + r * SP_BX + 8 * g;
+        *reinterpret_cast<float4 *>(trow) = make_float4(a[0], a[1], a[2], a[3]);
+        *reinterpret_cast<float4 *>(trow + 4) = make_float4(a[4], a[5], a[6], a[7]);
+    }
+    __syncthreads();
+
+    // pass 2 (dim 1): out[x][y] = IN( sum_g temp[y + rfl-1-g][x] * r[g] ),
+    // 4 x 4 outputs per thread, temp rows walked bottom-up
+    const int tx = threadIdx.x & 15;
+    const int ty = threadIdx.x >> 4;
+    float acc[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = 0.0f;
+#pragma unroll
+    for (int q = 3 + RMAX - 1; q >= 0; --q) {
+        if (q < 3 + rfl) {
+            float4 t4 = *reinterpret_cast<const float4 *>(temp + (4 * ty + q) * SP_BX + 4 * tx);
+            const float v[4] = {t4.x, t4.y, t4.z, t4.w};
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const int g = rr + rfl - 1 - q;
+                if (g >= 0 && g < rfl) {
+                    const float wv = rtap[g];
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) acc[rr][cc] = mac<EXACT>(acc[rr][cc], v[cc], wv);
+                }
+            }
+        }
+    }
+    const long long od0 = p.od[0], od1 = p.od[1];
+    const long long x = i0 + 4 * tx;
+    const bool vec_ok = (x + 3 < od0) && (p.os[0] == 1) &&
+                        ((reinterpret_cast<uintptr_t>(out) % (4 * sizeof(T))) == 0) &&
+                        ((p.os[1] % 4) == 0);
+#pragma unroll
+    for (int rr = 0; rr < 4; ++rr) {
+        long long y = j0 + 4 * ty + rr;
+        if (y >= od1) break;
+        T *dst = out + y * p.os[1] + x * p.os[0];
+        if (vec_ok) {
+            store4<T>(dst, acc[rr], true);
+        } else {
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc)
+                if (x + cc < od0) dst[cc * p.os[0]] = from_acc_any(acc[rr][cc], T{});
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// generic separable passes (every other dtype): one 1-D pass per launch
+// through a temporary, exactly as the reference CPU backend's two calls
+// (src/backend/cpu/kernel/convolve.hpp:213-255)
+// ---------------------------------------------------------------------------
+template <typename T, typename A, bool EXACT, int DIM>
+__global__ void sep_pass_kernel(const T *in, long long id0, long long id1, long long is0,
+                                long long is1, long long is2, long long is3, const A *filt,
+                                int flen, T *out, long long od0, long long od1, long long os1,
+                                long long os2, long long os3, long long n2, long long n3,
+                                int expand) {
+    const long long total = od0 * od1 * n2 * n3;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        long long i = t % od0;
+        long long j = (t / od0) % od1;
+        long long bb = t / (od0 * od1);
+        long long b2 = bb % n2, b3 = bb / n2;
+        const T *src = in + b2 * is2 + b3 * is3;
+        long long ci = i + (DIM == 0 ? (expand ? 0 : flen / 2) : 0);
+        long long cj = j + (DIM == 1 ? (expand ? 0 : flen / 2) : 0);
+        A acc = acc_zero<A>();
+        for (int f = 0; f < flen; ++f) {
+            long long ii = DIM == 0 ? ci - f : ci;
+            long long jj = DIM == 1 ? cj - f : cj;
+            T s{};
+            if (ii >= 0 && ii < id0 && jj >= 0 && jj < id1) s = src[ii * is0 + jj * is1];
+            if constexpr (IsInt<T>::value) {
+                T fv = from_acc<T>(filt[f]);
+                acc = __fadd_rn(acc, int_prod(s, fv));
+            } else {
+                acc = mac<EXACT>(acc, to_acc(s, A{}), filt[f]);
+            }
+        }
+        out[b2 * os2 + b3 * os3 + j * os1 + i] = from_acc_any(acc, T{});
+    }
+}
+
+// ---------------------------------------------------------------------------
+// casts and copies
+// ---------------------------------------------------------------------------
+template <typename F> __device__ __forceinline__ double real_of(F v) { return (double)v; }
+__device__ __forceinline__ double real_of(__half v) { return (double)__half2float(v); }
+__device__ __forceinline__ double mag_of(cf32 v) { return (double)hypotf(v.x, v.y); }
+__device__ __forceinline__ double mag_of(cf64 v) { return hypot(v.x, v.y); }
+
+template <typename F, typename To> struct CastOp {
+    __device__ static To run(F v) {
+        if constexpr (std::is_same<To, float>::value) {
+            if constexpr (std::is_same<F, __half>::value) return __half2float(v);
+            else return (float)v;
+        } else if constexpr (std::is_same<To, double>::value) {
+            if constexpr (std::is_same<F, __half>::value) return (double)__half2float(v);
+            else return (double)v;
+        } else if constexpr (std::is_same<To, cf32>::value) {
+            if constexpr (std::is_same<F, __half>::value) return cf32{__half2float(v), 0.f};
+            else return cf32{(float)v, 0.f};
+        } else {
+            if constexpr (std::is_same<F, __half>::value) return cf64{(double)__half2float(v), 0.0};
+            else return cf64{(double)v, 0.0};
+        }
+    }
+};
+template <typename To> struct CastOp<cf32, To> {
+    __device__ static To run(cf32 v) {
+        if constexpr (std::is_same<To, cf32>::value) return v;
+        else if constexpr (std::is_same<To, cf64>::value) return cf64{(double)v.x, (double)v.y};
+        else return (To)mag_of(v);
+    }
+};
+template <typename To> struct CastOp<cf64, To> {
+    __device__ static To run(cf64 v) {
+        if constexpr (std::is_same<To, cf64>::value) return v;
+        else if constexpr (std::is_same<To, cf32>::value) return cf32{(float)v.x, (float)v.y};
+        else return (To)mag_of(v);
+    }
+};
+
+template <typename F, typename To>
+__global__ void cast_kernel(const F *in, long long d0, long long d1, long long d2,
+                            long long s0, long long s1, long long s2, long long s3, To *out,
+                            long long total) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        long long i = t % d0, j = (t / d0) % d1, k = (t / (d0 * d1)) % d2, l = t / (d0 * d1 * d2);
+        out[t] = CastOp<F, To>::run(in[i * s0 + j * s1 + k * s2 + l * s3]);
+    }
+}
+
+template <int BYTES> struct Blob {
+    unsigned char b[BYTES];
+};
+template <int BYTES>
+__global__ void dense_copy_kernel(const Blob<BYTES> *in, long long d0, long long d1, long long d2,
+                                  long long s0, long long s1, long long s2, long long s3,
+                                  Blob<BYTES> *out, long long total) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        long long i = t % d0, j = (t / d0) % d1, k = (t / (d0 * d1)) % d2, l = t / (d0 * d1 * d2);
+        out[t] = in[i * s0 + j * s1 + k * s2 + l * s3];
+    }
+}
+
+template <typename T, typename A>
+__global__ void sep_scalar_kernel(const T *in, long long d0, long long d1, long long d2,
+                                  long long s0, long long s1, long long s2, long long s3,
+                                  const A *cf, const A *rf, T *out, long long total) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        long long i = t % d0, j = (t / d0) % d1, k = (t / (d0 * d1)) % d2, l = t / (d0 * d1 * d2);
+        A s = to_acc(in[i * s0 + j * s1 + k * s2 + l * s3], A{});
+        A f;
+        if constexpr (std::is_same<A, cf32>::value) {
+            cf32 c = cf[0], r = rf[0];
+            f = cf32{__fsub_rn(__fmul_rn(c.x, r.x), __fmul_rn(c.y, r.y)),
+                     __fadd_rn(__fmul_rn(c.x, r.y), __fmul_rn(c.y, r.x))};
+            A prod = cf32{__fsub_rn(__fmul_rn(s.x, f.x), __fmul_rn(s.y, f.y)),
+                          __fadd_rn(__fmul_rn(s.x, f.y), __fmul_rn(s.y, f.x))};
+            out[t] = prod;
+        } else if constexpr (std::is_same<A, cf64>::value) {
+            cf64 c = cf[0], r = rf[0];
+            f = cf64{__dsub_rn(__dmul_rn(c.x, r.x), __dmul_rn(c.y, r.y)),
+                     __dadd_rn(__dmul_rn(c.x, r.y), __dmul_rn(c.y, r.x))};
+            A prod = cf64{__dsub_rn(__dmul_rn(s.x, f.x), __dmul_rn(s.y, f.y)),
+                          __dadd_rn(__dmul_rn(s.x, f.y), __dmul_rn(s.y, f.x))};
+            out[t] = prod;
+        } else if constexpr (std::is_same<A, double>::value) {
+            out[t] = __dmul_rn(s, __dmul_rn(cf[0], rf[0]));
+        } else {
+            out[t] = from_acc_any(__fmul_rn(s, __fmul_rn(cf[0], rf[0])), T{});
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static unsigned grid_for(long long total, int threads) {
+    long long blocks = (total + threads - 1) / threads;
+    long long cap = (long long)num_sms() * 32;
+    if (blocks > cap) blocks = cap;
+    if (blocks < 1) blocks = 1;
+    return (unsigned)blocks;
+}
+
+#define AFGB_DISPATCH_ALL(dt, FN)                       \
+    switch (dt) {                                       \
+        case f32: FN(float); break;                     \
+        case f64: FN(double); break;                    \
+        case c32: FN(cf32); break;                      \
+        case c64: FN(cf64); break;                      \
+        case b8: FN(int8_t); break;                     \
+        case s8: FN(int8_t); break;                     \
+        case u8: FN(uint8_t); break;                    \
+        case s16: FN(int16_t); break;                   \
+        case u16: FN(uint16_t); break;                  \
+        case s32: FN(int32_t); break;                   \
+        case u32: FN(uint32_t); break;                  \
+        case s64: FN(long long); break;                 \
+        case u64: FN(unsigned long long); break;        \
+        default: AFGB_TYPE_ERROR(1, dt);                \
+    }
+
+static DirectParams make_params(const Array &sig, const Array &filt, Array &out, int kind,
+                                int rank, bool expand) {
+    DirectParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.sig = sig.data();
+    p.filt = filt.data();
+    p.out = out.data();
+    p.rank = rank;
+    p.expand = expand ? 1 : 0;
+    for (int i = 0; i < 4; ++i) {
+        p.sd[i] = sig.dims[i];
+        p.ss[i] = sig.strides[i];
+        p.od[i] = out.dims[i];
+        p.os[i] = out.strides[i];
+        p.fd[i] = filt.dims[i];
+        p.fs[i] = filt.strides[i];
+        p.batch[i] = 1;
+    }
+    // batch steps per kind (src/backend/cpu/kernel/convolve.hpp:160-180)
+    for (int i = 1; i < 4; ++i) {
+        switch (kind) {
+            case BATCH_LHS:
+                p.out_step[i] = out.strides[i];
+                p.in_step[i] = sig.strides[i];
+                if (i >= rank) p.batch[i] = sig.dims[i];
+                break;
+            case BATCH_SAME:
+                p.out_step[i] = out.strides[i];
+                p.in_step[i] = sig.strides[i];
+                p.filt_step[i] = filt.strides[i];
+                if (i >= rank) p.batch[i] = sig.dims[i];
+                break;
+            case BATCH_RHS:
+                p.out_step[i] = out.strides[i];
+                p.filt_step[i] = filt.strides[i];
+                if (i >= rank) p.batch[i] = filt.dims[i];
+                break;
+            default: break;
+        }
+    }
+    p.nbatch = p.batch[1] * p.batch[2] * p.batch[3];
+    return p;
+}
+
+template <typename T, int F0, int F1, bool EXACT>
+static void run_tile2(const DirectParams &p) {
+    dim3 grid((unsigned)((p.od[0] + T2_BX - 1) / T2_BX), (unsigned)((p.od[1] + T2_BY - 1) / T2_BY),
+              (unsigned)p.nbatch);
+    {
+        KernelTimer kt("conv2_tile_kernel");
+        conv2_tile_kernel<T, F0, F1, EXACT><<<grid, T2_THREADS, 0, stream()>>>(p);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("conv2_tile_kernel");
+}
+
+template <typename T, bool EXACT>
+static bool try_tile2(const DirectParams &p) {
+    const long long f0 = p.fd[0], f1 = p.fd[1];
+    if (p.nbatch > 65535) return false;
+    if (f0 == 3 && f1 == 3) { run_tile2<T, 3, 3, EXACT>(p); return true; }
+    if (f0 == 5 && f1 == 5) { run_tile2<T, 5, 5, EXACT>(p); return true; }
+    if (f0 == 7 && f1 == 7) { run_tile2<T, 7, 7, EXACT>(p); return true; }
+    return false;
+}
+
+template <typename T>
+static void run_generic(const DirectParams &p, bool exact) {
+    long long slice = p.od[0];
+    if (p.rank >= 2) slice *= p.od[1];
+    if (p.rank >= 3) slice *= p.od[2];
+    long long total = slice * p.nbatch;
+    if (total == 0) return;
+    unsigned g = grid_for(total, 256);
+    {
+        KernelTimer kt("conv_generic_kernel");
+        if (exact || IsInt<T>::value)
+            conv_generic_kernel<T, true><<<g, 256, 0, stream()>>>(p, slice);
+        else
+            conv_generic_kernel<T, false><<<g, 256, 0, stream()>>>(p, slice);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("conv_generic_kernel");
+}
+
+void launch_convolve_nd(const Array &sig, const Array &filt, Array &out, int kind, int rank,
+                        bool expand) {
+    if (out.elements() == 0) return;
+    DirectParams p = make_params(sig, filt, out, kind, rank, expand);
+    const bool exact = exact_fp();
+    if (rank == 2) {
+        bool done = false;
+        switch (sig.type) {
+            case f32: done = exact ? try_tile2<float, true>(p) : try_tile2<float, false>(p); break;
+            case u8: done = try_tile2<uint8_t, true>(p); break;
+            case s8:
+            case b8: done = try_tile2<int8_t, true>(p); break;
+            default: break;
+        }
+        if (done) return;
+    }
+#define AFGB_RUN_GENERIC(T) run_generic<T>(p, exact)
+    AFGB_DISPATCH_ALL(sig.type, AFGB_RUN_GENERIC);
+#undef AFGB_RUN_GENERIC
+}
+
+// ---- separable
+template <typename T, int CFL, int RFL, bool EXACT>
+static void run_sep_fused(const SepParams &p, long long nb) {
+    constexpr int CMAX = CFL ? CFL : 31;
+    constexpr int RMAX = RFL ? RFL : 31;
+    const int PITCH = ((SP_BX + CMAX - 1 + 3) / 4) * 4;
+    size_t smem = (size_t)(SP_BY + RMAX - 1) * PITCH * 4 + (size_t)(SP_BY + RMAX - 1) * SP_BX * 4;
+    auto kfn = sep_fused_kernel<T, CFL, RFL, EXACT>;
+    AFGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((unsigned)((p.od[0] + SP_BX - 1) / SP_BX), (unsigned)((p.od[1] + SP_BY - 1) / SP_BY),
+              (unsigned)nb);
+    {
+        KernelTimer kt("sep_fused_kernel");
+        kfn<<<grid, SP_THREADS, smem, stream()>>>(p);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("sep_fused_kernel");
+}
+
+template <typename T, bool EXACT>
+static void sep_fused_dispatch(const SepParams &p, long long nb) {
+    if (p.cflen == 15 && p.rflen == 15) run_sep_fused<T, 15, 15, EXACT>(p, nb);
+    else run_sep_fused<T, 0, 0, EXACT>(p, nb);
+}
+
+template <typename T>
+static void run_sep_generic(const Array &sig, const Array &cfilt, const Array &rfilt, Array &out,
+                            bool expand) {
+    using A = typename AccOf<T>::type;
+    const bool exact = exact_fp();
+    const long long cfl = cfilt.elements(), rfl = rfilt.elements();
+    const long long n2 = sig.dims[2], n3 = sig.dims[3];
+    long long tw = sig.dims[0] + (expand ? cfl - 1 : 0);
+    long long th = sig.dims[1];
+    size_t tbytes = (size_t)(tw * th * n2 * n3) * sizeof(T);
+    T *temp = static_cast<T *>(alloc_device(tbytes));
+    long long total1 = tw * th * n2 * n3;
+    long long total2 = out.elements();
+    const T *in = sig.ptr<T>();
+    const A *cf = cfilt.ptr<A>();
+    const A *rf = rfilt.ptr<A>();
+    if (total1 > 0) {
+        auto k0 = exact ? sep_pass_kernel<T, A, true, 0> : sep_pass_kernel<T, A, false, 0>;
+        k0<<<grid_for(total1, 256), 256, 0, stream()>>>(
+            in, sig.dims[0], sig.dims[1], sig.strides[0], sig.strides[1], sig.strides[2],
+            sig.strides[3], cf, (int)cfl, temp, tw, th, tw, tw * th, tw * th * n2, n2, n3,
+            expand ? 1 : 0);
+        count_launch();
+        AFGB_POST_LAUNCH("sep_pass_kernel<0>");
+    }
+    if (total2 > 0) {
+        auto k1 = exact ? sep_pass_kernel<T, A, true, 1> : sep_pass_kernel<T, A, false, 1>;
+        k1<<<grid_for(total2, 256), 256, 0, stream()>>>(
+            temp, tw, th, 1, tw, tw * th, tw * th * n2, rf, (int)rfl, out.ptr<T>(), out.dims[0],
+            out.dims[1], out.strides[1], out.strides[2], out.strides[3], n2, n3, expand ? 1 : 0);
+        count_launch();
+        AFGB_POST_LAUNCH("sep_pass_kernel<1>");
+    }
+    free_device(temp);
+}
+
+void launch_convolve2_sep(const Array &sig, const Array &cfilt, const Array &rfilt, Array &out,
+                          bool expand) {
+    if (out.elements() == 0) return;
+    const long long cfl = cfilt.elements(), rfl = rfilt.elements();
+    const long long nb = sig.dims[2] * sig.dims[3];
+    const af_dtype t = sig.type;
+    const bool fused_type = (t == f32 || t == u8 || t == s8 || t == b8);
+    if (fused_type && nb <= 65535 && cfl <= 31 && rfl <= 31) {
+        SepParams p;
+        std::memset(&p, 0, sizeof(p));
+        p.sig = sig.data();
+        p.cf = cfilt.ptr<float>();
+        p.rf = rfilt.ptr<float>();
+        p.out = out.data();
+        p.cflen = (int)cfl;
+        p.rflen = (int)rfl;
+        p.expand = expand ? 1 : 0;
+        for (int i = 0; i < 4; ++i) {
+            p.sd[i] = sig.dims[i];
+            p.ss[i] = sig.strides[i];
+            p.od[i] = out.dims[i];
+            p.os[i] = out.strides[i];
+        }
+        p.tw = sig.dims[0] + (expand ? cfl - 1 : 0);
+        // 8-bit inputs: taps become integers, every product and partial sum
+        // is an integer below 2^24, so fused multiply-add is exact
+        switch (t) {
+            case f32:
+                if (exact_fp()) sep_fused_dispatch<float, true>(p, nb);
+                else sep_fused_dispatch<float, false>(p, nb);
+                return;
+            case u8: sep_fused_dispatch<uint8_t, false>(p, nb); return;
+            default: sep_fused_dispatch<int8_t, false>(p, nb); return;
+        }
+    }
+#define AFGB_RUN_SEP(T) run_sep_generic<T>(sig, cfilt, rfilt, out, expand)
+    AFGB_DISPATCH_ALL(t, AFGB_RUN_SEP);
+#undef AFGB_RUN_SEP
+}
+
+// ---- casts
+template <typename F, typename To>
+static void run_cast(const Array &in, Array &out) {
+    long long total = in.elements();
+    if (!total) return;
+    cast_kernel<F, To><<<grid_for(total, 256), 256, 0, stream()>>>(
+        in.ptr<F>(), in.dims[0], in.dims[1], in.dims[2], in.strides[0], in.strides[1],
+        in.strides[2], in.strides[3], out.ptr<To>(), total);
+    count_launch();
+    AFGB_POST_LAUNCH("cast_kernel");
+}
+
+template <typename To>
+static void cast_from(const Array &in, Array &out) {
+    switch (in.type) {
+        case f32: run_cast<float, To>(in, out); break;
+        case f64: run_cast<double, To>(in, out); break;
+        case c32: run_cast<cf32, To>(in, out); break;
+        case c64: run_cast<cf64, To>(in, out); break;
+        case b8:
+        case s8: run_cast<int8_t, To>(in, out); break;
+        case u8: run_cast<uint8_t, To>(in, out); break;
+        case s16: run_cast<int16_t, To>(in, out); break;
+        case u16: run_cast<uint16_t, To>(in, out); break;
+        case s32: run_cast<int32_t, To>(in, out); break;
+        case u32: run_cast<uint32_t, To>(in, out); break;
+        case s64: run_cast<long long, To>(in, out); break;
+        case u64: run_cast<unsigned long long, To>(in, out); break;
+        case f16: run_cast<__half, To>(in, out); break;
+    }
+}
+
+Array make_dense(const Array &in) {
+    Array out = *create_array(in.type, in.dims);
+    long long total = in.elements();
+    if (!total) return out;
+    size_t es = dtype_size(in.type);
+#define AFGB_COPY(B)                                                                         \
+    dense_copy_kernel<B><<<grid_for(total, 256), 256, 0, stream()>>>(                        \
+        static_cast<const Blob<B> *>(in.data()), in.dims[0], in.dims[1], in.dims[2],         \
+        in.strides[0], in.strides[1], in.strides[2], in.strides[3],                          \
+        static_cast<Blob<B> *>(out.data()), total)
+    switch (es) {
+        case 1: AFGB_COPY(1); break;
+        case 2: AFGB_COPY(2); break;
+        case 4: AFGB_COPY(4); break;
+        case 8: AFGB_COPY(8); break;
+        default: AFGB_COPY(16); break;
+    }
+#undef AFGB_COPY
+    count_launch();
+    AFGB_POST_LAUNCH("dense_copy_kernel");
+    return out;
+}
+
+Array cast_array(const Array &in, af_dtype to) {
+    if (in.type == to) return in.is_linear() ? in : make_dense(in);
+    Array out = *create_array(to, in.dims);
+    switch (to) {
+        case f32: cast_from<float>(in, out); break;
+        case f64: cast_from<double>(in, out); break;
+        case c32: cast_from<cf32>(in, out); break;
+        case c64: cast_from<cf64>(in, out); break;
+        default: AFGB_TYPE_ERROR(1, to);
+    }
+    return out;
+}
+
+void launch_sep_scalar(const Array &sig, const Array &cfilt, const Array &rfilt, Array &out) {
+    long long total = sig.elements();
+    if (!total) return;
+#define AFGB_SCALAR(T)                                                                          \
+    {                                                                                           \
+        using A = typename AccOf<T>::type;                                                      \
+        sep_scalar_kernel<T, A><<<grid_for(total, 256), 256, 0, stream()>>>(                    \
+            sig.ptr<T>(), sig.dims[0], sig.dims[1], sig.dims[2], sig.strides[0], sig.strides[1], \
+            sig.strides[2], sig.strides[3], cfilt.ptr<A>(), rfilt.ptr<A>(), out.ptr<T>(), total); \
+    }
+    AFGB_DISPATCH_ALL(sig.type, AFGB_SCALAR);
+#undef AFGB_SCALAR
+    count_launch();
+    AFGB_POST_LAUNCH("sep_scalar_kernel");
+}
+
+}  // namespace afgb

@@ -1,0 +1,32 @@
+// Launch interface of the direct (small-filter) convolution kernels.
+#pragma once
+
+#include "afgb_internal.hpp"
+
+namespace afgb {
+
+// One direct convolution of rank 1..3 over every batch slice, in one launch.
+// `filt` has already been cast to the accumulator type of `sig`.
+// Semantics: src/backend/cpu/kernel/convolve.hpp:19-211 (convolve_nd).
+void launch_convolve_nd(const Array &sig, const Array &filt, Array &out, int kind, int rank,
+                        bool expand);
+
+// Separable 2-D convolution (column filter along dim0, then row filter along
+// dim1) over every d2*d3 slice.  Filters are contiguous accumulator-typed
+// vectors.  Semantics: src/backend/cpu/kernel/convolve.hpp:213-289.
+void launch_convolve2_sep(const Array &sig, const Array &cfilt, const Array &rfilt, Array &out,
+                          bool expand);
+
+// Element-wise dtype conversion into a new dense array (castArray,
+// src/api/c/handle.hpp:46; complex -> real takes the magnitude as in
+// src/backend/cpu/cast.hpp:75-121).
+Array cast_array(const Array &in, af_dtype to);
+
+// Dense copy of a strided array (same dtype).
+Array make_dense(const Array &in);
+
+// out = T( s * (c * r) ) element-wise: the scalar-filter shortcut of
+// af_convolve2_sep (src/api/c/convolve.cpp:57-68).
+void launch_sep_scalar(const Array &sig, const Array &cfilt, const Array &rfilt, Array &out);
+
+}  // namespace afgb

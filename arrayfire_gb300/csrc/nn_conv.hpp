@@ -1,0 +1,49 @@
+// Launch interface of the NN convolution (af_convolve2_nn and its
+// gradients).  Layout is ArrayFire's: signal (W,H,C,N), filter (fw,fh,C,K),
+// output (Wo,Ho,K,N), all column-major with dim 0 fastest.
+#pragma once
+
+#include "afgb_internal.hpp"
+
+namespace afgb {
+
+struct NNGeom {
+    long long W, H, C, N;
+    long long fw, fh, K;
+    long long sx, sy, px, py, dx, dy;
+    long long Wo, Ho;
+};
+
+// out[x,y,k,n] = sum_{c,u,v} in[x*sx-px+u*dx, y*sy-py+v*dy, c, n] *
+//                w[fw-1-u, fh-1-v, c, k]   (src/backend/cpu/convolve.cpp:123-158)
+void nn_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out,
+                afgb_precision prec, const Array *scales);
+// dX = col2im(G * flip(W)^T)   (src/backend/cpu/convolve.cpp:179-211)
+void nn_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &dx,
+                  afgb_precision prec);
+// dW = flip(im2col(X)^T * G)   (src/backend/cpu/convolve.cpp:213-243)
+void nn_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw,
+                    afgb_precision prec);
+// db[k] = sum_{x,y,n} g[x,y,k,n]  (no reference counterpart: the reference
+// returns the data gradient for AF_CONV_GRADIENT_BIAS, src/api/c/convolve.cpp:401-411)
+void nn_bias_grad(const NNGeom &g, const Array &grad, Array &db);
+
+// ---- plain CUDA-core implementations (nn_simt.cu)
+void simt_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out);
+void simt_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &dx);
+void simt_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw);
+
+// ---- tensor-core implementations (nn_tc.cu); return false when the shape
+// is outside what the tcgen05 kernels cover (the caller then reports
+// AF_ERR_NOT_SUPPORTED; there is no silent fallback to another precision)
+bool tc_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out,
+                afgb_precision prec, const Array *scales);
+bool tc_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &dx);
+bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw);
+
+// deterministic compensated reduction of `splits` fp32 partial matrices of
+// `rows x cols` into `out` (pairwise tree over splits with TwoSum carries)
+void reduce_partials(const float *partials, int splits, long long rows, long long cols,
+                     float *out);
+
+}  // namespace afgb

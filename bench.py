@@ -1,0 +1,523 @@
+"""Benchmark of the spatial-convolution hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--precision bf16|fp32] [--no-secondary]
+
+Headline (`value`): af_convolve2_nn forward + data gradient + filter
+gradient TFLOP/s on the 128x128x64x32 signal / 3x3x64x128 filter workload
+(stride 1, padding 1, dilation 1; 3 x 77.31 GFLOP per step), inputs resident
+in HBM, each step one pass of forward and both gradients.  Inputs are
+seeded synthetic N(0,1) / He-normal arrays (no dataset).  Timing: CUDA events
+on the launching stream around each step; between steps a 512 MB buffer is
+written to flush the 126 MB L2.
+
+`secondary` reports the bandwidth-bound direct convolutions (64 images of
+2048x2048 with the 15-tap separable filter in f32 and u8, 64 distinct 7x7
+filters in SAME batch mode, a 256^3 volume with a 3x3x3 filter) as HBM GB/s
+against the measured copy bandwidth.
+
+`e2e` is the same headline metric through the C ABI with host buffers:
+af_create_array from pinned host memory, the three calls, af_get_data_ptr
+back to host, all inside the timed region.
+
+`--impl reference` times the reference's CPU algorithm for the same metric
+(the oracle's C restatement of unwrap/wrap plus the BLAS sgemm bundled with
+numpy, as the reference CPU backend's unwrap + CBLAS path) on a bounded
+sample, with all host threads the BLAS can use.
+
+Multi-GPU: the path does not shard (replicas only): each rank runs the same
+workload on its own GPU; `value` sums the ranks' work over the slowest rank's
+time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = ("conv2_nn fwd+bwd TFLOP/s BF16-TC vs FP32 (rel err≤2e-2); convolve2 HBM GB/s")
+NN_SHAPE = dict(W=128, H=128, C=64, N=32, fw=3, fh=3, K=128, stride=(1, 1), pad=(1, 1), dil=(1, 1))
+
+
+def nn_flops(s=NN_SHAPE) -> float:
+    Wo = 1 + (s["W"] + 2 * s["pad"][0] - ((s["fw"] - 1) * s["dil"][0] + 1)) // s["stride"][0]
+    Ho = 1 + (s["H"] + 2 * s["pad"][1] - ((s["fh"] - 1) * s["dil"][1] + 1)) // s["stride"][1]
+    return 2.0 * Wo * Ho * s["N"] * s["K"] * s["fw"] * s["fh"] * s["C"]
+
+
+def load_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "bf16_tflops": d["bf16_tflops"],
+                "bf16_tflops_sustained": d.get("bf16_tflops_sustained", d["bf16_tflops"]),
+                "source": "measured"}
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
+            "source": "fallback"}
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines: list[str] = []
+        self._t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except FileNotFoundError:
+            self.proc = None
+            return
+        self._t = threading.Thread(target=self._read, daemon=True)
+        self._t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self._t:
+            self._t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# our implementation
+# ---------------------------------------------------------------------------
+def _timed_steps(step_fn, steps: int, warmup: int, flush) -> tuple[float, list[float]]:
+    import torch
+
+    for _ in range(warmup):
+        step_fn()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        flush()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        step_fn()
+        b.record()
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+    return sum(times), times
+
+
+def run_ours(args, peaks, rank: int, world: int) -> dict:
+    import torch
+
+    import arrayfire_gb300 as af
+
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    af.set_stream(torch.cuda.current_stream())
+    L = af.lib()
+    s = NN_SHAPE
+    g = np.random.Generator(np.random.Philox(1234 + rank))
+    X = np.asfortranarray(g.standard_normal((s["W"], s["H"], s["C"], s["N"]), dtype=np.float32))
+    std = np.sqrt(2.0 / (s["fw"] * s["fh"] * s["C"]))
+    Wt = np.asfortranarray((g.standard_normal((s["fw"], s["fh"], s["C"], s["K"])) * std
+                            ).astype(np.float32))
+    Xa, Wa = af.Array.from_numpy(X), af.Array.from_numpy(Wt)
+    st, pd, dl = s["stride"], s["pad"], s["dil"]
+    prec = args.precision
+    try:
+        Y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
+    except af.AfError as e:
+        if prec == "fp32" or e.code != af.AF_ERR_NOT_SUPPORTED:
+            raise
+        prec = "fp32"
+        Y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
+    Gd = np.asfortranarray(g.standard_normal(Y.dims, dtype=np.float32))
+    Ga = af.Array.from_numpy(Gd)
+    flush_buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def flush():
+        flush_buf.zero_()
+
+    def step():
+        y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
+        dx = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_DATA,
+                                      precision=prec)
+        dw = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_FILTER,
+                                      precision=prec)
+        return y, dx, dw
+
+    # parity of this exact workload against FP64 on sampled points
+    y, dx, dw = step()
+    import oracle.oracle as O  # checker only
+
+    idx = g.integers(0, int(np.prod(Y.dims)), 256)
+    ref = O.nn_forward_points_f64(X, Wt, st, pd, dl, idx)
+    got = y.to_numpy().ravel(order="F")[idx].astype(np.float64)
+    rel_fwd = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+    maxabs_fwd = float(np.abs(got - ref).max())
+    idx2 = g.integers(0, X.size, 128)
+    ref2 = O.nn_data_grad_points_f64(Gd, list(X.shape), Wt, st, pd, dl, idx2)
+    got2 = dx.to_numpy().ravel(order="F")[idx2].astype(np.float64)
+    rel_dx = float(np.linalg.norm(got2 - ref2) / np.linalg.norm(ref2))
+    idx3 = g.integers(0, Wt.size, 64)
+    ref3 = O.nn_filter_grad_points_f64(Gd, X, list(Wt.shape), st, pd, dl, idx3)
+    got3 = dw.to_numpy().ravel(order="F")[idx3].astype(np.float64)
+    rel_dw = float(np.linalg.norm(got3 - ref3) / np.linalg.norm(ref3))
+    del y, dx, dw
+
+    L.afgb_kernel_timing(1)
+    launches0 = af.launch_count()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    torch.cuda.synchronize()
+    clock = ClockSampler(dev)
+    clock.start()
+    total_ms, times = _timed_steps(step, args.steps, args.warmup, flush)
+    clocks = clock.stop()
+    launches = af.launch_count() - launches0
+    torch.cuda.synchronize()
+
+    # dominant kernel timing (events around each launch, same stream)
+    import ctypes
+
+    kt = {}
+    for name in ("simt_fwd_kernel", "simt_dgrad_kernel", "simt_wgrad_kernel", "tc_fwd_kernel",
+                 "tc_dgrad_kernel", "tc_wgrad_kernel"):
+        c = ctypes.c_ulonglong()
+        ms = ctypes.c_double()
+        L.afgb_kernel_time(name.encode(), ctypes.byref(c), ctypes.byref(ms))
+        if c.value:
+            kt[name] = (c.value, ms.value)
+    L.afgb_kernel_timing(0)
+    flops = nn_flops()
+    steps_total = args.warmup + args.steps
+    value = 3 * flops * args.steps / (total_ms / 1e3) / 1e12
+
+    dom = max(kt.items(), key=lambda kv: kv[1][1]) if kt else None
+    roofline = None
+    if dom:
+        name, (cnt, ms) = dom
+        avg_s = ms / cnt / 1e3
+        achieved = flops / avg_s / 1e12
+        peak = peaks["bf16_tflops"]
+        roofline = {"bound": "tensor", "kernel": name, "achieved": round(achieved, 2),
+                    "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+                    "peak_source": peaks["source"] + " bf16 dense", "traffic": None,
+                    "launches": cnt, "avg_ms": round(ms / cnt, 4)}
+
+    # e2e through the C ABI with pinned host buffers
+    e2e = run_e2e(af, X, Wt, Gd, prec, args)
+
+    res = {
+        "value": value, "ms_per_step": total_ms / args.steps, "precision": prec,
+        "errors_vs_fp64": {"fwd_rel": rel_fwd, "fwd_maxabs": maxabs_fwd, "dgrad_rel": rel_dx,
+                           "wgrad_rel": rel_dw, "points": [256, 128, 64]},
+        "kernel_times_ms": {k: round(v[1] / v[0], 4) for k, v in kt.items()},
+        "roofline": roofline, "clocks": clocks, "e2e": e2e,
+        "gpu_launches": int(launches), "step_times_ms": [round(t, 4) for t in times],
+    }
+    if not args.no_secondary:
+        res["secondary"] = run_direct_workloads(af, peaks, args)
+    return res
+
+
+def run_e2e(af, X, Wt, Gd, prec, args) -> dict:
+    import ctypes
+
+    import torch
+
+    L = af.lib()
+    s = NN_SHAPE
+    st, pd, dl = s["stride"], s["pad"], s["dil"]
+    pin = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).pin_memory()
+           for k, v in (("x", X), ("w", Wt), ("g", Gd))}
+    Wo, Ho = X.shape[0], X.shape[1]
+    y_host = torch.empty(Wo * Ho * s["K"] * s["N"], dtype=torch.float32).pin_memory()
+    dx_host = torch.empty(X.size, dtype=torch.float32).pin_memory()
+    dw_host = torch.empty(Wt.size, dtype=torch.float32).pin_memory()
+
+    def mk(t, dims):
+        out = ctypes.c_void_p()
+        d = (ctypes.c_longlong * 4)(*dims)
+        af._check(L.af_create_array(ctypes.byref(out), ctypes.c_void_p(t.data_ptr()), 4, d, af.f32))
+        return af.Array(out.value)
+
+    def step():
+        Xa = mk(pin["x"], X.shape)
+        Wa = mk(pin["w"], Wt.shape)
+        Ga = mk(pin["g"], Gd.shape)
+        y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
+        dx = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_DATA,
+                                      precision=prec)
+        dw = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_FILTER,
+                                      precision=prec)
+        af._check(L.af_get_data_ptr(ctypes.c_void_p(y_host.data_ptr()), y.handle))
+        af._check(L.af_get_data_ptr(ctypes.c_void_p(dx_host.data_ptr()), dx.handle))
+        af._check(L.af_get_data_ptr(ctypes.c_void_p(dw_host.data_ptr()), dw.handle))
+
+    for _ in range(max(1, args.warmup)):
+        step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    h2d = (X.size + Wt.size + Gd.size) * 4
+    d2h = (y_host.numel() + dx_host.numel() + dw_host.numel()) * 4
+    return {"value": 3 * nn_flops() * args.steps / dt / 1e12, "unit": "TFLOP/s",
+            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": dt * 1e3 / args.steps}
+
+
+def run_direct_workloads(af, peaks, args) -> dict:
+    """Bandwidth-bound direct convolutions (configuration 2), GB/s of
+    algorithmic traffic (each input and output counted once)."""
+    import ctypes
+
+    import torch
+
+    L = af.lib()
+    g = np.random.Generator(np.random.Philox(77))
+    flush_buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = {}
+
+    def measure(name, fn, nbytes, kernel):
+        for _ in range(3):
+            r = fn()
+        del r
+        torch.cuda.synchronize()
+        L.afgb_kernel_timing(1)
+        tot = 0.0
+        steps = max(3, min(args.steps, 10))
+        for _ in range(steps):
+            flush_buf.zero_()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            r = fn()
+            b.record()
+            b.synchronize()
+            tot += a.elapsed_time(b)
+            del r
+        c = ctypes.c_ulonglong()
+        ms = ctypes.c_double()
+        L.afgb_kernel_time(kernel.encode(), ctypes.byref(c), ctypes.byref(ms))
+        L.afgb_kernel_timing(0)
+        call_ms = tot / steps
+        k_ms = ms.value / c.value if c.value else None
+        gbs = nbytes / (call_ms / 1e3) / 1e9
+        kgbs = nbytes / (k_ms / 1e3) / 1e9 if k_ms else None
+        out[name] = {"ms": round(call_ms, 4), "GB/s": round(gbs, 1),
+                     "kernel": kernel, "kernel_ms": round(k_ms, 4) if k_ms else None,
+                     "kernel_GB/s": round(kgbs, 1) if kgbs else None,
+                     "frac_of_hbm": round((kgbs or gbs) / peaks["hbm_gbs"], 4),
+                     "bytes": int(nbytes)}
+
+    # 64 x 2048 x 2048 separable 15-tap, f32 and u8, LHS batch
+    t = g.standard_normal(15)
+    cf = (t / t.sum()).astype(np.float32)
+    t = g.standard_normal(15)
+    rf = (t / t.sum()).astype(np.float32)
+    CF, RF = af.Array.from_numpy(cf), af.Array.from_numpy(rf)
+    xs = torch.rand(64, 2048, 2048, device="cuda")
+    S = af.Array.view_torch(xs)
+    n = xs.numel()
+    measure("sep15_f32_64x2048x2048", lambda: af.convolve2_separable(CF, RF, S), n * 8 + 120,
+            "sep_fused_kernel")
+    xu = torch.randint(0, 256, (64, 2048, 2048), dtype=torch.uint8, device="cuda")
+    SU = af.Array.view_torch(xu)
+    measure("sep15_u8_64x2048x2048", lambda: af.convolve2_separable(CF, RF, SU), n * 2 + 120,
+            "sep_fused_kernel")
+    del SU, xu
+    # SAME batch, 64 distinct 7x7 filters (AF_CONV_SPATIAL: AUTO would pick FFT)
+    f7 = g.standard_normal((7, 7, 64))
+    f7 = (f7 / f7.sum(axis=(0, 1), keepdims=True)).astype(np.float32)
+    F7 = af.Array.from_numpy(np.asfortranarray(f7))
+    measure("same7x7_f32_64x2048x2048",
+            lambda: af.convolve2(S, F7, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL),
+            n * 8 + f7.size * 4, "conv2_tile_kernel")
+    del S, xs
+    # 256^3 volume, 3x3x3
+    v = torch.rand(256, 256, 256, device="cuda")
+    V = af.Array.view_torch(v)
+    k3 = g.standard_normal((3, 3, 3))
+    F3 = af.Array.from_numpy(np.asfortranarray((k3 / k3.sum()).astype(np.float32)))
+    measure("conv3_3x3x3_f32_256^3_default",
+            lambda: af.convolve3(V, F3, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL),
+            v.numel() * 8 + 108, "conv_generic_kernel")
+    measure("conv3_3x3x3_f32_256^3_expand",
+            lambda: af.convolve3(V, F3, af.AF_CONV_EXPAND, af.AF_CONV_SPATIAL),
+            v.numel() * 4 + 258 ** 3 * 4 + 108, "conv_generic_kernel")
+    return out
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference's algorithm on the host cores
+# ---------------------------------------------------------------------------
+def cpu_nn_sample(seconds_budget: float = 20.0) -> dict:
+    """Forward + both gradients of the headline workload for a subset of the
+    batch (images of the same 128x128x64 shape), timed on the host:
+    oracle unwrap/wrap (C restatement of the reference CPU kernels) + numpy's
+    BLAS sgemm in place of CBLAS (src/backend/cpu/convolve.cpp:123-243)."""
+    import oracle.oracle as O
+
+    s = NN_SHAPE
+    st, pd, dl = s["stride"], s["pad"], s["dil"]
+    g = np.random.Generator(np.random.Philox(99))
+    nimg = 1
+    X = np.asfortranarray(g.standard_normal((s["W"], s["H"], s["C"], nimg), dtype=np.float32))
+    Wt = np.asfortranarray((g.standard_normal((s["fw"], s["fh"], s["C"], s["K"])) * 0.06
+                            ).astype(np.float32))
+    Gd = np.asfortranarray(g.standard_normal((s["W"], s["H"], s["K"], nimg), dtype=np.float32))
+    fd = Wt.shape
+    wsz = fd[0] * fd[1]
+
+    def one():
+        y = O.nn_forward_unwrap_gemm_f32(X, Wt, st, pd, dl)
+        cols = O.unwrap(X, fd[0], fd[1], st[0], st[1], pd[0], pd[1], dl[0], dl[1])
+        npix = cols.shape[1]
+        A = np.ascontiguousarray(cols.transpose(1, 3, 2, 0)).reshape(npix * nimg, s["C"] * wsz)
+        G2 = np.asfortranarray(Gd).reshape(npix, s["K"], nimg, order="F").transpose(2, 0, 1
+                                                                                     ).reshape(-1, s["K"])
+        wflip = Wt[::-1, ::-1, :, :]
+        B = np.ascontiguousarray(wflip.reshape(wsz, s["C"], s["K"], order="F").transpose(1, 0, 2)
+                                 ).reshape(s["C"] * wsz, s["K"])
+        dw = A.T @ G2
+        colsg = (G2 @ B.T).reshape(nimg, npix, s["C"], wsz).transpose(3, 1, 2, 0)
+        dx = O.wrap_dilated(np.asfortranarray(colsg), list(X.shape), fd[0], fd[1], st[0], st[1],
+                            pd[0], pd[1], dl[0], dl[1])
+        return y, dx, dw
+
+    one()
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        one()
+        reps += 1
+        if time.perf_counter() - t0 > seconds_budget or reps >= 20:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    flops = 3 * nn_flops() * nimg / s["N"]
+    return {"value": flops / dt / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
+            "kind": "port",
+            "sample": f"{nimg} of {s['N']} images per step (fwd+dgrad+wgrad), {reps} reps; "
+                      "oracle unwrap/wrap + numpy BLAS sgemm",
+            "seconds_per_step": dt}
+
+
+# ---------------------------------------------------------------------------
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32", "fp8"])
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    peaks = load_peaks()
+    config = {"workload": "conv2_nn fwd+dgrad+wgrad, signal 128x128x64x32 (W,H,C,N), filter "
+                          "3x3x64x128, stride 1, pad 1, dilation 1",
+              "global_batch": NN_SHAPE["N"] * world, "flops_per_step": 3 * nn_flops() * world,
+              "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cpu = cpu_nn_sample(args.cpu_seconds)
+        line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": "TFLOP/s",
+                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": cpu["seconds_per_step"] * 1e3 * NN_SHAPE["N"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32", "data": "synthetic", "config": config,
+                "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cpu["value"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    res = run_ours(args, peaks, rank, world)
+    value = res["value"]
+    ms = res["ms_per_step"]
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        value = 3 * nn_flops() * world / (ms / 1e3) / 1e12
+    if rank != 0:
+        return
+    cpu = cpu_nn_sample(args.cpu_seconds)
+    line = {
+        "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16" if res["precision"] == "bf16" else
+        ("fp8_e4m3" if res["precision"] == "fp8" else "f32"),
+        "data": "synthetic (seeded Philox N(0,1) signal, He-normal filter)", "config": config,
+        "roofline": res["roofline"], "cpu_baseline": {k: cpu[k] for k in
+                                                      ("value", "unit", "cores", "kind", "sample")},
+        "e2e": res["e2e"], "clocks": res["clocks"], "gpu_launches": res["gpu_launches"],
+        "errors_vs_fp64": res["errors_vs_fp64"], "kernel_times_ms": res["kernel_times_ms"],
+        "secondary": res.get("secondary"), "peaks": peaks,
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

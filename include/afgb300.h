@@ -1,0 +1,238 @@
+/*
+ * afgb300.h — C ABI of the GB300-native spatial-convolution backend.
+ *
+ * This library is a drop-in for ArrayFire v3.10's convolution entry points
+ * on one GPU (sm_103a).  Every `af_*` symbol below has the same name,
+ * signature, argument meaning and error codes as the ArrayFire declaration
+ * cited beside it (paths are within the ArrayFire source tree).  The
+ * `afgb_*` symbols are extensions with no ArrayFire counterpart; each says
+ * what it adds.
+ *
+ * Data layout: arrays are column-major 4-D (d0 fastest), exactly as
+ * ArrayFire's `af::dim4` + strides.  All compute runs on the library's
+ * current CUDA stream (see afgb_set_stream); calls are asynchronous with
+ * respect to the host, as in ArrayFire's CUDA backend, and af_get_data_ptr /
+ * af_sync synchronise.
+ */
+#ifndef AFGB300_H
+#define AFGB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define AFGB_API __attribute__((visibility("default")))
+#else
+#define AFGB_API
+#endif
+
+/* ---- types (include/af/defines.h) ------------------------------------ */
+
+typedef long long dim_t;  /* include/af/defines.h:50 (64-bit dim_t) */
+typedef void *af_array;   /* include/af/defines.h:243 */
+
+/* include/af/defines.h:75-202 — numeric values identical */
+typedef enum {
+    AF_SUCCESS = 0,
+    AF_ERR_NO_MEM = 101,
+    AF_ERR_DRIVER = 102,
+    AF_ERR_RUNTIME = 103,
+    AF_ERR_INVALID_ARRAY = 201,
+    AF_ERR_ARG = 202,
+    AF_ERR_SIZE = 203,
+    AF_ERR_TYPE = 204,
+    AF_ERR_DIFF_TYPE = 205,
+    AF_ERR_BATCH = 207,
+    AF_ERR_DEVICE = 208,
+    AF_ERR_NOT_SUPPORTED = 301,
+    AF_ERR_NOT_CONFIGURED = 302,
+    AF_ERR_NONFREE = 303,
+    AF_ERR_NO_DBL = 401,
+    AF_ERR_NO_GFX = 402,
+    AF_ERR_NO_HALF = 403,
+    AF_ERR_LOAD_LIB = 501,
+    AF_ERR_LOAD_SYM = 502,
+    AF_ERR_ARR_BKND_MISMATCH = 503,
+    AF_ERR_INTERNAL = 998,
+    AF_ERR_UNKNOWN = 999
+} af_err;
+
+/* include/af/defines.h:211-233 — same order, same values */
+typedef enum {
+    f32 = 0, c32, f64, c64, b8, s32, u32, u8, s64, u64, s16, u16, f16, s8
+} af_dtype;
+
+/* include/af/defines.h:306-314 */
+typedef enum { AF_CONV_DEFAULT = 0, AF_CONV_EXPAND = 1 } af_conv_mode;
+
+/* include/af/defines.h:316-320 */
+typedef enum { AF_CONV_AUTO = 0, AF_CONV_SPATIAL = 1, AF_CONV_FREQ = 2 } af_conv_domain;
+
+/* include/af/defines.h:545-550 */
+typedef enum {
+    AF_CONV_GRADIENT_DEFAULT = 0,
+    AF_CONV_GRADIENT_FILTER = 1,
+    AF_CONV_GRADIENT_DATA = 2,
+    AF_CONV_GRADIENT_BIAS = 3
+} af_conv_gradient_type;
+
+/* ---- array lifecycle (the subset the convolution path needs) -------- */
+
+/* include/af/array.h:1657 — copies host data to a new device array */
+AFGB_API af_err af_create_array(af_array *arr, const void *const data, const unsigned ndims,
+                                const dim_t *const dims, const af_dtype type);
+/* include/af/array.h:1672 — uninitialised device array */
+AFGB_API af_err af_create_handle(af_array *arr, const unsigned ndims, const dim_t *const dims,
+                                 const af_dtype type);
+/* include/af/device.h:453 — adopts a cudaMalloc'd pointer; freed with the array */
+AFGB_API af_err af_device_array(af_array *arr, void *data, const unsigned ndims,
+                                const dim_t *const dims, const af_dtype type);
+/* include/af/array.h:1689 — device-to-host copy; synchronises */
+AFGB_API af_err af_get_data_ptr(void *data, const af_array arr);
+/* include/af/device.h:576 */
+AFGB_API af_err af_get_device_ptr(void **ptr, const af_array arr);
+/* include/af/array.h:1696 */
+AFGB_API af_err af_release_array(af_array arr);
+/* include/af/array.h:1701 — new handle sharing the same buffer */
+AFGB_API af_err af_retain_array(af_array *out, const af_array in);
+/* include/af/array.h:1744 */
+AFGB_API af_err af_get_elements(dim_t *elems, const af_array arr);
+/* include/af/array.h:1754 */
+AFGB_API af_err af_get_type(af_dtype *type, const af_array arr);
+/* include/af/array.h:1767 */
+AFGB_API af_err af_get_dims(dim_t *d0, dim_t *d1, dim_t *d2, dim_t *d3, const af_array arr);
+/* include/af/array.h:1778 */
+AFGB_API af_err af_get_numdims(unsigned *result, const af_array arr);
+/* include/af/internal.h:134 */
+AFGB_API af_err af_get_strides(dim_t *s0, dim_t *s1, dim_t *s2, dim_t *s3, const af_array arr);
+/* include/af/device.h:354 — waits for all work queued by this library */
+AFGB_API af_err af_sync(const int device);
+/* include/af/device.h:446 — frees strings returned by af_get_last_error */
+AFGB_API af_err af_free_host(void *ptr);
+/* include/af/exception.h:65 — thread-local message of the last failure */
+AFGB_API void af_get_last_error(char **msg, dim_t *len);
+/* include/af/exception.h:70 */
+AFGB_API const char *af_err_to_string(const af_err err);
+
+/* ---- the convolution hot path --------------------------------------- */
+
+/* include/af/signal.h:1391 (dispatcher src/api/c/convolve.cpp:217-226) */
+AFGB_API af_err af_convolve1(af_array *out, const af_array signal, const af_array filter,
+                             const af_conv_mode mode, af_conv_domain domain);
+/* include/af/signal.h:1408 (src/api/c/convolve.cpp:228-241) */
+AFGB_API af_err af_convolve2(af_array *out, const af_array signal, const af_array filter,
+                             const af_conv_mode mode, af_conv_domain domain);
+/* include/af/signal.h:1460 (src/api/c/convolve.cpp:243-256) */
+AFGB_API af_err af_convolve3(af_array *out, const af_array signal, const af_array filter,
+                             const af_conv_mode mode, af_conv_domain domain);
+/* include/af/signal.h:1478 (src/api/c/convolve.cpp:258-334) */
+AFGB_API af_err af_convolve2_sep(af_array *out, const af_array col_filter,
+                                 const af_array row_filter, const af_array signal,
+                                 const af_conv_mode mode);
+/* include/af/signal.h:1440 (src/api/c/convolve.cpp:344-392) */
+AFGB_API af_err af_convolve2_nn(af_array *out, const af_array signal, const af_array filter,
+                                const unsigned stride_dims, const dim_t *strides,
+                                const unsigned padding_dims, const dim_t *paddings,
+                                const unsigned dilation_dims, const dim_t *dilations);
+/* include/af/ml.h:84-92 (src/api/c/convolve.cpp:414-477).  As in the
+ * reference, every grad_type other than AF_CONV_GRADIENT_FILTER returns the
+ * data gradient; the real bias gradient is afgb_convolve2_gradient_nn_ex. */
+AFGB_API af_err af_convolve2_gradient_nn(af_array *out, const af_array incoming_gradient,
+                                         const af_array original_signal,
+                                         const af_array original_filter,
+                                         const af_array convolved_output,
+                                         const unsigned stride_dims, const dim_t *strides,
+                                         const unsigned padding_dims, const dim_t *paddings,
+                                         const unsigned dilation_dims, const dim_t *dilations,
+                                         af_conv_gradient_type grad_type);
+
+/* ---- extensions (no ArrayFire counterpart) -------------------------- */
+
+/* Arithmetic form of the NN convolution.  FP32 is the plain CUDA-core path
+ * (the af_* entry points always use it).  BF16 and FP8_E4M3 run on the
+ * tcgen05 tensor cores with FP32 accumulation; inputs and outputs stay f32
+ * af_arrays, conversion happens on the device. */
+typedef enum {
+    AFGB_PRECISION_FP32 = 0,
+    AFGB_PRECISION_BF16 = 1,
+    AFGB_PRECISION_FP8_E4M3 = 2
+} afgb_precision;
+
+/* af_convolve2_nn with a precision knob.  For FP8_E4M3, `out_channel_scales`
+ * (f32, K elements, may be 0) holds one dequantisation scale per output
+ * channel: the filter of channel k is quantised as w/scale[k] and the
+ * accumulator is multiplied back by scale[k].  When 0, the scales are derived
+ * on the device as amax(|w[...,k]|)/448. */
+AFGB_API af_err afgb_convolve2_nn_ex(af_array *out, const af_array signal, const af_array filter,
+                                     const unsigned stride_dims, const dim_t *strides,
+                                     const unsigned padding_dims, const dim_t *paddings,
+                                     const unsigned dilation_dims, const dim_t *dilations,
+                                     afgb_precision precision, const af_array out_channel_scales);
+
+/* af_convolve2_gradient_nn with a precision knob and a real bias gradient:
+ * AF_CONV_GRADIENT_BIAS returns db[k] = sum_{x,y,n} g[x,y,k,n] as a
+ * 1x1xKx1 array (FP32 compensated pairwise sum in a fixed order). */
+AFGB_API af_err afgb_convolve2_gradient_nn_ex(
+    af_array *out, const af_array incoming_gradient, const af_array original_signal,
+    const af_array original_filter, const af_array convolved_output, const unsigned stride_dims,
+    const dim_t *strides, const unsigned padding_dims, const dim_t *paddings,
+    const unsigned dilation_dims, const dim_t *dilations, af_conv_gradient_type grad_type,
+    afgb_precision precision);
+
+/* Non-owning view of device memory with explicit strides (elements).  The
+ * caller keeps ownership; releasing the view never frees `data`.  This is
+ * how a framework tensor enters the library without a copy. */
+AFGB_API af_err afgb_device_array_view(af_array *arr, void *data, const unsigned ndims,
+                                       const dim_t *const dims, const dim_t *const strides,
+                                       const af_dtype type);
+
+/* Route all subsequent work of the calling process to `stream`
+ * (a cudaStream_t; 0 restores the library's own non-blocking stream). */
+AFGB_API af_err afgb_set_stream(void *stream);
+AFGB_API af_err afgb_get_stream(void **stream);
+
+/* f32/f64/c32/c64 direct convolutions: 0 (default) lets the compiler fuse
+ * multiply-add (results within a stated tolerance of the reference); 1
+ * evaluates every product and sum separately in the reference's loop order,
+ * which reproduces the reference CPU backend bit for bit.  Integer inputs
+ * always use the exact order. */
+AFGB_API af_err afgb_set_exact_fp(int exact);
+
+/* Host-only helpers (no GPU needed): the reference's dispatch decisions,
+ * exposed so they can be tested without a device.
+ *   afgb_identify_batch_kind: src/api/c/convolve.cpp:77-97; returns
+ *     0 NONE, 1 LHS, 2 RHS, 3 SAME, 4 DIFF, 5 UNSUPPORTED
+ *     (src/backend/common/internal_enums.hpp:12-22 order).
+ *   afgb_conv_output_dims: src/backend/cpu/convolve.cpp:38-58.
+ *   afgb_nn_output_dims: src/backend/cpu/convolve.cpp:130-135. */
+AFGB_API int afgb_identify_batch_kind(int rank, const dim_t *sdims, const dim_t *fdims);
+AFGB_API int afgb_conv_output_dims(dim_t *odims, int rank, int kind, int expand,
+                                   const dim_t *sdims, const dim_t *fdims);
+AFGB_API int afgb_nn_output_dims(dim_t *odims, const dim_t *sdims, const dim_t *fdims,
+                                 const dim_t *stride, const dim_t *padding,
+                                 const dim_t *dilation);
+
+/* Fault injection for tests: the n-th device allocation from now fails with
+ * AF_ERR_NO_MEM (n <= 0 disables).  Host-side only. */
+AFGB_API void afgb_debug_fail_alloc_after(int n);
+
+/* Number of kernels this library has launched since load (all devices). */
+AFGB_API unsigned long long afgb_kernel_launch_count(void);
+
+/* Device timing of the library's main kernels, for benchmarks: while
+ * enabled, each main kernel launch is bracketed by CUDA events on its stream.
+ * afgb_kernel_time sums the recorded launches whose kernel name equals
+ * `name` (all launches when 0).  Disabling clears the record. */
+AFGB_API void afgb_kernel_timing(int enable);
+AFGB_API af_err afgb_kernel_time(const char *name, unsigned long long *count, double *total_ms);
+
+/* Library version string. */
+AFGB_API const char *afgb_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AFGB300_H */

@@ -1,0 +1,340 @@
+"""Python face of the oracle — TEST INFRASTRUCTURE ONLY (the checker, never the
+thing measured or shipped).
+
+Two implementations sit behind the same functions:
+
+* ``port``: ``conv_oracle.c``, a plain-C restatement of ArrayFire's CPU
+  convolution loops (built by ``make -C oracle port``; builds on any host);
+* ``ref``:  the reference's own CPU kernel templates compiled in place
+  (``make -C oracle ref``; only where an ArrayFire source tree is present).
+
+Arrays follow ArrayFire's layout: a numpy array of shape (d0, d1, d2, d3) in
+Fortran (column-major) order, so element (i,j,k,l) sits at
+i + d0*(j + d1*(k + d2*l)), exactly as ``af::array``.
+
+Host dispatch logic restated here (same decisions as the library):
+  identify_batch_kind  src/api/c/convolve.cpp:77-97
+  conv_output_dims     src/backend/cpu/convolve.cpp:38-58
+  nn_output_dims       src/backend/cpu/convolve.cpp:130-135
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_LIB = HERE / "_build" / "liboracle.so"
+REF_LIB = HERE / "_ref" / "libafref.so"
+
+# af_dtype numbering (include/af/defines.h:211-233)
+F32, C32, F64, C64, B8, S32, U32, U8, S64, U64, S16, U16, F16, S8 = range(14)
+NP_OF = {
+    F32: np.float32, C32: np.complex64, F64: np.float64, C64: np.complex128,
+    B8: np.int8, S32: np.int32, U32: np.uint32, U8: np.uint8, S64: np.int64,
+    U64: np.uint64, S16: np.int16, U16: np.uint16, F16: np.float16, S8: np.int8,
+}
+ACC_OF = {F32: np.float32, F64: np.float64, C32: np.complex64, C64: np.complex128}
+BATCH_NONE, BATCH_LHS, BATCH_RHS, BATCH_SAME, BATCH_DIFF, BATCH_UNSUPPORTED = range(6)
+
+_P = ctypes.c_void_p
+_LL4 = ctypes.POINTER(ctypes.c_longlong)
+
+
+def acc_np(dtype: int):
+    return ACC_OF.get(dtype, np.float32)
+
+
+def build_port() -> Path:
+    """Compile conv_oracle.c (gcc) if needed."""
+    src = HERE / "conv_oracle.c"
+    if not PORT_LIB.exists() or PORT_LIB.stat().st_mtime < src.stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE), "port"], check=True)
+    return PORT_LIB
+
+
+def build_ref(reference: str | None = None) -> Path | None:
+    """Compile the reference's CPU kernels in place, when its tree exists."""
+    ref = reference or os.environ.get("AF_REFERENCE_SRC", "/root/reference")
+    if not Path(ref, "src", "backend", "cpu", "kernel", "convolve.hpp").exists():
+        return None
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REFERENCE={ref}"], check=True)
+    return REF_LIB
+
+
+_libs: dict[str, ctypes.CDLL] = {}
+
+
+def lib(which: str = "port") -> ctypes.CDLL:
+    if which not in _libs:
+        if which == "port":
+            path = build_port()
+        elif which == "ref":
+            if not REF_LIB.exists():
+                raise FileNotFoundError("oracle/_ref/libafref.so not built (needs the reference tree)")
+            path = REF_LIB
+        else:
+            raise ValueError(which)
+        _libs[which] = ctypes.CDLL(str(path))
+    return _libs[which]
+
+
+def have_ref() -> bool:
+    return REF_LIB.exists()
+
+
+def _ll(vals) -> ctypes.Array:
+    return (ctypes.c_longlong * len(vals))(*[int(v) for v in vals])
+
+
+def _dims4(a: np.ndarray) -> list[int]:
+    d = list(a.shape) + [1] * (4 - a.ndim)
+    return d[:4]
+
+
+def _dense_strides(d) -> list[int]:
+    return [1, d[0], d[0] * d[1], d[0] * d[1] * d[2]]
+
+
+def as_af(a: np.ndarray, dtype=None) -> np.ndarray:
+    """Reshape to 4-D column-major (copying when needed)."""
+    a = np.asarray(a, dtype=dtype)
+    d = _dims4(a)
+    return np.asfortranarray(a.reshape(d, order="F"))
+
+
+def ndims(d) -> int:
+    """af::dim4::ndims (src/backend/common/dim4.cpp:48-58)."""
+    d = list(d) + [1] * (4 - len(d))
+    n = d[0] * d[1] * d[2] * d[3]
+    if n == 0:
+        return 0
+    if n == 1:
+        return 1
+    for i in (3, 2, 1):
+        if d[i] != 1:
+            return i + 1
+    return 1
+
+
+def identify_batch_kind(rank: int, sd, fd) -> int:
+    sn, fn = ndims(sd), ndims(fd)
+    if sn == rank and fn == rank:
+        return BATCH_NONE
+    if sn == rank and rank < fn <= 4:
+        return BATCH_RHS
+    if rank < sn <= 4 and fn == rank:
+        return BATCH_LHS
+    if rank < sn <= 4 and rank < fn <= 4:
+        match = all(sd[i] == fd[i] for i in range(rank, 4))
+        inter = all(sd[i] == 1 or fd[i] == 1 or sd[i] == fd[i] for i in range(rank, 4))
+        if match:
+            return BATCH_SAME
+        return BATCH_DIFF if inter else BATCH_UNSUPPORTED
+    return BATCH_UNSUPPORTED
+
+
+def conv_output_dims(rank, kind, expand, sd, fd):
+    if expand:
+        if kind in (BATCH_NONE, BATCH_RHS):
+            return [sd[d] + fd[d] - 1 for d in range(4)]
+        return [sd[d] + fd[d] - 1 if d < rank else sd[d] for d in range(4)]
+    od = list(sd)
+    if kind == BATCH_RHS:
+        for i in range(rank, 4):
+            od[i] = fd[i]
+    return od
+
+
+def _cdiv_trunc(a: int, b: int) -> int:
+    q = abs(a) // abs(b)
+    return q if (a >= 0) == (b > 0) else -q
+
+
+def nn_output_dims(sd, fd, stride, pad, dil):
+    wo = 1 + _cdiv_trunc(sd[0] + 2 * pad[0] - ((fd[0] - 1) * dil[0] + 1), stride[0])
+    ho = 1 + _cdiv_trunc(sd[1] + 2 * pad[1] - ((fd[1] - 1) * dil[1] + 1), stride[1])
+    return [wo, ho, fd[3], sd[3]]
+
+
+# ---------------------------------------------------------------------------
+# direct convolutions
+# ---------------------------------------------------------------------------
+def convolve(sig: np.ndarray, filt: np.ndarray, dtype: int, rank: int, expand: bool,
+             which: str = "port") -> np.ndarray:
+    """af_convolve{1,2,3} in the spatial domain: dispatch exactly like
+    src/api/c/convolve.cpp:132-215 then run convolve_nd."""
+    s = as_af(sig, NP_OF[dtype])
+    f = as_af(filt, acc_np(dtype))
+    sd, fd = _dims4(s), _dims4(f)
+    kind = identify_batch_kind(rank, sd, fd)
+    if kind in (BATCH_DIFF, BATCH_UNSUPPORTED):
+        raise ValueError("unsupported batch kind")
+    od = conv_output_dims(rank, kind, expand, sd, fd)
+    out = np.zeros(od, dtype=NP_OF[dtype], order="F")
+    fn = lib(which).oracle_convolve_nd if which == "port" else lib(which).ref_convolve_nd
+    rc = fn(ctypes.c_int(dtype), out.ctypes.data_as(_P), _ll(od), _ll(_dense_strides(od)),
+            s.ctypes.data_as(_P), _ll(sd), _ll(_dense_strides(sd)), f.ctypes.data_as(_P),
+            _ll(fd), _ll(_dense_strides(fd)), ctypes.c_int(kind), ctypes.c_int(rank),
+            ctypes.c_int(1 if expand else 0))
+    if rc != 0:
+        raise RuntimeError(f"oracle convolve failed ({rc})")
+    return out
+
+
+def convolve2_sep(sig: np.ndarray, cfilt: np.ndarray, rfilt: np.ndarray, dtype: int,
+                  expand: bool, which: str = "port") -> np.ndarray:
+    """af_convolve2_sep (src/api/c/convolve.cpp:258-334 ->
+    src/backend/cpu/convolve.cpp:68-99)."""
+    s = as_af(sig, NP_OF[dtype])
+    c = np.ascontiguousarray(np.asarray(cfilt, dtype=acc_np(dtype)).ravel(order="F"))
+    r = np.ascontiguousarray(np.asarray(rfilt, dtype=acc_np(dtype)).ravel(order="F"))
+    sd = _dims4(s)
+    od = list(sd)
+    if expand:
+        od[0] += c.size - 1
+        od[1] += r.size - 1
+    out = np.zeros(od, dtype=NP_OF[dtype], order="F")
+    fn = lib(which).oracle_convolve2_sep if which == "port" else lib(which).ref_convolve2_sep
+    rc = fn(ctypes.c_int(dtype), out.ctypes.data_as(_P), _ll(od), s.ctypes.data_as(_P), _ll(sd),
+            c.ctypes.data_as(_P), ctypes.c_longlong(c.size), r.ctypes.data_as(_P),
+            ctypes.c_longlong(r.size), ctypes.c_int(1 if expand else 0))
+    if rc != 0:
+        raise RuntimeError(f"oracle convolve2_sep failed ({rc})")
+    return out
+
+
+# ---------------------------------------------------------------------------
+# unwrap / wrap
+# ---------------------------------------------------------------------------
+def unwrap(sig: np.ndarray, wx, wy, sx, sy, px, py, dx, dy, which="port") -> np.ndarray:
+    s = as_af(sig)
+    t = s.dtype
+    assert t in (np.float32, np.float64)
+    sd = _dims4(s)
+    nx = 1 + _cdiv_trunc(sd[0] + 2 * px - ((wx - 1) * dx + 1), sx)
+    ny = 1 + _cdiv_trunc(sd[1] + 2 * py - ((wy - 1) * dy + 1), sy)
+    out = np.zeros([wx * wy, nx * ny, sd[2], sd[3]], dtype=t, order="F")
+    suffix = "f32" if t == np.float32 else "f64"
+    name = ("oracle_unwrap_" if which == "port" else "ref_unwrap_") + suffix
+    getattr(lib(which), name)(out.ctypes.data_as(_P), s.ctypes.data_as(_P), _ll(sd),
+                              *[ctypes.c_longlong(v) for v in (wx, wy, sx, sy, px, py, dx, dy)])
+    return out
+
+
+def wrap_dilated(cols: np.ndarray, odims, wx, wy, sx, sy, px, py, dx, dy, which="port"):
+    c = as_af(cols)
+    t = c.dtype
+    out = np.zeros(list(odims), dtype=t, order="F")
+    suffix = "f32" if t == np.float32 else "f64"
+    name = ("oracle_wrap_dilated_" if which == "port" else "ref_wrap_dilated_") + suffix
+    getattr(lib(which), name)(out.ctypes.data_as(_P), _ll(odims), c.ctypes.data_as(_P),
+                              *[ctypes.c_longlong(v) for v in (wx, wy, sx, sy, px, py, dx, dy)])
+    return out
+
+
+# ---------------------------------------------------------------------------
+# NN convolution, FP64
+# ---------------------------------------------------------------------------
+def _geom(sd, fd, stride, pad, dil):
+    return _ll([sd[0], sd[1], sd[2], sd[3], fd[0], fd[1], fd[3], stride[0], stride[1],
+                pad[0], pad[1], dil[0], dil[1]])
+
+
+def _f64(a):
+    return np.asfortranarray(as_af(a).astype(np.float64))
+
+
+def nn_forward_f64(sig, filt, stride, pad, dil):
+    s, f = _f64(sig), _f64(filt)
+    sd, fd = _dims4(s), _dims4(f)
+    od = nn_output_dims(sd, fd, stride, pad, dil)
+    out = np.zeros(od, dtype=np.float64, order="F")
+    lib().oracle_nn_fwd_f64(out.ctypes.data_as(_P), s.ctypes.data_as(_P), f.ctypes.data_as(_P),
+                            _geom(sd, fd, stride, pad, dil))
+    return out
+
+
+def nn_forward_points_f64(sig, filt, stride, pad, dil, idx):
+    s, f = _f64(sig), _f64(filt)
+    sd, fd = _dims4(s), _dims4(f)
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    vals = np.zeros(idx.size, dtype=np.float64)
+    lib().oracle_nn_fwd_points_f64(vals.ctypes.data_as(_P), idx.ctypes.data_as(_P),
+                                   ctypes.c_longlong(idx.size), s.ctypes.data_as(_P),
+                                   f.ctypes.data_as(_P), _geom(sd, fd, stride, pad, dil))
+    return vals
+
+
+def nn_data_grad_f64(grad, sig_dims, filt, stride, pad, dil):
+    g, f = _f64(grad), _f64(filt)
+    fd = _dims4(f)
+    sd = list(sig_dims)
+    out = np.zeros(sd, dtype=np.float64, order="F")
+    lib().oracle_nn_dgrad_f64(out.ctypes.data_as(_P), g.ctypes.data_as(_P), f.ctypes.data_as(_P),
+                              _geom(sd, fd, stride, pad, dil))
+    return out
+
+
+def nn_data_grad_points_f64(grad, sig_dims, filt, stride, pad, dil, idx):
+    g, f = _f64(grad), _f64(filt)
+    fd = _dims4(f)
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    vals = np.zeros(idx.size, dtype=np.float64)
+    lib().oracle_nn_dgrad_points_f64(vals.ctypes.data_as(_P), idx.ctypes.data_as(_P),
+                                     ctypes.c_longlong(idx.size), g.ctypes.data_as(_P),
+                                     f.ctypes.data_as(_P), _geom(list(sig_dims), fd, stride, pad, dil))
+    return vals
+
+
+def nn_filter_grad_f64(grad, sig, filt_dims, stride, pad, dil):
+    g, s = _f64(grad), _f64(sig)
+    sd = _dims4(s)
+    fd = list(filt_dims)
+    out = np.zeros(fd, dtype=np.float64, order="F")
+    lib().oracle_nn_wgrad_f64(out.ctypes.data_as(_P), s.ctypes.data_as(_P), g.ctypes.data_as(_P),
+                              _geom(sd, fd, stride, pad, dil))
+    return out
+
+
+def nn_filter_grad_points_f64(grad, sig, filt_dims, stride, pad, dil, idx):
+    g, s = _f64(grad), _f64(sig)
+    sd = _dims4(s)
+    idx = np.ascontiguousarray(idx, dtype=np.int64)
+    vals = np.zeros(idx.size, dtype=np.float64)
+    lib().oracle_nn_wgrad_points_f64(vals.ctypes.data_as(_P), idx.ctypes.data_as(_P),
+                                     ctypes.c_longlong(idx.size), s.ctypes.data_as(_P),
+                                     g.ctypes.data_as(_P), _geom(sd, list(filt_dims), stride, pad, dil))
+    return vals
+
+
+def nn_bias_grad_f64(grad, sig_dims, filt_dims, stride, pad, dil):
+    g = _f64(grad)
+    out = np.zeros([1, 1, filt_dims[3], 1], dtype=np.float64, order="F")
+    lib().oracle_nn_bgrad_f64(out.ctypes.data_as(_P), g.ctypes.data_as(_P),
+                              _geom(list(sig_dims), list(filt_dims), stride, pad, dil))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# the reference CPU backend's NN path, FP32: unwrap + GEMM
+# (src/backend/cpu/convolve.cpp:123-158).  Used as the timed CPU baseline; the
+# GEMM is numpy's bundled BLAS sgemm, standing in for the CBLAS call of
+# src/backend/cpu/blas.cpp:222-331.
+# ---------------------------------------------------------------------------
+def nn_forward_unwrap_gemm_f32(sig, filt, stride, pad, dil, which="port"):
+    s = as_af(sig, np.float32)
+    f = as_af(filt, np.float32)
+    sd, fd = _dims4(s), _dims4(f)
+    od = nn_output_dims(sd, fd, stride, pad, dil)
+    cols = unwrap(s, fd[0], fd[1], stride[0], stride[1], pad[0], pad[1], dil[0], dil[1], which)
+    wsz, npix, C, N = cols.shape  # cols[tap, pixel, c, n], tap = x + fw*y
+    A = np.ascontiguousarray(cols.transpose(1, 3, 2, 0)).reshape(npix * N, C * wsz)
+    wflip = f[::-1, ::-1, :, :]  # flip(filter, {1,1,0,0})
+    B = np.ascontiguousarray(
+        wflip.reshape(wsz, C, fd[3], order="F").transpose(1, 0, 2)).reshape(C * wsz, fd[3])
+    res = (A @ B).reshape(npix, N, fd[3]).transpose(0, 2, 1)  # (pixel, K, N)
+    return np.asfortranarray(res).reshape(od, order="F")

@@ -1,0 +1,220 @@
+"""Seeded case matrix shared by the golden-vector generator and the tests.
+
+Every input is regenerated from (seed, shape, distribution) with numpy's
+Philox bit generator, which gives the same numbers on every platform, so a
+fixture only needs to store the reference's outputs (or their hashes).
+
+Case matrix (after the reference's own test suites, test/convolve.cpp:36-214:
+dtypes x {vector, rectangle, cuboid} x {one2one, many2one, many2many,
+one2many} x {EXPAND, DEFAULT}); integer inputs are kept in range so that the
+reference's `InT(accum)` conversion is defined.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+F32, C32, F64, C64, B8, S32, U32, U8, S64, U64, S16, U16, F16, S8 = range(14)
+NP_OF = {F32: np.float32, C32: np.complex64, F64: np.float64, C64: np.complex128, B8: np.int8,
+         S32: np.int32, U32: np.uint32, U8: np.uint8, S64: np.int64, U64: np.uint64,
+         S16: np.int16, U16: np.uint16, S8: np.int8}
+ACC_OF = {F32: np.float32, F64: np.float64, C32: np.complex64, C64: np.complex128}
+DT_NAME = {F32: "f32", C32: "c32", F64: "f64", C64: "c64", B8: "b8", S32: "s32", U32: "u32",
+           U8: "u8", S64: "s64", U64: "u64", S16: "s16", U16: "u16", S8: "s8"}
+EIGHT_BIT = (U8, S8, B8)
+
+
+def rng(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.Philox(seed))
+
+
+def af_shape(dims):
+    d = list(dims) + [1] * (4 - len(dims))
+    return d[:4]
+
+
+def make_signal(dtype: int, dims, seed: int) -> np.ndarray:
+    g = rng(seed)
+    shape = af_shape(dims)
+    if dtype in (F32, F64):
+        a = g.standard_normal(shape)
+    elif dtype in (C32, C64):
+        a = g.standard_normal(shape) + 1j * g.standard_normal(shape)
+    elif dtype == B8:
+        a = g.integers(0, 2, shape)
+    else:
+        a = g.integers(0, 10, shape)
+    return np.asfortranarray(a.astype(NP_OF[dtype]))
+
+
+def make_filter(dtype: int, dims, seed: int, rank: int) -> np.ndarray:
+    """Filter in the accumulator type.  Integer signals get non-negative taps
+    normalised to unit sum per filter slice so every output stays in range."""
+    g = rng(seed)
+    shape = af_shape(dims)
+    acc = ACC_OF.get(dtype, np.float32)
+    if dtype in (F32, F64):
+        f = g.standard_normal(shape)
+    elif dtype in (C32, C64):
+        f = g.standard_normal(shape) + 1j * g.standard_normal(shape)
+    else:
+        f = g.random(shape) + 0.05
+        f = f / f.sum(axis=tuple(range(rank)), keepdims=True)
+        if dtype in (S16, U16, S32, U32, S64, U64):
+            f = f * 3.0
+    return np.asfortranarray(f.astype(acc))
+
+
+# (name, rank, signal dims, filter dims, kind label)
+DIRECT_SHAPES = [
+    # rank 1
+    ("v_one2one", 1, (37,), (5,)),
+    ("v_one2one_even", 1, (37,), (4,)),
+    ("v_many2one", 1, (23, 3, 2), (7,)),
+    ("v_one2many", 1, (23,), (5, 3)),
+    ("v_many2many", 1, (19, 3), (3, 3)),
+    # rank 2
+    ("r_one2one_3", 2, (33, 21), (3, 3)),
+    ("r_one2one_5", 2, (70, 65), (5, 5)),
+    ("r_one2one_7", 2, (67, 130), (7, 7)),
+    ("r_one2one_2x4", 2, (29, 17), (2, 4)),
+    ("r_one2one_9", 2, (31, 40), (9, 9)),
+    ("r_one2one_17", 2, (40, 33), (17, 17)),
+    ("r_many2one", 2, (45, 38, 3), (5, 5)),
+    ("r_many2one_4d", 2, (30, 20, 2, 2), (3, 3)),
+    ("r_one2many", 2, (41, 26), (3, 3, 3)),
+    ("r_many2many", 2, (66, 70, 3), (7, 7, 3)),
+    ("r_small", 2, (3, 2), (5, 5)),
+    # rank 3
+    ("c_one2one_3", 3, (17, 14, 9), (3, 3, 3)),
+    ("c_one2one_245", 3, (11, 13, 10), (2, 4, 5)),
+    ("c_many2one", 3, (9, 8, 7, 2), (3, 3, 3)),
+    ("c_one2many", 3, (9, 8, 7), (3, 3, 3, 2)),
+    ("c_many2many", 3, (9, 8, 7, 2), (3, 3, 3, 2)),
+]
+
+DIRECT_DTYPES_FULL = [F32, F64, C32, C64, U8, S8, B8, S16, U16, S32, U32, S64, U64]
+DIRECT_DTYPES_SHORT = [F32, F64, C32, U8, S32]
+
+
+def direct_cases():
+    """Yields (case_id, dtype, rank, sig_dims, filt_dims, expand, seed)."""
+    seed = 1000
+    for name, rank, sd, fd in DIRECT_SHAPES:
+        dts = DIRECT_DTYPES_FULL if name in ("r_one2one_5", "r_one2many", "v_many2one",
+                                             "c_one2one_3", "r_many2many") else DIRECT_DTYPES_SHORT
+        for dt in dts:
+            for expand in (False, True):
+                seed += 2
+                yield (f"{name}_{DT_NAME[dt]}_{'exp' if expand else 'def'}", dt, rank, sd, fd,
+                       expand, seed)
+
+
+SEP_SHAPES = [
+    ("sep_5x3", (40, 33), 5, 3),
+    ("sep_15", (70, 66, 2), 15, 15),
+    ("sep_1x7", (31, 29), 1, 7),
+    ("sep_31", (80, 70), 31, 31),
+    ("sep_batch4d", (20, 21, 2, 2), 3, 5),
+]
+SEP_DTYPES = [F32, F64, C32, U8, S8, S16, S32, U32, S64]
+
+
+def sep_taps(dtype: int, n: int, seed: int) -> np.ndarray:
+    g = rng(seed)
+    acc = ACC_OF.get(dtype, np.float32)
+    if dtype in (F32, F64):
+        t = g.standard_normal(n)
+    elif dtype in (C32, C64):
+        t = g.standard_normal(n) + 1j * g.standard_normal(n)
+    else:
+        # the CPU backend converts taps to the input type (truncation toward
+        # zero, src/backend/cpu/kernel/convolve.hpp:233): fractional taps in
+        # [0,1) become 0 and two taps in [1,2.5) become 1 or 2, which
+        # exercises the rule while keeping every product and sum in range
+        t = g.random(n)
+        for pos in g.choice(n, size=min(2, n), replace=False):
+            t[pos] = 1.0 + 1.5 * g.random()
+    return t.astype(acc)
+
+
+def sep_signal(dtype: int, dims, seed: int) -> np.ndarray:
+    g = rng(seed)
+    shape = af_shape(dims)
+    if dtype in (F32, F64):
+        a = g.standard_normal(shape)
+    elif dtype in (C32, C64):
+        a = g.standard_normal(shape) + 1j * g.standard_normal(shape)
+    else:
+        a = g.integers(0, 3, shape)
+    return np.asfortranarray(a.astype(NP_OF[dtype]))
+
+
+def sep_cases():
+    seed = 5000
+    for name, sd, cl, rl in SEP_SHAPES:
+        for dt in SEP_DTYPES:
+            for expand in (False, True):
+                seed += 3
+                yield (f"{name}_{DT_NAME[dt]}_{'exp' if expand else 'def'}", dt, sd, cl, rl, expand, seed)
+
+
+# NN geometry cases: (name, signal dims (W,H,C,N), filter dims (fw,fh,C,K), stride, pad, dil)
+NN_CASES = [
+    ("nn_s1p1", (10, 10, 1, 1), (3, 3, 1, 1), (1, 1), (1, 1), (1, 1)),
+    ("nn_s3p1", (10, 10, 1, 1), (3, 3, 1, 1), (3, 3), (1, 1), (1, 1)),
+    ("nn_5x5_s5", (10, 10, 1, 1), (5, 5, 1, 1), (5, 5), (1, 1), (1, 1)),
+    ("nn_d2", (10, 10, 1, 1), (3, 3, 1, 1), (1, 1), (1, 1), (2, 2)),
+    ("nn_d3", (10, 10, 1, 1), (3, 3, 1, 1), (1, 1), (1, 1), (3, 3)),
+    ("nn_35", (10, 10, 1, 1), (3, 5, 1, 1), (1, 1), (1, 1), (1, 1)),
+    ("nn_35_s31_d21", (10, 10, 1, 1), (3, 5, 1, 1), (3, 1), (1, 1), (2, 1)),
+    ("nn_multi", (8, 10, 3, 2), (3, 3, 3, 4), (1, 1), (1, 1), (1, 1)),
+    ("nn_s2_c16", (17, 15, 16, 2), (3, 3, 16, 24), (2, 2), (1, 1), (1, 1)),
+    ("nn_5x5_d2_s2", (20, 18, 8, 2), (5, 5, 8, 12), (2, 2), (4, 4), (2, 2)),
+    ("nn_1x1", (14, 14, 32, 2), (1, 1, 32, 40), (1, 1), (0, 0), (1, 1)),
+    ("nn_nopad", (12, 11, 5, 3), (3, 2, 5, 7), (1, 2), (0, 0), (1, 1)),
+]
+
+
+def nn_inputs(case, seed: int, dtype=np.float32):
+    name, sd, fd, st, pd, dl = case
+    g = rng(seed)
+    s = np.asfortranarray(g.standard_normal(af_shape(sd)).astype(dtype))
+    std = np.sqrt(2.0 / (fd[0] * fd[1] * fd[2]))
+    f = np.asfortranarray((g.standard_normal(af_shape(fd)) * std).astype(dtype))
+    return s, f
+
+
+def nn_out_dims(sd, fd, st, pd, dl):
+    def div(a, b):
+        q = abs(a) // abs(b)
+        return q if (a >= 0) == (b > 0) else -q
+    wo = 1 + div(sd[0] + 2 * pd[0] - ((fd[0] - 1) * dl[0] + 1), st[0])
+    ho = 1 + div(sd[1] + 2 * pd[1] - ((fd[1] - 1) * dl[1] + 1), st[1])
+    return [wo, ho, fd[3], af_shape(sd)[3]]
+
+
+def nn_grad(case, seed: int, dtype=np.float32):
+    name, sd, fd, st, pd, dl = case
+    g = rng(seed + 7)
+    od = nn_out_dims(af_shape(sd), af_shape(fd), st, pd, dl)
+    return np.asfortranarray(g.standard_normal(od).astype(dtype))
+
+
+# BASELINE config 1 (full size; outputs stored as SHA-256 of the reference's bytes)
+def config1a():
+    """512x512 f32 U[0,1) (Philox seed 0) with the 5x5 Gaussian sigma=1,
+    normalised to unit sum (src/api/c/gaussian_kernel.cpp:36-88)."""
+    sig = np.asfortranarray(rng(0).random((512, 512), dtype=np.float32))
+    x = np.arange(5) - 2
+    k = np.exp(-0.5 * (x[:, None] ** 2 + x[None, :] ** 2) / 1.0 ** 2)
+    k = (k / k.sum()).astype(np.float32)
+    return sig, np.asfortranarray(k)
+
+
+def config1b():
+    """1024x1024 Bernoulli(0.5) binary f32 grid with the 3x3 all-ones-except-
+    centre neighbour kernel (examples/graphics/conway.cpp:18)."""
+    sig = np.asfortranarray((rng(1).random((1024, 1024)) < 0.5).astype(np.float32))
+    k = np.ones((3, 3), np.float32)
+    k[1, 1] = 0
+    return sig, np.asfortranarray(k)
