@@ -199,14 +199,16 @@ def sync(device: int = -1) -> None:
 
 def set_stream(stream) -> None:
     """Run library work on `stream` (a torch.cuda.Stream, a raw cudaStream_t
-    int, or None for the library's own stream)."""
+    int where 0 means the legacy default stream, or None for the library's
+    own stream)."""
     if stream is None:
-        ptr = None
-    elif isinstance(stream, int):
-        ptr = stream
-    else:
-        ptr = stream.cuda_stream
-    _check(lib().afgb_set_stream(ctypes.c_void_p(ptr) if ptr else None))
+        _check(lib().afgb_set_stream(None))
+        return
+    ptr = stream if isinstance(stream, int) else stream.cuda_stream
+    # handle 0 is the legacy default stream (torch's default stream); pass it
+    # as cudaStreamLegacy because a null handle selects the library's own
+    # stream in afgb_set_stream
+    _check(lib().afgb_set_stream(ctypes.c_void_p(ptr if ptr else 1)))
 
 
 def set_exact_fp(exact: bool) -> None:

@@ -110,6 +110,10 @@ void free_device(void *p);
 // execution state
 // ---------------------------------------------------------------------------
 cudaStream_t stream();
+// error word of the tensor-core kernels (bounded waits that timed out);
+// read and cleared after the host has synchronised
+unsigned int tc_take_error();
+void check_device_errors();
 int device();
 bool exact_fp();
 int num_sms();

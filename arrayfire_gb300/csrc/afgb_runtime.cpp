@@ -154,6 +154,14 @@ cudaStream_t stream() {
 }
 
 int num_sms() { return dev_state(device()).sms; }
+
+void check_device_errors() {
+    unsigned int w = tc_take_error();
+    if (w) {
+        AFGB_THROW(AF_ERR_RUNTIME, "a tensor-core kernel pipeline wait timed out (code " +
+                                       std::to_string(w) + "); its results are invalid");
+    }
+}
 bool exact_fp() { return g_exact.load() != 0; }
 void count_launch(unsigned n) { g_launches += n; }
 
@@ -398,6 +406,7 @@ af_err af_get_data_ptr(void *data, const af_array arr) {
                 }
     }
     AFGB_CUDA(cudaStreamSynchronize(stream()));
+    check_device_errors();
     AFGB_CATCHALL
 }
 
@@ -469,9 +478,11 @@ af_err af_sync(const int dev) {
         int cur = device();
         if (dev != cur) AFGB_CUDA(cudaSetDevice(dev));
         AFGB_CUDA(cudaStreamSynchronize(stream()));
+        check_device_errors();
         if (dev != cur) AFGB_CUDA(cudaSetDevice(cur));
     } else {
         AFGB_CUDA(cudaStreamSynchronize(stream()));
+        check_device_errors();
     }
     AFGB_CATCHALL
 }

@@ -93,28 +93,30 @@ template <> __device__ __forceinline__ cf64 acc_zero<cf64>() { return cf64{0.0, 
 template <typename T> __device__ __forceinline__ T from_acc(float a);
 template <> __device__ __forceinline__ float from_acc<float>(float a) { return a; }
 
-__device__ __forceinline__ double trunc_sat(float a, double lo, double hi) {
-    if (a != a) return 0.0;
-    double t = trunc((double)a);
-    return t < lo ? lo : (t > hi ? hi : t);
+// truncate toward zero and saturate in single precision (the bounds of the
+// 8/16-bit types are exact floats); NaN -> 0
+__device__ __forceinline__ float trunc_sat_f(float a, float lo, float hi) {
+    if (a != a) return 0.0f;
+    return fminf(fmaxf(truncf(a), lo), hi);
 }
 template <> __device__ __forceinline__ uint8_t from_acc<uint8_t>(float a) {
-    return (uint8_t)trunc_sat(a, 0.0, 255.0);
+    return (uint8_t)trunc_sat_f(a, 0.0f, 255.0f);
 }
 template <> __device__ __forceinline__ int8_t from_acc<int8_t>(float a) {
-    return (int8_t)trunc_sat(a, -128.0, 127.0);
+    return (int8_t)trunc_sat_f(a, -128.0f, 127.0f);
 }
 template <> __device__ __forceinline__ uint16_t from_acc<uint16_t>(float a) {
-    return (uint16_t)trunc_sat(a, 0.0, 65535.0);
+    return (uint16_t)trunc_sat_f(a, 0.0f, 65535.0f);
 }
 template <> __device__ __forceinline__ int16_t from_acc<int16_t>(float a) {
-    return (int16_t)trunc_sat(a, -32768.0, 32767.0);
+    return (int16_t)trunc_sat_f(a, -32768.0f, 32767.0f);
 }
+// 32-bit: cvt.rzi saturates to the destination range; NaN -> 0
 template <> __device__ __forceinline__ int32_t from_acc<int32_t>(float a) {
-    return (int32_t)trunc_sat(a, -2147483648.0, 2147483647.0);
+    return (a != a) ? 0 : __float2int_rz(a);
 }
 template <> __device__ __forceinline__ uint32_t from_acc<uint32_t>(float a) {
-    return (uint32_t)trunc_sat(a, 0.0, 4294967295.0);
+    return (a != a) ? 0u : __float2uint_rz(a);
 }
 template <> __device__ __forceinline__ long long from_acc<long long>(float a) {
     if (a != a) return 0;

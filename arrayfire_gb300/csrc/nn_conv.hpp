@@ -41,6 +41,10 @@ bool tc_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out
 bool tc_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &dx);
 bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw);
 
+// fixed-order compensated sum of `splits` fp32 partials R[c + C*tap][k],
+// written flipped into the (fw,fh,C,K) f32 filter gradient
+void reduce_filter_partials(const NNGeom &g, const float *partials, int splits, float *dw);
+
 // deterministic compensated reduction of `splits` fp32 partial matrices of
 // `rows x cols` into `out` (pairwise tree over splits with TwoSum carries)
 void reduce_partials(const float *partials, int splits, long long rows, long long cols,

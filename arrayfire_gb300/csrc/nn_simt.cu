@@ -654,6 +654,19 @@ void reduce_partials(const float *partials, int splits, long long rows, long lon
     AFGB_POST_LAUNCH("reduce_partials_kernel");
 }
 
+void reduce_filter_partials(const NNGeom &g, const float *partials, int splits, float *dw) {
+    const long long rows = g.fw * g.fh * g.C;
+    const long long total = rows * g.K;
+    if (!total) return;
+    {
+        KernelTimer kt("wgrad_reduce_kernel");
+        wgrad_reduce_kernel<float, float><<<grid_cap(total, 256), 256, 0, stream()>>>(
+            partials, splits, rows, g.K, g.C, g.fw, g.fh, dw);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("wgrad_reduce_kernel");
+}
+
 template <typename T>
 static void bias_t(const NNGeom &g, const Array &grad, Array &db) {
     const long long WoHo = g.Wo * g.Ho;

@@ -1,14 +1,843 @@
-// Tensor-core (tcgen05/TMEM) NN convolution kernels: BF16 and FP8-E4M3
-// forms of af_convolve2_nn and its gradients.
+// Tensor-core (tcgen05 / TMEM) NN convolution for sm_103a: the BF16 form of
+// af_convolve2_nn and both of its input gradients, plus the filter gradient.
+//
+// The reference runs these as unwrap + GEMM (src/backend/cpu/convolve.cpp:
+// 123-243, src/backend/cuda/convolveNN.cpp:175-407) or hands them to cuDNN.
+// Here each is one implicit GEMM whose operands are gathered straight from
+// the image, so no unwrapped patch matrix exists:
+//
+//   gather kernel  D[och][pixel] = sum_{cchunk, tap} Wt[och][tap, c] * Img[pixel@tap][c]
+//       forward:   Img = signal (NHWC bf16), och = filter K, taps all (u,v)
+//       data grad: Img = incoming gradient, och = C, one launch covers every
+//                  stride phase (x' mod sx, y' mod sy) with that phase's taps,
+//                  so no zero-stuffed products are issued
+//     MMA M=128 output channels (weights, TMA-loaded, K-major, 128B swizzle),
+//     N=256 output pixels (cp.async row gather of 64-channel pixel rows,
+//     zero-filled outside the image), K=64 channels per stage, 4 stages.
+//     Persistent CTAs, warp-specialised: 4 gather warps, 4 epilogue warps
+//     (TMEM -> registers -> f32 ArrayFire layout), 1 MMA warp, 1 TMA warp;
+//     the 256-column accumulator is double-buffered in TMEM (512 columns)
+//     so the epilogue of one tile overlaps the main loop of the next.
+//
+//   wgrad kernel   D[k][(tap,c)] = sum_{pixels} G[pixel][k] * X[pixel@tap][c]
+//     reduction over pixels: both operands are pixel rows, i.e. MN-major
+//     shared-memory tiles; split-K over pixel ranges, FP32 partials combined
+//     by a fixed-order compensated reduction (deterministic).
+//
+// Inputs and outputs stay f32 ArrayFire arrays; conversion to bf16
+// channels-last happens on the device in bandwidth-bound pre-passes.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_fp8.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
 #include "nn_conv.hpp"
+#include "tc_ptx.cuh"
 
 namespace afgb {
+namespace tc {
 
-bool tc_forward(const NNGeom &, const Array &, const Array &, Array &, afgb_precision,
-                const Array *) {
-    return false;
+constexpr int BM = 128;            // output channels per tile (MMA M)
+constexpr int BN = 256;            // output pixels per tile (MMA N)
+constexpr int BK = 64;             // input channels per stage (128 bytes of bf16)
+constexpr int STAGES = 4;
+constexpr int A_BYTES = BM * BK * 2;   // 16 KB weight tile
+constexpr int B_BYTES = BN * BK * 2;   // 32 KB pixel tile
+constexpr int LAG = 2;             // cp.async groups in flight per producer
+constexpr int MAX_PH = 64;
+constexpr int MAX_T = 256;
+constexpr int NUM_THREADS = 320;   // warps 0-3 gather, 4-7 epilogue, 8 MMA, 9 TMA
+
+struct GatherParams {
+    const __nv_bfloat16 *src;  // [N][SH][SW][SCpad]
+    float *dst;                // ArrayFire layout (DW, DH, DC, N)
+    int SW, SH, SCpad, N;
+    int DW, DH, DC;
+    int mode;  // 0 forward, 1 data gradient
+    int sx, sy, px, py, dx, dy, fw;
+    int nchunk;       // SCpad / 64
+    int n_och_tiles;  // ceil(DC / 128)
+    int nphase, nphx;
+    int total_tiles;
+    int phase_tile_begin[MAX_PH + 1];
+    int phase_tap_begin[MAX_PH + 1];
+    short tap_u[MAX_T], tap_v[MAX_T];
+};
+
+struct Smem {
+    // operand stages are carved from the 1024-aligned dynamic buffer
+    uint64_t full[STAGES];
+    uint64_t empty[STAGES];
+    uint64_t tmem_full[2];
+    uint64_t tmem_empty[2];
+    uint64_t final_bar;
+    uint32_t tmem_base;
+    int abort;
+};
+
+struct TileInfo {
+    int ph, rx, ry, tap_begin, ntaps;
+    long long p0, npix;  // first pixel of the tile, pixels in this phase
+    int MX, MY;
+    int och0;
+};
+
+__device__ __forceinline__ TileInfo decode_tile(const GatherParams &p, int tile) {
+    TileInfo t;
+    int ph = 0;
+    while (ph + 1 < p.nphase && tile >= p.phase_tile_begin[ph + 1]) ++ph;
+    t.ph = ph;
+    t.rx = ph % p.nphx;
+    t.ry = ph / p.nphx;
+    t.tap_begin = p.phase_tap_begin[ph];
+    t.ntaps = p.phase_tap_begin[ph + 1] - p.phase_tap_begin[ph];
+    int local = tile - p.phase_tile_begin[ph];
+    t.och0 = (local % p.n_och_tiles) * BM;
+    int ptile = local / p.n_och_tiles;
+    if (p.mode == 0) {
+        t.MX = p.DW;
+        t.MY = p.DH;
+    } else {
+        t.MX = (p.DW - t.rx + p.sx - 1) / p.sx;
+        t.MY = (p.DH - t.ry + p.sy - 1) / p.sy;
+    }
+    t.npix = (long long)t.MX * t.MY * p.N;
+    t.p0 = (long long)ptile * BN;
+    return t;
 }
-bool tc_data_grad(const NNGeom &, const Array &, const Array &, Array &) { return false; }
-bool tc_filter_grad(const NNGeom &, const Array &, const Array &, Array &) { return false; }
+
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+    gather_conv_kernel(const __grid_constant__ GatherParams p,
+                       const __grid_constant__ CUtensorMap wmap) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base =
+        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char *a_stage = base;                       // STAGES x 16 KB
+    unsigned char *b_stage = base + STAGES * A_BYTES;    // STAGES x 32 KB
+    Smem *sm = reinterpret_cast<Smem *>(b_stage + STAGES * B_BYTES);
+    volatile int *abort = &sm->abort;
+
+    const int warp = threadIdx.x >> 5;
+    const int lane = threadIdx.x & 31;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; ++s) {
+            mbar_init(&sm->full[s], 128 + 1);
+            mbar_init(&sm->empty[s], 1);
+        }
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&sm->tmem_full[b], 1);
+            mbar_init(&sm->tmem_empty[b], 128);
+        }
+        mbar_init(&sm->final_bar, 1);
+        sm->abort = 0;
+        fence_barrier_init();
+    }
+    if (warp == 8) tmem_alloc(&sm->tmem_base, 512);
+    if (warp == 9 && lane == 0) prefetch_tmap(&wmap);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = sm->tmem_base;
+
+    if (warp < 4) {
+        // ---------------- pixel-row gather (128 threads)
+        const int t = threadIdx.x;
+        const int j = t & 7;          // 16-byte chunk within the 128-byte row
+        const int r0 = t >> 3;        // rows r0 + 16 i
+        const int alpha_x = p.mode == 0 ? p.sx : 1;
+        const int alpha_y = p.mode == 0 ? p.sy : 1;
+        const long long img_stride = (long long)p.SH * p.SW * p.SCpad;
+        uint32_t it = 0;
+        for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
+            TileInfo ti = decode_tile(p, tile);
+            if (ti.ntaps == 0) continue;
+            int xb[16], yb[16], nb[16];
+            uint32_t vmask = 0;
+#pragma unroll
+            for (int i = 0; i < 16; ++i) {
+                long long pix = ti.p0 + r0 + 16 * i;
+                if (pix < ti.npix) {
+                    int X = (int)(pix % ti.MX);
+                    long long rest = pix / ti.MX;
+                    int Y = (int)(rest % ti.MY);
+                    nb[i] = (int)(rest / ti.MY);
+                    xb[i] = X * alpha_x;
+                    yb[i] = Y * alpha_y;
+                    vmask |= 1u << i;
+                } else {
+                    xb[i] = yb[i] = nb[i] = 0;
+                }
+            }
+            const int iters = p.nchunk * ti.ntaps;
+            for (int kb = 0; kb < iters; ++kb, ++it) {
+                const int s = it % STAGES;
+                if (!mbar_wait(&sm->empty[s], ((it / STAGES) & 1) ^ 1, abort, 1u)) break;
+                const int cchunk = kb / ti.ntaps;
+                const int tq = ti.tap_begin + (kb - cchunk * ti.ntaps);
+                const int u = p.tap_u[tq], v = p.tap_v[tq];
+                int offx, offy;
+                if (p.mode == 0) {
+                    offx = u * p.dx - p.px;
+                    offy = v * p.dy - p.py;
+                } else {
+                    offx = (ti.rx + p.px - u * p.dx) / p.sx;
+                    offy = (ti.ry + p.py - v * p.dy) / p.sy;
+                }
+                const uint32_t sb = smem_u32(b_stage + s * B_BYTES);
+                const __nv_bfloat16 *cbase = p.src + cchunk * BK + 8 * j;
+#pragma unroll
+                for (int i = 0; i < 16; ++i) {
+                    const int r = r0 + 16 * i;
+                    const int xs = xb[i] + offx, ys = yb[i] + offy;
+                    const bool ok = ((vmask >> i) & 1u) && xs >= 0 && xs < p.SW && ys >= 0 &&
+                                    ys < p.SH;
+                    const __nv_bfloat16 *src =
+                        ok ? cbase + nb[i] * img_stride + ((long long)ys * p.SW + xs) * p.SCpad
+                           : p.src;
+                    cp_async_16(sb + r * 128 + ((j ^ (r & 7)) << 4), src, ok ? 16u : 0u);
+                }
+                cp_async_commit();
+                if (it >= LAG) {
+                    cp_async_wait<LAG>();
+                    fence_proxy_async_smem();
+                    mbar_arrive(&sm->full[(it - LAG) % STAGES]);
+                }
+            }
+        }
+        cp_async_wait_all();
+        fence_proxy_async_smem();
+        for (uint32_t k = (it >= LAG ? it - LAG : 0); k < it; ++k) mbar_arrive(&sm->full[k % STAGES]);
+    } else if (warp < 8) {
+        // ---------------- epilogue (128 threads, TMEM lanes 32*(warp%4) ..)
+        const int q = warp & 3;
+        uint32_t acc_it = 0;
+        const long long plane = (long long)p.DW * p.DH;
+        for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
+            TileInfo ti = decode_tile(p, tile);
+            const int och = ti.och0 + 32 * q + lane;
+            if (ti.ntaps == 0) {
+                // a stride phase no tap reaches: its gradient is zero
+                if (och < p.DC) {
+                    for (int e = 0; e < BN; ++e) {
+                        long long pix = ti.p0 + e;
+                        if (pix >= ti.npix) break;
+                        int X = (int)(pix % ti.MX);
+                        long long rest = pix / ti.MX;
+                        int Y = (int)(rest % ti.MY), n = (int)(rest / ti.MY);
+                        long long xo = ti.rx + (long long)p.sx * X, yo = ti.ry + (long long)p.sy * Y;
+                        p.dst[xo + p.DW * yo + plane * (och + (long long)p.DC * n)] = 0.0f;
+                    }
+                }
+                continue;
+            }
+            const int b = acc_it & 1;
+            if (!mbar_wait(&sm->tmem_full[b], (acc_it >> 1) & 1, abort, 2u)) break;
+            tc_fence_after();
+            const uint32_t taddr = tmem_base + (uint32_t)(b * BN) + ((uint32_t)(32 * q) << 16);
+            for (int cc = 0; cc < BN / 16; ++cc) {
+                uint32_t r[16];
+                tmem_ld16(taddr + cc * 16, r);
+                tmem_ld_wait();
+                if (och >= p.DC) continue;
+                const long long pix0 = ti.p0 + cc * 16;
+                if (pix0 >= ti.npix) continue;
+                if (p.mode == 0) {
+                    const long long n0 = pix0 / plane, n1 = (pix0 + 15) / plane;
+                    if (n0 == n1 && pix0 + 15 < ti.npix && (plane & 3) == 0) {
+                        float4 *d = reinterpret_cast<float4 *>(
+                            p.dst + (pix0 - n0 * plane) + plane * (och + (long long)p.DC * n0));
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            d[e] = make_float4(__uint_as_float(r[4 * e]), __uint_as_float(r[4 * e + 1]),
+                                               __uint_as_float(r[4 * e + 2]),
+                                               __uint_as_float(r[4 * e + 3]));
+                        continue;
+                    }
+                }
+#pragma unroll
+                for (int e = 0; e < 16; ++e) {
+                    const long long pix = pix0 + e;
+                    if (pix >= ti.npix) break;
+                    int X = (int)(pix % ti.MX);
+                    long long rest = pix / ti.MX;
+                    int Y = (int)(rest % ti.MY), n = (int)(rest / ti.MY);
+                    long long xo, yo;
+                    if (p.mode == 0) {
+                        xo = X;
+                        yo = Y;
+                    } else {
+                        xo = ti.rx + (long long)p.sx * X;
+                        yo = ti.ry + (long long)p.sy * Y;
+                    }
+                    p.dst[xo + p.DW * yo + plane * (och + (long long)p.DC * n)] = __uint_as_float(r[e]);
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&sm->tmem_empty[b]);
+            ++acc_it;
+        }
+    } else if (warp == 8) {
+        // ---------------- MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(BM, BN, 0, 0);
+            uint32_t it = 0, acc_it = 0;
+            bool issued = false;
+            for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
+                TileInfo ti = decode_tile(p, tile);
+                if (ti.ntaps == 0) continue;
+                const int b = acc_it & 1;
+                if (!mbar_wait(&sm->tmem_empty[b], ((acc_it >> 1) & 1) ^ 1, abort, 4u)) break;
+                tc_fence_after();
+                const uint32_t d_tmem = tmem_base + (uint32_t)(b * BN);
+                const int iters = p.nchunk * ti.ntaps;
+                bool ok = true;
+                for (int kb = 0; kb < iters; ++kb, ++it) {
+                    const int s = it % STAGES;
+                    if (!mbar_wait(&sm->full[s], (it / STAGES) & 1, abort, 8u)) {
+                        ok = false;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t sa = smem_u32(a_stage + s * A_BYTES);
+                    const uint32_t sbb = smem_u32(b_stage + s * B_BYTES);
+#pragma unroll
+                    for (int k = 0; k < BK / 16; ++k) {
+                        const uint64_t ad = smem_desc(sa + k * 32, 16, 1024);
+                        const uint64_t bd = smem_desc(sbb + k * 32, 16, 1024);
+                        mma_f16(d_tmem, ad, bd, idesc, (kb | k) != 0);
+                    }
+                    mma_commit(&sm->empty[s]);
+                    issued = true;
+                }
+                if (!ok) break;
+                mma_commit(&sm->tmem_full[b]);
+                ++acc_it;
+            }
+            if (issued) {
+                mma_commit(&sm->final_bar);
+                unsigned n = 0;
+                while (!mbar_try_wait(&sm->final_bar, 0) && ++n < kSpinLimit) {
+                }
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- weight tiles via TMA
+        if (lane == 0) {
+            uint32_t it = 0;
+            for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
+                TileInfo ti = decode_tile(p, tile);
+                if (ti.ntaps == 0) continue;
+                const int iters = p.nchunk * ti.ntaps;
+                for (int kb = 0; kb < iters; ++kb, ++it) {
+                    const int s = it % STAGES;
+                    if (!mbar_wait(&sm->empty[s], ((it / STAGES) & 1) ^ 1, abort, 16u)) break;
+                    const int cchunk = kb / ti.ntaps;
+                    const int tq = ti.tap_begin + (kb - cchunk * ti.ntaps);
+                    const int tap = p.tap_u[tq] + p.fw * p.tap_v[tq];
+                    mbar_arrive_expect_tx(&sm->full[s], A_BYTES);
+                    tma_load_2d(smem_u32(a_stage + s * A_BYTES), &wmap, &sm->full[s],
+                                tap * p.SCpad + cchunk * BK, ti.och0);
+                }
+            }
+        }
+        __syncwarp();
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 8) {
+        tc_fence_after();
+        tmem_dealloc(tmem_base, 512);
+    }
+}
+
+// ===========================================================================
+// filter gradient kernel
+// ===========================================================================
+constexpr int WG_STAGES = 4;
+constexpr int WG_KP = 64;                 // pixels per stage (MMA K)
+constexpr int WG_A_BYTES = 128 * WG_KP * 2;   // G^T tile: 128 k x 64 pixels, 16 KB
+constexpr int WG_B_GROUP = 64 * WG_KP * 2;    // one 64-channel group x 64 pixels, 8 KB
+constexpr int WG_MAXG = 4;
+constexpr int WG_B_BYTES = WG_B_GROUP * WG_MAXG;  // 32 KB
+constexpr int WG_THREADS = 256;           // warps 0-3 gather, 4-7 epilogue (+ MMA in warp 4)
+
+struct WgradParams {
+    const __nv_bfloat16 *x;  // [N][H][W][Cpad]
+    const __nv_bfloat16 *g;  // [N][Ho][Wo][Kpad]
+    float *partial;          // [splits][C*taps][K]
+    int W, H, Cpad, C, N;
+    int Wo, Ho, Kpad, K;
+    int sx, sy, px, py, dx, dy, fw, fh;
+    long long Q;        // Wo*Ho*N pixels
+    long long chunk;    // pixels per split (multiple of 64)
+    int ngroups_total;  // taps * (Cpad/64)
+    int groups_per_tile;
+    int n_k_tiles;
+};
+
+__global__ void __launch_bounds__(WG_THREADS, 1)
+    wgrad_tc_kernel(const __grid_constant__ WgradParams p) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base =
+        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char *a_stage = base;
+    unsigned char *b_stage = base + WG_STAGES * WG_A_BYTES;
+    Smem *sm = reinterpret_cast<Smem *>(b_stage + WG_STAGES * WG_B_BYTES);
+    volatile int *abort = &sm->abort;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    const int ktile = blockIdx.x % p.n_k_tiles;
+    const int gtile = blockIdx.x / p.n_k_tiles;
+    const int k0 = ktile * 128;
+    const int g0 = gtile * p.groups_per_tile;
+    const int ng = min(p.groups_per_tile, p.ngroups_total - g0);
+    const long long q_begin = (long long)blockIdx.y * p.chunk;
+    const long long q_end = min(p.Q, q_begin + p.chunk);
+    const int nstages = (int)((q_end - q_begin + WG_KP - 1) / WG_KP);
+    const int ncols = 64 * ng;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < WG_STAGES; ++s) {
+            mbar_init(&sm->full[s], 128);
+            mbar_init(&sm->empty[s], 1);
+        }
+        mbar_init(&sm->tmem_full[0], 1);
+        sm->abort = 0;
+        fence_barrier_init();
+    }
+    if (warp == 4) tmem_alloc(&sm->tmem_base, 256);
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = sm->tmem_base;
+    const int nchunk = p.Cpad / 64;
+
+    if (warp < 4) {
+        const int t = threadIdx.x;
+        uint32_t it = 0;
+        for (int st = 0; st < nstages && !*abort; ++st, ++it) {
+            const int s = it % WG_STAGES;
+            if (!mbar_wait(&sm->empty[s], ((it / WG_STAGES) & 1) ^ 1, abort, 32u)) break;
+            const uint32_t sa = smem_u32(a_stage + s * WG_A_BYTES);
+            const uint32_t sb = smem_u32(b_stage + s * WG_B_BYTES);
+            // A: 64 pixel rows x 256 bytes (128 k) -> two MN atoms; 1024 chunks
+            for (int e = t; e < WG_KP * 16; e += 128) {
+                const int row = e >> 4, ch = e & 15;  // ch: 16-byte chunk along k
+                const long long q = q_begin + (long long)st * WG_KP + row;
+                const int atom = ch >> 3, j = ch & 7;
+                bool ok = q < q_end;
+                const __nv_bfloat16 *src = p.g;
+                if (ok) src = p.g + q * p.Kpad + k0 + 8 * ch;
+                ok = ok && (k0 + 8 * ch < p.Kpad);
+                cp_async_16(sa + atom * 8192 + (row >> 3) * 1024 + (row & 7) * 128 + ((j ^ (row & 7)) << 4),
+                            ok ? src : p.g, ok ? 16u : 0u);
+            }
+            // B: 64 pixel rows x ng groups x 128 bytes
+            for (int e = t; e < WG_KP * 8 * ng; e += 128) {
+                const int grp = e / (WG_KP * 8);
+                const int rem = e - grp * (WG_KP * 8);
+                const int row = rem >> 3, j = rem & 7;
+                const long long q = q_begin + (long long)st * WG_KP + row;
+                const int gi = g0 + grp;
+                const int tap = gi / nchunk, cchunk = gi - tap * nchunk;
+                const int u = tap % p.fw, v = tap / p.fw;
+                bool ok = q < q_end;
+                const __nv_bfloat16 *src = p.x;
+                if (ok) {
+                    const int X = (int)(q % p.Wo);
+                    const long long rest = q / p.Wo;
+                    const int Y = (int)(rest % p.Ho), n = (int)(rest / p.Ho);
+                    const int xs = X * p.sx - p.px + u * p.dx, ys = Y * p.sy - p.py + v * p.dy;
+                    ok = xs >= 0 && xs < p.W && ys >= 0 && ys < p.H;
+                    if (ok)
+                        src = p.x + (((long long)n * p.H + ys) * p.W + xs) * p.Cpad + cchunk * 64 + 8 * j;
+                }
+                cp_async_16(sb + grp * 8192 + (row >> 3) * 1024 + (row & 7) * 128 + ((j ^ (row & 7)) << 4),
+                            ok ? src : p.x, ok ? 16u : 0u);
+            }
+            cp_async_commit();
+            if (it >= LAG) {
+                cp_async_wait<LAG>();
+                fence_proxy_async_smem();
+                mbar_arrive(&sm->full[(it - LAG) % WG_STAGES]);
+            }
+        }
+        cp_async_wait_all();
+        fence_proxy_async_smem();
+        for (uint32_t k = (it >= LAG ? it - LAG : 0); k < it; ++k) mbar_arrive(&sm->full[k % WG_STAGES]);
+    } else {
+        if (warp == 4 && lane == 0) {
+            // MMA: M = 128 (k), N = 64*ng, both operands MN-major
+            const uint32_t idesc = idesc_bf16(128, (uint32_t)ncols, 1, 1);
+            for (int st = 0; st < nstages; ++st) {
+                const int s = st % WG_STAGES;
+                if (!mbar_wait(&sm->full[s], (st / WG_STAGES) & 1, abort, 64u)) break;
+                tc_fence_after();
+                const uint32_t sa = smem_u32(a_stage + s * WG_A_BYTES);
+                const uint32_t sb = smem_u32(b_stage + s * WG_B_BYTES);
+#pragma unroll
+                for (int k = 0; k < WG_KP / 16; ++k) {
+                    const uint64_t ad = smem_desc(sa + k * 2048, 8192, 1024);
+                    const uint64_t bd = smem_desc(sb + k * 2048, 8192, 1024);
+                    mma_f16(tmem_base, ad, bd, idesc, (st | k) != 0);
+                }
+                mma_commit(&sm->empty[s]);
+            }
+            mma_commit(&sm->tmem_full[0]);
+        }
+        __syncwarp();
+        // epilogue: all four warps 4-7 (TMEM lanes 32*(warp-4) ...)
+        const int q = warp - 4;
+        // wait for the MMAs even when aborting, so TMEM is never freed under them
+        bool have = false;
+        if (nstages > 0) {
+            unsigned n = 0;
+            while (!(have = mbar_try_wait(&sm->tmem_full[0], 0)) && ++n < kSpinLimit) {
+            }
+            if (!have) {
+                *abort = 1;
+                atomicOr(&g_tc_error, 128u);
+            }
+        }
+        tc_fence_after();
+        const int k = k0 + 32 * q + lane;
+        const long long rows = (long long)p.C * p.fw * p.fh;
+        float *out = p.partial + (long long)blockIdx.y * rows * p.K;
+        for (int cc = 0; cc < ncols / 16; ++cc) {
+            uint32_t r[16];
+            if (have) {
+                tmem_ld16(tmem_base + cc * 16 + ((uint32_t)(32 * q) << 16), r);
+                tmem_ld_wait();
+            } else {
+#pragma unroll
+                for (int e = 0; e < 16; ++e) r[e] = 0u;
+            }
+            if (k >= p.K || *abort) continue;
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int col = cc * 16 + e;
+                const int gi = g0 + col / 64;
+                const int tap = gi / nchunk, c = (gi - tap * nchunk) * 64 + (col & 63);
+                if (c < p.C) out[((long long)c + (long long)p.C * tap) * p.K + k] = __uint_as_float(r[e]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 4) {
+        tc_fence_after();
+        tmem_dealloc(tmem_base, 256);
+    }
+}
+
+// ===========================================================================
+// layout conversions (bandwidth-bound pre-passes)
+// ===========================================================================
+// f32 ArrayFire (W,H,C,N) -> bf16 [N][H][W][Cpad], channels >= C zero
+__global__ void to_nhwc_bf16_kernel(const float *__restrict__ in, int W, int H, int C, int N,
+                                    int Cpad, __nv_bfloat16 *__restrict__ out) {
+    __shared__ float tile[64][33];
+    const int x0 = blockIdx.x * 32;
+    const int yn = blockIdx.y;  // y + H*n
+    const int y = yn % H, n = yn / H;
+    const long long plane = (long long)W * H;
+    for (int c0 = 0; c0 < Cpad; c0 += 64) {
+        for (int i = threadIdx.y; i < 64; i += blockDim.y) {
+            const int c = c0 + i, x = x0 + threadIdx.x;
+            float v = 0.f;
+            if (c < C && x < W) v = in[x + (long long)W * y + plane * (c + (long long)C * n)];
+            tile[i][threadIdx.x] = v;
+        }
+        __syncthreads();
+        for (int px = threadIdx.y; px < 32; px += blockDim.y) {
+            const int x = x0 + px;
+            if (x < W) {
+                __nv_bfloat162 v2 = __floats2bfloat162_rn(tile[2 * threadIdx.x][px], tile[2 * threadIdx.x + 1][px]);
+                *reinterpret_cast<__nv_bfloat162 *>(out + (((long long)n * H + y) * W + x) * Cpad + c0 +
+                                                    2 * threadIdx.x) = v2;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// weights (fw,fh,C,K) f32 -> bf16 GEMM operand with the reference's flip:
+// forward  Wt[och=k][tap*Cpad + c];  data grad Wt[och=c][tap*Kpad + k]
+// with tap = u + fw*v multiplying w[fw-1-u, fh-1-v, c, k]; padded rows and
+// channels are zero
+__global__ void weights_bf16_kernel(const float *__restrict__ w, int fw, int fh, int C, int K,
+                                    int mode, int och_pad, int in_pad, __nv_bfloat16 *__restrict__ out) {
+    const long long total = (long long)och_pad * fw * fh * in_pad;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int ci = (int)(t % in_pad);
+        const long long r = t / in_pad;
+        const int tap = (int)(r % (fw * fh));
+        const int och = (int)(r / (fw * fh));
+        const int u = tap % fw, v = tap / fw;
+        const int c = mode == 0 ? ci : och;
+        const int k = mode == 0 ? och : ci;
+        float val = 0.f;
+        if (c < C && k < K) val = w[(fw - 1 - u) + fw * ((fh - 1 - v) + fh * (c + (long long)C * k))];
+        out[t] = __float2bfloat16_rn(val);
+    }
+}
+
+// ===========================================================================
+// host side
+// ===========================================================================
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                             &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    });
+    if (!fn) AFGB_THROW(AF_ERR_DRIVER, "cuTensorMapEncodeTiled is unavailable");
+    return fn;
+}
+
+// 2-D bf16 tensor [rows][cols] (cols contiguous), box 64 x 128, 128B swizzle
+static CUtensorMap make_wmap(const __nv_bfloat16 *ptr, long long rows, long long cols) {
+    CUtensorMap m;
+    cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
+    cuuint32_t box[2] = {64, 128};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)ptr, dims, strides, box,
+                             es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) AFGB_THROW(AF_ERR_INTERNAL, "cuTensorMapEncodeTiled failed");
+    return m;
+}
+
+static int round_up(int v, int m) { return (v + m - 1) / m * m; }
+
+static __nv_bfloat16 *to_nhwc(const float *src, int W, int H, int C, int N, int Cpad) {
+    __nv_bfloat16 *out =
+        static_cast<__nv_bfloat16 *>(alloc_device((size_t)W * H * N * Cpad * sizeof(__nv_bfloat16)));
+    dim3 grid((unsigned)((W + 31) / 32), (unsigned)(H * N));
+    {
+        KernelTimer kt("tc_convert_kernel");
+        to_nhwc_bf16_kernel<<<grid, dim3(32, 8), 0, stream()>>>(src, W, H, C, N, Cpad, out);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("to_nhwc_bf16_kernel");
+    return out;
+}
+
+static size_t gather_smem() { return 1024 + STAGES * (A_BYTES + B_BYTES) + sizeof(Smem) + 64; }
+
+// forward (mode 0) or data gradient (mode 1)
+static void run_gather(const NNGeom &g, int mode, const float *img_f32, const float *w_f32,
+                       float *dst) {
+    const int SW = mode == 0 ? (int)g.W : (int)g.Wo;
+    const int SH = mode == 0 ? (int)g.H : (int)g.Ho;
+    const int SC = mode == 0 ? (int)g.C : (int)g.K;
+    const int DW = mode == 0 ? (int)g.Wo : (int)g.W;
+    const int DH = mode == 0 ? (int)g.Ho : (int)g.H;
+    const int DC = mode == 0 ? (int)g.K : (int)g.C;
+    const int SCpad = round_up(SC, 64);
+    const int OCpad = round_up(DC, 128);
+    const int taps = (int)(g.fw * g.fh);
+
+    __nv_bfloat16 *img = to_nhwc(img_f32, SW, SH, SC, (int)g.N, SCpad);
+    __nv_bfloat16 *wt =
+        static_cast<__nv_bfloat16 *>(alloc_device((size_t)OCpad * taps * SCpad * sizeof(__nv_bfloat16)));
+    {
+        long long total = (long long)OCpad * taps * SCpad;
+        unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
+        weights_bf16_kernel<<<blocks, 256, 0, stream()>>>(w_f32, (int)g.fw, (int)g.fh, (int)g.C,
+                                                          (int)g.K, mode, OCpad, SCpad, wt);
+        count_launch();
+        AFGB_POST_LAUNCH("weights_bf16_kernel");
+    }
+
+    GatherParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.src = img;
+    p.dst = dst;
+    p.SW = SW;
+    p.SH = SH;
+    p.SCpad = SCpad;
+    p.N = (int)g.N;
+    p.DW = DW;
+    p.DH = DH;
+    p.DC = DC;
+    p.mode = mode;
+    p.sx = (int)g.sx;
+    p.sy = (int)g.sy;
+    p.px = (int)g.px;
+    p.py = (int)g.py;
+    p.dx = (int)g.dx;
+    p.dy = (int)g.dy;
+    p.fw = (int)g.fw;
+    p.nchunk = SCpad / 64;
+    p.n_och_tiles = OCpad / 128;
+    p.nphx = mode == 0 ? 1 : (int)g.sx;
+    p.nphase = mode == 0 ? 1 : (int)(g.sx * g.sy);
+    int ntap = 0, ntile = 0;
+    for (int ph = 0; ph < p.nphase; ++ph) {
+        const int rx = ph % p.nphx, ry = ph / p.nphx;
+        p.phase_tap_begin[ph] = ntap;
+        p.phase_tile_begin[ph] = ntile;
+        for (int v = 0; v < g.fh; ++v) {
+            if (mode == 1 && (((ry + g.py - v * g.dy) % g.sy) + g.sy) % g.sy != 0) continue;
+            for (int u = 0; u < g.fw; ++u) {
+                if (mode == 1 && (((rx + g.px - u * g.dx) % g.sx) + g.sx) % g.sx != 0) continue;
+                p.tap_u[ntap] = (short)u;
+                p.tap_v[ntap] = (short)v;
+                ++ntap;
+            }
+        }
+        long long MX = mode == 0 ? DW : (DW - rx + g.sx - 1) / g.sx;
+        long long MY = mode == 0 ? DH : (DH - ry + g.sy - 1) / g.sy;
+        long long npix = std::max(0LL, MX) * std::max(0LL, MY) * g.N;
+        ntile += (int)((npix + BN - 1) / BN) * p.n_och_tiles;
+    }
+    p.phase_tap_begin[p.nphase] = ntap;
+    p.phase_tile_begin[p.nphase] = ntile;
+    p.total_tiles = ntile;
+
+    CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad);
+    const size_t smem = gather_smem();
+    AFGB_CUDA(cudaFuncSetAttribute(gather_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+    if (ntile > 0) {
+        const int grid = std::min(ntile, num_sms());
+        KernelTimer kt(mode == 0 ? "tc_fwd_kernel" : "tc_dgrad_kernel");
+        gather_conv_kernel<<<grid, NUM_THREADS, smem, stream()>>>(p, wmap);
+        count_launch();
+        AFGB_POST_LAUNCH("gather_conv_kernel");
+    }
+    free_device(wt);
+    free_device(img);
+}
+
+// the gather kernel's limits: phases and taps fit the parameter block,
+// 32-bit pixel indexing inside a tile
+static bool gather_fits(const NNGeom &g, int mode) {
+    if (g.fw * g.fh > MAX_T) return false;
+    if (mode == 1 && g.sx * g.sy > MAX_PH) return false;
+    if (g.W > (1 << 20) || g.H > (1 << 20)) return false;
+    return true;
+}
+
+}  // namespace tc
+
+using namespace tc;
+
+unsigned int tc_take_error() {
+    unsigned int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, g_tc_error, sizeof(v)) != cudaSuccess) return 0;
+    if (v) (void)cudaMemcpyToSymbol(g_tc_error, &zero, sizeof(zero));
+    return v;
+}
+
+bool tc_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out,
+                afgb_precision prec, const Array *scales) {
+    if (prec != AFGB_PRECISION_BF16) return false;  // FP8 arrives with its own kernel
+    (void)scales;
+    if (sig.type != f32 || !gather_fits(g, 0)) return false;
+    run_gather(g, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>());
+    return true;
+}
+
+bool tc_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &dx) {
+    if (grad.type != f32 || !gather_fits(g, 1)) return false;
+    run_gather(g, 1, grad.ptr<float>(), filt.ptr<float>(), dx.ptr<float>());
+    return true;
+}
+
+bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw) {
+    if (grad.type != f32) return false;
+    const int Cpad = round_up((int)g.C, 64);
+    const int Kpad = round_up((int)g.K, 128);
+    __nv_bfloat16 *x = to_nhwc(sig.ptr<float>(), (int)g.W, (int)g.H, (int)g.C, (int)g.N, Cpad);
+    __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kpad);
+    WgradParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.x = x;
+    p.g = gg;
+    p.W = (int)g.W;
+    p.H = (int)g.H;
+    p.Cpad = Cpad;
+    p.C = (int)g.C;
+    p.N = (int)g.N;
+    p.Wo = (int)g.Wo;
+    p.Ho = (int)g.Ho;
+    p.Kpad = Kpad;
+    p.K = (int)g.K;
+    p.sx = (int)g.sx;
+    p.sy = (int)g.sy;
+    p.px = (int)g.px;
+    p.py = (int)g.py;
+    p.dx = (int)g.dx;
+    p.dy = (int)g.dy;
+    p.fw = (int)g.fw;
+    p.fh = (int)g.fh;
+    p.Q = g.Wo * g.Ho * g.N;
+    p.ngroups_total = (int)(g.fw * g.fh) * (Cpad / 64);
+    // groups per tile: fewest tiles, then least padding
+    int best = 4, best_tiles = 1 << 30;
+    for (int gp = 4; gp >= 1; --gp) {
+        int tiles = (p.ngroups_total + gp - 1) / gp;
+        if (tiles < best_tiles) {
+            best_tiles = tiles;
+            best = gp;
+        }
+    }
+    // prefer a tile width that divides the groups evenly when it costs no extra tile
+    for (int gp = 4; gp >= 1; --gp) {
+        if (p.ngroups_total % gp == 0 && (p.ngroups_total / gp) <= best_tiles) {
+            best = gp;
+            break;
+        }
+    }
+    p.groups_per_tile = best;
+    p.n_k_tiles = Kpad / 128;
+    const long long ntiles = (long long)p.n_k_tiles * ((p.ngroups_total + best - 1) / best);
+    long long target = (long long)num_sms() * 2;
+    long long splits = std::max(1LL, target / std::max(1LL, ntiles));
+    long long chunk = (p.Q + splits - 1) / splits;
+    chunk = std::max<long long>(1024, (chunk + WG_KP - 1) / WG_KP * WG_KP);
+    splits = (p.Q + chunk - 1) / chunk;
+    p.chunk = chunk;
+    const long long rows = g.C * g.fw * g.fh;
+    float *partial = static_cast<float *>(alloc_device((size_t)(splits * rows * g.K) * sizeof(float)));
+    p.partial = partial;
+    const size_t smem = 1024 + WG_STAGES * (WG_A_BYTES + WG_B_BYTES) + sizeof(Smem) + 64;
+    AFGB_CUDA(cudaFuncSetAttribute(wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+    {
+        KernelTimer kt("tc_wgrad_kernel");
+        wgrad_tc_kernel<<<dim3((unsigned)ntiles, (unsigned)splits), WG_THREADS, smem, stream()>>>(p);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("wgrad_tc_kernel");
+    // fixed-order compensated reduction over splits, flipped into (fw,fh,C,K)
+    reduce_filter_partials(g, partial, (int)splits, dw.ptr<float>());
+    free_device(partial);
+    free_device(gg);
+    free_device(x);
+    return true;
+}
 
 }  // namespace afgb

@@ -112,7 +112,7 @@ def direct_cases():
 SEP_SHAPES = [
     ("sep_5x3", (40, 33), 5, 3),
     ("sep_15", (70, 66, 2), 15, 15),
-    ("sep_1x7", (31, 29), 1, 7),
+    ("sep_2x7", (31, 29), 2, 7),
     ("sep_31", (80, 70), 31, 31),
     ("sep_batch4d", (20, 21, 2, 2), 3, 5),
 ]

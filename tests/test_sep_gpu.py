@@ -80,7 +80,7 @@ def test_sep_scalar_filters(af, oracle):
     """Both filters scalar: element-wise shortcut (src/api/c/convolve.cpp:57-68)."""
     s = C.sep_signal(C.F32, (9, 7), 3)
     out = run(af, s, np.array([2.0], np.float32), np.array([0.5], np.float32), C.F32, True)
-    np.testing.assert_array_equal(out[:, :, 0, 0], s * np.float32(1.0))
+    np.testing.assert_array_equal(out[:, :, 0, 0], s[:, :, 0, 0] * np.float32(1.0))
 
 
 def test_sep_rejections(af):
@@ -95,6 +95,12 @@ def test_sep_rejections(af):
     m = af.Array.from_numpy(np.ones((3, 3), np.float32))
     with pytest.raises(af.AfError) as e:
         af.convolve2_separable(m, f4, S2, af.AF_CONV_DEFAULT)
+    assert e.value.code == af.AF_ERR_ARG
+    # a one-tap filter next to a longer one is not a vector and not a
+    # scalar pair: AF_ERR_ARG (src/api/c/convolve.cpp:57-71)
+    one = af.Array.from_numpy(np.ones(1, np.float32))
+    with pytest.raises(af.AfError) as e:
+        af.convolve2_separable(one, f4, S2, af.AF_CONV_DEFAULT)
     assert e.value.code == af.AF_ERR_ARG
     long = af.Array.from_numpy(np.ones(33, np.float32))
     with pytest.raises(af.AfError) as e:

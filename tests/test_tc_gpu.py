@@ -1,0 +1,97 @@
+"""GPU parity of the BF16 tensor-core (tcgen05) form of af_convolve2_nn and
+its gradients, through the C ABI (afgb_convolve2_nn_ex /
+afgb_convolve2_gradient_nn_ex), against the FP64 oracle.
+
+Tolerance: norm-wise relative error ||gpu - ref|| / ||ref|| <= 1e-2 per
+output (the target bound is 2e-2; bf16 operands with FP32 accumulation give
+~3e-3), and max-abs error <= 4e-2 * max|ref|.
+"""
+import numpy as np
+import pytest
+
+import cases as C
+
+pytestmark = pytest.mark.gpu
+
+REL = 1e-2
+
+TC_CASES = C.NN_CASES + [
+    ("tc_c64_k128", (24, 20, 64, 2), (3, 3, 64, 128), (1, 1), (1, 1), (1, 1)),
+    ("tc_c128_k256_s2", (33, 31, 128, 2), (3, 3, 128, 256), (2, 2), (1, 1), (1, 1)),
+    ("tc_5x5_d2_p4_s2", (30, 28, 32, 2), (5, 5, 32, 64), (2, 2), (4, 4), (2, 2)),
+    ("tc_c200_k130", (17, 19, 200, 3), (3, 3, 200, 130), (1, 1), (1, 1), (1, 1)),
+    ("tc_1x1_c256", (28, 28, 256, 2), (1, 1, 256, 192), (1, 1), (0, 0), (1, 1)),
+]
+
+
+def check(out, ref, what):
+    ref = np.asarray(ref, np.float64)
+    out = np.asarray(out, np.float64)
+    rel = np.linalg.norm(out - ref) / max(np.linalg.norm(ref), 1e-30)
+    mx = np.abs(out - ref).max() / max(np.abs(ref).max(), 1e-30)
+    assert rel <= REL and mx <= 4 * REL, f"{what}: rel {rel:.3e} max {mx:.3e}"
+    return rel
+
+
+@pytest.mark.parametrize("i,case", list(enumerate(TC_CASES)), ids=[c[0] for c in TC_CASES])
+def test_bf16_forward(af, oracle, i, case):
+    name, sd, fd, st, pd, dl = case
+    s, f = C.nn_inputs(case, 7000 + 10 * i)
+    out = af.convolve2_nn(af.Array.from_numpy(s), af.Array.from_numpy(f), st, pd, dl,
+                          precision="bf16").to_numpy()
+    ref = oracle.nn_forward_f64(s, f, st, pd, dl)
+    assert out.shape == ref.shape
+    check(out, ref, "fwd")
+
+
+@pytest.mark.parametrize("i,case", list(enumerate(TC_CASES)), ids=[c[0] for c in TC_CASES])
+def test_bf16_data_grad(af, oracle, i, case):
+    name, sd, fd, st, pd, dl = case
+    s, f = C.nn_inputs(case, 7000 + 10 * i)
+    g = C.nn_grad(case, 7000 + 10 * i)
+    S, F, G = af.Array.from_numpy(s), af.Array.from_numpy(f), af.Array.from_numpy(g)
+    O = af.convolve2_nn(S, F, st, pd, dl)
+    dx = af.convolve2_gradient_nn(G, S, F, O, st, pd, dl, af.AF_CONV_GRADIENT_DATA,
+                                  precision="bf16").to_numpy()
+    check(dx, oracle.nn_data_grad_f64(g, list(s.shape), f, st, pd, dl), "dgrad")
+
+
+@pytest.mark.parametrize("i,case", list(enumerate(TC_CASES)), ids=[c[0] for c in TC_CASES])
+def test_bf16_filter_grad(af, oracle, i, case):
+    name, sd, fd, st, pd, dl = case
+    s, f = C.nn_inputs(case, 7000 + 10 * i)
+    g = C.nn_grad(case, 7000 + 10 * i)
+    S, F, G = af.Array.from_numpy(s), af.Array.from_numpy(f), af.Array.from_numpy(g)
+    O = af.convolve2_nn(S, F, st, pd, dl)
+    dw = af.convolve2_gradient_nn(G, S, F, O, st, pd, dl, af.AF_CONV_GRADIENT_FILTER,
+                                  precision="bf16").to_numpy()
+    check(dw, oracle.nn_filter_grad_f64(g, s, list(f.shape), st, pd, dl), "wgrad")
+
+
+def test_bf16_filter_grad_deterministic(af):
+    """The split-K reduction order is fixed: two calls give identical bits."""
+    case = TC_CASES[-4]
+    name, sd, fd, st, pd, dl = case
+    s, f = C.nn_inputs(case, 1)
+    g = C.nn_grad(case, 1)
+    S, F, G = af.Array.from_numpy(s), af.Array.from_numpy(f), af.Array.from_numpy(g)
+    O = af.convolve2_nn(S, F, st, pd, dl)
+    a = af.convolve2_gradient_nn(G, S, F, O, st, pd, dl, af.AF_CONV_GRADIENT_FILTER,
+                                 precision="bf16").to_numpy()
+    b = af.convolve2_gradient_nn(G, S, F, O, st, pd, dl, af.AF_CONV_GRADIENT_FILTER,
+                                 precision="bf16").to_numpy()
+    assert a.tobytes() == b.tobytes()
+
+
+def test_bf16_config3a_sampled(af, oracle):
+    """The benchmark forward shape (128x128x64x32 * 3x3x64x128) against FP64
+    on 512 sampled outputs."""
+    g = C.rng(33)
+    s = np.asfortranarray(g.standard_normal((128, 128, 64, 32), dtype=np.float32))
+    f = np.asfortranarray((g.standard_normal((3, 3, 64, 128)) * np.sqrt(2 / 576)).astype(np.float32))
+    out = af.convolve2_nn(af.Array.from_numpy(s), af.Array.from_numpy(f), (1, 1), (1, 1), (1, 1),
+                          precision="bf16").to_numpy().ravel(order="F")
+    idx = g.integers(0, out.size, 512)
+    ref = oracle.nn_forward_points_f64(s, f, (1, 1), (1, 1), (1, 1), idx)
+    rel = np.linalg.norm(out[idx] - ref) / np.linalg.norm(ref)
+    assert rel <= REL
