@@ -3,26 +3,29 @@
 //
 // The reference runs these as unwrap + GEMM (src/backend/cpu/convolve.cpp:
 // 123-243, src/backend/cuda/convolveNN.cpp:175-407) or hands them to cuDNN.
-// Here each is one implicit GEMM whose operands are gathered straight from
-// the image, so no unwrapped patch matrix exists:
+// Here each is one implicit GEMM whose operands are fetched straight from the
+// image, so no unwrapped patch matrix exists:
 //
 //   gather kernel  D[och][pixel] = sum_{cchunk, tap} Wt[och][tap, c] * Img[pixel@tap][c]
 //       forward:   Img = signal (NHWC bf16), och = filter K, taps all (u,v)
-//       data grad: Img = incoming gradient, och = C, one launch covers every
-//                  stride phase (x' mod sx, y' mod sy) with that phase's taps,
-//                  so no zero-stuffed products are issued
-//     MMA M=128 output channels (weights, TMA-loaded, K-major, 128B swizzle),
-//     N=256 output pixels (cp.async row gather of 64-channel pixel rows,
-//     zero-filled outside the image), K=64 channels per stage, 4 stages.
-//     Persistent CTAs, warp-specialised: 4 gather warps, 4 epilogue warps
-//     (TMEM -> registers -> f32 ArrayFire layout), 1 MMA warp, 1 TMA warp;
-//     the 256-column accumulator is double-buffered in TMEM (512 columns)
-//     so the epilogue of one tile overlaps the main loop of the next.
+//       data grad: Img = incoming gradient, och = C; with stride > 1 one
+//                  launch covers every stride phase (x' mod sx, y' mod sy)
+//                  with that phase's taps, so no zero-stuffed products run
+//     MMA M=128 output channels (weights: TMA, K-major, 128B swizzle),
+//     N=256 output pixels, K=64 channels per stage, 4 stages.
+//     Pixel operand: for stride 1 a 4-D TMA box {64 ch, BX, BY, 1} over the
+//     NHWC tensor — a BX x BY pixel rectangle shifted by the tap, zero-filled
+//     outside the image (the convolution's padding); for other strides a
+//     cp.async row gather by four producer warps.
+//     Persistent CTAs, warp-specialised (producers, 4 epilogue warps, one MMA
+//     warp, one TMA warp); the 256-column accumulator is double-buffered in
+//     TMEM (512 columns) so one tile's epilogue overlaps the next main loop.
 //
 //   wgrad kernel   D[k][(tap,c)] = sum_{pixels} G[pixel][k] * X[pixel@tap][c]
 //     reduction over pixels: both operands are pixel rows, i.e. MN-major
-//     shared-memory tiles; split-K over pixel ranges, FP32 partials combined
-//     by a fixed-order compensated reduction (deterministic).
+//     shared-memory tiles (TMA boxes for stride 1, cp.async rows otherwise);
+//     split-K over pixel blocks, FP32 partials combined by a fixed-order
+//     compensated reduction (deterministic).
 //
 // Inputs and outputs stay f32 ArrayFire arrays; conversion to bf16
 // channels-last happens on the device in bandwidth-bound pre-passes.
@@ -42,16 +45,16 @@
 namespace afgb {
 namespace tc {
 
-constexpr int BM = 128;            // output channels per tile (MMA M)
-constexpr int BN = 256;            // output pixels per tile (MMA N)
-constexpr int BK = 64;             // input channels per stage (128 bytes of bf16)
+constexpr int BM = 128;               // output channels per tile (MMA M)
+constexpr int BN = 256;               // output pixels per tile (MMA N)
+constexpr int BK = 64;                // input channels per stage (128 bytes of bf16)
 constexpr int STAGES = 4;
-constexpr int A_BYTES = BM * BK * 2;   // 16 KB weight tile
-constexpr int B_BYTES = BN * BK * 2;   // 32 KB pixel tile
-constexpr int LAG = 2;             // cp.async groups in flight per producer
+constexpr int A_BYTES = BM * BK * 2;  // 16 KB weight tile
+constexpr int B_BYTES = BN * BK * 2;  // 32 KB pixel tile
+constexpr int LAG = 2;                // cp.async groups in flight per producer
 constexpr int MAX_PH = 64;
 constexpr int MAX_T = 256;
-constexpr int NUM_THREADS = 320;   // warps 0-3 gather, 4-7 epilogue, 8 MMA, 9 TMA
+constexpr int NUM_THREADS = 320;      // warps 0-3 gather, 4-7 epilogue, 8 MMA, 9 TMA
 
 struct GatherParams {
     const __nv_bfloat16 *src;  // [N][SH][SW][SCpad]
@@ -64,13 +67,13 @@ struct GatherParams {
     int n_och_tiles;  // ceil(DC / 128)
     int nphase, nphx;
     int total_tiles;
+    int BX, BY, ntx, nty;  // pixel rectangles (TMA path)
     int phase_tile_begin[MAX_PH + 1];
     int phase_tap_begin[MAX_PH + 1];
     short tap_u[MAX_T], tap_v[MAX_T];
 };
 
 struct Smem {
-    // operand stages are carved from the 1024-aligned dynamic buffer
     uint64_t full[STAGES];
     uint64_t empty[STAGES];
     uint64_t tmem_full[2];
@@ -81,24 +84,45 @@ struct Smem {
 };
 
 struct TileInfo {
-    int ph, rx, ry, tap_begin, ntaps;
-    long long p0, npix;  // first pixel of the tile, pixels in this phase
-    int MX, MY;
+    int rx, ry, tap_begin, ntaps;
     int och0;
+    // gather path: linear pixel range of one stride phase
+    long long p0, npix;
+    int MX, MY;
+    // TMA path: pixel rectangle
+    int x0, y0, n;
 };
 
+template <bool TMA_B>
 __device__ __forceinline__ TileInfo decode_tile(const GatherParams &p, int tile) {
     TileInfo t;
+    if (TMA_B) {
+        t.rx = t.ry = 0;
+        t.tap_begin = 0;
+        t.ntaps = p.phase_tap_begin[1];
+        t.och0 = (tile % p.n_och_tiles) * BM;
+        int r = tile / p.n_och_tiles;
+        const int tx = r % p.ntx;
+        r /= p.ntx;
+        const int ty = r % p.nty;
+        t.n = r / p.nty;
+        t.x0 = tx * p.BX;
+        t.y0 = ty * p.BY;
+        t.p0 = 0;
+        t.npix = 0;
+        t.MX = p.DW;
+        t.MY = p.DH;
+        return t;
+    }
     int ph = 0;
     while (ph + 1 < p.nphase && tile >= p.phase_tile_begin[ph + 1]) ++ph;
-    t.ph = ph;
     t.rx = ph % p.nphx;
     t.ry = ph / p.nphx;
     t.tap_begin = p.phase_tap_begin[ph];
     t.ntaps = p.phase_tap_begin[ph + 1] - p.phase_tap_begin[ph];
-    int local = tile - p.phase_tile_begin[ph];
+    const int local = tile - p.phase_tile_begin[ph];
     t.och0 = (local % p.n_och_tiles) * BM;
-    int ptile = local / p.n_och_tiles;
+    const int ptile = local / p.n_och_tiles;
     if (p.mode == 0) {
         t.MX = p.DW;
         t.MY = p.DH;
@@ -108,17 +132,31 @@ __device__ __forceinline__ TileInfo decode_tile(const GatherParams &p, int tile)
     }
     t.npix = (long long)t.MX * t.MY * p.N;
     t.p0 = (long long)ptile * BN;
+    t.x0 = t.y0 = t.n = 0;
     return t;
 }
 
+__device__ __forceinline__ void tap_offsets(const GatherParams &p, const TileInfo &ti, int u, int v,
+                                            int &offx, int &offy) {
+    if (p.mode == 0) {
+        offx = u * p.dx - p.px;
+        offy = v * p.dy - p.py;
+    } else {
+        offx = (ti.rx + p.px - u * p.dx) / p.sx;
+        offy = (ti.ry + p.py - v * p.dy) / p.sy;
+    }
+}
+
+template <bool TMA_B>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     gather_conv_kernel(const __grid_constant__ GatherParams p,
-                       const __grid_constant__ CUtensorMap wmap) {
+                       const __grid_constant__ CUtensorMap wmap,
+                       const __grid_constant__ CUtensorMap xmap) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char *base =
-        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    unsigned char *a_stage = base;                       // STAGES x 16 KB
-    unsigned char *b_stage = base + STAGES * A_BYTES;    // STAGES x 32 KB
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char *a_stage = base;                     // STAGES x 16 KB
+    unsigned char *b_stage = base + STAGES * A_BYTES;  // STAGES x 32 KB
     Smem *sm = reinterpret_cast<Smem *>(b_stage + STAGES * B_BYTES);
     volatile int *abort = &sm->abort;
 
@@ -127,7 +165,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; ++s) {
-            mbar_init(&sm->full[s], 128 + 1);
+            mbar_init(&sm->full[s], TMA_B ? 1 : 128 + 1);
             mbar_init(&sm->empty[s], 1);
         }
         for (int b = 0; b < 2; ++b) {
@@ -139,98 +177,99 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         fence_barrier_init();
     }
     if (warp == 8) tmem_alloc(&sm->tmem_base, 512);
-    if (warp == 9 && lane == 0) prefetch_tmap(&wmap);
+    if (warp == 9 && lane == 0) {
+        prefetch_tmap(&wmap);
+        if (TMA_B) prefetch_tmap(&xmap);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = sm->tmem_base;
 
     if (warp < 4) {
-        // ---------------- pixel-row gather (128 threads)
-        const int t = threadIdx.x;
-        const int j = t & 7;          // 16-byte chunk within the 128-byte row
-        const int r0 = t >> 3;        // rows r0 + 16 i
-        const int alpha_x = p.mode == 0 ? p.sx : 1;
-        const int alpha_y = p.mode == 0 ? p.sy : 1;
-        const long long img_stride = (long long)p.SH * p.SW * p.SCpad;
-        uint32_t it = 0;
-        for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
-            TileInfo ti = decode_tile(p, tile);
-            if (ti.ntaps == 0) continue;
-            int xb[16], yb[16], nb[16];
-            uint32_t vmask = 0;
-#pragma unroll
-            for (int i = 0; i < 16; ++i) {
-                long long pix = ti.p0 + r0 + 16 * i;
-                if (pix < ti.npix) {
-                    int X = (int)(pix % ti.MX);
-                    long long rest = pix / ti.MX;
-                    int Y = (int)(rest % ti.MY);
-                    nb[i] = (int)(rest / ti.MY);
-                    xb[i] = X * alpha_x;
-                    yb[i] = Y * alpha_y;
-                    vmask |= 1u << i;
-                } else {
-                    xb[i] = yb[i] = nb[i] = 0;
-                }
-            }
-            const int iters = p.nchunk * ti.ntaps;
-            for (int kb = 0; kb < iters; ++kb, ++it) {
-                const int s = it % STAGES;
-                if (!mbar_wait(&sm->empty[s], ((it / STAGES) & 1) ^ 1, abort, 1u)) break;
-                const int cchunk = kb / ti.ntaps;
-                const int tq = ti.tap_begin + (kb - cchunk * ti.ntaps);
-                const int u = p.tap_u[tq], v = p.tap_v[tq];
-                int offx, offy;
-                if (p.mode == 0) {
-                    offx = u * p.dx - p.px;
-                    offy = v * p.dy - p.py;
-                } else {
-                    offx = (ti.rx + p.px - u * p.dx) / p.sx;
-                    offy = (ti.ry + p.py - v * p.dy) / p.sy;
-                }
-                const uint32_t sb = smem_u32(b_stage + s * B_BYTES);
-                const __nv_bfloat16 *cbase = p.src + cchunk * BK + 8 * j;
+        if (!TMA_B) {
+            // ---------------- pixel-row gather (128 threads)
+            const int t = threadIdx.x;
+            const int j = t & 7;    // 16-byte chunk within the 128-byte row
+            const int r0 = t >> 3;  // rows r0 + 16 i
+            const int alpha_x = p.mode == 0 ? p.sx : 1;
+            const int alpha_y = p.mode == 0 ? p.sy : 1;
+            const long long img_stride = (long long)p.SH * p.SW * p.SCpad;
+            uint32_t it = 0;
+            for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
+                TileInfo ti = decode_tile<false>(p, tile);
+                if (ti.ntaps == 0) continue;
+                int xb[16], yb[16], nb[16];
+                uint32_t vmask = 0;
 #pragma unroll
                 for (int i = 0; i < 16; ++i) {
-                    const int r = r0 + 16 * i;
-                    const int xs = xb[i] + offx, ys = yb[i] + offy;
-                    const bool ok = ((vmask >> i) & 1u) && xs >= 0 && xs < p.SW && ys >= 0 &&
-                                    ys < p.SH;
-                    const __nv_bfloat16 *src =
-                        ok ? cbase + nb[i] * img_stride + ((long long)ys * p.SW + xs) * p.SCpad
-                           : p.src;
-                    cp_async_16(sb + r * 128 + ((j ^ (r & 7)) << 4), src, ok ? 16u : 0u);
+                    const long long pix = ti.p0 + r0 + 16 * i;
+                    if (pix < ti.npix) {
+                        const int X = (int)(pix % ti.MX);
+                        const long long rest = pix / ti.MX;
+                        const int Y = (int)(rest % ti.MY);
+                        nb[i] = (int)(rest / ti.MY);
+                        xb[i] = X * alpha_x;
+                        yb[i] = Y * alpha_y;
+                        vmask |= 1u << i;
+                    } else {
+                        xb[i] = yb[i] = nb[i] = 0;
+                    }
                 }
-                cp_async_commit();
-                if (it >= LAG) {
-                    cp_async_wait<LAG>();
-                    fence_proxy_async_smem();
-                    mbar_arrive(&sm->full[(it - LAG) % STAGES]);
+                const int iters = p.nchunk * ti.ntaps;
+                for (int kb = 0; kb < iters; ++kb, ++it) {
+                    const int s = it % STAGES;
+                    if (!mbar_wait(&sm->empty[s], ((it / STAGES) & 1) ^ 1, abort, 1u)) break;
+                    const int cchunk = kb / ti.ntaps;
+                    const int tq = ti.tap_begin + (kb - cchunk * ti.ntaps);
+                    int offx, offy;
+                    tap_offsets(p, ti, p.tap_u[tq], p.tap_v[tq], offx, offy);
+                    const uint32_t sb = smem_u32(b_stage + s * B_BYTES);
+                    const __nv_bfloat16 *cbase = p.src + cchunk * BK + 8 * j;
+#pragma unroll
+                    for (int i = 0; i < 16; ++i) {
+                        const int r = r0 + 16 * i;
+                        const int xs = xb[i] + offx, ys = yb[i] + offy;
+                        const bool ok = ((vmask >> i) & 1u) && xs >= 0 && xs < p.SW && ys >= 0 &&
+                                        ys < p.SH;
+                        const __nv_bfloat16 *src =
+                            ok ? cbase + nb[i] * img_stride + ((long long)ys * p.SW + xs) * p.SCpad
+                               : p.src;
+                        cp_async_16(sb + r * 128 + ((j ^ (r & 7)) << 4), src, ok ? 16u : 0u);
+                    }
+                    cp_async_commit();
+                    if (it >= LAG) {
+                        cp_async_wait<LAG>();
+                        fence_proxy_async_smem();
+                        mbar_arrive(&sm->full[(it - LAG) % STAGES]);
+                    }
                 }
             }
+            cp_async_wait_all();
+            fence_proxy_async_smem();
+            for (uint32_t k = (it >= LAG ? it - LAG : 0); k < it; ++k)
+                mbar_arrive(&sm->full[k % STAGES]);
         }
-        cp_async_wait_all();
-        fence_proxy_async_smem();
-        for (uint32_t k = (it >= LAG ? it - LAG : 0); k < it; ++k) mbar_arrive(&sm->full[k % STAGES]);
     } else if (warp < 8) {
         // ---------------- epilogue (128 threads, TMEM lanes 32*(warp%4) ..)
         const int q = warp & 3;
         uint32_t acc_it = 0;
         const long long plane = (long long)p.DW * p.DH;
+        const bool vec_rows = (p.DW & 3) == 0;
         for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
-            TileInfo ti = decode_tile(p, tile);
+            TileInfo ti = decode_tile<TMA_B>(p, tile);
             const int och = ti.och0 + 32 * q + lane;
-            if (ti.ntaps == 0) {
+            if (!TMA_B && ti.ntaps == 0) {
                 // a stride phase no tap reaches: its gradient is zero
                 if (och < p.DC) {
                     for (int e = 0; e < BN; ++e) {
-                        long long pix = ti.p0 + e;
+                        const long long pix = ti.p0 + e;
                         if (pix >= ti.npix) break;
-                        int X = (int)(pix % ti.MX);
-                        long long rest = pix / ti.MX;
-                        int Y = (int)(rest % ti.MY), n = (int)(rest / ti.MY);
-                        long long xo = ti.rx + (long long)p.sx * X, yo = ti.ry + (long long)p.sy * Y;
+                        const int X = (int)(pix % ti.MX);
+                        const long long rest = pix / ti.MX;
+                        const int Y = (int)(rest % ti.MY), n = (int)(rest / ti.MY);
+                        const long long xo = ti.rx + (long long)p.sx * X;
+                        const long long yo = ti.ry + (long long)p.sy * Y;
                         p.dst[xo + p.DW * yo + plane * (och + (long long)p.DC * n)] = 0.0f;
                     }
                 }
@@ -240,42 +279,50 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             if (!mbar_wait(&sm->tmem_full[b], (acc_it >> 1) & 1, abort, 2u)) break;
             tc_fence_after();
             const uint32_t taddr = tmem_base + (uint32_t)(b * BN) + ((uint32_t)(32 * q) << 16);
+            float *dplane = p.dst + plane * ((long long)och + (long long)p.DC * (TMA_B ? ti.n : 0));
             for (int cc = 0; cc < BN / 16; ++cc) {
                 uint32_t r[16];
                 tmem_ld16(taddr + cc * 16, r);
                 tmem_ld_wait();
                 if (och >= p.DC) continue;
-                const long long pix0 = ti.p0 + cc * 16;
-                if (pix0 >= ti.npix) continue;
-                if (p.mode == 0) {
-                    const long long n0 = pix0 / plane, n1 = (pix0 + 15) / plane;
-                    if (n0 == n1 && pix0 + 15 < ti.npix && (plane & 3) == 0) {
-                        float4 *d = reinterpret_cast<float4 *>(
-                            p.dst + (pix0 - n0 * plane) + plane * (och + (long long)p.DC * n0));
+                if (TMA_B) {
+                    // 16 consecutive pixels of one rectangle row (BX >= 16)
+                    const int e0 = cc * 16;
+                    const int x = ti.x0 + (e0 % p.BX), y = ti.y0 + e0 / p.BX;
+                    if (y >= p.DH || x >= p.DW) continue;
+                    float *d = dplane + x + (long long)p.DW * y;
+                    if (vec_rows && x + 15 < p.DW) {
 #pragma unroll
                         for (int e = 0; e < 4; ++e)
-                            d[e] = make_float4(__uint_as_float(r[4 * e]), __uint_as_float(r[4 * e + 1]),
-                                               __uint_as_float(r[4 * e + 2]),
-                                               __uint_as_float(r[4 * e + 3]));
-                        continue;
-                    }
-                }
-#pragma unroll
-                for (int e = 0; e < 16; ++e) {
-                    const long long pix = pix0 + e;
-                    if (pix >= ti.npix) break;
-                    int X = (int)(pix % ti.MX);
-                    long long rest = pix / ti.MX;
-                    int Y = (int)(rest % ti.MY), n = (int)(rest / ti.MY);
-                    long long xo, yo;
-                    if (p.mode == 0) {
-                        xo = X;
-                        yo = Y;
+                            reinterpret_cast<float4 *>(d)[e] =
+                                make_float4(__uint_as_float(r[4 * e]), __uint_as_float(r[4 * e + 1]),
+                                            __uint_as_float(r[4 * e + 2]), __uint_as_float(r[4 * e + 3]));
                     } else {
-                        xo = ti.rx + (long long)p.sx * X;
-                        yo = ti.ry + (long long)p.sy * Y;
+#pragma unroll
+                        for (int e = 0; e < 16; ++e)
+                            if (x + e < p.DW) d[e] = __uint_as_float(r[e]);
                     }
-                    p.dst[xo + p.DW * yo + plane * (och + (long long)p.DC * n)] = __uint_as_float(r[e]);
+                } else {
+                    const long long pix0 = ti.p0 + cc * 16;
+                    if (pix0 >= ti.npix) continue;
+                    int X = (int)(pix0 % ti.MX);
+                    long long rest = pix0 / ti.MX;
+                    int Y = (int)(rest % ti.MY), n = (int)(rest / ti.MY);
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) {
+                        if (pix0 + e >= ti.npix) break;
+                        const long long xo = p.mode == 0 ? X : ti.rx + (long long)p.sx * X;
+                        const long long yo = p.mode == 0 ? Y : ti.ry + (long long)p.sy * Y;
+                        p.dst[xo + p.DW * yo + plane * (och + (long long)p.DC * n)] =
+                            __uint_as_float(r[e]);
+                        if (++X == ti.MX) {
+                            X = 0;
+                            if (++Y == ti.MY) {
+                                Y = 0;
+                                ++n;
+                            }
+                        }
+                    }
                 }
             }
             tc_fence_before();
@@ -289,7 +336,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             uint32_t it = 0, acc_it = 0;
             bool issued = false;
             for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
-                TileInfo ti = decode_tile(p, tile);
+                TileInfo ti = decode_tile<TMA_B>(p, tile);
                 if (ti.ntaps == 0) continue;
                 const int b = acc_it & 1;
                 if (!mbar_wait(&sm->tmem_empty[b], ((acc_it >> 1) & 1) ^ 1, abort, 4u)) break;
@@ -328,11 +375,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
         __syncwarp();
     } else {
-        // ---------------- weight tiles via TMA
+        // ---------------- TMA: weight tiles (and pixel rectangles for stride 1)
         if (lane == 0) {
             uint32_t it = 0;
             for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
-                TileInfo ti = decode_tile(p, tile);
+                TileInfo ti = decode_tile<TMA_B>(p, tile);
                 if (ti.ntaps == 0) continue;
                 const int iters = p.nchunk * ti.ntaps;
                 for (int kb = 0; kb < iters; ++kb, ++it) {
@@ -340,10 +387,16 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     if (!mbar_wait(&sm->empty[s], ((it / STAGES) & 1) ^ 1, abort, 16u)) break;
                     const int cchunk = kb / ti.ntaps;
                     const int tq = ti.tap_begin + (kb - cchunk * ti.ntaps);
-                    const int tap = p.tap_u[tq] + p.fw * p.tap_v[tq];
-                    mbar_arrive_expect_tx(&sm->full[s], A_BYTES);
+                    const int u = p.tap_u[tq], v = p.tap_v[tq];
+                    mbar_arrive_expect_tx(&sm->full[s], TMA_B ? A_BYTES + B_BYTES : A_BYTES);
                     tma_load_2d(smem_u32(a_stage + s * A_BYTES), &wmap, &sm->full[s],
-                                tap * p.SCpad + cchunk * BK, ti.och0);
+                                (u + p.fw * v) * p.SCpad + cchunk * BK, ti.och0);
+                    if (TMA_B) {
+                        int offx, offy;
+                        tap_offsets(p, ti, u, v, offx, offy);
+                        tma_load_4d(smem_u32(b_stage + s * B_BYTES), &xmap, &sm->full[s],
+                                    cchunk * BK, ti.x0 + offx, ti.y0 + offy, ti.n);
+                    }
                 }
             }
         }
@@ -362,12 +415,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 // filter gradient kernel
 // ===========================================================================
 constexpr int WG_STAGES = 4;
-constexpr int WG_KP = 64;                 // pixels per stage (MMA K)
-constexpr int WG_A_BYTES = 128 * WG_KP * 2;   // G^T tile: 128 k x 64 pixels, 16 KB
-constexpr int WG_B_GROUP = 64 * WG_KP * 2;    // one 64-channel group x 64 pixels, 8 KB
+constexpr int WG_KP = 64;                      // pixels per stage (MMA K)
+constexpr int WG_A_BYTES = 128 * WG_KP * 2;    // G^T tile: 128 k x 64 pixels, 16 KB
+constexpr int WG_B_GROUP = 64 * WG_KP * 2;     // one 64-channel group x 64 pixels, 8 KB
 constexpr int WG_MAXG = 4;
 constexpr int WG_B_BYTES = WG_B_GROUP * WG_MAXG;  // 32 KB
-constexpr int WG_THREADS = 256;           // warps 0-3 gather, 4-7 epilogue (+ MMA in warp 4)
+constexpr int WG_THREADS = 256;  // warps 0-3 producers (warp 0 TMA), 4-7 epilogue, MMA in warp 4
 
 struct WgradParams {
     const __nv_bfloat16 *x;  // [N][H][W][Cpad]
@@ -376,18 +429,21 @@ struct WgradParams {
     int W, H, Cpad, C, N;
     int Wo, Ho, Kpad, K;
     int sx, sy, px, py, dx, dy, fw, fh;
-    long long Q;        // Wo*Ho*N pixels
-    long long chunk;    // pixels per split (multiple of 64)
+    long long Q;        // cp.async path: Wo*Ho*N pixels; TMA path: pixel blocks
+    long long chunk;    // pixels (cp.async) or pixel blocks (TMA) per split
     int ngroups_total;  // taps * (Cpad/64)
     int groups_per_tile;
     int n_k_tiles;
+    int BX, BY, ntx, nty;  // 64-pixel rectangles (TMA path)
 };
 
+template <bool TMA>
 __global__ void __launch_bounds__(WG_THREADS, 1)
-    wgrad_tc_kernel(const __grid_constant__ WgradParams p) {
+    wgrad_tc_kernel(const __grid_constant__ WgradParams p, const __grid_constant__ CUtensorMap gmap,
+                    const __grid_constant__ CUtensorMap xmap) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char *base =
-        reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *a_stage = base;
     unsigned char *b_stage = base + WG_STAGES * WG_A_BYTES;
     Smem *sm = reinterpret_cast<Smem *>(b_stage + WG_STAGES * WG_B_BYTES);
@@ -401,12 +457,13 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
     const int ng = min(p.groups_per_tile, p.ngroups_total - g0);
     const long long q_begin = (long long)blockIdx.y * p.chunk;
     const long long q_end = min(p.Q, q_begin + p.chunk);
-    const int nstages = (int)((q_end - q_begin + WG_KP - 1) / WG_KP);
+    const int nstages = TMA ? (int)(q_end - q_begin) : (int)((q_end - q_begin + WG_KP - 1) / WG_KP);
     const int ncols = 64 * ng;
+    const int nchunk = p.Cpad / 64;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < WG_STAGES; ++s) {
-            mbar_init(&sm->full[s], 128);
+            mbar_init(&sm->full[s], TMA ? 1 : 128);
             mbar_init(&sm->empty[s], 1);
         }
         mbar_init(&sm->tmem_full[0], 1);
@@ -414,65 +471,105 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
         fence_barrier_init();
     }
     if (warp == 4) tmem_alloc(&sm->tmem_base, 256);
+    if (TMA && warp == 0 && lane == 0) {
+        prefetch_tmap(&gmap);
+        prefetch_tmap(&xmap);
+    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem_base = sm->tmem_base;
-    const int nchunk = p.Cpad / 64;
 
     if (warp < 4) {
-        const int t = threadIdx.x;
-        uint32_t it = 0;
-        for (int st = 0; st < nstages && !*abort; ++st, ++it) {
-            const int s = it % WG_STAGES;
-            if (!mbar_wait(&sm->empty[s], ((it / WG_STAGES) & 1) ^ 1, abort, 32u)) break;
-            const uint32_t sa = smem_u32(a_stage + s * WG_A_BYTES);
-            const uint32_t sb = smem_u32(b_stage + s * WG_B_BYTES);
-            // A: 64 pixel rows x 256 bytes (128 k) -> two MN atoms; 1024 chunks
-            for (int e = t; e < WG_KP * 16; e += 128) {
-                const int row = e >> 4, ch = e & 15;  // ch: 16-byte chunk along k
-                const long long q = q_begin + (long long)st * WG_KP + row;
-                const int atom = ch >> 3, j = ch & 7;
-                bool ok = q < q_end;
-                const __nv_bfloat16 *src = p.g;
-                if (ok) src = p.g + q * p.Kpad + k0 + 8 * ch;
-                ok = ok && (k0 + 8 * ch < p.Kpad);
-                cp_async_16(sa + atom * 8192 + (row >> 3) * 1024 + (row & 7) * 128 + ((j ^ (row & 7)) << 4),
-                            ok ? src : p.g, ok ? 16u : 0u);
-            }
-            // B: 64 pixel rows x ng groups x 128 bytes
-            for (int e = t; e < WG_KP * 8 * ng; e += 128) {
-                const int grp = e / (WG_KP * 8);
-                const int rem = e - grp * (WG_KP * 8);
-                const int row = rem >> 3, j = rem & 7;
-                const long long q = q_begin + (long long)st * WG_KP + row;
-                const int gi = g0 + grp;
-                const int tap = gi / nchunk, cchunk = gi - tap * nchunk;
-                const int u = tap % p.fw, v = tap / p.fw;
-                bool ok = q < q_end;
-                const __nv_bfloat16 *src = p.x;
-                if (ok) {
-                    const int X = (int)(q % p.Wo);
-                    const long long rest = q / p.Wo;
-                    const int Y = (int)(rest % p.Ho), n = (int)(rest / p.Ho);
-                    const int xs = X * p.sx - p.px + u * p.dx, ys = Y * p.sy - p.py + v * p.dy;
-                    ok = xs >= 0 && xs < p.W && ys >= 0 && ys < p.H;
-                    if (ok)
-                        src = p.x + (((long long)n * p.H + ys) * p.W + xs) * p.Cpad + cchunk * 64 + 8 * j;
+        if (TMA) {
+            if (warp == 0 && lane == 0) {
+                const uint32_t bytes = WG_A_BYTES + WG_B_GROUP * ng;
+                for (int st = 0; st < nstages && !*abort; ++st) {
+                    const int s = st % WG_STAGES;
+                    if (!mbar_wait(&sm->empty[s], ((st / WG_STAGES) & 1) ^ 1, abort, 32u)) break;
+                    long long blk = q_begin + st;
+                    const int tx = (int)(blk % p.ntx);
+                    blk /= p.ntx;
+                    const int ty = (int)(blk % p.nty);
+                    const int n = (int)(blk / p.nty);
+                    const int x0 = tx * p.BX, y0 = ty * p.BY;
+                    mbar_arrive_expect_tx(&sm->full[s], bytes);
+                    const uint32_t sa = smem_u32(a_stage + s * WG_A_BYTES);
+                    const uint32_t sb = smem_u32(b_stage + s * WG_B_BYTES);
+                    tma_load_4d(sa, &gmap, &sm->full[s], k0, x0, y0, n);
+                    tma_load_4d(sa + 8192, &gmap, &sm->full[s], k0 + 64, x0, y0, n);
+                    for (int grp = 0; grp < ng; ++grp) {
+                        const int gi = g0 + grp;
+                        const int tap = gi / nchunk, cchunk = gi - tap * nchunk;
+                        const int u = tap % p.fw, v = tap / p.fw;
+                        tma_load_4d(sb + grp * WG_B_GROUP, &xmap, &sm->full[s], cchunk * 64,
+                                    x0 * p.sx - p.px + u * p.dx, y0 * p.sy - p.py + v * p.dy, n);
+                    }
                 }
-                cp_async_16(sb + grp * 8192 + (row >> 3) * 1024 + (row & 7) * 128 + ((j ^ (row & 7)) << 4),
-                            ok ? src : p.x, ok ? 16u : 0u);
             }
-            cp_async_commit();
-            if (it >= LAG) {
-                cp_async_wait<LAG>();
-                fence_proxy_async_smem();
-                mbar_arrive(&sm->full[(it - LAG) % WG_STAGES]);
+        } else {
+            // cp.async producers: thread t owns pixel row t/2 of every stage and
+            // half of its chunks; the pixel is tracked incrementally
+            const int t = threadIdx.x;
+            const int row = t >> 1, half = t & 1;
+            long long q = q_begin + row;
+            int X = (int)(q % p.Wo);
+            long long rest = q / p.Wo;
+            int Y = (int)(rest % p.Ho), n = (int)(rest / p.Ho);
+            uint32_t it = 0;
+            for (int st = 0; st < nstages && !*abort; ++st, ++it) {
+                const int s = it % WG_STAGES;
+                if (!mbar_wait(&sm->empty[s], ((it / WG_STAGES) & 1) ^ 1, abort, 32u)) break;
+                const uint32_t sa = smem_u32(a_stage + s * WG_A_BYTES);
+                const uint32_t sb = smem_u32(b_stage + s * WG_B_BYTES);
+                const bool qv = q < q_end;
+                const uint32_t rowoff = (row >> 3) * 1024 + (row & 7) * 128;
+                // A: G row (128 k = two 64-wide MN atoms)
+                const __nv_bfloat16 *gsrc = p.g + q * p.Kpad + k0;
+#pragma unroll
+                for (int e = 0; e < 8; ++e) {
+                    const int ch = half * 8 + e;  // 16-byte chunk along k
+                    const int atom = ch >> 3, j = ch & 7;
+                    cp_async_16(sa + atom * 8192 + rowoff + ((j ^ (row & 7)) << 4),
+                                qv ? gsrc + 8 * ch : p.g, qv ? 16u : 0u);
+                }
+                // B: X rows at the shifted pixel for each (tap, channel chunk)
+                for (int grp = 0; grp < ng; ++grp) {
+                    const int gi = g0 + grp;
+                    const int tap = gi / nchunk, cchunk = gi - tap * nchunk;
+                    const int u = tap % p.fw, v = tap / p.fw;
+                    const int xs = X * p.sx - p.px + u * p.dx, ys = Y * p.sy - p.py + v * p.dy;
+                    const bool ok = qv && xs >= 0 && xs < p.W && ys >= 0 && ys < p.H;
+                    const __nv_bfloat16 *xsrc =
+                        ok ? p.x + (((long long)n * p.H + ys) * p.W + xs) * p.Cpad + cchunk * 64 : p.x;
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int j = half * 4 + e;
+                        cp_async_16(sb + grp * WG_B_GROUP + rowoff + ((j ^ (row & 7)) << 4),
+                                    ok ? xsrc + 8 * j : p.x, ok ? 16u : 0u);
+                    }
+                }
+                cp_async_commit();
+                if (it >= LAG) {
+                    cp_async_wait<LAG>();
+                    fence_proxy_async_smem();
+                    mbar_arrive(&sm->full[(it - LAG) % WG_STAGES]);
+                }
+                q += WG_KP;
+                X += WG_KP;
+                while (X >= p.Wo) {
+                    X -= p.Wo;
+                    if (++Y == p.Ho) {
+                        Y = 0;
+                        ++n;
+                    }
+                }
             }
+            cp_async_wait_all();
+            fence_proxy_async_smem();
+            for (uint32_t k = (it >= LAG ? it - LAG : 0); k < it; ++k)
+                mbar_arrive(&sm->full[k % WG_STAGES]);
         }
-        cp_async_wait_all();
-        fence_proxy_async_smem();
-        for (uint32_t k = (it >= LAG ? it - LAG : 0); k < it; ++k) mbar_arrive(&sm->full[k % WG_STAGES]);
     } else {
         if (warp == 4 && lane == 0) {
             // MMA: M = 128 (k), N = 64*ng, both operands MN-major
@@ -494,9 +591,9 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
             mma_commit(&sm->tmem_full[0]);
         }
         __syncwarp();
-        // epilogue: all four warps 4-7 (TMEM lanes 32*(warp-4) ...)
+        // epilogue: warps 4-7 (TMEM lanes 32*(warp-4) ...); waits for the MMAs
+        // even when aborting, so TMEM is never freed under them
         const int q = warp - 4;
-        // wait for the MMAs even when aborting, so TMEM is never freed under them
         bool have = false;
         if (nstages > 0) {
             unsigned n = 0;
@@ -560,9 +657,10 @@ __global__ void to_nhwc_bf16_kernel(const float *__restrict__ in, int W, int H, 
         for (int px = threadIdx.y; px < 32; px += blockDim.y) {
             const int x = x0 + px;
             if (x < W) {
-                __nv_bfloat162 v2 = __floats2bfloat162_rn(tile[2 * threadIdx.x][px], tile[2 * threadIdx.x + 1][px]);
-                *reinterpret_cast<__nv_bfloat162 *>(out + (((long long)n * H + y) * W + x) * Cpad + c0 +
-                                                    2 * threadIdx.x) = v2;
+                __nv_bfloat162 v2 =
+                    __floats2bfloat162_rn(tile[2 * threadIdx.x][px], tile[2 * threadIdx.x + 1][px]);
+                *reinterpret_cast<__nv_bfloat162 *>(out + (((long long)n * H + y) * W + x) * Cpad +
+                                                    c0 + 2 * threadIdx.x) = v2;
             }
         }
         __syncthreads();
@@ -574,7 +672,8 @@ __global__ void to_nhwc_bf16_kernel(const float *__restrict__ in, int W, int H, 
 // with tap = u + fw*v multiplying w[fw-1-u, fh-1-v, c, k]; padded rows and
 // channels are zero
 __global__ void weights_bf16_kernel(const float *__restrict__ w, int fw, int fh, int C, int K,
-                                    int mode, int och_pad, int in_pad, __nv_bfloat16 *__restrict__ out) {
+                                    int mode, int och_pad, int in_pad,
+                                    __nv_bfloat16 *__restrict__ out) {
     const long long total = (long long)och_pad * fw * fh * in_pad;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
@@ -624,7 +723,24 @@ static CUtensorMap make_wmap(const __nv_bfloat16 *ptr, long long rows, long long
     CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)ptr, dims, strides, box,
                              es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) AFGB_THROW(AF_ERR_INTERNAL, "cuTensorMapEncodeTiled failed");
+    if (r != CUDA_SUCCESS) AFGB_THROW(AF_ERR_INTERNAL, "cuTensorMapEncodeTiled (weights) failed");
+    return m;
+}
+
+// 4-D bf16 NHWC tensor (Cpad, W, H, N), box {64, bx, by, 1}, 128B swizzle,
+// out-of-range elements read as zero
+static CUtensorMap make_imap(const __nv_bfloat16 *ptr, int Cpad, int W, int H, int N, int bx,
+                             int by) {
+    CUtensorMap m;
+    cuuint64_t dims[4] = {(cuuint64_t)Cpad, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
+    cuuint64_t strides[3] = {(cuuint64_t)Cpad * 2, (cuuint64_t)Cpad * 2 * W,
+                             (cuuint64_t)Cpad * 2 * W * H};
+    cuuint32_t box[4] = {64, (cuuint32_t)bx, (cuuint32_t)by, 1};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)ptr, dims, strides, box,
+                             es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) AFGB_THROW(AF_ERR_INTERNAL, "cuTensorMapEncodeTiled (image) failed");
     return m;
 }
 
@@ -643,6 +759,24 @@ static __nv_bfloat16 *to_nhwc(const float *src, int W, int H, int C, int N, int 
     return out;
 }
 
+// rectangle bx x by (bx*by == area, bx >= minx) covering W x H with the
+// least padding; ties prefer the wider rectangle
+static void pick_rect(int W, int H, int area, int minx, int &bx, int &by) {
+    long long best = -1;
+    bx = std::min(area, 256);
+    by = area / bx;
+    for (int x = std::min(area, 256); x >= minx; x >>= 1) {
+        const int y = area / x;
+        if (y > 256) break;
+        const long long cover = (long long)((W + x - 1) / x) * x * ((H + y - 1) / y) * y;
+        if (best < 0 || cover < best) {
+            best = cover;
+            bx = x;
+            by = y;
+        }
+    }
+}
+
 static size_t gather_smem() { return 1024 + STAGES * (A_BYTES + B_BYTES) + sizeof(Smem) + 64; }
 
 // forward (mode 0) or data gradient (mode 1)
@@ -657,10 +791,11 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     const int SCpad = round_up(SC, 64);
     const int OCpad = round_up(DC, 128);
     const int taps = (int)(g.fw * g.fh);
+    const bool tma_b = g.sx == 1 && g.sy == 1;
 
     __nv_bfloat16 *img = to_nhwc(img_f32, SW, SH, SC, (int)g.N, SCpad);
-    __nv_bfloat16 *wt =
-        static_cast<__nv_bfloat16 *>(alloc_device((size_t)OCpad * taps * SCpad * sizeof(__nv_bfloat16)));
+    __nv_bfloat16 *wt = static_cast<__nv_bfloat16 *>(
+        alloc_device((size_t)OCpad * taps * SCpad * sizeof(__nv_bfloat16)));
     {
         long long total = (long long)OCpad * taps * SCpad;
         unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
@@ -691,8 +826,8 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     p.fw = (int)g.fw;
     p.nchunk = SCpad / 64;
     p.n_och_tiles = OCpad / 128;
-    p.nphx = mode == 0 ? 1 : (int)g.sx;
-    p.nphase = mode == 0 ? 1 : (int)(g.sx * g.sy);
+    p.nphx = (mode == 0 || tma_b) ? 1 : (int)g.sx;
+    p.nphase = (mode == 0 || tma_b) ? 1 : (int)(g.sx * g.sy);
     int ntap = 0, ntile = 0;
     for (int ph = 0; ph < p.nphase; ++ph) {
         const int rx = ph % p.nphx, ry = ph / p.nphx;
@@ -714,16 +849,31 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     }
     p.phase_tap_begin[p.nphase] = ntap;
     p.phase_tile_begin[p.nphase] = ntile;
+    CUtensorMap xmap;
+    std::memset(&xmap, 0, sizeof(xmap));
+    if (tma_b) {
+        pick_rect(DW, DH, BN, 16, p.BX, p.BY);
+        p.ntx = (DW + p.BX - 1) / p.BX;
+        p.nty = (DH + p.BY - 1) / p.BY;
+        ntile = p.n_och_tiles * p.ntx * p.nty * (int)g.N;
+        xmap = make_imap(img, SCpad, SW, SH, (int)g.N, p.BX, p.BY);
+    }
     p.total_tiles = ntile;
 
     CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad);
     const size_t smem = gather_smem();
-    AFGB_CUDA(cudaFuncSetAttribute(gather_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
     if (ntile > 0) {
         const int grid = std::min(ntile, num_sms());
         KernelTimer kt(mode == 0 ? "tc_fwd_kernel" : "tc_dgrad_kernel");
-        gather_conv_kernel<<<grid, NUM_THREADS, smem, stream()>>>(p, wmap);
+        if (tma_b) {
+            AFGB_CUDA(cudaFuncSetAttribute(gather_conv_kernel<true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            gather_conv_kernel<true><<<grid, NUM_THREADS, smem, stream()>>>(p, wmap, xmap);
+        } else {
+            AFGB_CUDA(cudaFuncSetAttribute(gather_conv_kernel<false>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            gather_conv_kernel<false><<<grid, NUM_THREADS, smem, stream()>>>(p, wmap, xmap);
+        }
         count_launch();
         AFGB_POST_LAUNCH("gather_conv_kernel");
     }
@@ -732,11 +882,11 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
 }
 
 // the gather kernel's limits: phases and taps fit the parameter block,
-// 32-bit pixel indexing inside a tile
+// 32-bit pixel coordinates
 static bool gather_fits(const NNGeom &g, int mode) {
     if (g.fw * g.fh > MAX_T) return false;
     if (mode == 1 && g.sx * g.sy > MAX_PH) return false;
-    if (g.W > (1 << 20) || g.H > (1 << 20)) return false;
+    if (g.W > (1 << 24) || g.H > (1 << 24) || g.N > (1 << 24)) return false;
     return true;
 }
 
@@ -793,18 +943,16 @@ bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array 
     p.dy = (int)g.dy;
     p.fw = (int)g.fw;
     p.fh = (int)g.fh;
-    p.Q = g.Wo * g.Ho * g.N;
     p.ngroups_total = (int)(g.fw * g.fh) * (Cpad / 64);
-    // groups per tile: fewest tiles, then least padding
+    // groups per tile: fewest tiles, then an even split
     int best = 4, best_tiles = 1 << 30;
     for (int gp = 4; gp >= 1; --gp) {
-        int tiles = (p.ngroups_total + gp - 1) / gp;
+        const int tiles = (p.ngroups_total + gp - 1) / gp;
         if (tiles < best_tiles) {
             best_tiles = tiles;
             best = gp;
         }
     }
-    // prefer a tile width that divides the groups evenly when it costs no extra tile
     for (int gp = 4; gp >= 1; --gp) {
         if (p.ngroups_total % gp == 0 && (p.ngroups_total / gp) <= best_tiles) {
             best = gp;
@@ -813,22 +961,52 @@ bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array 
     }
     p.groups_per_tile = best;
     p.n_k_tiles = Kpad / 128;
+    // stride 1: 64-pixel rectangles by TMA; otherwise the cp.async row
+    // gather handles any stride
+    const bool tma = g.sx == 1 && g.sy == 1;
+    CUtensorMap gmap, xmap;
+    std::memset(&gmap, 0, sizeof(gmap));
+    std::memset(&xmap, 0, sizeof(xmap));
+    long long units;  // pixel blocks (TMA) or pixels (cp.async)
+    if (tma) {
+        pick_rect((int)g.Wo, (int)g.Ho, WG_KP, 8, p.BX, p.BY);
+        p.ntx = ((int)g.Wo + p.BX - 1) / p.BX;
+        p.nty = ((int)g.Ho + p.BY - 1) / p.BY;
+        units = (long long)p.ntx * p.nty * g.N;
+        gmap = make_imap(gg, Kpad, (int)g.Wo, (int)g.Ho, (int)g.N, p.BX, p.BY);
+        xmap = make_imap(x, Cpad, (int)g.W, (int)g.H, (int)g.N, p.BX, p.BY);
+    } else {
+        units = g.Wo * g.Ho * g.N;
+    }
+    p.Q = units;
     const long long ntiles = (long long)p.n_k_tiles * ((p.ngroups_total + best - 1) / best);
-    long long target = (long long)num_sms() * 2;
+    const long long target = (long long)num_sms() * 2;
     long long splits = std::max(1LL, target / std::max(1LL, ntiles));
-    long long chunk = (p.Q + splits - 1) / splits;
-    chunk = std::max<long long>(1024, (chunk + WG_KP - 1) / WG_KP * WG_KP);
-    splits = (p.Q + chunk - 1) / chunk;
+    long long chunk = (units + splits - 1) / splits;
+    if (tma) {
+        chunk = std::max<long long>(16, chunk);
+    } else {
+        chunk = std::max<long long>(1024, (chunk + WG_KP - 1) / WG_KP * WG_KP);
+    }
+    splits = (units + chunk - 1) / chunk;
     p.chunk = chunk;
     const long long rows = g.C * g.fw * g.fh;
     float *partial = static_cast<float *>(alloc_device((size_t)(splits * rows * g.K) * sizeof(float)));
     p.partial = partial;
     const size_t smem = 1024 + WG_STAGES * (WG_A_BYTES + WG_B_BYTES) + sizeof(Smem) + 64;
-    AFGB_CUDA(cudaFuncSetAttribute(wgrad_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
     {
         KernelTimer kt("tc_wgrad_kernel");
-        wgrad_tc_kernel<<<dim3((unsigned)ntiles, (unsigned)splits), WG_THREADS, smem, stream()>>>(p);
+        if (tma) {
+            AFGB_CUDA(cudaFuncSetAttribute(wgrad_tc_kernel<true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            wgrad_tc_kernel<true><<<dim3((unsigned)ntiles, (unsigned)splits), WG_THREADS, smem,
+                                    stream()>>>(p, gmap, xmap);
+        } else {
+            AFGB_CUDA(cudaFuncSetAttribute(wgrad_tc_kernel<false>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            wgrad_tc_kernel<false><<<dim3((unsigned)ntiles, (unsigned)splits), WG_THREADS, smem,
+                                     stream()>>>(p, gmap, xmap);
+        }
     }
     count_launch();
     AFGB_POST_LAUNCH("wgrad_tc_kernel");

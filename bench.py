@@ -226,7 +226,7 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
 
     kt = {}
     for name in ("simt_fwd_kernel", "simt_dgrad_kernel", "simt_wgrad_kernel", "tc_fwd_kernel",
-                 "tc_dgrad_kernel", "tc_wgrad_kernel"):
+                 "tc_dgrad_kernel", "tc_wgrad_kernel", "tc_convert_kernel", "wgrad_reduce_kernel"):
         c = ctypes.c_ulonglong()
         ms = ctypes.c_double()
         L.afgb_kernel_time(name.encode(), ctypes.byref(c), ctypes.byref(ms))
@@ -237,7 +237,8 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
     steps_total = args.warmup + args.steps
     value = 3 * flops * args.steps / (total_ms / 1e3) / 1e12
 
-    dom = max(kt.items(), key=lambda kv: kv[1][1]) if kt else None
+    mains = {k: v for k, v in kt.items() if k.endswith(("fwd_kernel", "dgrad_kernel", "wgrad_kernel"))}
+    dom = max(mains.items(), key=lambda kv: kv[1][1]) if mains else None
     roofline = None
     if dom:
         name, (cnt, ms) = dom
@@ -252,12 +253,27 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
     # e2e through the C ABI with pinned host buffers
     e2e = run_e2e(af, X, Wt, Gd, prec, args)
 
+    # the plain FP32 CUDA-core path on the same workload (the >= 5x target's
+    # denominator), fewer steps
+    fp32 = None
+    if prec != "fp32":
+        def step32():
+            y = af.convolve2_nn(Xa, Wa, st, pd, dl)
+            dx = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_DATA)
+            dw = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_FILTER)
+            return y, dx, dw
+        k32 = max(3, min(args.steps, 5))
+        t32, _ = _timed_steps(step32, k32, 3, flush)
+        v32 = 3 * flops * k32 / (t32 / 1e3) / 1e12
+        fp32 = {"value": v32, "ms_per_step": t32 / k32, "unit": "TFLOP/s",
+                "speedup_of_" + prec: value / v32}
+
     res = {
         "value": value, "ms_per_step": total_ms / args.steps, "precision": prec,
         "errors_vs_fp64": {"fwd_rel": rel_fwd, "fwd_maxabs": maxabs_fwd, "dgrad_rel": rel_dx,
                            "wgrad_rel": rel_dw, "points": [256, 128, 64]},
         "kernel_times_ms": {k: round(v[1] / v[0], 4) for k, v in kt.items()},
-        "roofline": roofline, "clocks": clocks, "e2e": e2e,
+        "roofline": roofline, "clocks": clocks, "e2e": e2e, "fp32_path": fp32,
         "gpu_launches": int(launches), "step_times_ms": [round(t, 4) for t in times],
     }
     if not args.no_secondary:
@@ -514,6 +530,7 @@ def main() -> None:
                                                       ("value", "unit", "cores", "kind", "sample")},
         "e2e": res["e2e"], "clocks": res["clocks"], "gpu_launches": res["gpu_launches"],
         "errors_vs_fp64": res["errors_vs_fp64"], "kernel_times_ms": res["kernel_times_ms"],
+        "fp32_path": res["fp32_path"],
         "secondary": res.get("secondary"), "peaks": peaks,
     }
     print(json.dumps(line))
