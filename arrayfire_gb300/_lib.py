@@ -62,6 +62,7 @@ SIGNATURES = [
     ("afgb_nn_output_dims", ctypes.c_int, [_DP, _DP, _DP, _DP, _DP, _DP]),
     ("afgb_debug_fail_alloc_after", None, [ctypes.c_int]),
     ("afgb_kernel_launch_count", ctypes.c_ulonglong, []),
+    ("afgb_convolve2_filter_grad_noalloc", af_err, [_P, _P, _P, _DP, _DP, _DP, _DP, _DP, _P]),
     ("afgb_kernel_timing", None, [ctypes.c_int]),
     ("afgb_kernel_time", af_err, [ctypes.c_char_p, ctypes.POINTER(ctypes.c_ulonglong),
                                   ctypes.POINTER(ctypes.c_double)]),

@@ -21,6 +21,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <mutex>
+#include <string>
 #include <type_traits>
 #include <vector>
 
@@ -692,6 +694,115 @@ void nn_bias_grad(const NNGeom &g, const Array &grad, Array &db) {
 }
 
 // ---------------------------------------------------------------------------
+// filter gradient without device allocation (afgb_convolve2_filter_grad_noalloc)
+//
+// Same kernels as the FP32 filter gradient above, but the split-K partial
+// sums live in a fixed file-scope device array instead of memory obtained
+// from the stream-ordered pool, so the call allocates nothing.  The array
+// exists once per GPU that loads this library and stays until exit; every
+// call shares it.
+// ---------------------------------------------------------------------------
+constexpr long long kNoAllocScratchFloats = 2LL * 1024 * 1024;  // 8 MiB
+static __device__ __align__(256) float g_noalloc_scratch[kNoAllocScratchFloats];
+
+// device address of g_noalloc_scratch, looked up once per device with that
+// device current (the host-side symbol is only a stand-in for it)
+static float *noalloc_scratch_ptr(int dev) {
+    static std::mutex mu;
+    static float *ptrs[64] = {nullptr};
+    if (dev < 0 || dev >= 64) AFGB_THROW(AF_ERR_DEVICE, "device ordinal out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    if (!ptrs[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            (void)cudaGetLastError();
+            AFGB_THROW(AF_ERR_RUNTIME, std::string("cudaGetSymbolAddress of the no-allocation "
+                                                   "scratch failed: ") + cudaGetErrorString(e));
+        }
+        ptrs[dev] = static_cast<float *>(p);
+    }
+    return ptrs[dev];
+}
+
+static void noalloc_check_launch(const char *what) {
+    cudaError_t e = cudaPeekAtLastError();
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        AFGB_THROW(AF_ERR_RUNTIME, std::string("kernel launch failed: ") + what + ": " +
+                                       cudaGetErrorString(e));
+    }
+}
+
+static void filter_grad_noalloc(const NNGeom &g, const float *grad, const float *sig, float *dw,
+                                cudaStream_t st) {
+    WgradParams<float> p;
+    std::memset(&p, 0, sizeof(p));
+    p.X = sig;
+    p.W = g.W;
+    p.H = g.H;
+    p.C = g.C;
+    p.N = g.N;
+    p.G = grad;
+    p.Wo = g.Wo;
+    p.Ho = g.Ho;
+    p.K = g.K;
+    p.fw = (int)g.fw;
+    p.fh = (int)g.fh;
+    p.sx = (int)g.sx;
+    p.sy = (int)g.sy;
+    p.px = (int)g.px;
+    p.py = (int)g.py;
+    p.dx = (int)g.dx;
+    p.dy = (int)g.dy;
+    p.rows = g.fw * g.fh * g.C;
+    p.Q = g.Wo * g.Ho * g.N;
+    const long long total = p.rows * g.K;
+    if (total == 0) return;
+    if (total > kNoAllocScratchFloats) {
+        AFGB_THROW(AF_ERR_SIZE, "the filter gradient needs " + std::to_string(total) +
+                                    " floats of scratch; the no-allocation entry point holds at "
+                                    "most " + std::to_string(kNoAllocScratchFloats));
+    }
+    int dev = device();
+    float *scratch = noalloc_scratch_ptr(dev);
+    int sms = 0;
+    AFGB_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    const long long mt = (p.rows + WG_M - 1) / WG_M, nt = (g.K + WG_N - 1) / WG_N;
+    const long long cap = kNoAllocScratchFloats / total;  // splits that fit
+    long long splits = std::max(1LL, std::min(cap, (long long)sms * 2 / std::max(1LL, mt * nt)));
+    long long chunk = (p.Q + splits - 1) / splits;
+    chunk = ((chunk + WG_K - 1) / WG_K) * WG_K;
+    if (chunk < 512) chunk = 512;
+    splits = std::max(1LL, (p.Q + chunk - 1) / chunk);
+    if (splits > cap) {  // the 512-pixel floor can only lower splits; keep the cap explicit
+        chunk = ((p.Q + cap - 1) / cap + WG_K - 1) / WG_K * WG_K;
+        splits = std::max(1LL, (p.Q + chunk - 1) / chunk);
+    }
+    p.chunk = chunk;
+    p.partial = scratch;
+    const size_t smem = (size_t)(WG_K * WG_M + WG_K * WG_N) * sizeof(float) + WG_M * (8 + 4 + 4);
+    AFGB_CUDA(cudaFuncSetAttribute(wgrad_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
+    if (p.Q > 0) {
+        // every split writes its whole rows x K slice, so the scratch left
+        // by an earlier call needs no clearing
+        wgrad_kernel<float><<<dim3((unsigned)mt, (unsigned)nt, (unsigned)splits), WG_THREADS, smem,
+                              st>>>(p);
+        count_launch();
+        noalloc_check_launch("wgrad_kernel");
+    } else {
+        // no output pixels: the gradient is zero (cudaMemsetAsync allocates nothing)
+        AFGB_CUDA(cudaMemsetAsync(scratch, 0, (size_t)total * sizeof(float), st));
+        splits = 1;
+    }
+    wgrad_reduce_kernel<float, float><<<grid_cap(total, 256), 256, 0, st>>>(
+        scratch, (int)splits, p.rows, g.K, g.C, g.fw, g.fh, dw);
+    count_launch();
+    noalloc_check_launch("wgrad_reduce_kernel");
+}
+
+// ---------------------------------------------------------------------------
 // precision routing
 // ---------------------------------------------------------------------------
 void nn_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out,
@@ -723,3 +834,45 @@ void nn_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array 
 }
 
 }  // namespace afgb
+
+extern "C" af_err afgb_convolve2_filter_grad_noalloc(
+    float *filter_grad, const float *incoming_gradient, const float *signal,
+    const dim_t *signal_dims, const dim_t *filter_dims, const dim_t *strides,
+    const dim_t *paddings, const dim_t *dilations, void *stream) {
+    using namespace afgb;
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, filter_grad != nullptr);
+    AFGB_ARG_ASSERT(1, incoming_gradient != nullptr);
+    AFGB_ARG_ASSERT(2, signal != nullptr);
+    AFGB_ARG_ASSERT(3, signal_dims != nullptr && filter_dims != nullptr);
+    AFGB_ARG_ASSERT(5, strides != nullptr && paddings != nullptr && dilations != nullptr);
+    for (int i = 0; i < 4; ++i) {
+        AFGB_DIM_ASSERT(3, signal_dims[i] > 0);
+        AFGB_DIM_ASSERT(4, filter_dims[i] > 0);
+    }
+    AFGB_DIM_ASSERT(4, signal_dims[2] == filter_dims[2]);
+    AFGB_ARG_ASSERT(5, strides[0] > 0 && strides[1] > 0);
+    AFGB_ARG_ASSERT(6, paddings[0] >= 0 && paddings[1] >= 0);
+    AFGB_ARG_ASSERT(7, dilations[0] > 0 && dilations[1] > 0);
+    NNGeom g;
+    std::memset(&g, 0, sizeof(g));
+    g.W = signal_dims[0];
+    g.H = signal_dims[1];
+    g.C = signal_dims[2];
+    g.N = signal_dims[3];
+    g.fw = filter_dims[0];
+    g.fh = filter_dims[1];
+    g.K = filter_dims[3];
+    g.sx = strides[0];
+    g.sy = strides[1];
+    g.px = paddings[0];
+    g.py = paddings[1];
+    g.dx = dilations[0];
+    g.dy = dilations[1];
+    g.Wo = 1 + (g.W + 2 * g.px - (((g.fw - 1) * g.dx) + 1)) / g.sx;
+    g.Ho = 1 + (g.H + 2 * g.py - (((g.fh - 1) * g.dy) + 1)) / g.sy;
+    AFGB_DIM_ASSERT(3, g.Wo > 0 && g.Ho > 0);
+    cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : afgb::stream();
+    filter_grad_noalloc(g, incoming_gradient, signal, filter_grad, st);
+    AFGB_CATCHALL
+}

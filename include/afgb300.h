@@ -222,6 +222,28 @@ AFGB_API void afgb_debug_fail_alloc_after(int n);
 /* Number of kernels this library has launched since load (all devices). */
 AFGB_API unsigned long long afgb_kernel_launch_count(void);
 
+/* Filter gradient of the NN convolution (FP32) with no device allocation.
+ * No counterpart in the reference.  It computes what af_convolve2_gradient_nn
+ * returns for AF_CONV_GRADIENT_FILTER, for callers that cannot allocate GPU
+ * memory — a host application whose device memory is wholly reserved by
+ * another allocator, or a service with a fixed memory budget that forbids
+ * allocation after start-up.  Inputs and the output are caller-owned device
+ * buffers in ArrayFire layout: incoming_gradient (Wo,Ho,K,N), signal
+ * (W,H,C,N) = signal_dims, filter_grad (fw,fh,C,K) = filter_dims; strides,
+ * paddings and dilations hold two values each.  Work runs on `stream`
+ * (0: the library's current stream).
+ * Scratch: a fixed 8 MiB device array inside the library (2,097,152 floats;
+ * fw*fh*C*K must not exceed that, else AF_ERR_SIZE), present on every GPU
+ * that loads the library until the process exits.  The first call on a
+ * device looks up that array's device address, so make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU (other
+ * streams, other host threads) race and give wrong results. */
+AFGB_API af_err afgb_convolve2_filter_grad_noalloc(float *filter_grad, const float *incoming_gradient,
+                                                   const float *signal, const dim_t *signal_dims,
+                                                   const dim_t *filter_dims, const dim_t *strides,
+                                                   const dim_t *paddings, const dim_t *dilations,
+                                                   void *stream);
+
 /* Device timing of the library's main kernels, for benchmarks: while
  * enabled, each main kernel launch is bracketed by CUDA events on its stream.
  * afgb_kernel_time sums the recorded launches whose kernel name equals
