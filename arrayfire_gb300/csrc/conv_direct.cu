@@ -139,6 +139,47 @@ __device__ __forceinline__ float load_as_float<float>(const float *p) {
     return __ldg(p);
 }
 
+// Stage a TH x TW input window (origin ox, oy; zero outside the signal) into
+// a shared tile of pitch PITCH floats.  f32 uses 4-byte cp.async with zero
+// fill, so every load of the tile is in flight at once; other types load
+// through registers in a division-free 2-D loop.
+template <typename T>
+__device__ __forceinline__ void stage_tile(float *tile, int PITCH, int TH, int TW, const T *in,
+                                           long long ox, long long oy, long long sd0,
+                                           long long sd1, long long ss0, long long ss1) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nwarps = blockDim.x >> 5;
+    if constexpr (sizeof(T) == 4 && !IsInt<T>::value) {
+        const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(tile));
+        for (int r = warp; r < TH; r += nwarps) {
+            const long long gy = oy + r;
+            const bool rv = gy >= 0 && gy < sd1;
+            for (int c = lane; c < TW; c += 32) {
+                const long long gx = ox + c;
+                const bool v = rv && gx >= 0 && gx < sd0;
+                const T *src = v ? in + gx * ss0 + gy * ss1 : in;
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(
+                                 sbase + 4u * (uint32_t)(r * PITCH + c)),
+                             "l"(src), "r"(v ? 4u : 0u)
+                             : "memory");
+            }
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    } else {
+        for (int r = warp; r < TH; r += nwarps) {
+            const long long gy = oy + r;
+            const bool rv = gy >= 0 && gy < sd1;
+#pragma unroll 4
+            for (int c = lane; c < TW; c += 32) {
+                const long long gx = ox + c;
+                float v = 0.0f;
+                if (rv && gx >= 0 && gx < sd0) v = load_as_float<T>(in + gx * ss0 + gy * ss1);
+                tile[r * PITCH + c] = v;
+            }
+        }
+    }
+}
+
 template <typename T>
 __device__ __forceinline__ void store4(T *dst, const float *v, bool vec_ok) {
     if (vec_ok) {
@@ -184,14 +225,7 @@ __global__ void __launch_bounds__(T2_THREADS) conv2_tile_kernel(DirectParams p) 
     const long long ss0 = p.ss[0], ss1 = p.ss[1];
 
     // stage the haloed input tile (zero outside the signal)
-    for (int idx = threadIdx.x; idx < TH * TW; idx += T2_THREADS) {
-        int r = idx / TW;
-        int c = idx - r * TW;
-        long long gx = ox + c, gy = oy + r;
-        float v = 0.0f;
-        if (gx >= 0 && gx < sd0 && gy >= 0 && gy < sd1) v = load_as_float<T>(in + gx * ss0 + gy * ss1);
-        tile[r * PITCH + c] = v;
-    }
+    stage_tile<T>(tile, PITCH, TH, TW, in, ox, oy, sd0, sd1, ss0, ss1);
     float wr[F0 * F1];
 #pragma unroll
     for (int fj = 0; fj < F1; ++fj)
@@ -252,6 +286,126 @@ __global__ void __launch_bounds__(T2_THREADS) conv2_tile_kernel(DirectParams p) 
 #pragma unroll
             for (int cc = 0; cc < 4; ++cc)
                 if (x + cc < od0) dst[cc * p.os[0]] = from_acc_any(acc[rr][cc], T{});
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// 3-D tile kernel (f32): output block 64 (x) x 8 (y) x 8 (z) per CTA; each
+// thread produces 4 consecutive x for one y and 4 consecutive z.  Input
+// planes are walked from high z to low so every output sees its dim-2 taps
+// in ascending order, dim-1 taps ascending inside, dim-0 taps innermost —
+// the reference's order (src/backend/cpu/kernel/convolve.hpp:77-130).
+// ---------------------------------------------------------------------------
+constexpr int T3_BX = 64, T3_BY = 8, T3_BZ = 8, T3_THREADS = 256;
+
+template <int F0, int F1, int F2, bool EXACT>
+__global__ void __launch_bounds__(T3_THREADS) conv3_tile_kernel(DirectParams p) {
+    constexpr int TW = T3_BX + F0 - 1;
+    constexpr int TH = T3_BY + F1 - 1;
+    constexpr int TD = T3_BZ + F2 - 1;
+    constexpr int PITCH = ((TW + 3) / 4) * 4;
+    constexpr int WIN = 4 + F0 - 1;
+    constexpr int WIN4 = (WIN + 3) / 4;
+    __shared__ __align__(16) float tile[TD * TH * PITCH];
+
+    const long long b = blockIdx.z / ((p.od[2] + T3_BZ - 1) / T3_BZ);
+    const long long zt = blockIdx.z - b * ((p.od[2] + T3_BZ - 1) / T3_BZ);
+    BatchOff bo = batch_offsets(p, b);
+    const float *in = static_cast<const float *>(p.sig) + bo.in;
+    const float *w = static_cast<const float *>(p.filt) + bo.filt;
+    float *out = static_cast<float *>(p.out) + bo.out;
+
+    const long long i0 = (long long)blockIdx.x * T3_BX;
+    const long long j0 = (long long)blockIdx.y * T3_BY;
+    const long long k0 = zt * T3_BZ;
+    const int ci = p.expand ? 0 : F0 / 2, cj = p.expand ? 0 : F1 / 2, ck = p.expand ? 0 : F2 / 2;
+    const long long ox = i0 + ci - (F0 - 1), oy = j0 + cj - (F1 - 1), oz = k0 + ck - (F2 - 1);
+
+    // stage (TD*TH) rows of TW floats with 4-byte cp.async, zero outside
+    {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        const uint32_t sbase = static_cast<uint32_t>(__cvta_generic_to_shared(tile));
+        for (int r = warp; r < TD * TH; r += T3_THREADS / 32) {
+            const int rz = r / TH, ry = r - rz * TH;
+            const long long gy = oy + ry, gz = oz + rz;
+            const bool rv = gy >= 0 && gy < p.sd[1] && gz >= 0 && gz < p.sd[2];
+            for (int c = lane; c < TW; c += 32) {
+                const long long gx = ox + c;
+                const bool v = rv && gx >= 0 && gx < p.sd[0];
+                const float *src = v ? in + gx * p.ss[0] + gy * p.ss[1] + gz * p.ss[2] : in;
+                asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(
+                                 sbase + 4u * (uint32_t)(r * PITCH + c)),
+                             "l"(src), "r"(v ? 4u : 0u)
+                             : "memory");
+            }
+        }
+        asm volatile("cp.async.wait_all;" ::: "memory");
+    }
+    float wr[F0 * F1 * F2];
+#pragma unroll
+    for (int fk = 0; fk < F2; ++fk)
+#pragma unroll
+        for (int fj = 0; fj < F1; ++fj)
+#pragma unroll
+            for (int fi = 0; fi < F0; ++fi)
+                wr[(fk * F1 + fj) * F0 + fi] = __ldg(w + fi * p.fs[0] + fj * p.fs[1] + fk * p.fs[2]);
+    __syncthreads();
+
+    const int tx = threadIdx.x & 15;
+    const int ty = (threadIdx.x >> 4) & 7;
+    const int tz = threadIdx.x >> 7;  // 0..1, four z each
+    float acc[4][4];  // [z][x]
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
+
+#pragma unroll
+    for (int q = 3 + F2 - 1; q >= 0; --q) {        // input plane (relative), high to low
+#pragma unroll
+        for (int fj = 0; fj < F1; ++fj) {          // dim-1 tap, ascending
+            float v[WIN4 * 4];
+            const float *row = tile + ((4 * tz + q) * TH + (ty + F1 - 1 - fj)) * PITCH + 4 * tx;
+#pragma unroll
+            for (int u = 0; u < WIN4; ++u) {
+                float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
+                v[4 * u] = t4.x;
+                v[4 * u + 1] = t4.y;
+                v[4 * u + 2] = t4.z;
+                v[4 * u + 3] = t4.w;
+            }
+#pragma unroll
+            for (int rz = 0; rz < 4; ++rz) {
+                const int fk = rz + F2 - 1 - q;
+                if (fk >= 0 && fk < F2) {
+#pragma unroll
+                    for (int fi = 0; fi < F0; ++fi) {
+                        const float wv = wr[(fk * F1 + fj) * F0 + fi];
+#pragma unroll
+                        for (int cc = 0; cc < 4; ++cc)
+                            acc[rz][cc] = mac<EXACT>(acc[rz][cc], v[cc + F0 - 1 - fi], wv);
+                    }
+                }
+            }
+        }
+    }
+    const long long x = i0 + 4 * tx, y = j0 + ty;
+    if (y >= p.od[1]) return;
+    const bool vec_ok = (x + 3 < p.od[0]) && (p.os[0] == 1) &&
+                        ((reinterpret_cast<uintptr_t>(out) & 15) == 0) && ((p.os[1] & 3) == 0) &&
+                        ((p.os[2] & 3) == 0);
+#pragma unroll
+    for (int rz = 0; rz < 4; ++rz) {
+        const long long z = k0 + 4 * tz + rz;
+        if (z >= p.od[2]) break;
+        float *dst = out + x + y * p.os[1] + z * p.os[2];
+        if (vec_ok) {
+            *reinterpret_cast<float4 *>(dst) = make_float4(acc[rz][0], acc[rz][1], acc[rz][2], acc[rz][3]);
+        } else {
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc)
+                if (x + cc < p.od[0]) dst[cc] = acc[rz][cc];
         }
     }
 }
@@ -322,15 +476,7 @@ __global__ void __launch_bounds__(SP_THREADS) sep_fused_kernel(SepParams p) {
         ctap[threadIdx.x] = threadIdx.x < cfl ? sep_tap<T>(p.cf[threadIdx.x]) : 0.0f;
         rtap[threadIdx.x] = threadIdx.x < rfl ? sep_tap<T>(p.rf[threadIdx.x]) : 0.0f;
     }
-    for (int idx = threadIdx.x; idx < TH * TW; idx += SP_THREADS) {
-        int r = idx / TW;
-        int c = idx - r * TW;
-        long long gx = ox + c, gy = oy + r;
-        float v = 0.0f;
-        if (gx >= 0 && gx < sd0 && gy >= 0 && gy < sd1)
-            v = load_as_float<T>(in + gx * p.ss[0] + gy * p.ss[1]);
-        tile[r * PITCH + c] = v;
-    }
+    stage_tile<T>(tile, PITCH, TH, TW, in, ox, oy, sd0, sd1, p.ss[0], p.ss[1]);
     __syncthreads();
 
     // pass 1 (dim 0): temp[r][x] = IN( sum_f tile[r][x + cfl-1-f] * c[f] ),
@@ -691,6 +837,21 @@ void launch_convolve_nd(const Array &sig, const Array &filt, Array &out, int kin
             default: break;
         }
         if (done) return;
+    }
+    if (rank == 3 && sig.type == f32 && p.fd[0] == 3 && p.fd[1] == 3 && p.fd[2] == 3) {
+        const long long nz = (p.od[2] + T3_BZ - 1) / T3_BZ;
+        if (p.nbatch * nz <= 65535 && (p.od[1] + T3_BY - 1) / T3_BY <= 65535) {
+            dim3 grid((unsigned)((p.od[0] + T3_BX - 1) / T3_BX),
+                      (unsigned)((p.od[1] + T3_BY - 1) / T3_BY), (unsigned)(p.nbatch * nz));
+            KernelTimer kt("conv3_tile_kernel");
+            if (exact)
+                conv3_tile_kernel<3, 3, 3, true><<<grid, T3_THREADS, 0, stream()>>>(p);
+            else
+                conv3_tile_kernel<3, 3, 3, false><<<grid, T3_THREADS, 0, stream()>>>(p);
+            count_launch();
+            AFGB_POST_LAUNCH("conv3_tile_kernel");
+            return;
+        }
     }
 #define AFGB_RUN_GENERIC(T) run_generic<T>(p, exact)
     AFGB_DISPATCH_ALL(sig.type, AFGB_RUN_GENERIC);

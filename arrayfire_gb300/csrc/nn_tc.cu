@@ -638,32 +638,64 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
 // ===========================================================================
 // layout conversions (bandwidth-bound pre-passes)
 // ===========================================================================
-// f32 ArrayFire (W,H,C,N) -> bf16 [N][H][W][Cpad], channels >= C zero
-__global__ void to_nhwc_bf16_kernel(const float *__restrict__ in, int W, int H, int C, int N,
-                                    int Cpad, __nv_bfloat16 *__restrict__ out) {
-    __shared__ float tile[64][33];
-    const int x0 = blockIdx.x * 32;
+// f32 ArrayFire (W,H,C,N) -> bf16 [N][H][W][Cpad], channels >= C zero.
+// One CTA converts a 64-pixel x 64-channel block of one image row: float4
+// loads along x (256 bytes per channel row), a padded shared tile, then
+// 16-byte stores of eight bf16 channels, four pixels (512 bytes) per warp.
+__global__ void __launch_bounds__(256) to_nhwc_bf16_kernel(const float *__restrict__ in, int W,
+                                                           int H, int C, int N, int Cpad,
+                                                           __nv_bfloat16 *__restrict__ out) {
+    __shared__ float tile[64][65];
+    const int x0 = blockIdx.x * 64;
     const int yn = blockIdx.y;  // y + H*n
     const int y = yn % H, n = yn / H;
+    const int c0 = blockIdx.z * 64;
     const long long plane = (long long)W * H;
-    for (int c0 = 0; c0 < Cpad; c0 += 64) {
-        for (int i = threadIdx.y; i < 64; i += blockDim.y) {
-            const int c = c0 + i, x = x0 + threadIdx.x;
+    const int t = threadIdx.x;
+    const bool vec = ((W & 3) == 0) && (x0 + 64 <= W) && ((reinterpret_cast<uintptr_t>(in) & 15) == 0);
+    if (vec) {
+        const int x4 = (t & 15) * 4;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            const int ci = (t >> 4) + 16 * i;
+            const int c = c0 + ci;
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (c < C)
+                v = __ldg(reinterpret_cast<const float4 *>(
+                    in + x0 + x4 + (long long)W * y + plane * (c + (long long)C * n)));
+            tile[ci][x4] = v.x;
+            tile[ci][x4 + 1] = v.y;
+            tile[ci][x4 + 2] = v.z;
+            tile[ci][x4 + 3] = v.w;
+        }
+    } else {
+        for (int e = t; e < 64 * 64; e += 256) {
+            const int ci = e >> 6, xi = e & 63;
+            const int c = c0 + ci, x = x0 + xi;
             float v = 0.f;
             if (c < C && x < W) v = in[x + (long long)W * y + plane * (c + (long long)C * n)];
-            tile[i][threadIdx.x] = v;
+            tile[ci][xi] = v;
         }
-        __syncthreads();
-        for (int px = threadIdx.y; px < 32; px += blockDim.y) {
-            const int x = x0 + px;
-            if (x < W) {
-                __nv_bfloat162 v2 =
-                    __floats2bfloat162_rn(tile[2 * threadIdx.x][px], tile[2 * threadIdx.x + 1][px]);
-                *reinterpret_cast<__nv_bfloat162 *>(out + (((long long)n * H + y) * W + x) * Cpad +
-                                                    c0 + 2 * threadIdx.x) = v2;
-            }
+    }
+    __syncthreads();
+    const int lane = t & 31, warp = t >> 5;
+    const int cg = lane & 7;  // eight channels
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+        const int xi = pass * 32 + warp * 4 + (lane >> 3);
+        const int x = x0 + xi;
+        if (x < W) {
+            uint4 w;
+            __nv_bfloat162 b0 = __floats2bfloat162_rn(tile[cg * 8 + 0][xi], tile[cg * 8 + 1][xi]);
+            __nv_bfloat162 b1 = __floats2bfloat162_rn(tile[cg * 8 + 2][xi], tile[cg * 8 + 3][xi]);
+            __nv_bfloat162 b2 = __floats2bfloat162_rn(tile[cg * 8 + 4][xi], tile[cg * 8 + 5][xi]);
+            __nv_bfloat162 b3 = __floats2bfloat162_rn(tile[cg * 8 + 6][xi], tile[cg * 8 + 7][xi]);
+            w.x = *reinterpret_cast<uint32_t *>(&b0);
+            w.y = *reinterpret_cast<uint32_t *>(&b1);
+            w.z = *reinterpret_cast<uint32_t *>(&b2);
+            w.w = *reinterpret_cast<uint32_t *>(&b3);
+            *reinterpret_cast<uint4 *>(out + (((long long)n * H + y) * W + x) * Cpad + c0 + cg * 8) = w;
         }
-        __syncthreads();
     }
 }
 
@@ -749,10 +781,10 @@ static int round_up(int v, int m) { return (v + m - 1) / m * m; }
 static __nv_bfloat16 *to_nhwc(const float *src, int W, int H, int C, int N, int Cpad) {
     __nv_bfloat16 *out =
         static_cast<__nv_bfloat16 *>(alloc_device((size_t)W * H * N * Cpad * sizeof(__nv_bfloat16)));
-    dim3 grid((unsigned)((W + 31) / 32), (unsigned)(H * N));
+    dim3 grid((unsigned)((W + 63) / 64), (unsigned)(H * N), (unsigned)(Cpad / 64));
     {
         KernelTimer kt("tc_convert_kernel");
-        to_nhwc_bf16_kernel<<<grid, dim3(32, 8), 0, stream()>>>(src, W, H, C, N, Cpad, out);
+        to_nhwc_bf16_kernel<<<grid, 256, 0, stream()>>>(src, W, H, C, N, Cpad, out);
     }
     count_launch();
     AFGB_POST_LAUNCH("to_nhwc_bf16_kernel");

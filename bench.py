@@ -405,10 +405,10 @@ def run_direct_workloads(af, peaks, args) -> dict:
     F3 = af.Array.from_numpy(np.asfortranarray((k3 / k3.sum()).astype(np.float32)))
     measure("conv3_3x3x3_f32_256^3_default",
             lambda: af.convolve3(V, F3, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL),
-            v.numel() * 8 + 108, "conv_generic_kernel")
+            v.numel() * 8 + 108, "conv3_tile_kernel")
     measure("conv3_3x3x3_f32_256^3_expand",
             lambda: af.convolve3(V, F3, af.AF_CONV_EXPAND, af.AF_CONV_SPATIAL),
-            v.numel() * 4 + 258 ** 3 * 4 + 108, "conv_generic_kernel")
+            v.numel() * 4 + 258 ** 3 * 4 + 108, "conv3_tile_kernel")
     return out
 
 
@@ -466,6 +466,72 @@ def cpu_nn_sample(seconds_budget: float = 20.0) -> dict:
             "seconds_per_step": dt}
 
 
+def run_only(args) -> None:
+    """One operation of the bench workload, same shapes and inputs."""
+    import torch
+
+    import arrayfire_gb300 as af
+
+    torch.cuda.set_device(0)
+    af.set_stream(torch.cuda.current_stream())
+    s = NN_SHAPE
+    st, pd, dl = s["stride"], s["pad"], s["dil"]
+    g = np.random.Generator(np.random.Philox(1234))
+    if args.only in ("fwd", "dgrad", "wgrad"):
+        X = np.asfortranarray(g.standard_normal((s["W"], s["H"], s["C"], s["N"]), dtype=np.float32))
+        Wt = np.asfortranarray((g.standard_normal((s["fw"], s["fh"], s["C"], s["K"])) * 0.06
+                                ).astype(np.float32))
+        Xa, Wa = af.Array.from_numpy(X), af.Array.from_numpy(Wt)
+        Y = af.convolve2_nn(Xa, Wa, st, pd, dl)
+        Ga = af.Array.from_numpy(np.asfortranarray(g.standard_normal(Y.dims, dtype=np.float32)))
+        prec = args.precision
+        fn = {"fwd": lambda: af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec),
+              "dgrad": lambda: af.convolve2_gradient_nn(Ga, Xa, Wa, Y, st, pd, dl,
+                                                        af.AF_CONV_GRADIENT_DATA, precision=prec),
+              "wgrad": lambda: af.convolve2_gradient_nn(Ga, Xa, Wa, Y, st, pd, dl,
+                                                        af.AF_CONV_GRADIENT_FILTER, precision=prec)
+              }[args.only]
+    else:
+        t = g.standard_normal(15)
+        CF = af.Array.from_numpy((t / t.sum()).astype(np.float32))
+        RF = af.Array.from_numpy((t[::-1] / t.sum()).astype(np.float32))
+        if args.only == "conv3":
+            v = torch.rand(256, 256, 256, device="cuda")
+            V = af.Array.view_torch(v)
+            k3 = g.standard_normal((3, 3, 3))
+            F3 = af.Array.from_numpy(np.asfortranarray((k3 / k3.sum()).astype(np.float32)))
+            fn = lambda: af.convolve3(V, F3, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL)  # noqa: E731
+        elif args.only == "sep_u8":
+            xu = torch.randint(0, 256, (64, 2048, 2048), dtype=torch.uint8, device="cuda")
+            S = af.Array.view_torch(xu)
+            fn = lambda: af.convolve2_separable(CF, RF, S)  # noqa: E731
+        else:
+            xs = torch.rand(64, 2048, 2048, device="cuda")
+            S = af.Array.view_torch(xs)
+            if args.only == "sep_f32":
+                fn = lambda: af.convolve2_separable(CF, RF, S)  # noqa: E731
+            else:
+                f7 = g.standard_normal((7, 7, 64))
+                F7 = af.Array.from_numpy(np.asfortranarray(
+                    (f7 / f7.sum(axis=(0, 1), keepdims=True)).astype(np.float32)))
+                fn = lambda: af.convolve2(S, F7, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL)  # noqa: E731
+    for _ in range(args.warmup):
+        r = fn()
+    del r
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(args.steps):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        r = fn()
+        b.record()
+        b.synchronize()
+        times.append(a.elapsed_time(b))
+        del r
+    print(json.dumps({"only": args.only, "precision": args.precision, "ms": times}))
+
+
 # ---------------------------------------------------------------------------
 def main() -> None:
     ap = argparse.ArgumentParser()
@@ -476,12 +542,19 @@ def main() -> None:
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32", "fp8"])
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--only", default=None,
+                    choices=["fwd", "dgrad", "wgrad", "sep_f32", "sep_u8", "same7", "conv3"],
+                    help="run one operation of the workload --steps times after --warmup "
+                         "(for profiler captures); prints its timing, not the bench line")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     peaks = load_peaks()
+    if args.only:
+        run_only(args)
+        return
     config = {"workload": "conv2_nn fwd+dgrad+wgrad, signal 128x128x64x32 (W,H,C,N), filter "
                           "3x3x64x128, stride 1, pad 1, dilation 1",
               "global_batch": NN_SHAPE["N"] * world, "flops_per_step": 3 * nn_flops() * world,
