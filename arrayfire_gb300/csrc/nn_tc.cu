@@ -55,10 +55,12 @@ constexpr int LAG = 2;                // cp.async groups in flight per producer
 constexpr int MAX_PH = 64;
 constexpr int MAX_T = 256;
 constexpr int NUM_THREADS = 320;      // warps 0-3 gather, 4-7 epilogue, 8 MMA, 9 TMA
+constexpr int EP_PITCH = 36;          // epilogue staging row pitch (floats): 32 pixels + 4
 
 struct GatherParams {
-    const __nv_bfloat16 *src;  // [N][SH][SW][SCpad]
+    const unsigned char *src;  // [N][SH][SW][SCpad] elements (bf16, or e4m3 bytes)
     float *dst;                // ArrayFire layout (DW, DH, DC, N)
+    const float *out_scale;    // FP8: per-output-channel dequantisation factor
     int SW, SH, SCpad, N;
     int DW, DH, DC;
     int mode;  // 0 forward, 1 data gradient
@@ -147,7 +149,8 @@ __device__ __forceinline__ void tap_offsets(const GatherParams &p, const TileInf
     }
 }
 
-template <bool TMA_B>
+// FP8: e4m3 operands, 128 channels per 128-byte row, kind::f8f6f4 MMA
+template <bool TMA_B, bool FP8>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     gather_conv_kernel(const __grid_constant__ GatherParams p,
                        const __grid_constant__ CUtensorMap wmap,
@@ -157,7 +160,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *a_stage = base;                     // STAGES x 16 KB
     unsigned char *b_stage = base + STAGES * A_BYTES;  // STAGES x 32 KB
-    Smem *sm = reinterpret_cast<Smem *>(b_stage + STAGES * B_BYTES);
+    float *ep_stage = reinterpret_cast<float *>(b_stage + STAGES * B_BYTES);  // 4 x 32 x 36
+    Smem *sm = reinterpret_cast<Smem *>(ep_stage + 4 * 32 * EP_PITCH);
     volatile int *abort = &sm->abort;
 
     const int warp = threadIdx.x >> 5;
@@ -194,7 +198,9 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             const int r0 = t >> 3;  // rows r0 + 16 i
             const int alpha_x = p.mode == 0 ? p.sx : 1;
             const int alpha_y = p.mode == 0 ? p.sy : 1;
-            const long long img_stride = (long long)p.SH * p.SW * p.SCpad;
+            constexpr int ES = FP8 ? 1 : 2;  // bytes per element
+            const long long img_stride = (long long)p.SH * p.SW * p.SCpad * ES;
+            const long long pix_stride = (long long)p.SCpad * ES;
             uint32_t it = 0;
             for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
                 TileInfo ti = decode_tile<false>(p, tile);
@@ -225,15 +231,15 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     int offx, offy;
                     tap_offsets(p, ti, p.tap_u[tq], p.tap_v[tq], offx, offy);
                     const uint32_t sb = smem_u32(b_stage + s * B_BYTES);
-                    const __nv_bfloat16 *cbase = p.src + cchunk * BK + 8 * j;
+                    const unsigned char *cbase = p.src + cchunk * 128 + 16 * j;
 #pragma unroll
                     for (int i = 0; i < 16; ++i) {
                         const int r = r0 + 16 * i;
                         const int xs = xb[i] + offx, ys = yb[i] + offy;
                         const bool ok = ((vmask >> i) & 1u) && xs >= 0 && xs < p.SW && ys >= 0 &&
                                         ys < p.SH;
-                        const __nv_bfloat16 *src =
-                            ok ? cbase + nb[i] * img_stride + ((long long)ys * p.SW + xs) * p.SCpad
+                        const unsigned char *src =
+                            ok ? cbase + nb[i] * img_stride + ((long long)ys * p.SW + xs) * pix_stride
                                : p.src;
                         cp_async_16(sb + r * 128 + ((j ^ (r & 7)) << 4), src, ok ? 16u : 0u);
                     }
@@ -279,30 +285,55 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             if (!mbar_wait(&sm->tmem_full[b], (acc_it >> 1) & 1, abort, 2u)) break;
             tc_fence_after();
             const uint32_t taddr = tmem_base + (uint32_t)(b * BN) + ((uint32_t)(32 * q) << 16);
-            float *dplane = p.dst + plane * ((long long)och + (long long)p.DC * (TMA_B ? ti.n : 0));
+            if (TMA_B) {
+                // 32 channels x 32 pixels at a time: TMEM -> registers -> this
+                // warp's shared staging block -> 128-byte rows per channel
+                float *stg = ep_stage + q * (32 * EP_PITCH);
+                const int orow = lane >> 3;         // 0..3: channel within a group of 4
+                const int ocol = (lane & 7) * 4;    // pixel offset within the 32
+                for (int cc = 0; cc < BN / 32; ++cc) {
+                    uint32_t r[32];
+                    tmem_ld16(taddr + cc * 32, *reinterpret_cast<uint32_t(*)[16]>(&r[0]));
+                    tmem_ld16(taddr + cc * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&r[16]));
+                    tmem_ld_wait();
+#pragma unroll
+                    const float sc = (FP8 && och < p.DC) ? p.out_scale[och] : 1.0f;
+#pragma unroll
+                    for (int e = 0; e < 8; ++e)
+                        *reinterpret_cast<float4 *>(stg + lane * EP_PITCH + 4 * e) =
+                            make_float4(sc * __uint_as_float(r[4 * e]), sc * __uint_as_float(r[4 * e + 1]),
+                                        sc * __uint_as_float(r[4 * e + 2]), sc * __uint_as_float(r[4 * e + 3]));
+                    __syncwarp();
+                    const int e0 = cc * 32;  // BX >= 32 keeps the 32 pixels in one row
+                    const int x = ti.x0 + (e0 % p.BX) + ocol, y = ti.y0 + e0 / p.BX;
+                    if (y < p.DH && x < p.DW) {
+#pragma unroll
+                        for (int i = 0; i < 8; ++i) {
+                            const int cl = orow + 4 * i;
+                            const int oc = ti.och0 + 32 * q + cl;
+                            if (oc >= p.DC) continue;
+                            const float4 v = *reinterpret_cast<const float4 *>(stg + cl * EP_PITCH + ocol);
+                            float *d = p.dst + plane * ((long long)oc + (long long)p.DC * ti.n) + x +
+                                       (long long)p.DW * y;
+                            if (vec_rows && x + 3 < p.DW) {
+                                *reinterpret_cast<float4 *>(d) = v;
+                            } else {
+                                d[0] = v.x;
+                                if (x + 1 < p.DW) d[1] = v.y;
+                                if (x + 2 < p.DW) d[2] = v.z;
+                                if (x + 3 < p.DW) d[3] = v.w;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+            } else {
             for (int cc = 0; cc < BN / 16; ++cc) {
                 uint32_t r[16];
                 tmem_ld16(taddr + cc * 16, r);
                 tmem_ld_wait();
                 if (och >= p.DC) continue;
-                if (TMA_B) {
-                    // 16 consecutive pixels of one rectangle row (BX >= 16)
-                    const int e0 = cc * 16;
-                    const int x = ti.x0 + (e0 % p.BX), y = ti.y0 + e0 / p.BX;
-                    if (y >= p.DH || x >= p.DW) continue;
-                    float *d = dplane + x + (long long)p.DW * y;
-                    if (vec_rows && x + 15 < p.DW) {
-#pragma unroll
-                        for (int e = 0; e < 4; ++e)
-                            reinterpret_cast<float4 *>(d)[e] =
-                                make_float4(__uint_as_float(r[4 * e]), __uint_as_float(r[4 * e + 1]),
-                                            __uint_as_float(r[4 * e + 2]), __uint_as_float(r[4 * e + 3]));
-                    } else {
-#pragma unroll
-                        for (int e = 0; e < 16; ++e)
-                            if (x + e < p.DW) d[e] = __uint_as_float(r[e]);
-                    }
-                } else {
+                {
                     const long long pix0 = ti.p0 + cc * 16;
                     if (pix0 >= ti.npix) continue;
                     int X = (int)(pix0 % ti.MX);
@@ -314,7 +345,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         const long long xo = p.mode == 0 ? X : ti.rx + (long long)p.sx * X;
                         const long long yo = p.mode == 0 ? Y : ti.ry + (long long)p.sy * Y;
                         p.dst[xo + p.DW * yo + plane * (och + (long long)p.DC * n)] =
-                            __uint_as_float(r[e]);
+                            (FP8 ? p.out_scale[och] : 1.0f) * __uint_as_float(r[e]);
                         if (++X == ti.MX) {
                             X = 0;
                             if (++Y == ti.MY) {
@@ -325,6 +356,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     }
                 }
             }
+            }
             tc_fence_before();
             mbar_arrive(&sm->tmem_empty[b]);
             ++acc_it;
@@ -332,7 +364,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     } else if (warp == 8) {
         // ---------------- MMA issuer
         if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(BM, BN, 0, 0);
+            const uint32_t idesc = FP8 ? idesc_e4m3(BM, BN) : idesc_bf16(BM, BN, 0, 0);
             uint32_t it = 0, acc_it = 0;
             bool issued = false;
             for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
@@ -354,10 +386,13 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     const uint32_t sa = smem_u32(a_stage + s * A_BYTES);
                     const uint32_t sbb = smem_u32(b_stage + s * B_BYTES);
 #pragma unroll
-                    for (int k = 0; k < BK / 16; ++k) {
+                    for (int k = 0; k < 4; ++k) {  // 4 x 32 bytes of K per stage
                         const uint64_t ad = smem_desc(sa + k * 32, 16, 1024);
                         const uint64_t bd = smem_desc(sbb + k * 32, 16, 1024);
-                        mma_f16(d_tmem, ad, bd, idesc, (kb | k) != 0);
+                        if (FP8)
+                            mma_f8(d_tmem, ad, bd, idesc, (kb | k) != 0);
+                        else
+                            mma_f16(d_tmem, ad, bd, idesc, (kb | k) != 0);
                     }
                     mma_commit(&sm->empty[s]);
                     issued = true;
@@ -390,12 +425,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     const int u = p.tap_u[tq], v = p.tap_v[tq];
                     mbar_arrive_expect_tx(&sm->full[s], TMA_B ? A_BYTES + B_BYTES : A_BYTES);
                     tma_load_2d(smem_u32(a_stage + s * A_BYTES), &wmap, &sm->full[s],
-                                (u + p.fw * v) * p.SCpad + cchunk * BK, ti.och0);
+                                (u + p.fw * v) * p.SCpad + cchunk * (FP8 ? 128 : 64), ti.och0);
                     if (TMA_B) {
                         int offx, offy;
                         tap_offsets(p, ti, u, v, offx, offy);
                         tma_load_4d(smem_u32(b_stage + s * B_BYTES), &xmap, &sm->full[s],
-                                    cchunk * BK, ti.x0 + offx, ti.y0 + offy, ti.n);
+                                    cchunk * (FP8 ? 128 : 64), ti.x0 + offx, ti.y0 + offy, ti.n);
                     }
                 }
             }
@@ -722,6 +757,107 @@ __global__ void weights_bf16_kernel(const float *__restrict__ w, int fw, int fh,
     }
 }
 
+// ---- FP8-E4M3 operands -----------------------------------------------------
+// |x| maximum over n floats, as float bits (non-negative floats order like
+// their bit patterns); *out must start at 0
+__global__ void amax_kernel(const float *__restrict__ x, long long n, unsigned int *out) {
+    float m = 0.f;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        m = fmaxf(m, fabsf(x[i]));
+    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(m));
+}
+
+// per-output-channel |w| maximum of a (fw,fh,C,K) filter -> scale = amax/448
+__global__ void weight_scale_kernel(const float *__restrict__ w, long long per_k, int K,
+                                    float *__restrict__ scale) {
+    const int k = blockIdx.x;
+    if (k >= K) return;
+    float m = 0.f;
+    for (long long i = threadIdx.x; i < per_k; i += blockDim.x) m = fmaxf(m, fabsf(w[i + per_k * k]));
+    __shared__ float red[32];
+    for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+        for (int off = 16; off > 0; off >>= 1) m = fmaxf(m, __shfl_down_sync(0xffffffffu, m, off));
+        if (threadIdx.x == 0) scale[k] = m > 0.f ? m / 448.0f : 1.0f;
+    }
+}
+
+// activation scale = amax/448; combined epilogue factor per output channel
+__global__ void combine_scale_kernel(const unsigned int *amax_bits, const float *wscale, int K,
+                                     float *act_scale, float *out_scale) {
+    const float a = __uint_as_float(*amax_bits);
+    const float as = a > 0.f ? a / 448.0f : 1.0f;
+    if (blockIdx.x == 0 && threadIdx.x == 0) *act_scale = as;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < K; k += gridDim.x * blockDim.x)
+        out_scale[k] = as * wscale[k];
+}
+
+__device__ __forceinline__ unsigned char to_e4m3(float v) {
+    return (unsigned char)__nv_cvt_float_to_fp8(v, __NV_SATFINITE, __NV_E4M3);
+}
+
+// f32 ArrayFire (W,H,C,N) -> e4m3 [N][H][W][Cpad] of x / act_scale
+__global__ void __launch_bounds__(256) to_nhwc_e4m3_kernel(const float *__restrict__ in, int W,
+                                                           int H, int C, int N, int Cpad,
+                                                           const float *act_scale,
+                                                           unsigned char *__restrict__ out) {
+    __shared__ float tile[64][65];
+    const int x0 = blockIdx.x * 64;
+    const int yn = blockIdx.y;
+    const int y = yn % H, n = yn / H;
+    const int c0 = blockIdx.z * 64;
+    const long long plane = (long long)W * H;
+    const int t = threadIdx.x;
+    const float inv = 1.0f / *act_scale;
+    for (int e = t; e < 64 * 64; e += 256) {
+        const int ci = e >> 6, xi = e & 63;
+        const int c = c0 + ci, x = x0 + xi;
+        float v = 0.f;
+        if (c < C && x < W) v = in[x + (long long)W * y + plane * (c + (long long)C * n)];
+        tile[ci][xi] = v * inv;
+    }
+    __syncthreads();
+    const int lane = t & 31, warp = t >> 5;
+    const int cg = lane & 7;
+#pragma unroll
+    for (int pass = 0; pass < 2; ++pass) {
+        const int xi = pass * 32 + warp * 4 + (lane >> 3);
+        const int x = x0 + xi;
+        if (x < W) {
+            uint2 w;
+            w.x = (uint32_t)to_e4m3(tile[cg * 8 + 0][xi]) | ((uint32_t)to_e4m3(tile[cg * 8 + 1][xi]) << 8) |
+                  ((uint32_t)to_e4m3(tile[cg * 8 + 2][xi]) << 16) | ((uint32_t)to_e4m3(tile[cg * 8 + 3][xi]) << 24);
+            w.y = (uint32_t)to_e4m3(tile[cg * 8 + 4][xi]) | ((uint32_t)to_e4m3(tile[cg * 8 + 5][xi]) << 8) |
+                  ((uint32_t)to_e4m3(tile[cg * 8 + 6][xi]) << 16) | ((uint32_t)to_e4m3(tile[cg * 8 + 7][xi]) << 24);
+            *reinterpret_cast<uint2 *>(out + (((long long)n * H + y) * W + x) * Cpad + c0 + cg * 8) = w;
+        }
+    }
+}
+
+// forward weights -> e4m3 Wt[k][tap*Cpad + c] of w[fw-1-u, fh-1-v, c, k] / wscale[k]
+__global__ void weights_e4m3_kernel(const float *__restrict__ w, int fw, int fh, int C, int K,
+                                    int och_pad, int in_pad, const float *__restrict__ wscale,
+                                    unsigned char *__restrict__ out) {
+    const long long total = (long long)och_pad * fw * fh * in_pad;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int c = (int)(t % in_pad);
+        const long long r = t / in_pad;
+        const int tap = (int)(r % (fw * fh));
+        const int k = (int)(r / (fw * fh));
+        const int u = tap % fw, v = tap / fw;
+        float val = 0.f;
+        if (c < C && k < K)
+            val = w[(fw - 1 - u) + fw * ((fh - 1 - v) + fh * (c + (long long)C * k))] / wscale[k];
+        out[t] = to_e4m3(val);
+    }
+}
+
 // ===========================================================================
 // host side
 // ===========================================================================
@@ -745,31 +881,34 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 2-D bf16 tensor [rows][cols] (cols contiguous), box 64 x 128, 128B swizzle
-static CUtensorMap make_wmap(const __nv_bfloat16 *ptr, long long rows, long long cols) {
+// 2-D tensor [rows][cols] (cols contiguous) of bf16 (esize 2) or e4m3 bytes
+// (esize 1), box 128 bytes x 128 rows, 128B swizzle
+static CUtensorMap make_wmap(const void *ptr, long long rows, long long cols, int esize = 2) {
     CUtensorMap m;
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
-    cuuint64_t strides[1] = {(cuuint64_t)cols * 2};
-    cuuint32_t box[2] = {64, 128};
+    cuuint64_t strides[1] = {(cuuint64_t)cols * esize};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / esize), 128};
     cuuint32_t es[2] = {1, 1};
-    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, (void *)ptr, dims, strides, box,
+    CUresult r = encode_fn()(&m, esize == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8,
+                             2, (void *)ptr, dims, strides, box,
                              es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) AFGB_THROW(AF_ERR_INTERNAL, "cuTensorMapEncodeTiled (weights) failed");
     return m;
 }
 
-// 4-D bf16 NHWC tensor (Cpad, W, H, N), box {64, bx, by, 1}, 128B swizzle,
-// out-of-range elements read as zero
-static CUtensorMap make_imap(const __nv_bfloat16 *ptr, int Cpad, int W, int H, int N, int bx,
-                             int by) {
+// 4-D NHWC tensor (Cpad, W, H, N) of bf16 (esize 2) or e4m3 bytes (esize 1),
+// box {128 bytes, bx, by, 1}, 128B swizzle, out-of-range elements read as zero
+static CUtensorMap make_imap(const void *ptr, int Cpad, int W, int H, int N, int bx, int by,
+                             int esize = 2) {
     CUtensorMap m;
     cuuint64_t dims[4] = {(cuuint64_t)Cpad, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
-    cuuint64_t strides[3] = {(cuuint64_t)Cpad * 2, (cuuint64_t)Cpad * 2 * W,
-                             (cuuint64_t)Cpad * 2 * W * H};
-    cuuint32_t box[4] = {64, (cuuint32_t)bx, (cuuint32_t)by, 1};
+    cuuint64_t strides[3] = {(cuuint64_t)Cpad * esize, (cuuint64_t)Cpad * esize * W,
+                             (cuuint64_t)Cpad * esize * W * H};
+    cuuint32_t box[4] = {(cuuint32_t)(128 / esize), (cuuint32_t)bx, (cuuint32_t)by, 1};
     cuuint32_t es[4] = {1, 1, 1, 1};
-    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, (void *)ptr, dims, strides, box,
+    CUresult r = encode_fn()(&m, esize == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8,
+                             4, (void *)ptr, dims, strides, box,
                              es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) AFGB_THROW(AF_ERR_INTERNAL, "cuTensorMapEncodeTiled (image) failed");
@@ -809,38 +948,86 @@ static void pick_rect(int W, int H, int area, int minx, int &bx, int &by) {
     }
 }
 
-static size_t gather_smem() { return 1024 + STAGES * (A_BYTES + B_BYTES) + sizeof(Smem) + 64; }
+static size_t gather_smem() {
+    return 1024 + STAGES * (A_BYTES + B_BYTES) + 4 * 32 * EP_PITCH * sizeof(float) + sizeof(Smem) + 64;
+}
 
-// forward (mode 0) or data gradient (mode 1)
+// forward (mode 0) or data gradient (mode 1); fp8 (forward only): e4m3
+// operands with a per-tensor activation scale and per-output-channel weight
+// scales (`user_wscale`, K floats, or amax/448 computed on the device)
 static void run_gather(const NNGeom &g, int mode, const float *img_f32, const float *w_f32,
-                       float *dst) {
+                       float *dst, bool fp8 = false, const float *user_wscale = nullptr) {
     const int SW = mode == 0 ? (int)g.W : (int)g.Wo;
     const int SH = mode == 0 ? (int)g.H : (int)g.Ho;
     const int SC = mode == 0 ? (int)g.C : (int)g.K;
     const int DW = mode == 0 ? (int)g.Wo : (int)g.W;
     const int DH = mode == 0 ? (int)g.Ho : (int)g.H;
     const int DC = mode == 0 ? (int)g.K : (int)g.C;
-    const int SCpad = round_up(SC, 64);
+    const int CH = fp8 ? 128 : 64;  // channels per 128-byte row
+    const int SCpad = round_up(SC, CH);
     const int OCpad = round_up(DC, 128);
     const int taps = (int)(g.fw * g.fh);
     const bool tma_b = g.sx == 1 && g.sy == 1;
+    const int esize = fp8 ? 1 : 2;
 
-    __nv_bfloat16 *img = to_nhwc(img_f32, SW, SH, SC, (int)g.N, SCpad);
-    __nv_bfloat16 *wt = static_cast<__nv_bfloat16 *>(
-        alloc_device((size_t)OCpad * taps * SCpad * sizeof(__nv_bfloat16)));
-    {
+    void *img = nullptr, *wt = nullptr;
+    float *scales = nullptr;  // [0] activation scale, [1..K] weight scales, [K+1..2K] output factors
+    unsigned int *amax = nullptr;
+    if (!fp8) {
+        img = to_nhwc(img_f32, SW, SH, SC, (int)g.N, SCpad);
+        wt = alloc_device((size_t)OCpad * taps * SCpad * 2);
         long long total = (long long)OCpad * taps * SCpad;
         unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
         weights_bf16_kernel<<<blocks, 256, 0, stream()>>>(w_f32, (int)g.fw, (int)g.fh, (int)g.C,
-                                                          (int)g.K, mode, OCpad, SCpad, wt);
+                                                          (int)g.K, mode, OCpad, SCpad,
+                                                          static_cast<__nv_bfloat16 *>(wt));
         count_launch();
         AFGB_POST_LAUNCH("weights_bf16_kernel");
+    } else {
+        const int K = (int)g.K;
+        scales = static_cast<float *>(alloc_device((size_t)(2 * K + 1) * sizeof(float)));
+        amax = static_cast<unsigned int *>(alloc_device(sizeof(unsigned int)));
+        AFGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned int), stream()));
+        const long long nx = (long long)SW * SH * SC * g.N;
+        amax_kernel<<<std::max(1, std::min(num_sms() * 8, (int)((nx + 255) / 256))), 256, 0, stream()>>>(
+            img_f32, nx, amax);
+        count_launch();
+        AFGB_POST_LAUNCH("amax_kernel");
+        const float *wscale = user_wscale;
+        if (!wscale) {
+            weight_scale_kernel<<<K, 256, 0, stream()>>>(w_f32, g.fw * g.fh * g.C, K, scales + 1);
+            count_launch();
+            AFGB_POST_LAUNCH("weight_scale_kernel");
+            wscale = scales + 1;
+        }
+        combine_scale_kernel<<<(K + 255) / 256, 256, 0, stream()>>>(amax, wscale, K, scales,
+                                                                  scales + 1 + K);
+        count_launch();
+        AFGB_POST_LAUNCH("combine_scale_kernel");
+        img = alloc_device((size_t)SW * SH * g.N * SCpad);
+        dim3 cgrid((unsigned)((SW + 63) / 64), (unsigned)(SH * g.N), (unsigned)(SCpad / 64));
+        {
+            KernelTimer kt("tc_convert_kernel");
+            to_nhwc_e4m3_kernel<<<cgrid, 256, 0, stream()>>>(img_f32, SW, SH, SC, (int)g.N, SCpad,
+                                                             scales, static_cast<unsigned char *>(img));
+        }
+        count_launch();
+        AFGB_POST_LAUNCH("to_nhwc_e4m3_kernel");
+        wt = alloc_device((size_t)OCpad * taps * SCpad);
+        long long total = (long long)OCpad * taps * SCpad;
+        unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
+        weights_e4m3_kernel<<<blocks, 256, 0, stream()>>>(w_f32, (int)g.fw, (int)g.fh, (int)g.C, K,
+                                                          OCpad, SCpad, wscale,
+                                                          static_cast<unsigned char *>(wt));
+        count_launch();
+        AFGB_POST_LAUNCH("weights_e4m3_kernel");
     }
 
     GatherParams p;
     std::memset(&p, 0, sizeof(p));
-    p.src = img;
+    p.src = static_cast<const unsigned char *>(img);
     p.dst = dst;
+    p.out_scale = fp8 ? scales + 1 + g.K : nullptr;
     p.SW = SW;
     p.SH = SH;
     p.SCpad = SCpad;
@@ -856,7 +1043,7 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     p.dx = (int)g.dx;
     p.dy = (int)g.dy;
     p.fw = (int)g.fw;
-    p.nchunk = SCpad / 64;
+    p.nchunk = SCpad / CH;
     p.n_och_tiles = OCpad / 128;
     p.nphx = (mode == 0 || tma_b) ? 1 : (int)g.sx;
     p.nphase = (mode == 0 || tma_b) ? 1 : (int)(g.sx * g.sy);
@@ -884,33 +1071,37 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     CUtensorMap xmap;
     std::memset(&xmap, 0, sizeof(xmap));
     if (tma_b) {
-        pick_rect(DW, DH, BN, 16, p.BX, p.BY);
+        pick_rect(DW, DH, BN, 32, p.BX, p.BY);
         p.ntx = (DW + p.BX - 1) / p.BX;
         p.nty = (DH + p.BY - 1) / p.BY;
         ntile = p.n_och_tiles * p.ntx * p.nty * (int)g.N;
-        xmap = make_imap(img, SCpad, SW, SH, (int)g.N, p.BX, p.BY);
+        xmap = make_imap(img, SCpad, SW, SH, (int)g.N, p.BX, p.BY, esize);
     }
     p.total_tiles = ntile;
 
-    CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad);
+    CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad, esize);
     const size_t smem = gather_smem();
     if (ntile > 0) {
         const int grid = std::min(ntile, num_sms());
-        KernelTimer kt(mode == 0 ? "tc_fwd_kernel" : "tc_dgrad_kernel");
-        if (tma_b) {
-            AFGB_CUDA(cudaFuncSetAttribute(gather_conv_kernel<true>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            gather_conv_kernel<true><<<grid, NUM_THREADS, smem, stream()>>>(p, wmap, xmap);
-        } else {
-            AFGB_CUDA(cudaFuncSetAttribute(gather_conv_kernel<false>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-            gather_conv_kernel<false><<<grid, NUM_THREADS, smem, stream()>>>(p, wmap, xmap);
-        }
+        KernelTimer kt(fp8 ? "tc_fwd_fp8_kernel" : (mode == 0 ? "tc_fwd_kernel" : "tc_dgrad_kernel"));
+#define AFGB_LAUNCH_GATHER(TB, F8)                                                               \
+    do {                                                                                         \
+        AFGB_CUDA(cudaFuncSetAttribute(gather_conv_kernel<TB, F8>,                               \
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+        gather_conv_kernel<TB, F8><<<grid, NUM_THREADS, smem, stream()>>>(p, wmap, xmap);        \
+    } while (0)
+        if (tma_b && fp8) AFGB_LAUNCH_GATHER(true, true);
+        else if (tma_b) AFGB_LAUNCH_GATHER(true, false);
+        else if (fp8) AFGB_LAUNCH_GATHER(false, true);
+        else AFGB_LAUNCH_GATHER(false, false);
+#undef AFGB_LAUNCH_GATHER
         count_launch();
         AFGB_POST_LAUNCH("gather_conv_kernel");
     }
     free_device(wt);
     free_device(img);
+    if (scales) free_device(scales);
+    if (amax) free_device(amax);
 }
 
 // the gather kernel's limits: phases and taps fit the parameter block,
@@ -935,9 +1126,13 @@ unsigned int tc_take_error() {
 
 bool tc_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out,
                 afgb_precision prec, const Array *scales) {
-    if (prec != AFGB_PRECISION_BF16) return false;  // FP8 arrives with its own kernel
-    (void)scales;
     if (sig.type != f32 || !gather_fits(g, 0)) return false;
+    if (prec == AFGB_PRECISION_FP8_E4M3) {
+        run_gather(g, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>(), true,
+                   scales ? scales->ptr<float>() : nullptr);
+        return true;
+    }
+    if (prec != AFGB_PRECISION_BF16) return false;
     run_gather(g, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>());
     return true;
 }

@@ -97,3 +97,51 @@ def test_bf16_config3a_sampled(af, oracle):
     ref = oracle.nn_forward_points_f64(s, f, (1, 1), (1, 1), (1, 1), idx)
     rel = np.linalg.norm(out[idx] - ref) / np.linalg.norm(ref)
     assert rel <= REL
+
+
+# ---- FP8-E4M3 forward ------------------------------------------------------
+# e4m3 keeps 3 mantissa bits: with amax scaling each operand carries up to
+# 2^-4 relative rounding error (rms ~3.6%), so the norm-wise relative error of
+# the forward is a few percent.  Bound: 8e-2 norm-wise, 0.3 * max|ref| max-abs.
+FP8_REL = 8e-2
+FP8_CASES = [c for c in TC_CASES if c[0] in ("nn_multi", "nn_s2_c16", "nn_1x1", "tc_c64_k128",
+                                              "tc_c128_k256_s2", "tc_c200_k130", "tc_1x1_c256")]
+
+
+@pytest.mark.parametrize("case", FP8_CASES, ids=[c[0] for c in FP8_CASES])
+def test_fp8_forward(af, oracle, case):
+    name, sd, fd, st, pd, dl = case
+    s, f = C.nn_inputs(case, 8100)
+    out = af.convolve2_nn(af.Array.from_numpy(s), af.Array.from_numpy(f), st, pd, dl,
+                          precision="fp8").to_numpy()
+    ref = oracle.nn_forward_f64(s, f, st, pd, dl)
+    rel = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+    mx = np.abs(out - ref).max() / np.abs(ref).max()
+    assert rel <= FP8_REL and mx <= 0.3, f"rel {rel:.3e} max {mx:.3e}"
+
+
+def test_fp8_forward_user_scales(af, oracle):
+    """Per-output-channel scales supplied by the caller (afgb_convolve2_nn_ex
+    out_channel_scales): same result quality as the device-derived scales."""
+    case = FP8_CASES[3]
+    name, sd, fd, st, pd, dl = case
+    s, f = C.nn_inputs(case, 8200)
+    scales = (np.abs(f).reshape(-1, fd[3], order="F").max(axis=0) / 448.0).astype(np.float32)
+    out = af.convolve2_nn(af.Array.from_numpy(s), af.Array.from_numpy(f), st, pd, dl,
+                          precision="fp8", scales=af.Array.from_numpy(scales)).to_numpy()
+    ref = oracle.nn_forward_f64(s, f, st, pd, dl)
+    rel = np.linalg.norm(out - ref) / np.linalg.norm(ref)
+    assert rel <= FP8_REL
+
+
+def test_fp8_gradients_not_supported(af):
+    """FP8 is a forward-only form; gradients report AF_ERR_NOT_SUPPORTED."""
+    case = C.NN_CASES[7]
+    name, sd, fd, st, pd, dl = case
+    s, f = C.nn_inputs(case, 1)
+    g = C.nn_grad(case, 1)
+    S, F, G = af.Array.from_numpy(s), af.Array.from_numpy(f), af.Array.from_numpy(g)
+    O = af.convolve2_nn(S, F, st, pd, dl)
+    with pytest.raises(af.AfError) as e:
+        af.convolve2_gradient_nn(G, S, F, O, st, pd, dl, af.AF_CONV_GRADIENT_DATA, precision="fp8")
+    assert e.value.code == af.AF_ERR_NOT_SUPPORTED
