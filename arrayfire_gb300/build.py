@@ -24,6 +24,7 @@ SOURCES = [
     "afgb_runtime.cpp",
     "afgb_conv_api.cpp",
     "conv_direct.cu",
+    "conv_tma.cu",
     "nn_simt.cu",
     "nn_tc.cu",
 ]

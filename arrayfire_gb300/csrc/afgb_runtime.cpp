@@ -155,8 +155,10 @@ cudaStream_t stream() {
 
 int num_sms() { return dev_state(device()).sms; }
 
+unsigned int tma_take_error();
+
 void check_device_errors() {
-    unsigned int w = tc_take_error();
+    unsigned int w = tc_take_error() | tma_take_error();
     if (w) {
         AFGB_THROW(AF_ERR_RUNTIME, "a tensor-core kernel pipeline wait timed out (code " +
                                        std::to_string(w) + "); its results are invalid");

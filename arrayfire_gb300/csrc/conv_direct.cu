@@ -29,41 +29,10 @@
 
 #include "conv_common.cuh"
 #include "conv_direct.hpp"
+#include "conv_params.cuh"
+#include "conv_tma.hpp"
 
 namespace afgb {
-
-// ---------------------------------------------------------------------------
-// parameters
-// ---------------------------------------------------------------------------
-struct DirectParams {
-    const void *sig;
-    const void *filt;
-    void *out;
-    int rank;
-    int expand;
-    long long sd[4], ss[4];
-    long long od[4], os[4];
-    long long fd[4], fs[4];
-    long long in_step[4], out_step[4], filt_step[4];
-    long long batch[4];
-    long long nbatch;
-};
-
-struct BatchOff {
-    long long in, out, filt;
-};
-
-__device__ __forceinline__ BatchOff batch_offsets(const DirectParams &p, long long b) {
-    long long b1 = b % p.batch[1];
-    long long r = b / p.batch[1];
-    long long b2 = r % p.batch[2];
-    long long b3 = r / p.batch[2];
-    BatchOff o;
-    o.in = b1 * p.in_step[1] + b2 * p.in_step[2] + b3 * p.in_step[3];
-    o.out = b1 * p.out_step[1] + b2 * p.out_step[2] + b3 * p.out_step[3];
-    o.filt = b1 * p.filt_step[1] + b2 * p.filt_step[2] + b3 * p.filt_step[3];
-    return o;
-}
 
 // ---------------------------------------------------------------------------
 // generic kernel: one output per thread, any rank/dtype/stride
@@ -827,6 +796,7 @@ void launch_convolve_nd(const Array &sig, const Array &filt, Array &out, int kin
     if (out.elements() == 0) return;
     DirectParams p = make_params(sig, filt, out, kind, rank, expand);
     const bool exact = exact_fp();
+    if (rank == 2 && p.nbatch > 0 && dtma::tma_convolve2(p, sig.type, exact)) return;
     if (rank == 2) {
         bool done = false;
         switch (sig.type) {
@@ -926,6 +896,9 @@ void launch_convolve2_sep(const Array &sig, const Array &cfilt, const Array &rfi
     const long long nb = sig.dims[2] * sig.dims[3];
     const af_dtype t = sig.type;
     const bool fused_type = (t == f32 || t == u8 || t == s8 || t == b8);
+    if (fused_type && dtma::tma_convolve2_sep(sig, cfilt.ptr<float>(), rfilt.ptr<float>(), (int)cfl,
+                                              (int)rfl, out, expand, exact_fp()))
+        return;
     if (fused_type && nb <= 65535 && cfl <= 31 && rfl <= 31) {
         SepParams p;
         std::memset(&p, 0, sizeof(p));

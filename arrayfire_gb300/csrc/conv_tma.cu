@@ -1,0 +1,592 @@
+// TMA-staged direct convolutions (2-D filters and the fused separable pair)
+// for dense, 16-byte-aligned f32 and 8-bit images.
+//
+// Each CTA is persistent: it walks 64x64 output tiles with a stride of the
+// grid, and one thread keeps the next tile's haloed input window in flight
+// with a 3-D TMA box load (x, y, image) while the CTA computes the current
+// one.  The TMA fills coordinates outside the image with zeros, which is the
+// convolution's zero padding, so no thread computes an address or a bounds
+// check for the input.  The box's x origin is rounded down to the 16-byte
+// TMA alignment; the compute loops absorb that shift with compile-time
+// indices.
+//
+// Arithmetic is the reference's (src/backend/cpu/kernel/convolve.hpp):
+// products accumulate from zero with the outer-dimension taps outside and
+// dim-0 taps inside.  Two outputs share one packed f32x2 instruction where
+// their operands form aligned register pairs; packed multiply and add round
+// each lane separately, so the exact mode stays bit-identical.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <mutex>
+
+#include "conv_common.cuh"
+#include "conv_params.cuh"
+#include "conv_tma.hpp"
+#include "tc_ptx.cuh"
+
+namespace afgb {
+namespace dtma {
+
+using tc::fence_barrier_init;
+using tc::mbar_arrive_expect_tx;
+using tc::mbar_init;
+using tc::mbar_try_wait;
+using tc::smem_u32;
+
+constexpr int TILE = 64;
+constexpr int THREADS = 256;
+
+// ---------------------------------------------------------------- f32x2
+typedef unsigned long long f2;
+__device__ __forceinline__ f2 pk(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void upk(f2 r, float &a, float &b) {
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+template <bool EXACT>
+__device__ __forceinline__ f2 mac2(f2 acc, f2 a, f2 b) {
+    f2 d;
+    if (EXACT) {
+        f2 p;
+        asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(p) : "l"(a), "l"(b));
+        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(acc), "l"(p));
+    } else {
+        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(acc));
+    }
+    return d;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, uint64_t *bar,
+                                            int c0, int c1, int c2) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+        "[%0], [%1, {%3, %4, %5}], [%2];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
+        : "memory");
+}
+
+// bounded wait on a TMA barrier; false (and the error word raised) on timeout
+__device__ __forceinline__ bool wait_tile(uint64_t *bar, uint32_t parity) {
+    unsigned n = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if (++n > tc::kSpinLimit) {
+            atomicOr(&tc::g_tc_error, 256u);
+            return false;
+        }
+    }
+    return true;
+}
+
+template <typename T> __device__ __forceinline__ float to_f(T v) { return (float)v; }
+
+// geometry of a haloed tile for an F0 x F1 filter (shared by both kernels)
+template <typename T, int F0, int F1, bool EXPAND>
+struct Halo {
+    static constexpr int ES = sizeof(T);
+    static constexpr int A = 16 / ES;                 // TMA x alignment (elements)
+    static constexpr int C0 = EXPAND ? 0 : F0 / 2;
+    static constexpr int C1 = EXPAND ? 0 : F1 / 2;
+    static constexpr int LX = F0 - 1 - C0;            // halo left of the tile
+    static constexpr int LY = F1 - 1 - C1;            // halo above the tile
+    static constexpr int LT = (LX + A - 1) / A * A;   // TMA lead (aligned)
+    static constexpr int LF = (LX + 3) / 4 * 4;       // float tile lead
+    static constexpr int OFF = LF - LX;               // window shift, 0..3
+    static constexpr int BH = TILE + F1 - 1;
+    // float tile pitch: covers the right halo and the widest window read
+    static constexpr int PF0 = (LF + TILE + C0 + 3) / 4 * 4;
+    static constexpr int PF = PF0 + 8;
+    // TMA box width (elements); f32 loads straight into the float layout
+    static constexpr int BW = ES == 4 ? PF : (LT + TILE + C0 + A - 1) / A * A;
+    static constexpr int TBYTES = BH * BW * ES;
+    static constexpr int TB_ALIGNED = (TBYTES + 127) / 128 * 128;
+    static constexpr int FT_BYTES = ES == 4 ? 0 : (BH * PF * 4 + 127) / 128 * 128;
+};
+
+// 8-bit tile -> float tile (shifted so that the float tile starts at x0 - LF)
+template <typename T, typename H>
+__device__ __forceinline__ void widen_tile(const T *tb, float *ft) {
+    constexpr int SHIFT = H::LT - H::LF;
+    for (int e = threadIdx.x; e < H::BH * H::PF; e += THREADS) {
+        const int r = e / H::PF, c = e - r * H::PF;
+        const int cs = c + SHIFT;
+        ft[e] = cs < H::BW ? to_f<T>(tb[r * H::BW + cs]) : 0.0f;
+    }
+}
+
+// ===========================================================================
+// 2-D direct convolution, F0 x F1 filter, 64x64 tile, 4x4 outputs per thread
+// ===========================================================================
+template <typename T, int F0, int F1, bool EXACT, bool EXPAND>
+__global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constant__ CUtensorMap smap,
+                                                            const DirectParams p, long long tiles_x,
+                                                            long long tiles_y, long long ntiles) {
+    using H = Halo<T, F0, F1, EXPAND>;
+    constexpr int NW4 = (H::OFF + 4 + F0 - 1 + 3) / 4;
+    static_assert(60 + 4 * NW4 <= H::PF, "window exceeds the tile pitch");
+    extern __shared__ __align__(128) unsigned char sm[];
+    T *tb[2] = {reinterpret_cast<T *>(sm), reinterpret_cast<T *>(sm + H::TB_ALIGNED)};
+    float *ft = reinterpret_cast<float *>(sm + 2 * H::TB_ALIGNED);
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + 2 * H::TB_ALIGNED + H::FT_BYTES);
+    const int tid = threadIdx.x;
+    const long long slice = p.sd[0] * p.sd[1];
+
+    if (tid == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](long long t, int buf) {
+        const long long tx = t % tiles_x, r = t / tiles_x;
+        const long long ty = r % tiles_y, b = r / tiles_y;
+        const BatchOff bo = batch_offsets(p, b);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive_expect_tx(&full[buf], H::TBYTES);
+        tma_load_3d(smem_u32(tb[buf]), &smap, &full[buf], (int)(tx * TILE - H::LT),
+                    (int)(ty * TILE - H::LY), (int)(bo.in / slice));
+    };
+
+    long long tile = blockIdx.x;
+    if (tid == 0 && tile < ntiles) issue(tile, 0);
+    const int tx = tid & 15, ty = tid >> 4;
+    for (int k = 0; tile < ntiles; tile += gridDim.x, ++k) {
+        const int buf = k & 1;
+        if (tid == 0 && tile + gridDim.x < ntiles) issue(tile + gridDim.x, buf ^ 1);
+        const long long ttx = tile % tiles_x, r = tile / tiles_x;
+        const long long tty = r % tiles_y, b = r / tiles_y;
+        const BatchOff bo = batch_offsets(p, b);
+        const float *w = static_cast<const float *>(p.filt) + bo.filt;
+        float wr[F0 * F1];
+#pragma unroll
+        for (int fj = 0; fj < F1; ++fj)
+#pragma unroll
+            for (int fi = 0; fi < F0; ++fi) wr[fj * F0 + fi] = __ldg(w + fi * p.fs[0] + fj * p.fs[1]);
+        if (!wait_tile(&full[buf], (k >> 1) & 1)) break;
+        const float *tile_f;
+        if (sizeof(T) == 4) {
+            tile_f = reinterpret_cast<const float *>(tb[buf]);
+        } else {
+            widen_tile<T, H>(tb[buf], ft);
+            __syncthreads();
+            tile_f = ft;
+        }
+
+        float acc[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
+#pragma unroll
+        for (int q = 3 + F1 - 1; q >= 0; --q) {
+            float v[NW4 * 4];
+            const float *row = tile_f + (4 * ty + q) * H::PF + 4 * tx;
+#pragma unroll
+            for (int u = 0; u < NW4; ++u) {
+                const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
+                v[4 * u] = t4.x;
+                v[4 * u + 1] = t4.y;
+                v[4 * u + 2] = t4.z;
+                v[4 * u + 3] = t4.w;
+            }
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const int fj = rr + F1 - 1 - q;
+                if (fj >= 0 && fj < F1) {
+#pragma unroll
+                    for (int fi = 0; fi < F0; ++fi) {
+                        const float wv = wr[fj * F0 + fi];
+#pragma unroll
+                        for (int cc = 0; cc < 4; ++cc)
+                            acc[rr][cc] = mac<EXACT>(acc[rr][cc], v[cc + H::OFF + F0 - 1 - fi], wv);
+                    }
+                }
+            }
+        }
+        T *out = static_cast<T *>(p.out) + bo.out;
+        const long long x = ttx * TILE + 4 * tx;
+        const bool vec = (x + 3 < p.od[0]) && ((p.os[1] & 3) == 0) &&
+                         ((reinterpret_cast<uintptr_t>(out) % (4 * sizeof(T))) == 0);
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+            const long long y = tty * TILE + 4 * ty + rr;
+            if (y >= p.od[1] || x >= p.od[0]) continue;
+            T *dst = out + y * p.os[1] + x;
+            if (vec) {
+                if constexpr (sizeof(T) == 4) {
+                    *reinterpret_cast<float4 *>(dst) =
+                        make_float4(acc[rr][0], acc[rr][1], acc[rr][2], acc[rr][3]);
+                } else {
+                    const uint32_t w4 = (uint32_t)(uint8_t)from_acc<T>(acc[rr][0]) |
+                                        ((uint32_t)(uint8_t)from_acc<T>(acc[rr][1]) << 8) |
+                                        ((uint32_t)(uint8_t)from_acc<T>(acc[rr][2]) << 16) |
+                                        ((uint32_t)(uint8_t)from_acc<T>(acc[rr][3]) << 24);
+                    *reinterpret_cast<uint32_t *>(dst) = w4;
+                }
+            } else {
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc)
+                    if (x + cc < p.od[0]) dst[cc] = from_acc_any(acc[rr][cc], T{});
+            }
+        }
+        __syncthreads();  // the buffer is reloaded two tiles from now
+    }
+}
+
+// ===========================================================================
+// fused separable convolution: column pass (dim 0) into a shared temp image,
+// row pass (dim 1) to the output; CFL/RFL compile-time filter lengths
+// ===========================================================================
+template <typename T>
+__device__ __forceinline__ float sep_tap(float f) {
+    if constexpr (IsInt<T>::value) return (float)from_acc<T>(f);
+    return f;
+}
+template <typename T>
+__device__ __forceinline__ float sep_round(float a) {
+    if constexpr (IsInt<T>::value) return (float)from_acc<T>(a);
+    return a;
+}
+
+template <typename T, int CFL, int RFL, bool EXACT, bool EXPAND>
+__global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant__ CUtensorMap smap,
+                                                          const SepTmaParams p) {
+    using H = Halo<T, CFL, RFL, EXPAND>;
+    constexpr int NWP = (H::OFF + 8 + CFL - 1 + 3) / 4;  // pass-1 window (float4 chunks)
+    static_assert(56 + 4 * NWP <= H::PF, "window exceeds the tile pitch");
+    extern __shared__ __align__(128) unsigned char sm[];
+    T *tb[2] = {reinterpret_cast<T *>(sm), reinterpret_cast<T *>(sm + H::TB_ALIGNED)};
+    float *ft = reinterpret_cast<float *>(sm + 2 * H::TB_ALIGNED);
+    float *temp = reinterpret_cast<float *>(sm + 2 * H::TB_ALIGNED + H::FT_BYTES);  // BH x 64
+    uint64_t *full = reinterpret_cast<uint64_t *>(temp + H::BH * TILE);
+    __shared__ float ctap[CFL], rtap[RFL];
+    const int tid = threadIdx.x;
+
+    if (tid == 0) {
+        mbar_init(&full[0], 1);
+        mbar_init(&full[1], 1);
+        fence_barrier_init();
+    }
+    if (tid < CFL) ctap[tid] = sep_tap<T>(p.cf[tid]);
+    if (tid < RFL) rtap[tid] = sep_tap<T>(p.rf[tid]);
+    __syncthreads();
+    f2 c2[CFL], r2[RFL];
+#pragma unroll
+    for (int f = 0; f < CFL; ++f) c2[f] = pk(ctap[f], ctap[f]);
+#pragma unroll
+    for (int f = 0; f < RFL; ++f) r2[f] = pk(rtap[f], rtap[f]);
+
+    auto issue = [&](long long t, int buf) {
+        const long long tx = t % p.tiles_x, r = t / p.tiles_x;
+        const long long ty = r % p.tiles_y, b = r / p.tiles_y;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive_expect_tx(&full[buf], H::TBYTES);
+        tma_load_3d(smem_u32(tb[buf]), &smap, &full[buf], (int)(tx * TILE - H::LT),
+                    (int)(ty * TILE - H::LY), (int)b);
+    };
+
+    long long tile = blockIdx.x;
+    if (tid == 0 && tile < p.ntiles) issue(tile, 0);
+    for (int k = 0; tile < p.ntiles; tile += gridDim.x, ++k) {
+        const int buf = k & 1;
+        if (tid == 0 && tile + gridDim.x < p.ntiles) issue(tile + gridDim.x, buf ^ 1);
+        const long long ttx = tile % p.tiles_x, r = tile / p.tiles_x;
+        const long long tty = r % p.tiles_y, b = r / p.tiles_y;
+        if (!wait_tile(&full[buf], (k >> 1) & 1)) break;
+        const float *tile_f;
+        if (sizeof(T) == 4) {
+            tile_f = reinterpret_cast<const float *>(tb[buf]);
+        } else {
+            widen_tile<T, H>(tb[buf], ft);
+            __syncthreads();
+            tile_f = ft;
+        }
+        // pass 1: temp[row][x] = IN( sum_f tile[row][x + OFF + CFL-1-f] * c[f] ),
+        // 8 consecutive x per item; rows outside the image stay zero (the
+        // reference reads zero for them in its second pass)
+        const long long y_top = tty * TILE - H::LY;
+        for (int it = tid; it < H::BH * 8; it += THREADS) {
+            const int row = it >> 3, g = it & 7;
+            const long long gy = y_top + row;
+            f2 a2[4] = {0ull, 0ull, 0ull, 0ull};
+            if (gy >= 0 && gy < p.sd1) {
+                float v[NWP * 4];
+                const float *src = tile_f + row * H::PF + 8 * g;
+#pragma unroll
+                for (int u = 0; u < NWP; ++u) {
+                    const float4 t4 = *reinterpret_cast<const float4 *>(src + 4 * u);
+                    v[4 * u] = t4.x;
+                    v[4 * u + 1] = t4.y;
+                    v[4 * u + 2] = t4.z;
+                    v[4 * u + 3] = t4.w;
+                }
+                // aligned pairs (v0,v1),(v2,v3).. and shifted pairs (v1,v2),(v3,v4)..
+                f2 ve[NWP * 2], vo[NWP * 2 - 1];
+#pragma unroll
+                for (int i = 0; i < NWP * 2; ++i) ve[i] = pk(v[2 * i], v[2 * i + 1]);
+#pragma unroll
+                for (int i = 0; i < NWP * 2 - 1; ++i) vo[i] = pk(v[2 * i + 1], v[2 * i + 2]);
+#pragma unroll
+                for (int f = 0; f < CFL; ++f) {
+                    constexpr int dummy = 0;
+                    (void)dummy;
+                    const int j0 = H::OFF + CFL - 1 - f;  // window index of output 0
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) {
+                        const int j = j0 + 2 * e;
+                        const f2 in2 = (j & 1) ? vo[(j - 1) >> 1] : ve[j >> 1];
+                        a2[e] = mac2<EXACT>(a2[e], in2, c2[f]);
+                    }
+                }
+            }
+            float a[8];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) upk(a2[e], a[2 * e], a[2 * e + 1]);
+#pragma unroll
+            for (int e = 0; e < 8; ++e) a[e] = sep_round<T>(a[e]);
+            float *trow = temp + row * TILE + 8 * g;
+            *reinterpret_cast<float4 *>(trow) = make_float4(a[0], a[1], a[2], a[3]);
+            *reinterpret_cast<float4 *>(trow + 4) = make_float4(a[4], a[5], a[6], a[7]);
+        }
+        __syncthreads();
+        // pass 2: out[x][y] = IN( sum_g temp[y + RFL-1-g][x] * r[g] ), 4x4 per thread
+        const int tx = tid & 15, ty = tid >> 4;
+        f2 acc[4][2];
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) acc[rr][0] = acc[rr][1] = 0ull;
+#pragma unroll
+        for (int q = 3 + RFL - 1; q >= 0; --q) {
+            const float4 t4 = *reinterpret_cast<const float4 *>(temp + (4 * ty + q) * TILE + 4 * tx);
+            const f2 lo = pk(t4.x, t4.y), hi = pk(t4.z, t4.w);
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const int g = rr + RFL - 1 - q;
+                if (g >= 0 && g < RFL) {
+                    acc[rr][0] = mac2<EXACT>(acc[rr][0], lo, r2[g]);
+                    acc[rr][1] = mac2<EXACT>(acc[rr][1], hi, r2[g]);
+                }
+            }
+        }
+        T *out = static_cast<T *>(p.out) + b * p.out_slice;
+        const long long x = ttx * TILE + 4 * tx;
+        const bool vec = (x + 3 < p.od0) && ((p.od0 & 3) == 0) &&
+                         ((reinterpret_cast<uintptr_t>(out) % (4 * sizeof(T))) == 0);
+#pragma unroll
+        for (int rr = 0; rr < 4; ++rr) {
+            const long long y = tty * TILE + 4 * ty + rr;
+            if (y >= p.od1 || x >= p.od0) continue;
+            float o[4];
+            upk(acc[rr][0], o[0], o[1]);
+            upk(acc[rr][1], o[2], o[3]);
+            T *dst = out + y * p.od0 + x;
+            if (vec) {
+                if constexpr (sizeof(T) == 4) {
+                    *reinterpret_cast<float4 *>(dst) = make_float4(o[0], o[1], o[2], o[3]);
+                } else {
+                    const uint32_t w4 = (uint32_t)(uint8_t)from_acc<T>(o[0]) |
+                                        ((uint32_t)(uint8_t)from_acc<T>(o[1]) << 8) |
+                                        ((uint32_t)(uint8_t)from_acc<T>(o[2]) << 16) |
+                                        ((uint32_t)(uint8_t)from_acc<T>(o[3]) << 24);
+                    *reinterpret_cast<uint32_t *>(dst) = w4;
+                }
+            } else {
+#pragma unroll
+                for (int cc = 0; cc < 4; ++cc)
+                    if (x + cc < p.od0) dst[cc] = from_acc_any(o[cc], T{});
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ===========================================================================
+// host side
+// ===========================================================================
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *ptr = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000,
+                                             cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(ptr);
+    });
+    return fn;
+}
+
+// 3-D map over dense images (W, H, slices) with a BW x BH x 1 box
+static bool make_map(CUtensorMap &m, const void *base, int esize, long long W, long long Hh,
+                     long long slices, int bw, int bh) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[3] = {(cuuint64_t)W, (cuuint64_t)Hh, (cuuint64_t)slices};
+    cuuint64_t strides[2] = {(cuuint64_t)(W * esize), (cuuint64_t)(W * Hh * esize)};
+    cuuint32_t box[3] = {(cuuint32_t)bw, (cuuint32_t)bh, 1};
+    cuuint32_t es[3] = {1, 1, 1};
+    CUresult r = fn(&m, esize == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT8,
+                    3, const_cast<void *>(base), dims, strides, box, es,
+                    CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                    CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
+static bool dense_aligned(const void *base, int esize, long long W) {
+    return (reinterpret_cast<uintptr_t>(base) & 15) == 0 && ((W * esize) & 15) == 0;
+}
+
+template <typename K>
+static int persistent_grid(K kernel, size_t smem, long long ntiles) {
+    int per_sm = 1;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, THREADS, smem) != cudaSuccess ||
+        per_sm < 1)
+        per_sm = 1;
+    return (int)std::max(1LL, std::min<long long>(ntiles, (long long)num_sms() * per_sm));
+}
+
+template <typename T, int F0, int F1, bool EXACT, bool EXPAND>
+static bool run_conv2(const DirectParams &p) {
+    using H = Halo<T, F0, F1, EXPAND>;
+    const long long slices = p.sd[2] * p.sd[3];
+    CUtensorMap m;
+    if (!make_map(m, p.sig, (int)sizeof(T), p.sd[0], p.sd[1], slices, H::BW, H::BH)) return false;
+    const long long tx = (p.od[0] + TILE - 1) / TILE, ty = (p.od[1] + TILE - 1) / TILE;
+    const long long ntiles = tx * ty * p.nbatch;
+    const size_t smem = 2 * H::TB_ALIGNED + H::FT_BYTES + 16;
+    auto kfn = conv2_tma_kernel<T, F0, F1, EXACT, EXPAND>;
+    AFGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = persistent_grid(kfn, smem, ntiles);
+    {
+        KernelTimer kt("conv2_tile_kernel");
+        kfn<<<grid, THREADS, smem, stream()>>>(m, p, tx, ty, ntiles);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("conv2_tma_kernel");
+    return true;
+}
+
+template <typename T, int F, bool EXACT>
+static bool conv2_square(const DirectParams &p) {
+    return p.expand ? run_conv2<T, F, F, EXACT, true>(p) : run_conv2<T, F, F, EXACT, false>(p);
+}
+
+bool tma_convolve2(const DirectParams &p, af_dtype t, bool exact) {
+    // dense signal and output (the tile's slice index and output offsets
+    // assume column-major packing), TMA-aligned rows
+    const int es = (t == f32) ? 4 : 1;
+    if (!(t == f32 || t == u8 || t == s8 || t == b8)) return false;
+    if (p.ss[0] != 1 || p.ss[1] != p.sd[0] || p.ss[2] != p.sd[0] * p.sd[1] ||
+        p.ss[3] != p.sd[0] * p.sd[1] * p.sd[2])
+        return false;
+    if (p.os[0] != 1 || p.os[1] != p.od[0]) return false;
+    if (!dense_aligned(p.sig, es, p.sd[0])) return false;
+    if (p.sd[0] > (1LL << 30) || p.sd[1] > (1LL << 30)) return false;
+    const long long f0 = p.fd[0], f1 = p.fd[1];
+    if (f0 != f1 || !(f0 == 3 || f0 == 5 || f0 == 7)) return false;
+    const bool ex = exact || es == 1;
+#define AFGB_SQ(T, E)                                                    \
+    switch (f0) {                                                        \
+        case 3: return conv2_square<T, 3, E>(p);                         \
+        case 5: return conv2_square<T, 5, E>(p);                         \
+        default: return conv2_square<T, 7, E>(p);                        \
+    }
+    if (t == f32) {
+        if (ex) { AFGB_SQ(float, true) }
+        else { AFGB_SQ(float, false) }
+    } else if (t == u8) {
+        AFGB_SQ(uint8_t, true)
+    } else {
+        AFGB_SQ(int8_t, true)
+    }
+#undef AFGB_SQ
+}
+
+template <typename T, int CL, int RL, bool EXACT, bool EXPAND>
+static bool run_sep(SepTmaParams p, const void *sig, long long W, long long Hh, long long slices) {
+    using H = Halo<T, CL, RL, EXPAND>;
+    CUtensorMap m;
+    if (!make_map(m, sig, (int)sizeof(T), W, Hh, slices, H::BW, H::BH)) return false;
+    const size_t smem = 2 * H::TB_ALIGNED + H::FT_BYTES + (size_t)H::BH * TILE * 4 + 16;
+    auto kfn = sep_tma_kernel<T, CL, RL, EXACT, EXPAND>;
+    AFGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = persistent_grid(kfn, smem, p.ntiles);
+    {
+        KernelTimer kt("sep_fused_kernel");
+        kfn<<<grid, THREADS, smem, stream()>>>(m, p);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("sep_tma_kernel");
+    return true;
+}
+
+template <typename T, int L, bool EXACT>
+static bool sep_len(const SepTmaParams &p, bool expand, const void *sig, long long W, long long Hh,
+                    long long slices) {
+    return expand ? run_sep<T, L, L, EXACT, true>(p, sig, W, Hh, slices)
+                  : run_sep<T, L, L, EXACT, false>(p, sig, W, Hh, slices);
+}
+
+bool tma_convolve2_sep(const Array &sig, const float *cf, const float *rf, int cl, int rl,
+                       Array &out, bool expand, bool exact) {
+    const af_dtype t = sig.type;
+    const int es = (t == f32) ? 4 : 1;
+    if (!(t == f32 || t == u8 || t == s8 || t == b8)) return false;
+    if (cl != rl || !(cl == 3 || cl == 5 || cl == 7 || cl == 15)) return false;
+    if (!sig.is_linear() || !dense_aligned(sig.data(), es, sig.dims[0])) return false;
+    if (sig.dims[0] > (1LL << 30) || sig.dims[1] > (1LL << 30)) return false;
+    SepTmaParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.cf = cf;
+    p.rf = rf;
+    p.out = out.data();
+    p.od0 = out.dims[0];
+    p.od1 = out.dims[1];
+    p.out_slice = out.dims[0] * out.dims[1];
+    p.sd1 = sig.dims[1];
+    p.tiles_x = (p.od0 + TILE - 1) / TILE;
+    p.tiles_y = (p.od1 + TILE - 1) / TILE;
+    const long long slices = sig.dims[2] * sig.dims[3];
+    p.ntiles = p.tiles_x * p.tiles_y * slices;
+    if (p.ntiles == 0) return true;
+    const bool ex = exact && es == 4;  // 8-bit sums are exact integers either way
+#define AFGB_SEPL(T, E)                                                                   \
+    switch (cl) {                                                                         \
+        case 3: return sep_len<T, 3, E>(p, expand, sig.data(), sig.dims[0], sig.dims[1], slices);   \
+        case 5: return sep_len<T, 5, E>(p, expand, sig.data(), sig.dims[0], sig.dims[1], slices);   \
+        case 7: return sep_len<T, 7, E>(p, expand, sig.data(), sig.dims[0], sig.dims[1], slices);   \
+        default: return sep_len<T, 15, E>(p, expand, sig.data(), sig.dims[0], sig.dims[1], slices); \
+    }
+    if (t == f32) {
+        if (ex) { AFGB_SEPL(float, true) }
+        else { AFGB_SEPL(float, false) }
+    } else if (t == u8) {
+        AFGB_SEPL(uint8_t, false)
+    } else {
+        AFGB_SEPL(int8_t, false)
+    }
+#undef AFGB_SEPL
+}
+
+}  // namespace dtma
+
+unsigned int tma_take_error() {
+    unsigned int v = 0, zero = 0;
+    if (cudaMemcpyFromSymbol(&v, tc::g_tc_error, sizeof(v)) != cudaSuccess) return 0;
+    if (v) (void)cudaMemcpyToSymbol(tc::g_tc_error, &zero, sizeof(zero));
+    return v;
+}
+
+}  // namespace afgb

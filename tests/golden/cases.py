@@ -84,6 +84,11 @@ DIRECT_SHAPES = [
     ("r_one2many", 2, (41, 26), (3, 3, 3)),
     ("r_many2many", 2, (66, 70, 3), (7, 7, 3)),
     ("r_small", 2, (3, 2), (5, 5)),
+    # widths that are 16-byte multiples for f32 and 8-bit data (TMA-staged path)
+    ("r_tma_7_lhs", 2, (128, 96, 3), (7, 7)),
+    ("r_tma_5_same", 2, (64, 70, 2), (5, 5, 2)),
+    ("r_tma_3_rhs", 2, (96, 33), (3, 3, 2)),
+    ("r_tma_7_4d", 2, (64, 65, 2, 2), (7, 7)),
     # rank 3
     ("c_one2one_3", 3, (17, 14, 9), (3, 3, 3)),
     ("c_one2one_245", 3, (11, 13, 10), (2, 4, 5)),
@@ -115,6 +120,10 @@ SEP_SHAPES = [
     ("sep_2x7", (31, 29), 2, 7),
     ("sep_31", (80, 70), 31, 31),
     ("sep_batch4d", (20, 21, 2, 2), 3, 5),
+    # 16-byte-multiple widths (TMA-staged path)
+    ("sep_15_tma", (128, 80, 2), 15, 15),
+    ("sep_3_tma", (64, 50), 3, 3),
+    ("sep_7_tma", (96, 70, 3), 7, 7),
 ]
 SEP_DTYPES = [F32, F64, C32, U8, S8, S16, S32, U32, S64]
 
