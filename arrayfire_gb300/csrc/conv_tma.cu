@@ -22,6 +22,7 @@
 #include <cstdint>
 #include <cstring>
 #include <mutex>
+#include <type_traits>
 
 #include "conv_common.cuh"
 #include "conv_params.cuh"
@@ -50,16 +51,20 @@ __device__ __forceinline__ f2 pk(float a, float b) {
 __device__ __forceinline__ void upk(f2 r, float &a, float &b) {
     asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
 }
+// acc + a*b on both lanes.  The exact mode rounds the product and the sum
+// separately in each lane with __fmul_rn/__fadd_rn, which the compiler never
+// contracts (a packed mul.rn/add.rn pair may be fused into one FMA).
 template <bool EXACT>
 __device__ __forceinline__ f2 mac2(f2 acc, f2 a, f2 b) {
-    f2 d;
     if (EXACT) {
-        f2 p;
-        asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(p) : "l"(a), "l"(b));
-        asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(acc), "l"(p));
-    } else {
-        asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(acc));
+        float a0, a1, b0, b1, c0, c1;
+        upk(a, a0, a1);
+        upk(b, b0, b1);
+        upk(acc, c0, c1);
+        return pk(__fadd_rn(c0, __fmul_rn(a0, b0)), __fadd_rn(c1, __fmul_rn(a1, b1)));
     }
+    f2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(acc));
     return d;
 }
 
@@ -109,14 +114,31 @@ struct Halo {
     static constexpr int FT_BYTES = ES == 4 ? 0 : (BH * PF * 4 + 127) / 128 * 128;
 };
 
-// 8-bit tile -> float tile (shifted so that the float tile starts at x0 - LF)
+// 8-bit tile -> float tile (shifted so that the float tile starts at x0 - LF),
+// four bytes per shared load; LT, LF, BW and PF are multiples of four
 template <typename T, typename H>
 __device__ __forceinline__ void widen_tile(const T *tb, float *ft) {
     constexpr int SHIFT = H::LT - H::LF;
-    for (int e = threadIdx.x; e < H::BH * H::PF; e += THREADS) {
-        const int r = e / H::PF, c = e - r * H::PF;
-        const int cs = c + SHIFT;
-        ft[e] = cs < H::BW ? to_f<T>(tb[r * H::BW + cs]) : 0.0f;
+    constexpr int Q = H::PF / 4, BQ = H::BW / 4;
+    static_assert(SHIFT % 4 == 0 && H::PF % 4 == 0 && H::BW % 4 == 0, "widening needs 4-byte words");
+    const uint32_t *tw = reinterpret_cast<const uint32_t *>(tb);
+    constexpr int RPP = THREADS / Q;  // rows per pass
+    if (threadIdx.x >= RPP * Q) return;
+    for (int r = threadIdx.x / Q; r < H::BH; r += RPP) {
+        const int c4 = threadIdx.x % Q;
+        const int src = c4 + SHIFT / 4;
+        float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (src < BQ) {
+            const uint32_t w = tw[r * BQ + src];
+            if constexpr (std::is_same<T, uint8_t>::value) {
+                o = make_float4((float)(w & 0xFFu), (float)((w >> 8) & 0xFFu),
+                                (float)((w >> 16) & 0xFFu), (float)(w >> 24));
+            } else {
+                o = make_float4((float)(int8_t)(w & 0xFFu), (float)(int8_t)((w >> 8) & 0xFFu),
+                                (float)(int8_t)((w >> 16) & 0xFFu), (float)(int8_t)(w >> 24));
+            }
+        }
+        reinterpret_cast<float4 *>(ft)[r * Q + c4] = o;
     }
 }
 
@@ -249,9 +271,13 @@ __device__ __forceinline__ float sep_tap(float f) {
     if constexpr (IsInt<T>::value) return (float)from_acc<T>(f);
     return f;
 }
+// InT(accum) of the separable passes.  8-bit inputs: taps and samples are
+// integers, so every sum is an exact integer and the conversion reduces to
+// saturation (NaN cannot arise).
 template <typename T>
 __device__ __forceinline__ float sep_round(float a) {
-    if constexpr (IsInt<T>::value) return (float)from_acc<T>(a);
+    if constexpr (std::is_same<T, uint8_t>::value) return fminf(fmaxf(a, 0.0f), 255.0f);
+    if constexpr (std::is_same<T, int8_t>::value) return fminf(fmaxf(a, -128.0f), 127.0f);
     return a;
 }
 
@@ -390,10 +416,10 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
                 if constexpr (sizeof(T) == 4) {
                     *reinterpret_cast<float4 *>(dst) = make_float4(o[0], o[1], o[2], o[3]);
                 } else {
-                    const uint32_t w4 = (uint32_t)(uint8_t)from_acc<T>(o[0]) |
-                                        ((uint32_t)(uint8_t)from_acc<T>(o[1]) << 8) |
-                                        ((uint32_t)(uint8_t)from_acc<T>(o[2]) << 16) |
-                                        ((uint32_t)(uint8_t)from_acc<T>(o[3]) << 24);
+                    const uint32_t w4 = (uint32_t)(uint8_t)(int)sep_round<T>(o[0]) |
+                                        ((uint32_t)(uint8_t)(int)sep_round<T>(o[1]) << 8) |
+                                        ((uint32_t)(uint8_t)(int)sep_round<T>(o[2]) << 16) |
+                                        ((uint32_t)(uint8_t)(int)sep_round<T>(o[3]) << 24);
                     *reinterpret_cast<uint32_t *>(dst) = w4;
                 }
             } else {
