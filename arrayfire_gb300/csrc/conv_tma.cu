@@ -40,6 +40,7 @@ using tc::smem_u32;
 
 constexpr int TILE = 64;
 constexpr int THREADS = 256;
+constexpr int NST = 3;  // tile buffers per CTA: one computed, two in flight
 
 // ---------------------------------------------------------------- f32x2
 typedef unsigned long long f2;
@@ -153,15 +154,16 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
     constexpr int NW4 = (H::OFF + 4 + F0 - 1 + 3) / 4;
     static_assert(60 + 4 * NW4 <= H::PF, "window exceeds the tile pitch");
     extern __shared__ __align__(128) unsigned char sm[];
-    T *tb[2] = {reinterpret_cast<T *>(sm), reinterpret_cast<T *>(sm + H::TB_ALIGNED)};
-    float *ft = reinterpret_cast<float *>(sm + 2 * H::TB_ALIGNED);
-    uint64_t *full = reinterpret_cast<uint64_t *>(sm + 2 * H::TB_ALIGNED + H::FT_BYTES);
+    T *tb[NST];
+#pragma unroll
+    for (int i = 0; i < NST; ++i) tb[i] = reinterpret_cast<T *>(sm + i * H::TB_ALIGNED);
+    float *ft = reinterpret_cast<float *>(sm + NST * H::TB_ALIGNED);
+    uint64_t *full = reinterpret_cast<uint64_t *>(sm + NST * H::TB_ALIGNED + H::FT_BYTES);
     const int tid = threadIdx.x;
     const long long slice = p.sd[0] * p.sd[1];
 
     if (tid == 0) {
-        mbar_init(&full[0], 1);
-        mbar_init(&full[1], 1);
+        for (int i = 0; i < NST; ++i) mbar_init(&full[i], 1);
         fence_barrier_init();
     }
     __syncthreads();
@@ -177,11 +179,14 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
     };
 
     long long tile = blockIdx.x;
-    if (tid == 0 && tile < ntiles) issue(tile, 0);
+    if (tid == 0)
+        for (int i = 0; i < NST - 1; ++i)
+            if (tile + (long long)i * gridDim.x < ntiles) issue(tile + (long long)i * gridDim.x, i);
     const int tx = tid & 15, ty = tid >> 4;
     for (int k = 0; tile < ntiles; tile += gridDim.x, ++k) {
-        const int buf = k & 1;
-        if (tid == 0 && tile + gridDim.x < ntiles) issue(tile + gridDim.x, buf ^ 1);
+        const int buf = k % NST;
+        const long long ahead = tile + (long long)(NST - 1) * gridDim.x;
+        if (tid == 0 && ahead < ntiles) issue(ahead, (k + NST - 1) % NST);
         const long long ttx = tile % tiles_x, r = tile / tiles_x;
         const long long tty = r % tiles_y, b = r / tiles_y;
         const BatchOff bo = batch_offsets(p, b);
@@ -191,7 +196,7 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
         for (int fj = 0; fj < F1; ++fj)
 #pragma unroll
             for (int fi = 0; fi < F0; ++fi) wr[fj * F0 + fi] = __ldg(w + fi * p.fs[0] + fj * p.fs[1]);
-        if (!wait_tile(&full[buf], (k >> 1) & 1)) break;
+        if (!wait_tile(&full[buf], (k / NST) & 1)) break;
         const float *tile_f;
         if (sizeof(T) == 4) {
             tile_f = reinterpret_cast<const float *>(tb[buf]);
@@ -258,7 +263,7 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
                     if (x + cc < p.od[0]) dst[cc] = from_acc_any(acc[rr][cc], T{});
             }
         }
-        __syncthreads();  // the buffer is reloaded two tiles from now
+        __syncthreads();  // this buffer is reloaded at the next iteration's issue
     }
 }
 
@@ -288,16 +293,17 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
     constexpr int NWP = (H::OFF + 8 + CFL - 1 + 3) / 4;  // pass-1 window (float4 chunks)
     static_assert(56 + 4 * NWP <= H::PF, "window exceeds the tile pitch");
     extern __shared__ __align__(128) unsigned char sm[];
-    T *tb[2] = {reinterpret_cast<T *>(sm), reinterpret_cast<T *>(sm + H::TB_ALIGNED)};
-    float *ft = reinterpret_cast<float *>(sm + 2 * H::TB_ALIGNED);
-    float *temp = reinterpret_cast<float *>(sm + 2 * H::TB_ALIGNED + H::FT_BYTES);  // BH x 64
+    T *tb[NST];
+#pragma unroll
+    for (int i = 0; i < NST; ++i) tb[i] = reinterpret_cast<T *>(sm + i * H::TB_ALIGNED);
+    float *ft = reinterpret_cast<float *>(sm + NST * H::TB_ALIGNED);
+    float *temp = reinterpret_cast<float *>(sm + NST * H::TB_ALIGNED + H::FT_BYTES);  // BH x 64
     uint64_t *full = reinterpret_cast<uint64_t *>(temp + H::BH * TILE);
     __shared__ float ctap[CFL], rtap[RFL];
     const int tid = threadIdx.x;
 
     if (tid == 0) {
-        mbar_init(&full[0], 1);
-        mbar_init(&full[1], 1);
+        for (int i = 0; i < NST; ++i) mbar_init(&full[i], 1);
         fence_barrier_init();
     }
     if (tid < CFL) ctap[tid] = sep_tap<T>(p.cf[tid]);
@@ -319,13 +325,16 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
     };
 
     long long tile = blockIdx.x;
-    if (tid == 0 && tile < p.ntiles) issue(tile, 0);
+    if (tid == 0)
+        for (int i = 0; i < NST - 1; ++i)
+            if (tile + (long long)i * gridDim.x < p.ntiles) issue(tile + (long long)i * gridDim.x, i);
     for (int k = 0; tile < p.ntiles; tile += gridDim.x, ++k) {
-        const int buf = k & 1;
-        if (tid == 0 && tile + gridDim.x < p.ntiles) issue(tile + gridDim.x, buf ^ 1);
+        const int buf = k % NST;
+        const long long ahead = tile + (long long)(NST - 1) * gridDim.x;
+        if (tid == 0 && ahead < p.ntiles) issue(ahead, (k + NST - 1) % NST);
         const long long ttx = tile % p.tiles_x, r = tile / p.tiles_x;
         const long long tty = r % p.tiles_y, b = r / p.tiles_y;
-        if (!wait_tile(&full[buf], (k >> 1) & 1)) break;
+        if (!wait_tile(&full[buf], (k / NST) & 1)) break;
         const float *tile_f;
         if (sizeof(T) == 4) {
             tile_f = reinterpret_cast<const float *>(tb[buf]);
@@ -491,7 +500,7 @@ static bool run_conv2(const DirectParams &p) {
     if (!make_map(m, p.sig, (int)sizeof(T), p.sd[0], p.sd[1], slices, H::BW, H::BH)) return false;
     const long long tx = (p.od[0] + TILE - 1) / TILE, ty = (p.od[1] + TILE - 1) / TILE;
     const long long ntiles = tx * ty * p.nbatch;
-    const size_t smem = 2 * H::TB_ALIGNED + H::FT_BYTES + 16;
+    const size_t smem = NST * H::TB_ALIGNED + H::FT_BYTES + 8 * NST;
     auto kfn = conv2_tma_kernel<T, F0, F1, EXACT, EXPAND>;
     AFGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = persistent_grid(kfn, smem, ntiles);
@@ -545,7 +554,7 @@ static bool run_sep(SepTmaParams p, const void *sig, long long W, long long Hh, 
     using H = Halo<T, CL, RL, EXPAND>;
     CUtensorMap m;
     if (!make_map(m, sig, (int)sizeof(T), W, Hh, slices, H::BW, H::BH)) return false;
-    const size_t smem = 2 * H::TB_ALIGNED + H::FT_BYTES + (size_t)H::BH * TILE * 4 + 16;
+    const size_t smem = NST * H::TB_ALIGNED + H::FT_BYTES + (size_t)H::BH * TILE * 4 + 8 * NST;
     auto kfn = sep_tma_kernel<T, CL, RL, EXACT, EXPAND>;
     AFGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = persistent_grid(kfn, smem, p.ntiles);
