@@ -219,6 +219,25 @@ def launch_count() -> int:
     return int(lib().afgb_kernel_launch_count())
 
 
+def device_mem_info() -> dict:
+    """af_device_mem_info: pool bytes reserved, bytes/buffers held by live arrays."""
+    v = [ctypes.c_size_t() for _ in range(4)]
+    _check(lib().af_device_mem_info(*[ctypes.byref(x) for x in v]))
+    return {"alloc_bytes": v[0].value, "alloc_buffers": v[1].value,
+            "lock_bytes": v[2].value, "lock_buffers": v[3].value}
+
+
+def device_gc() -> None:
+    _check(lib().af_device_gc())
+
+
+def device_mem_peak(reset: bool = False) -> int:
+    """Peak bytes held by this library's arrays and scratch since load or the last reset."""
+    v = ctypes.c_size_t()
+    _check(lib().afgb_device_mem_peak(ctypes.byref(v), 1 if reset else 0))
+    return v.value
+
+
 def version() -> str:
     return lib().afgb_version().decode()
 

@@ -60,6 +60,9 @@ SIGNATURES = [
     ("afgb_identify_batch_kind", ctypes.c_int, [ctypes.c_int, _DP, _DP]),
     ("afgb_conv_output_dims", ctypes.c_int, [_DP, ctypes.c_int, ctypes.c_int, ctypes.c_int, _DP, _DP]),
     ("afgb_nn_output_dims", ctypes.c_int, [_DP, _DP, _DP, _DP, _DP, _DP]),
+    ("af_device_mem_info", ctypes.c_int, [ctypes.POINTER(ctypes.c_size_t)] * 4),
+    ("af_device_gc", ctypes.c_int, []),
+    ("afgb_device_mem_peak", ctypes.c_int, [ctypes.POINTER(ctypes.c_size_t), ctypes.c_int]),
     ("afgb_debug_fail_alloc_after", None, [ctypes.c_int]),
     ("afgb_kernel_launch_count", ctypes.c_ulonglong, []),
     ("afgb_convolve2_filter_grad_noalloc", af_err, [_P, _P, _P, _DP, _DP, _DP, _DP, _DP, _P]),

@@ -16,6 +16,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "afgb_internal.hpp"
@@ -168,6 +169,35 @@ bool exact_fp() { return g_exact.load() != 0; }
 void count_launch(unsigned n) { g_launches += n; }
 
 // ---------------------------------------------------------------- memory
+// Every pool allocation is recorded with its size so that af_device_mem_info
+// can report the bytes and buffers in use and the peak since the last reset.
+namespace {
+struct MemBook {
+    std::mutex mu;
+    std::unordered_map<void *, size_t> live;
+    size_t bytes = 0, peak = 0;
+};
+MemBook &mem_book() {
+    static MemBook *b = new MemBook();  // outlives static destructors of callers
+    return *b;
+}
+void book_alloc(void *p, size_t bytes) {
+    MemBook &b = mem_book();
+    std::lock_guard<std::mutex> lk(b.mu);
+    b.live[p] = bytes;
+    b.bytes += bytes;
+    if (b.bytes > b.peak) b.peak = b.bytes;
+}
+void book_free(void *p) {
+    MemBook &b = mem_book();
+    std::lock_guard<std::mutex> lk(b.mu);
+    auto it = b.live.find(p);
+    if (it == b.live.end()) return;
+    b.bytes -= it->second;
+    b.live.erase(it);
+}
+}  // namespace
+
 void *alloc_device(size_t bytes) {
     int fa = g_fail_after.load();
     if (fa > 0) {
@@ -183,17 +213,20 @@ void *alloc_device(size_t bytes) {
         AFGB_THROW(AF_ERR_NO_MEM, "device allocation of " + std::to_string(bytes) +
                                       " bytes failed: " + cudaGetErrorString(e));
     }
+    book_alloc(p, bytes);
     return p;
 }
 
 void free_device(void *p) {
-    if (p) (void)cudaFreeAsync(p, stream());
+    if (!p) return;
+    book_free(p);
+    (void)cudaFreeAsync(p, stream());
 }
 
 Buffer::~Buffer() {
     if (!ptr) return;
     if (kind == BufKind::Pool) {
-        (void)cudaFreeAsync(ptr, stream());
+        free_device(ptr);
     } else if (kind == BufKind::Adopted) {
         (void)cudaFree(ptr);
     }
@@ -486,6 +519,54 @@ af_err af_sync(const int dev) {
         AFGB_CUDA(cudaStreamSynchronize(stream()));
         check_device_errors();
     }
+    AFGB_CATCHALL
+}
+
+af_err af_device_mem_info(size_t *alloc_bytes, size_t *alloc_buffers, size_t *lock_bytes,
+                          size_t *lock_buffers) {
+    AFGB_TRY
+    MemBook &b = mem_book();
+    size_t live_bytes, live_bufs;
+    {
+        std::lock_guard<std::mutex> lk(b.mu);
+        live_bytes = b.bytes;
+        live_bufs = b.live.size();
+    }
+    uint64_t reserved = live_bytes;
+    cudaMemPool_t pool;
+    int d = device();
+    (void)dev_state(d);
+    if (cudaDeviceGetDefaultMemPool(&pool, d) == cudaSuccess) {
+        uint64_t r = 0;
+        if (cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &r) == cudaSuccess)
+            reserved = r;
+    }
+    (void)cudaGetLastError();
+    if (alloc_bytes) *alloc_bytes = (size_t)reserved;
+    if (alloc_buffers) *alloc_buffers = live_bufs;
+    if (lock_bytes) *lock_bytes = live_bytes;
+    if (lock_buffers) *lock_buffers = live_bufs;
+    AFGB_CATCHALL
+}
+
+af_err af_device_gc() {
+    AFGB_TRY
+    int d = device();
+    (void)dev_state(d);
+    AFGB_CUDA(cudaStreamSynchronize(stream()));
+    cudaMemPool_t pool;
+    AFGB_CUDA(cudaDeviceGetDefaultMemPool(&pool, d));
+    AFGB_CUDA(cudaMemPoolTrimTo(pool, 0));
+    AFGB_CATCHALL
+}
+
+af_err afgb_device_mem_peak(size_t *peak_bytes, int reset) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, peak_bytes != nullptr);
+    MemBook &b = mem_book();
+    std::lock_guard<std::mutex> lk(b.mu);
+    *peak_bytes = b.peak;
+    if (reset) b.peak = b.bytes;
     AFGB_CATCHALL
 }
 

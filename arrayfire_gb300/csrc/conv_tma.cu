@@ -40,7 +40,59 @@ using tc::smem_u32;
 
 constexpr int TILE = 64;
 constexpr int THREADS = 256;
-constexpr int NST = 3;  // tile buffers per CTA: one computed, two in flight
+// tile buffers per CTA (one computed, the rest in flight): three for the 2-D
+// kernel, whose registers already hold it at two CTAs per SM; two for the
+// separable kernel, whose shared temp image would otherwise cost a CTA per SM
+constexpr int NST_2D = 3;
+constexpr int NST_SEP = 2;
+// separable temp-image pitch (floats): 17 16-byte words, odd for the same reason
+constexpr int SEP_TP = TILE + 4;
+
+// n / d for 0 <= n < 2^31 by multiply-high (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", PLDI 1994, with
+// l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1: q = (mulhi(n, m) + n) >> l;
+// n < 2^31 keeps the sum within 32 bits)
+struct FastDiv {
+    uint32_t d, m, s;
+};
+static FastDiv make_fastdiv(uint32_t d) {
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    const uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+    return FastDiv{d, (uint32_t)m, l};
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+    return (__umulhi(n, f.m) + n) >> f.s;
+}
+
+// tile -> (x tile, y tile, batch) decoding shared by both kernels; every
+// thread decodes its tile with a few multiply-high steps
+struct TileGrid {
+    FastDiv tx, ty;       // tiles along x, along y
+    FastDiv b1, b2;       // batch extents of dims 2 and 3 (2-D kernel)
+    int ntiles;
+    int zstep[4];         // slice index step per batch coordinate (2-D kernel)
+};
+struct TileRec {
+    int tx, ty, z;
+    long long out, filt;  // element offsets of the tile's output slice and filter
+};
+__device__ __forceinline__ TileRec decode_tile(int t, const TileGrid &tg, const long long *out_step,
+                                               const long long *filt_step) {
+    const uint32_t r = fdiv((uint32_t)t, tg.tx);
+    const uint32_t b = fdiv(r, tg.ty);
+    const uint32_t r2 = fdiv(b, tg.b1);
+    const uint32_t b3 = fdiv(r2, tg.b2);
+    const uint32_t b1 = b - r2 * tg.b1.d, b2 = r2 - b3 * tg.b2.d;
+    TileRec tr;
+    tr.tx = (int)((uint32_t)t - r * tg.tx.d);
+    tr.ty = (int)(r - b * tg.ty.d);
+    tr.z = (int)b1 * tg.zstep[1] + (int)b2 * tg.zstep[2] + (int)b3 * tg.zstep[3];
+    tr.out = (long long)b1 * out_step[1] + (long long)b2 * out_step[2] + (long long)b3 * out_step[3];
+    tr.filt = (long long)b1 * filt_step[1] + (long long)b2 * filt_step[2] +
+              (long long)b3 * filt_step[3];
+    return tr;
+}
 
 // ---------------------------------------------------------------- f32x2
 typedef unsigned long long f2;
@@ -92,6 +144,8 @@ __device__ __forceinline__ bool wait_tile(uint64_t *bar, uint32_t parity) {
 
 template <typename T> __device__ __forceinline__ float to_f(T v) { return (float)v; }
 
+
+
 // geometry of a haloed tile for an F0 x F1 filter (shared by both kernels)
 template <typename T, int F0, int F1, bool EXPAND>
 struct Halo {
@@ -105,9 +159,11 @@ struct Halo {
     static constexpr int LF = (LX + 3) / 4 * 4;       // float tile lead
     static constexpr int OFF = LF - LX;               // window shift, 0..3
     static constexpr int BH = TILE + F1 - 1;
-    // float tile pitch: covers the right halo and the widest window read
+    // float tile pitch: covers the right halo; an odd number of 16-byte
+    // words, so eight rows at the same column fall in eight different bank
+    // groups (a conflict-free 128-bit access by eight lanes on eight rows)
     static constexpr int PF0 = (LF + TILE + C0 + 3) / 4 * 4;
-    static constexpr int PF = PF0 + 8;
+    static constexpr int PF = (PF0 / 4) % 2 ? PF0 : PF0 + 4;
     // TMA box width (elements); f32 loads straight into the float layout
     static constexpr int BW = ES == 4 ? PF : (LT + TILE + C0 + A - 1) / A * A;
     static constexpr int TBYTES = BH * BW * ES;
@@ -148,19 +204,17 @@ __device__ __forceinline__ void widen_tile(const T *tb, float *ft) {
 // ===========================================================================
 template <typename T, int F0, int F1, bool EXACT, bool EXPAND>
 __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constant__ CUtensorMap smap,
-                                                            const DirectParams p, long long tiles_x,
-                                                            long long tiles_y, long long ntiles) {
+                                                            const DirectParams p,
+                                                            const TileGrid tg) {
     using H = Halo<T, F0, F1, EXPAND>;
+    constexpr int NST = NST_2D;
     constexpr int NW4 = (H::OFF + 4 + F0 - 1 + 3) / 4;
     static_assert(60 + 4 * NW4 <= H::PF, "window exceeds the tile pitch");
     extern __shared__ __align__(128) unsigned char sm[];
-    T *tb[NST];
-#pragma unroll
-    for (int i = 0; i < NST; ++i) tb[i] = reinterpret_cast<T *>(sm + i * H::TB_ALIGNED);
+    auto tb = [&](int i) { return reinterpret_cast<T *>(sm + i * H::TB_ALIGNED); };
     float *ft = reinterpret_cast<float *>(sm + NST * H::TB_ALIGNED);
     uint64_t *full = reinterpret_cast<uint64_t *>(sm + NST * H::TB_ALIGNED + H::FT_BYTES);
     const int tid = threadIdx.x;
-    const long long slice = p.sd[0] * p.sd[1];
 
     if (tid == 0) {
         for (int i = 0; i < NST; ++i) mbar_init(&full[i], 1);
@@ -168,29 +222,28 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
     }
     __syncthreads();
 
-    auto issue = [&](long long t, int buf) {
-        const long long tx = t % tiles_x, r = t / tiles_x;
-        const long long ty = r % tiles_y, b = r / tiles_y;
-        const BatchOff bo = batch_offsets(p, b);
+    auto issue = [&](int t, int buf) {
+        const TileRec tr = decode_tile(t, tg, p.out_step, p.filt_step);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive_expect_tx(&full[buf], H::TBYTES);
-        tma_load_3d(smem_u32(tb[buf]), &smap, &full[buf], (int)(tx * TILE - H::LT),
-                    (int)(ty * TILE - H::LY), (int)(bo.in / slice));
+        tma_load_3d(smem_u32(tb(buf)), &smap, &full[buf], tr.tx * TILE - H::LT,
+                    tr.ty * TILE - H::LY, tr.z);
     };
 
-    long long tile = blockIdx.x;
+    int tile = blockIdx.x;
     if (tid == 0)
         for (int i = 0; i < NST - 1; ++i)
-            if (tile + (long long)i * gridDim.x < ntiles) issue(tile + (long long)i * gridDim.x, i);
+            if (tile + i * (int)gridDim.x < tg.ntiles) issue(tile + i * (int)gridDim.x, i);
     const int tx = tid & 15, ty = tid >> 4;
-    for (int k = 0; tile < ntiles; tile += gridDim.x, ++k) {
+    for (int k = 0; tile < tg.ntiles; tile += gridDim.x, ++k) {
         const int buf = k % NST;
-        const long long ahead = tile + (long long)(NST - 1) * gridDim.x;
-        if (tid == 0 && ahead < ntiles) issue(ahead, (k + NST - 1) % NST);
-        const long long ttx = tile % tiles_x, r = tile / tiles_x;
-        const long long tty = r % tiles_y, b = r / tiles_y;
-        const BatchOff bo = batch_offsets(p, b);
-        const float *w = static_cast<const float *>(p.filt) + bo.filt;
+        const int ahead = tile + (NST - 1) * (int)gridDim.x;
+        if (tid == 0 && ahead < tg.ntiles) issue(ahead, (k + NST - 1) % NST);
+        const TileRec tr = decode_tile(tile, tg, p.out_step, p.filt_step);
+        const int ttx = tr.tx, tty = tr.ty;
+        const long long out_off = tr.out;
+        // taps go to registers before the wait, overlapping the tile load
+        const float *w = static_cast<const float *>(p.filt) + tr.filt;
         float wr[F0 * F1];
 #pragma unroll
         for (int fj = 0; fj < F1; ++fj)
@@ -199,9 +252,9 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
         if (!wait_tile(&full[buf], (k / NST) & 1)) break;
         const float *tile_f;
         if (sizeof(T) == 4) {
-            tile_f = reinterpret_cast<const float *>(tb[buf]);
+            tile_f = reinterpret_cast<const float *>(tb(buf));
         } else {
-            widen_tile<T, H>(tb[buf], ft);
+            widen_tile<T, H>(tb(buf), ft);
             __syncthreads();
             tile_f = ft;
         }
@@ -237,13 +290,13 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
                 }
             }
         }
-        T *out = static_cast<T *>(p.out) + bo.out;
-        const long long x = ttx * TILE + 4 * tx;
+        T *out = static_cast<T *>(p.out) + out_off;
+        const long long x = (long long)ttx * TILE + 4 * tx;
         const bool vec = (x + 3 < p.od[0]) && ((p.os[1] & 3) == 0) &&
                          ((reinterpret_cast<uintptr_t>(out) % (4 * sizeof(T))) == 0);
 #pragma unroll
         for (int rr = 0; rr < 4; ++rr) {
-            const long long y = tty * TILE + 4 * ty + rr;
+            const long long y = (long long)tty * TILE + 4 * ty + rr;
             if (y >= p.od[1] || x >= p.od[0]) continue;
             T *dst = out + y * p.os[1] + x;
             if (vec) {
@@ -288,17 +341,17 @@ __device__ __forceinline__ float sep_round(float a) {
 
 template <typename T, int CFL, int RFL, bool EXACT, bool EXPAND>
 __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant__ CUtensorMap smap,
-                                                          const SepTmaParams p) {
+                                                          const SepTmaParams p,
+                                                          const TileGrid tg) {
     using H = Halo<T, CFL, RFL, EXPAND>;
+    constexpr int NST = NST_SEP;
     constexpr int NWP = (H::OFF + 8 + CFL - 1 + 3) / 4;  // pass-1 window (float4 chunks)
     static_assert(56 + 4 * NWP <= H::PF, "window exceeds the tile pitch");
     extern __shared__ __align__(128) unsigned char sm[];
-    T *tb[NST];
-#pragma unroll
-    for (int i = 0; i < NST; ++i) tb[i] = reinterpret_cast<T *>(sm + i * H::TB_ALIGNED);
+    auto tb = [&](int i) { return reinterpret_cast<T *>(sm + i * H::TB_ALIGNED); };
     float *ft = reinterpret_cast<float *>(sm + NST * H::TB_ALIGNED);
-    float *temp = reinterpret_cast<float *>(sm + NST * H::TB_ALIGNED + H::FT_BYTES);  // BH x 64
-    uint64_t *full = reinterpret_cast<uint64_t *>(temp + H::BH * TILE);
+    float *temp = reinterpret_cast<float *>(sm + NST * H::TB_ALIGNED + H::FT_BYTES);  // BH x TP
+    uint64_t *full = reinterpret_cast<uint64_t *>(temp + H::BH * SEP_TP);
     __shared__ float ctap[CFL], rtap[RFL];
     const int tid = threadIdx.x;
 
@@ -315,40 +368,46 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
 #pragma unroll
     for (int f = 0; f < RFL; ++f) r2[f] = pk(rtap[f], rtap[f]);
 
-    auto issue = [&](long long t, int buf) {
-        const long long tx = t % p.tiles_x, r = t / p.tiles_x;
-        const long long ty = r % p.tiles_y, b = r / p.tiles_y;
+    auto issue = [&](int t, int buf) {
+        const uint32_t r = fdiv((uint32_t)t, tg.tx);
+        const uint32_t b = fdiv(r, tg.ty);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive_expect_tx(&full[buf], H::TBYTES);
-        tma_load_3d(smem_u32(tb[buf]), &smap, &full[buf], (int)(tx * TILE - H::LT),
-                    (int)(ty * TILE - H::LY), (int)b);
+        tma_load_3d(smem_u32(tb(buf)), &smap, &full[buf], (int)((uint32_t)t - r * tg.tx.d) * TILE - H::LT,
+                    (int)(r - b * tg.ty.d) * TILE - H::LY, (int)b);
     };
 
-    long long tile = blockIdx.x;
+    int tile = blockIdx.x;
     if (tid == 0)
         for (int i = 0; i < NST - 1; ++i)
-            if (tile + (long long)i * gridDim.x < p.ntiles) issue(tile + (long long)i * gridDim.x, i);
-    for (int k = 0; tile < p.ntiles; tile += gridDim.x, ++k) {
+            if (tile + i * (int)gridDim.x < tg.ntiles) issue(tile + i * (int)gridDim.x, i);
+    for (int k = 0; tile < tg.ntiles; tile += gridDim.x, ++k) {
         const int buf = k % NST;
-        const long long ahead = tile + (long long)(NST - 1) * gridDim.x;
-        if (tid == 0 && ahead < p.ntiles) issue(ahead, (k + NST - 1) % NST);
-        const long long ttx = tile % p.tiles_x, r = tile / p.tiles_x;
-        const long long tty = r % p.tiles_y, b = r / p.tiles_y;
+        const int ahead = tile + (NST - 1) * (int)gridDim.x;
+        if (tid == 0 && ahead < tg.ntiles) issue(ahead, (k + NST - 1) % NST);
+        const uint32_t tr_ = fdiv((uint32_t)tile, tg.tx);
+        const uint32_t tb_ = fdiv(tr_, tg.ty);
+        const int ttx = (int)((uint32_t)tile - tr_ * tg.tx.d), tty = (int)(tr_ - tb_ * tg.ty.d);
+        const long long out_off = (long long)tb_ * p.out_slice;
         if (!wait_tile(&full[buf], (k / NST) & 1)) break;
         const float *tile_f;
         if (sizeof(T) == 4) {
-            tile_f = reinterpret_cast<const float *>(tb[buf]);
+            tile_f = reinterpret_cast<const float *>(tb(buf));
         } else {
-            widen_tile<T, H>(tb[buf], ft);
+            widen_tile<T, H>(tb(buf), ft);
             __syncthreads();
             tile_f = ft;
         }
         // pass 1: temp[row][x] = IN( sum_f tile[row][x + OFF + CFL-1-f] * c[f] ),
         // 8 consecutive x per item; rows outside the image stay zero (the
         // reference reads zero for them in its second pass)
-        const long long y_top = tty * TILE - H::LY;
-        for (int it = tid; it < H::BH * 8; it += THREADS) {
-            const int row = it >> 3, g = it & 7;
+        // Items go eight rows to a group of eight lanes (same 8-column group
+        // g), so each 128-bit access of eight lanes hits eight bank groups.
+        const long long y_top = (long long)tty * TILE - H::LY;
+        constexpr int ITEMS = (H::BH + 7) / 8 * 64;
+        for (int it = tid; it < ITEMS; it += THREADS) {
+            const int row = (it >> 6) * 8 + (it & 7), g = (it >> 3) & 7;
+            if (row >= H::BH) continue;
             const long long gy = y_top + row;
             f2 a2[4] = {0ull, 0ull, 0ull, 0ull};
             if (gy >= 0 && gy < p.sd1) {
@@ -386,7 +445,7 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
             for (int e = 0; e < 4; ++e) upk(a2[e], a[2 * e], a[2 * e + 1]);
 #pragma unroll
             for (int e = 0; e < 8; ++e) a[e] = sep_round<T>(a[e]);
-            float *trow = temp + row * TILE + 8 * g;
+            float *trow = temp + row * SEP_TP + 8 * g;
             *reinterpret_cast<float4 *>(trow) = make_float4(a[0], a[1], a[2], a[3]);
             *reinterpret_cast<float4 *>(trow + 4) = make_float4(a[4], a[5], a[6], a[7]);
         }
@@ -398,7 +457,7 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
         for (int rr = 0; rr < 4; ++rr) acc[rr][0] = acc[rr][1] = 0ull;
 #pragma unroll
         for (int q = 3 + RFL - 1; q >= 0; --q) {
-            const float4 t4 = *reinterpret_cast<const float4 *>(temp + (4 * ty + q) * TILE + 4 * tx);
+            const float4 t4 = *reinterpret_cast<const float4 *>(temp + (4 * ty + q) * SEP_TP + 4 * tx);
             const f2 lo = pk(t4.x, t4.y), hi = pk(t4.z, t4.w);
 #pragma unroll
             for (int rr = 0; rr < 4; ++rr) {
@@ -409,13 +468,13 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
                 }
             }
         }
-        T *out = static_cast<T *>(p.out) + b * p.out_slice;
-        const long long x = ttx * TILE + 4 * tx;
+        T *out = static_cast<T *>(p.out) + out_off;
+        const long long x = (long long)ttx * TILE + 4 * tx;
         const bool vec = (x + 3 < p.od0) && ((p.od0 & 3) == 0) &&
                          ((reinterpret_cast<uintptr_t>(out) % (4 * sizeof(T))) == 0);
 #pragma unroll
         for (int rr = 0; rr < 4; ++rr) {
-            const long long y = tty * TILE + 4 * ty + rr;
+            const long long y = (long long)tty * TILE + 4 * ty + rr;
             if (y >= p.od1 || x >= p.od0) continue;
             float o[4];
             upk(acc[rr][0], o[0], o[1]);
@@ -492,21 +551,46 @@ static int persistent_grid(K kernel, size_t smem, long long ntiles) {
     return (int)std::max(1LL, std::min<long long>(ntiles, (long long)num_sms() * per_sm));
 }
 
+// tile grid of a launch; false when a count exceeds the 31-bit decoder
+static bool make_grid(TileGrid &tg, long long tiles_x, long long tiles_y, long long nbatch,
+                      long long b1 = 1, long long b2 = 1) {
+    const long long lim = 1LL << 31;
+    if (tiles_x < 1 || tiles_y < 1 || b1 < 1 || b2 < 1) return false;
+    if (tiles_x * tiles_y * nbatch >= lim || b1 >= lim || b2 >= lim) return false;
+    std::memset(&tg, 0, sizeof(tg));
+    tg.tx = make_fastdiv((uint32_t)tiles_x);
+    tg.ty = make_fastdiv((uint32_t)tiles_y);
+    tg.b1 = make_fastdiv((uint32_t)b1);
+    tg.b2 = make_fastdiv((uint32_t)b2);
+    tg.ntiles = (int)(tiles_x * tiles_y * nbatch);
+    return true;
+}
+
 template <typename T, int F0, int F1, bool EXACT, bool EXPAND>
 static bool run_conv2(const DirectParams &p) {
     using H = Halo<T, F0, F1, EXPAND>;
+    const long long slice = p.sd[0] * p.sd[1];
     const long long slices = p.sd[2] * p.sd[3];
+    const long long tx = (p.od[0] + TILE - 1) / TILE, ty = (p.od[1] + TILE - 1) / TILE;
+    TileGrid tg;
+    if (!make_grid(tg, tx, ty, p.nbatch, p.batch[1], p.batch[2])) return false;
+    // slice index of a batch coordinate: the signal is dense, so each batch
+    // step is a whole number of W x H slices
+    for (int i = 1; i < 4; ++i) {
+        if (p.batch[i] <= 1) continue;  // coordinate always 0
+        if (p.in_step[i] % slice != 0 || p.in_step[i] / slice >= (1LL << 31)) return false;
+        tg.zstep[i] = (int)(p.in_step[i] / slice);
+    }
+    if (slices >= (1LL << 31)) return false;
     CUtensorMap m;
     if (!make_map(m, p.sig, (int)sizeof(T), p.sd[0], p.sd[1], slices, H::BW, H::BH)) return false;
-    const long long tx = (p.od[0] + TILE - 1) / TILE, ty = (p.od[1] + TILE - 1) / TILE;
-    const long long ntiles = tx * ty * p.nbatch;
-    const size_t smem = NST * H::TB_ALIGNED + H::FT_BYTES + 8 * NST;
+    const size_t smem = NST_2D * H::TB_ALIGNED + H::FT_BYTES + 8 * NST_2D;
     auto kfn = conv2_tma_kernel<T, F0, F1, EXACT, EXPAND>;
     AFGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int grid = persistent_grid(kfn, smem, ntiles);
+    const int grid = persistent_grid(kfn, smem, tg.ntiles);
     {
-        KernelTimer kt("conv2_tile_kernel");
-        kfn<<<grid, THREADS, smem, stream()>>>(m, p, tx, ty, ntiles);
+        KernelTimer kt("conv2_tma_kernel");
+        kfn<<<grid, THREADS, smem, stream()>>>(m, p, tg);
     }
     count_launch();
     AFGB_POST_LAUNCH("conv2_tma_kernel");
@@ -552,15 +636,18 @@ bool tma_convolve2(const DirectParams &p, af_dtype t, bool exact) {
 template <typename T, int CL, int RL, bool EXACT, bool EXPAND>
 static bool run_sep(SepTmaParams p, const void *sig, long long W, long long Hh, long long slices) {
     using H = Halo<T, CL, RL, EXPAND>;
+    TileGrid tg;
+    if (!make_grid(tg, p.tiles_x, p.tiles_y, slices)) return false;
     CUtensorMap m;
     if (!make_map(m, sig, (int)sizeof(T), W, Hh, slices, H::BW, H::BH)) return false;
-    const size_t smem = NST * H::TB_ALIGNED + H::FT_BYTES + (size_t)H::BH * TILE * 4 + 8 * NST;
+    const size_t smem = NST_SEP * H::TB_ALIGNED + H::FT_BYTES + (size_t)H::BH * SEP_TP * 4 +
+                        8 * NST_SEP;
     auto kfn = sep_tma_kernel<T, CL, RL, EXACT, EXPAND>;
     AFGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const int grid = persistent_grid(kfn, smem, p.ntiles);
+    const int grid = persistent_grid(kfn, smem, tg.ntiles);
     {
-        KernelTimer kt("sep_fused_kernel");
-        kfn<<<grid, THREADS, smem, stream()>>>(m, p);
+        KernelTimer kt("sep_tma_kernel");
+        kfn<<<grid, THREADS, smem, stream()>>>(m, p, tg);
     }
     count_launch();
     AFGB_POST_LAUNCH("sep_tma_kernel");

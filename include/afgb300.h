@@ -215,6 +215,20 @@ AFGB_API int afgb_nn_output_dims(dim_t *odims, const dim_t *sdims, const dim_t *
                                  const dim_t *stride, const dim_t *padding,
                                  const dim_t *dilation);
 
+/* Memory manager statistics of this library's device pool.
+ *   af_device_mem_info: include/af/device.h:459 — alloc_bytes is the pool's
+ *     reserved bytes, lock_bytes / lock_buffers the bytes and buffers held by
+ *     live arrays and in-flight scratch (alloc_buffers = lock_buffers: a
+ *     stream-ordered pool keeps no per-buffer free list).
+ *   af_device_gc: include/af/device.h:492 — waits for the stream and returns
+ *     unused pool memory to the device. */
+AFGB_API af_err af_device_mem_info(size_t *alloc_bytes, size_t *alloc_buffers,
+                                   size_t *lock_bytes, size_t *lock_buffers);
+AFGB_API af_err af_device_gc(void);
+/* Peak of lock_bytes since load or the last reset (reset != 0 restarts it at
+ * the current value).  No counterpart in the reference. */
+AFGB_API af_err afgb_device_mem_peak(size_t *peak_bytes, int reset);
+
 /* Fault injection for tests: the n-th device allocation from now fails with
  * AF_ERR_NO_MEM (n <= 0 disables).  Host-side only. */
 AFGB_API void afgb_debug_fail_alloc_after(int n);

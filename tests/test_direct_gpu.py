@@ -199,3 +199,39 @@ def test_allocation_failure_reports_no_mem(af):
     # the library is still usable afterwards
     out = af.convolve2(S, F, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL).to_numpy()
     assert out[8, 8, 0, 0] == 9.0
+
+
+def _ran(af, name, fn):
+    """Runs fn with the library's kernel timing on; the number of launches
+    recorded under `name`."""
+    import ctypes
+
+    L = af.lib()
+    L.afgb_kernel_timing(1)
+    try:
+        fn()
+        af.sync()
+        c = ctypes.c_ulonglong()
+        ms = ctypes.c_double()
+        L.afgb_kernel_time(name.encode(), ctypes.byref(c), ctypes.byref(ms))
+    finally:
+        L.afgb_kernel_timing(0)
+    return c.value
+
+
+TMA_2D = [c for c in CASES if c[0].startswith("r_tma_") and c[1] in (C.F32, C.U8, C.S8)]
+
+
+@pytest.mark.parametrize("case", TMA_2D, ids=lambda c: c[0])
+def test_tma_2d_path_taken(af, oracle, case):
+    """Dense images with 16-byte rows and 3/5/7 square filters run on the
+    TMA-staged kernel, in every batch kind (a fallback would still be
+    correct, so the path itself is checked)."""
+    cid, dt, rank, sd, fd, expand, seed = case
+    s = C.make_signal(dt, sd, seed)
+    f = C.make_filter(dt, fd, seed + 1, rank)
+    out = {}
+    n = _ran(af, "conv2_tma_kernel", lambda: out.setdefault("o", run(af, s, f, dt, rank, expand)))
+    assert n == 1
+    if dt != C.F32:
+        assert out["o"].tobytes() == oracle.convolve(s, f, dt, rank, expand).tobytes()

@@ -106,3 +106,29 @@ def test_sep_rejections(af):
     with pytest.raises(af.AfError) as e:
         af.convolve2_separable(long, f4, S2, af.AF_CONV_DEFAULT)
     assert e.value.code == af.AF_ERR_NOT_SUPPORTED
+
+
+TMA_SEP = [c for c in CASES if c[0].startswith("sep_") and "_tma_" in c[0]
+           and c[1] in (C.F32, C.U8, C.S8)]
+
+
+@pytest.mark.parametrize("case", TMA_SEP, ids=lambda c: c[0])
+def test_sep_tma_path_taken(af, oracle, case):
+    """Dense 16-byte-row images with equal 3/5/7/15-tap filters run on the
+    fused TMA-staged kernel (no temporary image)."""
+    import ctypes
+
+    cid, dt, sd, cl, rl, expand, seed = case
+    s = C.sep_signal(dt, sd, seed)
+    cf, rf = C.sep_taps(dt, cl, seed + 1), C.sep_taps(dt, rl, seed + 2)
+    L = af.lib()
+    L.afgb_kernel_timing(1)
+    try:
+        out = run(af, s, cf, rf, dt, expand)
+        c, ms = ctypes.c_ulonglong(), ctypes.c_double()
+        L.afgb_kernel_time(b"sep_tma_kernel", ctypes.byref(c), ctypes.byref(ms))
+    finally:
+        L.afgb_kernel_timing(0)
+    assert c.value == 1
+    if dt != C.F32:
+        assert out.tobytes() == oracle.convolve2_sep(s, cf, rf, dt, expand).tobytes()
