@@ -260,32 +260,100 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
         }
 
         float acc[4][4];
+        if constexpr (!EXACT && sizeof(T) == 4) {
+            // Fused mode: taps u = 2m, 2m+1 of one output share a packed FMA
+            // (even taps accumulate in the low lane, odd taps in the high
+            // lane); the odd filter's last tap takes a scalar FMA into the low
+            // lane, so no lane ever reads a pixel outside the filter window.
+            constexpr int NP = F0 / 2;
+            static_assert(H::OFF + F0 + 2 < NW4 * 4, "packed window exceeds the loaded row");
+            f2 wp[F1][NP > 0 ? NP : 1];
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
+            for (int fj = 0; fj < F1; ++fj)
 #pragma unroll
-            for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
+                for (int m = 0; m < NP; ++m)
+                    wp[fj][m] = pk(wr[fj * F0 + F0 - 1 - 2 * m], wr[fj * F0 + F0 - 2 - 2 * m]);
+            f2 acc2[4][4];
 #pragma unroll
-        for (int q = 3 + F1 - 1; q >= 0; --q) {
-            float v[NW4 * 4];
-            const float *row = tile_f + (4 * ty + q) * H::PF + 4 * tx;
+            for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int u = 0; u < NW4; ++u) {
-                const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
-                v[4 * u] = t4.x;
-                v[4 * u + 1] = t4.y;
-                v[4 * u + 2] = t4.z;
-                v[4 * u + 3] = t4.w;
+                for (int c = 0; c < 4; ++c) acc2[a][c] = 0ull;
+#pragma unroll
+            for (int q = 3 + F1 - 1; q >= 0; --q) {
+                float v[NW4 * 4];
+                const float *row = tile_f + (4 * ty + q) * H::PF + 4 * tx;
+#pragma unroll
+                for (int u = 0; u < NW4; ++u) {
+                    const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
+                    v[4 * u] = t4.x;
+                    v[4 * u + 1] = t4.y;
+                    v[4 * u + 2] = t4.z;
+                    v[4 * u + 3] = t4.w;
+                }
+                f2 ve[NW4 * 2], vo[NW4 * 2 - 1];
+#pragma unroll
+                for (int i = 0; i < NW4 * 2; ++i) ve[i] = pk(v[2 * i], v[2 * i + 1]);
+#pragma unroll
+                for (int i = 0; i < NW4 * 2 - 1; ++i) vo[i] = pk(v[2 * i + 1], v[2 * i + 2]);
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr) {
+                    const int fj = rr + F1 - 1 - q;
+                    if (fj >= 0 && fj < F1) {
+#pragma unroll
+                        for (int cc = 0; cc < 4; ++cc) {
+                            const int b0 = cc + H::OFF;  // window index of tap u = 0
+#pragma unroll
+                            for (int m = 0; m < NP; ++m) {
+                                const int j = b0 + 2 * m;
+                                const f2 in2 = (j & 1) ? vo[(j - 1) >> 1] : ve[j >> 1];
+                                acc2[rr][cc] = mac2<false>(acc2[rr][cc], in2, wp[fj][m]);
+                            }
+                            if (F0 & 1) {
+                                float lo, hi;
+                                upk(acc2[rr][cc], lo, hi);
+                                lo = fmaf(v[b0 + F0 - 1], wr[fj * F0], lo);
+                                acc2[rr][cc] = pk(lo, hi);
+                            }
+                        }
+                    }
+                }
             }
 #pragma unroll
-            for (int rr = 0; rr < 4; ++rr) {
-                const int fj = rr + F1 - 1 - q;
-                if (fj >= 0 && fj < F1) {
+            for (int a = 0; a < 4; ++a)
 #pragma unroll
-                    for (int fi = 0; fi < F0; ++fi) {
-                        const float wv = wr[fj * F0 + fi];
+                for (int c = 0; c < 4; ++c) {
+                    float lo, hi;
+                    upk(acc2[a][c], lo, hi);
+                    acc[a][c] = lo + hi;
+                }
+        } else {
 #pragma unroll
-                        for (int cc = 0; cc < 4; ++cc)
-                            acc[rr][cc] = mac<EXACT>(acc[rr][cc], v[cc + H::OFF + F0 - 1 - fi], wv);
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
+#pragma unroll
+            for (int q = 3 + F1 - 1; q >= 0; --q) {
+                float v[NW4 * 4];
+                const float *row = tile_f + (4 * ty + q) * H::PF + 4 * tx;
+#pragma unroll
+                for (int u = 0; u < NW4; ++u) {
+                    const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
+                    v[4 * u] = t4.x;
+                    v[4 * u + 1] = t4.y;
+                    v[4 * u + 2] = t4.z;
+                    v[4 * u + 3] = t4.w;
+                }
+#pragma unroll
+                for (int rr = 0; rr < 4; ++rr) {
+                    const int fj = rr + F1 - 1 - q;
+                    if (fj >= 0 && fj < F1) {
+#pragma unroll
+                        for (int fi = 0; fi < F0; ++fi) {
+                            const float wv = wr[fj * F0 + fi];
+#pragma unroll
+                            for (int cc = 0; cc < 4; ++cc)
+                                acc[rr][cc] = mac<EXACT>(acc[rr][cc], v[cc + H::OFF + F0 - 1 - fi], wv);
+                        }
                     }
                 }
             }

@@ -84,7 +84,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "100"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except FileNotFoundError:
             self.proc = None
@@ -278,6 +278,7 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
     }
     if not args.no_secondary:
         res["secondary"] = run_direct_workloads(af, peaks, args)
+        res["cnn4"] = run_cnn(af, args)
     return res
 
 
@@ -328,6 +329,91 @@ def run_e2e(af, X, Wt, Gd, prec, args) -> dict:
     return {"value": 3 * nn_flops() * args.steps / dt / 1e12, "unit": "TFLOP/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "ms_per_step": dt * 1e3 / args.steps}
+
+
+CNN_CHANNELS = [(3, 32), (32, 64), (64, 128), (128, 128)]
+CNN_GEOMS = [((2, 2), (1, 1), (1, 1)), ((2, 2), (1, 1), (1, 1)), ((1, 1), (1, 1), (1, 1)),
+             ((1, 1), (2, 2), (2, 2))]
+
+
+def _nn_out_hw(h, w, k, s, p, d):
+    return (1 + (h + 2 * p[1] - ((k - 1) * d[1] + 1)) // s[1],
+            1 + (w + 2 * p[0] - ((k - 1) * d[0] + 1)) // s[0])
+
+
+def run_cnn(af, args) -> dict:
+    """Four conv2_nn + ReLU layers on 224x224x3x64 (loss = sum of squares of
+    the output), forward + backward with activation recomputation, BF16 and
+    the plain FP32 path: step time, useful TFLOP/s, peak device memory and
+    the error of each filter gradient against the same network in FP64."""
+    import torch
+    import torch.nn.functional as F
+
+    from arrayfire_gb300.autograd import cnn_step
+    from arrayfire_gb300.autograd import nn_flops as layer_flops
+
+    gen = torch.Generator(device="cuda").manual_seed(5)
+    n = 64
+    x0 = torch.rand((n, 3, 224, 224), device="cuda", generator=gen) * 2 - 1
+    ws = [torch.randn((k, c, 3, 3), device="cuda", generator=gen) * (2.0 / (9 * c)) ** 0.5
+          for c, k in CNN_CHANNELS]
+    # useful work: every layer's forward and filter gradient, data gradients of layers 2-4
+    shape, fl, patch = tuple(x0.shape), [], []
+    for (c, k), (st, pd, dl) in zip(CNN_CHANNELS, CNN_GEOMS):
+        fl.append(layer_flops(shape, (k, c, 3, 3), st, pd, dl))
+        ho, wo = _nn_out_hw(shape[2], shape[3], 3, st, pd, dl)
+        patch.append(wo * ho * 9 * c * n * 4)  # the reference's unwrap buffer of this layer
+        shape = (n, k, ho, wo)
+    useful = 2 * sum(fl) + sum(fl[1:])
+
+    # FP64 reference gradients (torch float64 on the flipped filters)
+    wl = [w.double().requires_grad_() for w in ws]
+    h = x0.double()
+    for w, (st, pd, dl) in zip(wl, CNN_GEOMS):
+        h = torch.relu(F.conv2d(h, w.flip([2, 3]), stride=(st[1], st[0]), padding=(pd[1], pd[0]),
+                                dilation=(dl[1], dl[0])))
+    (h ** 2).sum().backward()
+    ref = [w.grad for w in wl]
+    del wl, h
+    torch.cuda.empty_cache()
+
+    out = {"workload": "4 x (conv2_nn + ReLU), input 224x224x3x64 U[-1,1), 3->32 s2, 32->64 s2, "
+                       "64->128, 128->128 d2 p2; loss = sum(out^2)",
+           "useful_gflop_per_step": round(useful / 1e9, 2),
+           "reference_unwrap_bytes": {"largest_layer": int(max(patch)), "all_layers": int(sum(patch))}}
+    for prec in ("bf16", "fp32"):
+        for _ in range(2):
+            loss, grads, rfl = cnn_step(x0, ws, CNN_GEOMS, precision=prec, recompute=True)
+        del grads
+        torch.cuda.synchronize()
+        af.device_mem_peak(reset=True)
+        base = torch.cuda.memory_allocated()
+        torch.cuda.reset_peak_memory_stats()
+        loss, grads, rfl = cnn_step(x0, ws, CNN_GEOMS, precision=prec, recompute=True)
+        torch.cuda.synchronize()
+        lib_peak = af.device_mem_peak()
+        torch_peak = torch.cuda.max_memory_allocated() - base
+        errs = [float(torch.linalg.vector_norm(g.double() - r) / torch.linalg.vector_norm(r))
+                for g, r in zip(grads, ref)]
+        del grads
+        k = 5
+        tot = 0.0
+        for _ in range(k):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            loss, grads, rfl = cnn_step(x0, ws, CNN_GEOMS, precision=prec, recompute=True)
+            b.record()
+            b.synchronize()
+            tot += a.elapsed_time(b)
+            del grads
+        ms = tot / k
+        out[prec] = {"ms_per_step": round(ms, 3), "TFLOP/s": round(useful / (ms / 1e3) / 1e12, 2),
+                     "recompute_gflop": round(rfl / 1e9, 2),
+                     "peak_library_bytes": int(lib_peak), "peak_torch_harness_bytes": int(torch_peak),
+                     "filter_grad_rel_err_vs_fp64": [float(f"{e:.3e}") for e in errs]}
+    out["bf16_speedup_over_fp32"] = round(out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"], 2)
+    return out
 
 
 def run_direct_workloads(af, peaks, args) -> dict:
@@ -483,7 +569,16 @@ def run_only(args) -> None:
     s = NN_SHAPE
     st, pd, dl = s["stride"], s["pad"], s["dil"]
     g = np.random.Generator(np.random.Philox(1234))
-    if args.only in ("fwd", "dgrad", "wgrad"):
+    if args.only == "cnn":
+        from arrayfire_gb300.autograd import cnn_step
+
+        gen = torch.Generator(device="cuda").manual_seed(5)
+        x0 = torch.rand((64, 3, 224, 224), device="cuda", generator=gen) * 2 - 1
+        ws = [torch.randn((k, c, 3, 3), device="cuda", generator=gen) * (2.0 / (9 * c)) ** 0.5
+              for c, k in CNN_CHANNELS]
+        prec = "fp32" if args.precision == "fp32" else "bf16"
+        fn = lambda: cnn_step(x0, ws, CNN_GEOMS, precision=prec, recompute=True)  # noqa: E731
+    elif args.only in ("fwd", "dgrad", "wgrad"):
         X = np.asfortranarray(g.standard_normal((s["W"], s["H"], s["C"], s["N"]), dtype=np.float32))
         Wt = np.asfortranarray((g.standard_normal((s["fw"], s["fh"], s["C"], s["K"])) * 0.06
                                 ).astype(np.float32))
@@ -542,14 +637,14 @@ def run_only(args) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32", "fp8"])
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--only", default=None,
-                    choices=["fwd", "dgrad", "wgrad", "sep_f32", "sep_u8", "same7", "conv3"],
+                    choices=["fwd", "dgrad", "wgrad", "sep_f32", "sep_u8", "same7", "conv3", "cnn"],
                     help="run one operation of the workload --steps times after --warmup "
                          "(for profiler captures); prints its timing, not the bench line")
     args = ap.parse_args()
@@ -610,7 +705,7 @@ def main() -> None:
         "e2e": res["e2e"], "clocks": res["clocks"], "gpu_launches": res["gpu_launches"],
         "errors_vs_fp64": res["errors_vs_fp64"], "kernel_times_ms": res["kernel_times_ms"],
         "fp32_path": res["fp32_path"],
-        "secondary": res.get("secondary"), "peaks": peaks,
+        "secondary": res.get("secondary"), "cnn4": res.get("cnn4"), "peaks": peaks,
     }
     print(json.dumps(line))
 
