@@ -429,8 +429,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     if (TMA_B) {
                         int offx, offy;
                         tap_offsets(p, ti, u, v, offx, offy);
+                        // forward: input origin x0*s (traversal stride s in the map);
+                        // data gradient (stride 1 only here): x0
+                        const int bx0 = p.mode == 0 ? ti.x0 * p.sx : ti.x0;
+                        const int by0 = p.mode == 0 ? ti.y0 * p.sy : ti.y0;
                         tma_load_4d(smem_u32(b_stage + s * B_BYTES), &xmap, &sm->full[s],
-                                    cchunk * (FP8 ? 128 : 64), ti.x0 + offx, ti.y0 + offy, ti.n);
+                                    cchunk * (FP8 ? 128 : 64), bx0 + offx, by0 + offy, ti.n);
                     }
                 }
             }
@@ -898,15 +902,17 @@ static CUtensorMap make_wmap(const void *ptr, long long rows, long long cols, in
 }
 
 // 4-D NHWC tensor (Cpad, W, H, N) of bf16 (esize 2) or e4m3 bytes (esize 1),
-// box {128 bytes, bx, by, 1}, 128B swizzle, out-of-range elements read as zero
+// 128B swizzle, out-of-range elements read as zero.  A load brings bx x by
+// pixels of 128 bytes; with traversal strides (sx, sy) those pixels are every
+// sx-th along x and every sy-th along y (the box then spans bx*sx x by*sy).
 static CUtensorMap make_imap(const void *ptr, int Cpad, int W, int H, int N, int bx, int by,
-                             int esize = 2) {
+                             int esize = 2, int sx = 1, int sy = 1) {
     CUtensorMap m;
     cuuint64_t dims[4] = {(cuuint64_t)Cpad, (cuuint64_t)W, (cuuint64_t)H, (cuuint64_t)N};
     cuuint64_t strides[3] = {(cuuint64_t)Cpad * esize, (cuuint64_t)Cpad * esize * W,
                              (cuuint64_t)Cpad * esize * W * H};
-    cuuint32_t box[4] = {(cuuint32_t)(128 / esize), (cuuint32_t)bx, (cuuint32_t)by, 1};
-    cuuint32_t es[4] = {1, 1, 1, 1};
+    cuuint32_t box[4] = {(cuuint32_t)(128 / esize), (cuuint32_t)(bx * sx), (cuuint32_t)(by * sy), 1};
+    cuuint32_t es[4] = {1, (cuuint32_t)sx, (cuuint32_t)sy, 1};
     CUresult r = encode_fn()(&m, esize == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8,
                              4, (void *)ptr, dims, strides, box,
                              es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -931,14 +937,19 @@ static __nv_bfloat16 *to_nhwc(const float *src, int W, int H, int C, int N, int 
 }
 
 // rectangle bx x by (bx*by == area, bx >= minx) covering W x H with the
-// least padding; ties prefer the wider rectangle
-static void pick_rect(int W, int H, int area, int minx, int &bx, int &by) {
+// least padding; ties prefer the wider rectangle.  With traversal strides the
+// box spans bx*sx x by*sy elements, at most 256 each.  False when no
+// rectangle fits.
+static bool pick_rect(int W, int H, int area, int minx, int &bx, int &by, int sx = 1, int sy = 1) {
     long long best = -1;
-    bx = std::min(area, 256);
+    int x = 1;  // widest power of two within the area and the box limit
+    while (x * 2 <= std::min(area, 256 / sx)) x *= 2;
+    bx = x;
     by = area / bx;
-    for (int x = std::min(area, 256); x >= minx; x >>= 1) {
+    for (; x >= minx; x >>= 1) {
         const int y = area / x;
-        if (y > 256) break;
+        if (x * y != area) continue;
+        if ((long long)y * sy > 256) break;
         const long long cover = (long long)((W + x - 1) / x) * x * ((H + y - 1) / y) * y;
         if (best < 0 || cover < best) {
             best = cover;
@@ -946,6 +957,7 @@ static void pick_rect(int W, int H, int area, int minx, int &bx, int &by) {
             by = y;
         }
     }
+    return best >= 0;
 }
 
 static size_t gather_smem() {
@@ -967,7 +979,12 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     const int SCpad = round_up(SC, CH);
     const int OCpad = round_up(DC, 128);
     const int taps = (int)(g.fw * g.fh);
-    const bool tma_b = g.sx == 1 && g.sy == 1;
+    // pixel operand by TMA: stride 1 in both modes; strided forwards too,
+    // through the tensor map's traversal strides (at most 8)
+    int rbx = 0, rby = 0;
+    const bool tma_b = (g.sx == 1 && g.sy == 1) ||
+                       (mode == 0 && g.sx <= 8 && g.sy <= 8 &&
+                        pick_rect((int)g.Wo, (int)g.Ho, BN, 32, rbx, rby, (int)g.sx, (int)g.sy));
     const int esize = fp8 ? 1 : 2;
 
     void *img = nullptr, *wt = nullptr;
@@ -1071,11 +1088,12 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     CUtensorMap xmap;
     std::memset(&xmap, 0, sizeof(xmap));
     if (tma_b) {
-        pick_rect(DW, DH, BN, 32, p.BX, p.BY);
+        const int tsx = mode == 0 ? (int)g.sx : 1, tsy = mode == 0 ? (int)g.sy : 1;
+        pick_rect(DW, DH, BN, 32, p.BX, p.BY, tsx, tsy);
         p.ntx = (DW + p.BX - 1) / p.BX;
         p.nty = (DH + p.BY - 1) / p.BY;
         ntile = p.n_och_tiles * p.ntx * p.nty * (int)g.N;
-        xmap = make_imap(img, SCpad, SW, SH, (int)g.N, p.BX, p.BY, esize);
+        xmap = make_imap(img, SCpad, SW, SH, (int)g.N, p.BX, p.BY, esize, tsx, tsy);
     }
     p.total_tiles = ntile;
 
@@ -1188,20 +1206,22 @@ bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array 
     }
     p.groups_per_tile = best;
     p.n_k_tiles = Kpad / 128;
-    // stride 1: 64-pixel rectangles by TMA; otherwise the cp.async row
-    // gather handles any stride
-    const bool tma = g.sx == 1 && g.sy == 1;
+    // 64-pixel rectangles by TMA; the signal map walks every s-th pixel
+    // (traversal strides up to 8); otherwise the cp.async row gather
+    int rbx = 0, rby = 0;
+    const bool tma = g.sx <= 8 && g.sy <= 8 &&
+                     pick_rect((int)g.Wo, (int)g.Ho, WG_KP, 8, rbx, rby, (int)g.sx, (int)g.sy);
     CUtensorMap gmap, xmap;
     std::memset(&gmap, 0, sizeof(gmap));
     std::memset(&xmap, 0, sizeof(xmap));
     long long units;  // pixel blocks (TMA) or pixels (cp.async)
     if (tma) {
-        pick_rect((int)g.Wo, (int)g.Ho, WG_KP, 8, p.BX, p.BY);
+        pick_rect((int)g.Wo, (int)g.Ho, WG_KP, 8, p.BX, p.BY, (int)g.sx, (int)g.sy);
         p.ntx = ((int)g.Wo + p.BX - 1) / p.BX;
         p.nty = ((int)g.Ho + p.BY - 1) / p.BY;
         units = (long long)p.ntx * p.nty * g.N;
         gmap = make_imap(gg, Kpad, (int)g.Wo, (int)g.Ho, (int)g.N, p.BX, p.BY);
-        xmap = make_imap(x, Cpad, (int)g.W, (int)g.H, (int)g.N, p.BX, p.BY);
+        xmap = make_imap(x, Cpad, (int)g.W, (int)g.H, (int)g.N, p.BX, p.BY, 2, (int)g.sx, (int)g.sy);
     } else {
         units = g.Wo * g.Ho * g.N;
     }

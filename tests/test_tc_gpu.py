@@ -145,3 +145,41 @@ def test_fp8_gradients_not_supported(af):
     with pytest.raises(af.AfError) as e:
         af.convolve2_gradient_nn(G, S, F, O, st, pd, dl, af.AF_CONV_GRADIENT_DATA, precision="fp8")
     assert e.value.code == af.AF_ERR_NOT_SUPPORTED
+
+
+def _launches(af, name, fn):
+    import ctypes
+
+    L = af.lib()
+    L.afgb_kernel_timing(1)
+    try:
+        r = fn()
+        af.sync()
+        c, ms = ctypes.c_ulonglong(), ctypes.c_double()
+        L.afgb_kernel_time(name.encode(), ctypes.byref(c), ctypes.byref(ms))
+    finally:
+        L.afgb_kernel_timing(0)
+    return c.value, r
+
+
+STRIDED = [("s2_c64", (33, 30, 64, 2), (3, 3, 64, 96), (2, 2), (1, 1), (1, 1)),
+           ("s3x2_d2_c64", (40, 37, 64, 1), (3, 3, 64, 128), (3, 2), (2, 1), (2, 2)),
+           ("s2_5x5_c128", (30, 28, 128, 2), (5, 5, 128, 64), (2, 2), (4, 4), (2, 2))]
+
+
+@pytest.mark.parametrize("case", STRIDED, ids=lambda c: c[0])
+def test_bf16_strided_tma_paths(af, oracle, case):
+    """Strided forwards and filter gradients load the pixel operand by TMA
+    with traversal strides (the map walks every s-th pixel); results against
+    FP64 and the kernels that ran."""
+    name, sd, fd, st, pd, dl = case
+    s, f = C.nn_inputs(case, 6100)
+    g = C.nn_grad(case, 6100)
+    S, F, G = af.Array.from_numpy(s), af.Array.from_numpy(f), af.Array.from_numpy(g)
+    n, Y = _launches(af, "tc_fwd_kernel", lambda: af.convolve2_nn(S, F, st, pd, dl, precision="bf16"))
+    assert n == 1
+    check(Y.to_numpy(), oracle.nn_forward_f64(s, f, st, pd, dl), name + " fwd")
+    n, DW = _launches(af, "tc_wgrad_kernel", lambda: af.convolve2_gradient_nn(
+        G, S, F, Y, st, pd, dl, af.AF_CONV_GRADIENT_FILTER, precision="bf16"))
+    assert n == 1
+    check(DW.to_numpy(), oracle.nn_filter_grad_f64(g, s, C.af_shape(fd), st, pd, dl), name + " wgrad")
