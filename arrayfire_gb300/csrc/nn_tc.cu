@@ -761,6 +761,72 @@ __global__ void weights_bf16_kernel(const float *__restrict__ w, int fw, int fh,
     }
 }
 
+// ---- taps folded into channels ---------------------------------------------
+// When C*fw*fh <= 64 (an RGB input layer, a 1x1 layer with few channels) a
+// per-tap reduction would be mostly channel padding.  Folding gives each
+// output pixel one 64-channel bf16 row holding every (c, u, v) its output
+// reads: row[c + C*(u + fw*v)] = x[xo*sx - px + u*dx, yo*sy - py + v*dy, c, n]
+// (zero outside the image), so the forward and the filter gradient become
+// 1x1, stride-1 problems on the output grid.
+__global__ void __launch_bounds__(256) fold_taps_bf16_kernel(
+    const float *__restrict__ x, int W, int H, int C, int N, int fw, int fh, int sx, int sy,
+    int px, int py, int dx, int dy, int Wo, int Ho, __nv_bfloat16 *__restrict__ out) {
+    const long long npix = (long long)Wo * Ho * N;
+    const int KC = C * fw * fh;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < npix;
+         q += (long long)gridDim.x * blockDim.x) {
+        const int xo = (int)(q % Wo);
+        const long long r = q / Wo;
+        const int yo = (int)(r % Ho);
+        const int n = (int)(r / Ho);
+        uint4 *dst = reinterpret_cast<uint4 *>(out + q * 64);
+#pragma unroll 1
+        for (int j8 = 0; j8 < 8; ++j8) {
+            uint32_t wd[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                float v2[2];
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int j = j8 * 8 + e * 2 + h;
+                    float val = 0.f;
+                    if (j < KC) {
+                        const int c = j % C, tap = j / C;
+                        const int u = tap % fw, v = tap / fw;
+                        const int xs = xo * sx - px + u * dx, ys = yo * sy - py + v * dy;
+                        if (xs >= 0 && xs < W && ys >= 0 && ys < H)
+                            val = __ldg(x + xs + (long long)W * (ys + (long long)H * (c + (long long)C * n)));
+                    }
+                    v2[h] = val;
+                }
+                const __nv_bfloat162 b = __floats2bfloat162_rn(v2[0], v2[1]);
+                wd[e] = *reinterpret_cast<const uint32_t *>(&b);
+            }
+            dst[j8] = make_uint4(wd[0], wd[1], wd[2], wd[3]);
+        }
+    }
+}
+
+// folded filter: Wt[och][c + C*(u + fw*v)] = w[fw-1-u, fh-1-v, c, och], zero
+// beyond C*fw*fh channels and K output channels; och_pad x 64 bf16
+__global__ void weights_fold_bf16_kernel(const float *__restrict__ w, int fw, int fh, int C, int K,
+                                         int och_pad, __nv_bfloat16 *__restrict__ out) {
+    const long long total = (long long)och_pad * 64;
+    const int KC = C * fw * fh;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        const int j = (int)(t % 64);
+        const int och = (int)(t / 64);
+        float val = 0.f;
+        if (j < KC && och < K) {
+            const int c = j % C, tap = j / C;
+            const int u = tap % fw, v = tap / fw;
+            val = w[(fw - 1 - u) + fw * ((fh - 1 - v) + fh * (c + (long long)C * och))];
+        }
+        out[t] = __float2bfloat16_rn(val);
+    }
+}
+
 // ---- FP8-E4M3 operands -----------------------------------------------------
 // |x| maximum over n floats, as float bits (non-negative floats order like
 // their bit patterns); *out must start at 0
@@ -936,6 +1002,37 @@ static __nv_bfloat16 *to_nhwc(const float *src, int W, int H, int C, int N, int 
     return out;
 }
 
+static bool foldable(const NNGeom &g) { return g.C * g.fw * g.fh <= 64; }
+
+// the 1x1, stride-1 problem over the output grid that tap folding turns g into
+static NNGeom folded_geometry(const NNGeom &g) {
+    NNGeom f = g;
+    f.W = g.Wo;
+    f.H = g.Ho;
+    f.C = g.C * g.fw * g.fh;
+    f.fw = f.fh = 1;
+    f.sx = f.sy = 1;
+    f.px = f.py = 0;
+    f.dx = f.dy = 1;
+    return f;
+}
+
+static __nv_bfloat16 *fold_taps(const float *x, const NNGeom &g) {
+    const long long npix = g.Wo * g.Ho * g.N;
+    __nv_bfloat16 *out = static_cast<__nv_bfloat16 *>(alloc_device((size_t)npix * 64 * 2));
+    const unsigned blocks = (unsigned)std::max(1LL, std::min<long long>((npix + 255) / 256,
+                                                                        num_sms() * 16LL));
+    {
+        KernelTimer kt("tc_convert_kernel");
+        fold_taps_bf16_kernel<<<blocks, 256, 0, stream()>>>(
+            x, (int)g.W, (int)g.H, (int)g.C, (int)g.N, (int)g.fw, (int)g.fh, (int)g.sx, (int)g.sy,
+            (int)g.px, (int)g.py, (int)g.dx, (int)g.dy, (int)g.Wo, (int)g.Ho, out);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("fold_taps_bf16_kernel");
+    return out;
+}
+
 // rectangle bx x by (bx*by == area, bx >= minx) covering W x H with the
 // least padding; ties prefer the wider rectangle.  With traversal strides the
 // box spans bx*sx x by*sy elements, at most 256 each.  False when no
@@ -967,8 +1064,11 @@ static size_t gather_smem() {
 // forward (mode 0) or data gradient (mode 1); fp8 (forward only): e4m3
 // operands with a per-tensor activation scale and per-output-channel weight
 // scales (`user_wscale`, K floats, or amax/448 computed on the device)
+// `unfolded`: g is the folded geometry of *unfolded (bf16 forward only); the
+// image and filter are folded from the f32 operands of *unfolded
 static void run_gather(const NNGeom &g, int mode, const float *img_f32, const float *w_f32,
-                       float *dst, bool fp8 = false, const float *user_wscale = nullptr) {
+                       float *dst, bool fp8 = false, const float *user_wscale = nullptr,
+                       const NNGeom *unfolded = nullptr) {
     const int SW = mode == 0 ? (int)g.W : (int)g.Wo;
     const int SH = mode == 0 ? (int)g.H : (int)g.Ho;
     const int SC = mode == 0 ? (int)g.C : (int)g.K;
@@ -990,7 +1090,17 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     void *img = nullptr, *wt = nullptr;
     float *scales = nullptr;  // [0] activation scale, [1..K] weight scales, [K+1..2K] output factors
     unsigned int *amax = nullptr;
-    if (!fp8) {
+    if (!fp8 && unfolded) {
+        img = fold_taps(img_f32, *unfolded);
+        wt = alloc_device((size_t)OCpad * 64 * 2);
+        const long long total = (long long)OCpad * 64;
+        const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
+        weights_fold_bf16_kernel<<<blocks, 256, 0, stream()>>>(
+            w_f32, (int)unfolded->fw, (int)unfolded->fh, (int)unfolded->C, (int)unfolded->K, OCpad,
+            static_cast<__nv_bfloat16 *>(wt));
+        count_launch();
+        AFGB_POST_LAUNCH("weights_fold_bf16_kernel");
+    } else if (!fp8) {
         img = to_nhwc(img_f32, SW, SH, SC, (int)g.N, SCpad);
         wt = alloc_device((size_t)OCpad * taps * SCpad * 2);
         long long total = (long long)OCpad * taps * SCpad;
@@ -1151,6 +1261,11 @@ bool tc_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out
         return true;
     }
     if (prec != AFGB_PRECISION_BF16) return false;
+    if (foldable(g)) {
+        const NNGeom f = folded_geometry(g);
+        run_gather(f, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>(), false, nullptr, &g);
+        return true;
+    }
     run_gather(g, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>());
     return true;
 }
@@ -1161,11 +1276,16 @@ bool tc_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &
     return true;
 }
 
-bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw) {
+bool tc_filter_grad(const NNGeom &g0, const Array &grad, const Array &sig, Array &dw) {
     if (grad.type != f32) return false;
+    // folded taps: the signal operand is the folded image and the problem is
+    // 1x1 on the output grid; its partial rows c + C*tap are the unfolded ones
+    const bool fold = foldable(g0);
+    const NNGeom g = fold ? folded_geometry(g0) : g0;
     const int Cpad = round_up((int)g.C, 64);
     const int Kpad = round_up((int)g.K, 128);
-    __nv_bfloat16 *x = to_nhwc(sig.ptr<float>(), (int)g.W, (int)g.H, (int)g.C, (int)g.N, Cpad);
+    __nv_bfloat16 *x = fold ? fold_taps(sig.ptr<float>(), g0)
+                            : to_nhwc(sig.ptr<float>(), (int)g.W, (int)g.H, (int)g.C, (int)g.N, Cpad);
     __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kpad);
     WgradParams p;
     std::memset(&p, 0, sizeof(p));
@@ -1258,7 +1378,7 @@ bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array 
     count_launch();
     AFGB_POST_LAUNCH("wgrad_tc_kernel");
     // fixed-order compensated reduction over splits, flipped into (fw,fh,C,K)
-    reduce_filter_partials(g, partial, (int)splits, dw.ptr<float>());
+    reduce_filter_partials(g0, partial, (int)splits, dw.ptr<float>());
     free_device(partial);
     free_device(gg);
     free_device(x);

@@ -23,6 +23,10 @@ TC_CASES = C.NN_CASES + [
     ("tc_5x5_d2_p4_s2", (30, 28, 32, 2), (5, 5, 32, 64), (2, 2), (4, 4), (2, 2)),
     ("tc_c200_k130", (17, 19, 200, 3), (3, 3, 200, 130), (1, 1), (1, 1), (1, 1)),
     ("tc_1x1_c256", (28, 28, 256, 2), (1, 1, 256, 192), (1, 1), (0, 0), (1, 1)),
+    # C*fw*fh <= 64: taps folded into channels (1x1 problem on the output grid)
+    ("tc_rgb_s2", (34, 30, 3, 2), (3, 3, 3, 32), (2, 2), (1, 1), (1, 1)),
+    ("tc_fold_d2_s3", (29, 31, 6, 2), (3, 3, 6, 40), (3, 2), (2, 1), (2, 2)),
+    ("tc_fold_5x5_c2", (23, 19, 2, 3), (5, 5, 2, 130), (1, 1), (2, 2), (1, 1)),
 ]
 
 
