@@ -121,7 +121,8 @@ def cnn_step(x0: torch.Tensor, weights: Sequence[torch.Tensor], geoms, precision
         if not recompute or l == L - 1:
             kept[l + 1] = h
     out = h
-    loss = (out.double() ** 2).sum()
+    flat = out.reshape(-1)
+    loss = torch.dot(flat, flat)       # sum of squares
     gp = _grad_precision(precision)
     grads = [None] * L
     g = out * 2.0                      # dL/d out
@@ -135,7 +136,8 @@ def cnn_step(x0: torch.Tensor, weights: Sequence[torch.Tensor], geoms, precision
                 rflops += nn_flops(x_l.shape, weights[j].shape, *geoms[j])
                 x_l = _layer(x_l, weights[j], geoms[j], precision)
         s, p, d = geoms[l]
-        g.mul_(above > 0)              # through the ReLU: dL/dz
+        # through the ReLU: dL/dz = dL/dh where h > 0 (one fused kernel)
+        g = torch.ops.aten.threshold_backward(g, above, 0.0)
         G, X, W = _view(g), _view(x_l), _view(weights[l])
         grads[l] = convolve2_gradient_nn(G, X, W, G, s, p, d, AF_CONV_GRADIENT_FILTER,
                                          precision=gp).to_torch()

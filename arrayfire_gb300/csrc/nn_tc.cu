@@ -69,7 +69,8 @@ struct GatherParams {
     int n_och_tiles;  // ceil(DC / 128)
     int nphase, nphx;
     int total_tiles;
-    int BX, BY, ntx, nty;  // pixel rectangles (TMA path)
+    int BX, BY;            // pixel rectangles (TMA path)
+    int ph_ntx[MAX_PH], ph_nty[MAX_PH];  // rectangles per stride phase (TMA path)
     int phase_tile_begin[MAX_PH + 1];
     int phase_tap_begin[MAX_PH + 1];
     short tap_u[MAX_T], tap_v[MAX_T];
@@ -99,21 +100,33 @@ template <bool TMA_B>
 __device__ __forceinline__ TileInfo decode_tile(const GatherParams &p, int tile) {
     TileInfo t;
     if (TMA_B) {
-        t.rx = t.ry = 0;
-        t.tap_begin = 0;
-        t.ntaps = p.phase_tap_begin[1];
-        t.och0 = (tile % p.n_och_tiles) * BM;
-        int r = tile / p.n_och_tiles;
-        const int tx = r % p.ntx;
-        r /= p.ntx;
-        const int ty = r % p.nty;
-        t.n = r / p.nty;
+        // rectangles of one stride phase (a single phase for the forward):
+        // the phase's outputs are (rx + sx*i, ry + sy*j), i < MX, j < MY
+        int ph = 0;
+        while (ph + 1 < p.nphase && tile >= p.phase_tile_begin[ph + 1]) ++ph;
+        t.rx = ph % p.nphx;
+        t.ry = ph / p.nphx;
+        t.tap_begin = p.phase_tap_begin[ph];
+        t.ntaps = p.phase_tap_begin[ph + 1] - p.phase_tap_begin[ph];
+        const int local = tile - p.phase_tile_begin[ph];
+        t.och0 = (local % p.n_och_tiles) * BM;
+        int r = local / p.n_och_tiles;
+        const int ntx = p.ph_ntx[ph], nty = p.ph_nty[ph];
+        const int tx = r % ntx;
+        r /= ntx;
+        const int ty = r % nty;
+        t.n = r / nty;
         t.x0 = tx * p.BX;
         t.y0 = ty * p.BY;
         t.p0 = 0;
         t.npix = 0;
-        t.MX = p.DW;
-        t.MY = p.DH;
+        if (p.mode == 0) {
+            t.MX = p.DW;
+            t.MY = p.DH;
+        } else {
+            t.MX = (p.DW - t.rx + p.sx - 1) / p.sx;
+            t.MY = (p.DH - t.ry + p.sy - 1) / p.sy;
+        }
         return t;
     }
     int ph = 0;
@@ -265,15 +278,24 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
             TileInfo ti = decode_tile<TMA_B>(p, tile);
             const int och = ti.och0 + 32 * q + lane;
-            if (!TMA_B && ti.ntaps == 0) {
+            if (ti.ntaps == 0) {
                 // a stride phase no tap reaches: its gradient is zero
                 if (och < p.DC) {
                     for (int e = 0; e < BN; ++e) {
-                        const long long pix = ti.p0 + e;
-                        if (pix >= ti.npix) break;
-                        const int X = (int)(pix % ti.MX);
-                        const long long rest = pix / ti.MX;
-                        const int Y = (int)(rest % ti.MY), n = (int)(rest / ti.MY);
+                        int X, Y, n;
+                        if (TMA_B) {
+                            X = ti.x0 + e % p.BX;
+                            Y = ti.y0 + e / p.BX;
+                            n = ti.n;
+                            if (X >= ti.MX || Y >= ti.MY) continue;
+                        } else {
+                            const long long pix = ti.p0 + e;
+                            if (pix >= ti.npix) break;
+                            X = (int)(pix % ti.MX);
+                            const long long rest = pix / ti.MX;
+                            Y = (int)(rest % ti.MY);
+                            n = (int)(rest / ti.MY);
+                        }
                         const long long xo = ti.rx + (long long)p.sx * X;
                         const long long yo = ti.ry + (long long)p.sy * Y;
                         p.dst[xo + p.DW * yo + plane * (och + (long long)p.DC * n)] = 0.0f;
@@ -304,24 +326,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                             make_float4(sc * __uint_as_float(r[4 * e]), sc * __uint_as_float(r[4 * e + 1]),
                                         sc * __uint_as_float(r[4 * e + 2]), sc * __uint_as_float(r[4 * e + 3]));
                     __syncwarp();
-                    const int e0 = cc * 32;  // BX >= 32 keeps the 32 pixels in one row
+                    // BX >= 32 keeps the 32 pixels in one row; (x, y) are
+                    // coordinates in the phase grid, output (rx + osx*x, ry + osy*y)
+                    const int e0 = cc * 32;
                     const int x = ti.x0 + (e0 % p.BX) + ocol, y = ti.y0 + e0 / p.BX;
-                    if (y < p.DH && x < p.DW) {
+                    const int osx = p.mode == 0 ? 1 : p.sx, osy = p.mode == 0 ? 1 : p.sy;
+                    if (y < ti.MY && x < ti.MX) {
+                        const long long xo = ti.rx + (long long)osx * x;
+                        const long long yo = ti.ry + (long long)osy * y;
 #pragma unroll
                         for (int i = 0; i < 8; ++i) {
                             const int cl = orow + 4 * i;
                             const int oc = ti.och0 + 32 * q + cl;
                             if (oc >= p.DC) continue;
                             const float4 v = *reinterpret_cast<const float4 *>(stg + cl * EP_PITCH + ocol);
-                            float *d = p.dst + plane * ((long long)oc + (long long)p.DC * ti.n) + x +
-                                       (long long)p.DW * y;
-                            if (vec_rows && x + 3 < p.DW) {
+                            float *d = p.dst + plane * ((long long)oc + (long long)p.DC * ti.n) + xo +
+                                       (long long)p.DW * yo;
+                            if (osx == 1 && vec_rows && x + 3 < ti.MX) {
                                 *reinterpret_cast<float4 *>(d) = v;
                             } else {
                                 d[0] = v.x;
-                                if (x + 1 < p.DW) d[1] = v.y;
-                                if (x + 2 < p.DW) d[2] = v.z;
-                                if (x + 3 < p.DW) d[3] = v.w;
+                                if (x + 1 < ti.MX) d[osx] = v.y;
+                                if (x + 2 < ti.MX) d[2 * osx] = v.z;
+                                if (x + 3 < ti.MX) d[3 * osx] = v.w;
                             }
                         }
                     }
@@ -771,36 +798,47 @@ __global__ void weights_bf16_kernel(const float *__restrict__ w, int fw, int fh,
 __global__ void __launch_bounds__(256) fold_taps_bf16_kernel(
     const float *__restrict__ x, int W, int H, int C, int N, int fw, int fh, int sx, int sy,
     int px, int py, int dx, int dy, int Wo, int Ho, __nv_bfloat16 *__restrict__ out) {
-    const long long npix = (long long)Wo * Ho * N;
+    // per folded channel j: source channel and tap offset (c < 0: padding)
+    __shared__ int tc[64], tdx[64], tdy[64];
     const int KC = C * fw * fh;
+    if (threadIdx.x < 64) {
+        const int j = threadIdx.x;
+        const int tap = j / C, u = tap % fw, v = tap / fw;
+        tc[j] = j < KC ? j % C : -1;
+        tdx[j] = u * dx - px;
+        tdy[j] = v * dy - py;
+    }
+    __syncthreads();
+    const long long npix = (long long)Wo * Ho * N;
+    const long long plane = (long long)W * H;
+    const int nj8 = (KC + 7) / 8;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < npix;
          q += (long long)gridDim.x * blockDim.x) {
         const int xo = (int)(q % Wo);
         const long long r = q / Wo;
         const int yo = (int)(r % Ho);
         const int n = (int)(r / Ho);
+        const float *img = x + plane * C * n;
+        const int xb = xo * sx, yb = yo * sy;
         uint4 *dst = reinterpret_cast<uint4 *>(out + q * 64);
-#pragma unroll 1
         for (int j8 = 0; j8 < 8; ++j8) {
-            uint32_t wd[4];
+            uint32_t wd[4] = {0u, 0u, 0u, 0u};
+            if (j8 < nj8) {
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                float v2[2];
+                for (int e = 0; e < 4; ++e) {
+                    float v2[2];
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    const int j = j8 * 8 + e * 2 + h;
-                    float val = 0.f;
-                    if (j < KC) {
-                        const int c = j % C, tap = j / C;
-                        const int u = tap % fw, v = tap / fw;
-                        const int xs = xo * sx - px + u * dx, ys = yo * sy - py + v * dy;
-                        if (xs >= 0 && xs < W && ys >= 0 && ys < H)
-                            val = __ldg(x + xs + (long long)W * (ys + (long long)H * (c + (long long)C * n)));
+                    for (int h = 0; h < 2; ++h) {
+                        const int j = j8 * 8 + e * 2 + h;
+                        const int c = tc[j];
+                        const int xs = xb + tdx[j], ys = yb + tdy[j];
+                        v2[h] = (c >= 0 && xs >= 0 && xs < W && ys >= 0 && ys < H)
+                                    ? __ldg(img + plane * c + (long long)W * ys + xs)
+                                    : 0.f;
                     }
-                    v2[h] = val;
+                    const __nv_bfloat162 b2 = __floats2bfloat162_rn(v2[0], v2[1]);
+                    wd[e] = *reinterpret_cast<const uint32_t *>(&b2);
                 }
-                const __nv_bfloat162 b = __floats2bfloat162_rn(v2[0], v2[1]);
-                wd[e] = *reinterpret_cast<const uint32_t *>(&b);
             }
             dst[j8] = make_uint4(wd[0], wd[1], wd[2], wd[3]);
         }
@@ -1079,12 +1117,14 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     const int SCpad = round_up(SC, CH);
     const int OCpad = round_up(DC, 128);
     const int taps = (int)(g.fw * g.fh);
-    // pixel operand by TMA: stride 1 in both modes; strided forwards too,
-    // through the tensor map's traversal strides (at most 8)
+    // pixel operand by TMA: strided forwards through the tensor map's
+    // traversal strides (at most 8); data gradients per stride phase, whose
+    // operand rectangles are unit-stride in the incoming gradient
     int rbx = 0, rby = 0;
-    const bool tma_b = (g.sx == 1 && g.sy == 1) ||
-                       (mode == 0 && g.sx <= 8 && g.sy <= 8 &&
-                        pick_rect((int)g.Wo, (int)g.Ho, BN, 32, rbx, rby, (int)g.sx, (int)g.sy));
+    const int tsx = mode == 0 ? (int)g.sx : 1, tsy = mode == 0 ? (int)g.sy : 1;
+    const int MX0 = mode == 0 ? DW : (int)((DW + g.sx - 1) / g.sx);
+    const int MY0 = mode == 0 ? DH : (int)((DH + g.sy - 1) / g.sy);
+    const bool tma_b = tsx <= 8 && tsy <= 8 && pick_rect(MX0, MY0, BN, 32, rbx, rby, tsx, tsy);
     const int esize = fp8 ? 1 : 2;
 
     void *img = nullptr, *wt = nullptr;
@@ -1172,8 +1212,12 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     p.fw = (int)g.fw;
     p.nchunk = SCpad / CH;
     p.n_och_tiles = OCpad / 128;
-    p.nphx = (mode == 0 || tma_b) ? 1 : (int)g.sx;
-    p.nphase = (mode == 0 || tma_b) ? 1 : (int)(g.sx * g.sy);
+    p.nphx = mode == 0 ? 1 : (int)g.sx;
+    p.nphase = mode == 0 ? 1 : (int)(g.sx * g.sy);
+    if (tma_b) {
+        p.BX = rbx;
+        p.BY = rby;
+    }
     int ntap = 0, ntile = 0;
     for (int ph = 0; ph < p.nphase; ++ph) {
         const int rx = ph % p.nphx, ry = ph / p.nphx;
@@ -1190,21 +1234,20 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
         }
         long long MX = mode == 0 ? DW : (DW - rx + g.sx - 1) / g.sx;
         long long MY = mode == 0 ? DH : (DH - ry + g.sy - 1) / g.sy;
-        long long npix = std::max(0LL, MX) * std::max(0LL, MY) * g.N;
-        ntile += (int)((npix + BN - 1) / BN) * p.n_och_tiles;
+        if (tma_b) {
+            p.ph_ntx[ph] = (int)((std::max(0LL, MX) + p.BX - 1) / p.BX);
+            p.ph_nty[ph] = (int)((std::max(0LL, MY) + p.BY - 1) / p.BY);
+            ntile += p.n_och_tiles * p.ph_ntx[ph] * p.ph_nty[ph] * (int)g.N;
+        } else {
+            long long npix = std::max(0LL, MX) * std::max(0LL, MY) * g.N;
+            ntile += (int)((npix + BN - 1) / BN) * p.n_och_tiles;
+        }
     }
     p.phase_tap_begin[p.nphase] = ntap;
     p.phase_tile_begin[p.nphase] = ntile;
     CUtensorMap xmap;
     std::memset(&xmap, 0, sizeof(xmap));
-    if (tma_b) {
-        const int tsx = mode == 0 ? (int)g.sx : 1, tsy = mode == 0 ? (int)g.sy : 1;
-        pick_rect(DW, DH, BN, 32, p.BX, p.BY, tsx, tsy);
-        p.ntx = (DW + p.BX - 1) / p.BX;
-        p.nty = (DH + p.BY - 1) / p.BY;
-        ntile = p.n_och_tiles * p.ntx * p.nty * (int)g.N;
-        xmap = make_imap(img, SCpad, SW, SH, (int)g.N, p.BX, p.BY, esize, tsx, tsy);
-    }
+    if (tma_b) xmap = make_imap(img, SCpad, SW, SH, (int)g.N, p.BX, p.BY, esize, tsx, tsy);
     p.total_tiles = ntile;
 
     CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad, esize);

@@ -27,6 +27,9 @@ TC_CASES = C.NN_CASES + [
     ("tc_rgb_s2", (34, 30, 3, 2), (3, 3, 3, 32), (2, 2), (1, 1), (1, 1)),
     ("tc_fold_d2_s3", (29, 31, 6, 2), (3, 3, 6, 40), (3, 2), (2, 1), (2, 2)),
     ("tc_fold_5x5_c2", (23, 19, 2, 3), (5, 5, 2, 130), (1, 1), (2, 2), (1, 1)),
+    # stride 4 with a 3x3 filter: data-gradient phases that no tap reaches are zero
+    ("tc_s4_zero_phases", (21, 18, 16, 2), (3, 3, 16, 24), (4, 4), (1, 1), (1, 1)),
+    ("tc_s2x3_c96", (35, 40, 96, 1), (3, 5, 96, 64), (2, 3), (1, 2), (1, 1)),
 ]
 
 
