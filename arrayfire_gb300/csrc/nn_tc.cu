@@ -74,6 +74,7 @@ struct GatherParams {
     int phase_tile_begin[MAX_PH + 1];
     int phase_tap_begin[MAX_PH + 1];
     short tap_u[MAX_T], tap_v[MAX_T];
+    short tap_ox[MAX_T], tap_oy[MAX_T];  // operand offset of each tap (TMA path)
 };
 
 struct Smem {
@@ -392,6 +393,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         // ---------------- MMA issuer
         if (lane == 0) {
             const uint32_t idesc = FP8 ? idesc_e4m3(BM, BN) : idesc_bf16(BM, BN, 0, 0);
+            // descriptors: precomputed bases plus 16-byte-unit offsets (the
+            // issuing thread is latency-bound on its scalar work)
+            const uint64_t a0 = smem_desc(smem_u32(a_stage), 16, 1024);
+            const uint64_t b0 = smem_desc(smem_u32(b_stage), 16, 1024);
             uint32_t it = 0, acc_it = 0;
             bool issued = false;
             for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
@@ -410,12 +415,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         break;
                     }
                     tc_fence_after();
-                    const uint32_t sa = smem_u32(a_stage + s * A_BYTES);
-                    const uint32_t sbb = smem_u32(b_stage + s * B_BYTES);
+                    const uint64_t as = a0 + (uint32_t)(s * (A_BYTES >> 4));
+                    const uint64_t bs = b0 + (uint32_t)(s * (B_BYTES >> 4));
 #pragma unroll
                     for (int k = 0; k < 4; ++k) {  // 4 x 32 bytes of K per stage
-                        const uint64_t ad = smem_desc(sa + k * 32, 16, 1024);
-                        const uint64_t bd = smem_desc(sbb + k * 32, 16, 1024);
+                        const uint64_t ad = as + (uint32_t)(2 * k);
+                        const uint64_t bd = bs + (uint32_t)(2 * k);
                         if (FP8)
                             mma_f8(d_tmem, ad, bd, idesc, (kb | k) != 0);
                         else
@@ -443,27 +448,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
                 TileInfo ti = decode_tile<TMA_B>(p, tile);
                 if (ti.ntaps == 0) continue;
-                const int iters = p.nchunk * ti.ntaps;
-                for (int kb = 0; kb < iters; ++kb, ++it) {
-                    const int s = it % STAGES;
-                    if (!mbar_wait(&sm->empty[s], ((it / STAGES) & 1) ^ 1, abort, 16u)) break;
-                    const int cchunk = kb / ti.ntaps;
-                    const int tq = ti.tap_begin + (kb - cchunk * ti.ntaps);
-                    const int u = p.tap_u[tq], v = p.tap_v[tq];
-                    mbar_arrive_expect_tx(&sm->full[s], TMA_B ? A_BYTES + B_BYTES : A_BYTES);
-                    tma_load_2d(smem_u32(a_stage + s * A_BYTES), &wmap, &sm->full[s],
-                                (u + p.fw * v) * p.SCpad + cchunk * (FP8 ? 128 : 64), ti.och0);
-                    if (TMA_B) {
-                        int offx, offy;
-                        tap_offsets(p, ti, u, v, offx, offy);
-                        // forward: input origin x0*s (traversal stride s in the map);
-                        // data gradient (stride 1 only here): x0
-                        const int bx0 = p.mode == 0 ? ti.x0 * p.sx : ti.x0;
-                        const int by0 = p.mode == 0 ? ti.y0 * p.sy : ti.y0;
-                        tma_load_4d(smem_u32(b_stage + s * B_BYTES), &xmap, &sm->full[s],
-                                    cchunk * (FP8 ? 128 : 64), bx0 + offx, by0 + offy, ti.n);
+                // forward: input origin x0*s (traversal stride s in the map);
+                // data gradient: the phase-grid origin x0; tap offsets from the host
+                const int bx0 = p.mode == 0 ? ti.x0 * p.sx : ti.x0;
+                const int by0 = p.mode == 0 ? ti.y0 * p.sy : ti.y0;
+                bool stop = false;
+                for (int cchunk = 0; cchunk < p.nchunk && !stop; ++cchunk) {
+                    for (int tq = ti.tap_begin; tq < ti.tap_begin + ti.ntaps; ++tq, ++it) {
+                        const int s = it % STAGES;
+                        if (!mbar_wait(&sm->empty[s], ((it / STAGES) & 1) ^ 1, abort, 16u)) {
+                            stop = true;
+                            break;
+                        }
+                        const int u = p.tap_u[tq], v = p.tap_v[tq];
+                        mbar_arrive_expect_tx(&sm->full[s], TMA_B ? A_BYTES + B_BYTES : A_BYTES);
+                        tma_load_2d(smem_u32(a_stage + s * A_BYTES), &wmap, &sm->full[s],
+                                    (u + p.fw * v) * p.SCpad + cchunk * (FP8 ? 128 : 64), ti.och0);
+                        if (TMA_B)
+                            tma_load_4d(smem_u32(b_stage + s * B_BYTES), &xmap, &sm->full[s],
+                                        cchunk * (FP8 ? 128 : 64), bx0 + p.tap_ox[tq], by0 + p.tap_oy[tq],
+                                        ti.n);
                     }
                 }
+                if (stop) break;
             }
         }
         __syncwarp();
@@ -662,9 +669,7 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
         const int q = warp - 4;
         bool have = false;
         if (nstages > 0) {
-            unsigned n = 0;
-            while (!(have = mbar_try_wait(&sm->tmem_full[0], 0)) && ++n < kSpinLimit) {
-            }
+            have = mbar_wait_sleep(&sm->tmem_full[0], 0);
             if (!have) {
                 *abort = 1;
                 atomicOr(&g_tc_error, 128u);
@@ -689,6 +694,202 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
                 const int col = cc * 16 + e;
                 const int gi = g0 + col / 64;
                 const int tap = gi / nchunk, c = (gi - tap * nchunk) * 64 + (col & 63);
+                if (c < p.C) out[((long long)c + (long long)p.C * tap) * p.K + k] = __uint_as_float(r[e]);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 4) {
+        tc_fence_after();
+        tmem_dealloc(tmem_base, 256);
+    }
+}
+
+// ===========================================================================
+// filter gradient, stride 1 along x: one signal strip per filter row
+// ===========================================================================
+// A stage is a rectangle of 64 output pixels (BY rows of BX).  For each of
+// its rows the producer loads one strip of BX + (nu-1)*dx signal pixels
+// (64 channels each), and the nu taps u0..u0+nu-1 of filter row v read it at
+// row offsets u*dx: nine shifted 8 KB tiles become three ~8.5 KB strips for
+// a 3x3 filter.  One MMA per K step covers the row's taps: B (MN-major) has
+// one 64-channel N atom per tap, the atoms dx rows apart (LBO = dx * 128
+// bytes, overlapping), each starting inside the strip at any 128-byte row;
+// the 128-byte
+// swizzle is keyed on the shared-memory address bits, as the TMA wrote the
+// strip, so the base-offset field stays 0 (the parity tests cover every tap
+// offset, dilation and strip width).
+constexpr int WS_MAXST = 8;
+constexpr int WS_SMEM = 200 * 1024;  // stage area budget
+
+struct StripParams {
+    const __nv_bfloat16 *x;  // [N][H][W][Cpad]
+    const __nv_bfloat16 *g;  // [N][Ho][Wo][Kpad]
+    float *partial;          // [splits][C*taps][K]
+    int W, H, Cpad, C, N;
+    int Wo, Ho, Kpad, K;
+    int sy, px, py, dx, dy, fw, fh;
+    int BX, BY, ntx, nty;
+    int UB, nub;             // taps per tile along u, u-blocks per filter row
+    int nchunk, n_k_tiles;
+    int SL, strip_bytes, stage_bytes, nst;
+    long long Q, chunk;      // pixel blocks, blocks per split
+};
+
+struct StripSmem {
+    uint64_t full[WS_MAXST];
+    uint64_t empty[WS_MAXST];
+    uint64_t tmem_full;
+    uint32_t tmem_base;
+    int abort;
+};
+
+__global__ void __launch_bounds__(WG_THREADS, 1)
+    wgrad_strip_kernel(const __grid_constant__ StripParams p, const __grid_constant__ CUtensorMap gmap,
+                       const __grid_constant__ CUtensorMap smap) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    StripSmem *sm = reinterpret_cast<StripSmem *>(base + p.nst * p.stage_bytes);
+    volatile int *abort = &sm->abort;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    // tile: (k tile, u block, channel chunk, filter row)
+    int t = blockIdx.x;
+    const int ktile = t % p.n_k_tiles;
+    t /= p.n_k_tiles;
+    const int ub = t % p.nub;
+    t /= p.nub;
+    const int cchunk = t % p.nchunk;
+    const int v = t / p.nchunk;
+    const int k0 = ktile * 128;
+    const int u0 = ub * p.UB;
+    const int nu = min(p.UB, p.fw - u0);
+    const long long q_begin = (long long)blockIdx.y * p.chunk;
+    const long long q_end = min(p.Q, q_begin + p.chunk);
+    const int nstages = (int)max(0LL, q_end - q_begin);
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < p.nst; ++s) {
+            mbar_init(&sm->full[s], 1);
+            mbar_init(&sm->empty[s], 1);
+        }
+        mbar_init(&sm->tmem_full, 1);
+        sm->abort = 0;
+        fence_barrier_init();
+    }
+    if (warp == 4) tmem_alloc(&sm->tmem_base, 256);
+    if (warp == 0 && lane == 0) {
+        prefetch_tmap(&gmap);
+        prefetch_tmap(&smap);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = sm->tmem_base;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            const uint32_t bytes = WG_A_BYTES + (uint32_t)(p.BY * p.SL * 128);
+            // consecutive pixel blocks: (tx, ty, n) advance without division
+            int tx = (int)(q_begin % p.ntx);
+            const long long r0 = q_begin / p.ntx;
+            int ty = (int)(r0 % p.nty), n = (int)(r0 / p.nty);
+            int s = 0;
+            uint32_t phase = 1;
+            for (int st = 0; st < nstages && !*abort; ++st) {
+                if (!mbar_wait(&sm->empty[s], phase, abort, 32u)) break;
+                const int x0 = tx * p.BX, y0 = ty * p.BY;
+                unsigned char *stage = base + s * p.stage_bytes;
+                mbar_arrive_expect_tx(&sm->full[s], bytes);
+                const uint32_t sa = smem_u32(stage);
+                tma_load_4d(sa, &gmap, &sm->full[s], k0, x0, y0, n);
+                tma_load_4d(sa + 8192, &gmap, &sm->full[s], k0 + 64, x0, y0, n);
+                for (int j = 0; j < p.BY; ++j)
+                    tma_load_4d(sa + WG_A_BYTES + j * p.strip_bytes, &smap, &sm->full[s], cchunk * 64,
+                                x0 - p.px + u0 * p.dx, (y0 + j) * p.sy - p.py + v * p.dy, n);
+                if (++s == p.nst) {
+                    s = 0;
+                    phase ^= 1u;
+                }
+                if (++tx == p.ntx) {
+                    tx = 0;
+                    if (++ty == p.nty) {
+                        ty = 0;
+                        ++n;
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp >= 4) {
+        if (warp == 4 && lane == 0) {
+            // The issuing thread is latency-bound on its own scalar work, so
+            // every descriptor is a precomputed base plus a 16-byte-unit
+            // offset (the 14-bit start field holds any shared address), and
+            // the stage index and barrier phase advance without division.
+            // one MMA per K step covers all nu taps: B's N atoms (64 channels
+            // each) are the tap-shifted views of the strip, dx rows apart
+            const uint32_t idesc = idesc_bf16(128, (uint32_t)(64 * nu), 1, 1);
+            const uint64_t a0 = smem_desc(smem_u32(base), 8192, 1024);
+            const uint64_t b0 = smem_desc(smem_u32(base) + WG_A_BYTES, (uint32_t)p.dx * 128u, 1024);
+            uint32_t bk[WG_KP / 16];  // per K step: strip 16k/BX, row 16k%BX
+#pragma unroll
+            for (int k = 0; k < WG_KP / 16; ++k)
+                bk[k] = (uint32_t)(((16 * k) / p.BX) * p.strip_bytes + ((16 * k) % p.BX) * 128) >> 4;
+            const uint32_t stage_step = (uint32_t)p.stage_bytes >> 4;
+            uint32_t soff = 0, phase = 0;
+            int s = 0;
+            for (int st = 0; st < nstages; ++st) {
+                if (!mbar_wait(&sm->full[s], phase, abort, 64u)) break;
+                tc_fence_after();
+#pragma unroll
+                for (int k = 0; k < WG_KP / 16; ++k) {
+                    mma_f16(tmem_base, a0 + soff + (uint32_t)k * 128u, b0 + soff + bk[k], idesc,
+                            (st | k) != 0);
+                }
+                mma_commit(&sm->empty[s]);
+                if (++s == p.nst) {
+                    s = 0;
+                    soff = 0;
+                    phase ^= 1u;
+                } else {
+                    soff += stage_step;
+                }
+            }
+            mma_commit(&sm->tmem_full);
+        }
+        __syncwarp();
+        // epilogue: warps 4-7 (TMEM lanes 32*(warp-4) ...); waits for the
+        // MMAs even when aborting, so TMEM is never freed under them
+        const int q = warp - 4;
+        bool have = false;
+        if (nstages > 0) {
+            have = mbar_wait_sleep(&sm->tmem_full, 0);
+            if (!have) {
+                *abort = 1;
+                atomicOr(&g_tc_error, 128u);
+            }
+        }
+        tc_fence_after();
+        const int k = k0 + 32 * q + lane;
+        const long long rows = (long long)p.C * p.fw * p.fh;
+        float *out = p.partial + (long long)blockIdx.y * rows * p.K;
+        for (int cc = 0; cc < nu * 4; ++cc) {
+            uint32_t r[16];
+            if (have) {
+                tmem_ld16(tmem_base + cc * 16 + ((uint32_t)(32 * q) << 16), r);
+                tmem_ld_wait();
+            } else {
+#pragma unroll
+                for (int e = 0; e < 16; ++e) r[e] = 0u;
+            }
+            if (k >= p.K || *abort) continue;
+            const int tap = (u0 + cc / 4) + p.fw * v;
+#pragma unroll
+            for (int e = 0; e < 16; ++e) {
+                const int c = cchunk * 64 + (cc & 3) * 16 + e;
                 if (c < p.C) out[((long long)c + (long long)p.C * tap) * p.K + k] = __uint_as_float(r[e]);
             }
         }
@@ -1229,6 +1430,11 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
                 if (mode == 1 && (((rx + g.px - u * g.dx) % g.sx) + g.sx) % g.sx != 0) continue;
                 p.tap_u[ntap] = (short)u;
                 p.tap_v[ntap] = (short)v;
+                // the tap's operand offset: forward u*dx - px (input
+                // pixels); data gradient (rx + px - u*dx)/sx (exact for
+                // the phase's taps; gradient pixels)
+                p.tap_ox[ntap] = (short)(mode == 0 ? u * g.dx - g.px : (rx + g.px - u * g.dx) / g.sx);
+                p.tap_oy[ntap] = (short)(mode == 0 ? v * g.dy - g.py : (ry + g.py - v * g.dy) / g.sy);
                 ++ntap;
             }
         }
@@ -1279,6 +1485,8 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
 // 32-bit pixel coordinates
 static bool gather_fits(const NNGeom &g, int mode) {
     if (g.fw * g.fh > MAX_T) return false;
+    // per-tap operand offsets are 16-bit
+    if ((g.fw - 1) * g.dx + g.px >= 32768 || (g.fh - 1) * g.dy + g.py >= 32768) return false;
     if (mode == 1 && g.sx * g.sy > MAX_PH) return false;
     if (g.W > (1 << 24) || g.H > (1 << 24) || g.N > (1 << 24)) return false;
     return true;
@@ -1319,6 +1527,71 @@ bool tc_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &
     return true;
 }
 
+// the strip kernel (stride 1 along x); false when its shape limits do not hold
+static bool run_wgrad_strip(const NNGeom &g, const __nv_bfloat16 *x, const __nv_bfloat16 *gg,
+                            int Cpad, int Kpad, const NNGeom &g0, float *dw) {
+    if (g.sx != 1 || g.sy > 8 || g.fw * g.fh > 64) return false;
+    StripParams p;
+    std::memset(&p, 0, sizeof(p));
+    if (!pick_rect((int)g.Wo, (int)g.Ho, WG_KP, 16, p.BX, p.BY)) return false;
+    p.nub = (int)((g.fw + 3) / 4);
+    p.UB = (int)((g.fw + p.nub - 1) / p.nub);
+    p.SL = p.BX + (p.UB - 1) * (int)g.dx;
+    if (p.SL > 256) return false;
+    p.strip_bytes = (p.SL * 128 + 1023) / 1024 * 1024;
+    p.stage_bytes = WG_A_BYTES + p.BY * p.strip_bytes;
+    p.nst = std::min(WS_MAXST, WS_SMEM / p.stage_bytes);
+    if (p.nst < 2) return false;
+    p.x = x;
+    p.g = gg;
+    p.W = (int)g.W;
+    p.H = (int)g.H;
+    p.Cpad = Cpad;
+    p.C = (int)g.C;
+    p.N = (int)g.N;
+    p.Wo = (int)g.Wo;
+    p.Ho = (int)g.Ho;
+    p.Kpad = Kpad;
+    p.K = (int)g.K;
+    p.sy = (int)g.sy;
+    p.px = (int)g.px;
+    p.py = (int)g.py;
+    p.dx = (int)g.dx;
+    p.dy = (int)g.dy;
+    p.fw = (int)g.fw;
+    p.fh = (int)g.fh;
+    p.nchunk = Cpad / 64;
+    p.n_k_tiles = Kpad / 128;
+    p.ntx = ((int)g.Wo + p.BX - 1) / p.BX;
+    p.nty = ((int)g.Ho + p.BY - 1) / p.BY;
+    p.Q = (long long)p.ntx * p.nty * g.N;
+    CUtensorMap gmap = make_imap(gg, Kpad, (int)g.Wo, (int)g.Ho, (int)g.N, p.BX, p.BY);
+    // strips: SL pixels of one row (box {64 channels, SL, 1, 1}), every sy-th row
+    CUtensorMap smap = make_imap(x, Cpad, (int)g.W, (int)g.H, (int)g.N, p.SL, 1);
+    const long long ntiles = (long long)p.n_k_tiles * p.nub * p.nchunk * g.fh;
+    const long long target = (long long)num_sms() * 2;
+    long long splits = std::max(1LL, target / std::max(1LL, ntiles));
+    long long chunk = std::max<long long>(16, (p.Q + splits - 1) / splits);
+    splits = (p.Q + chunk - 1) / chunk;
+    p.chunk = chunk;
+    const long long rows = g.C * g.fw * g.fh;
+    float *partial = static_cast<float *>(alloc_device((size_t)(splits * rows * g.K) * sizeof(float)));
+    p.partial = partial;
+    const size_t smem = 1024 + (size_t)p.nst * p.stage_bytes + sizeof(StripSmem) + 64;
+    {
+        KernelTimer kt("tc_wgrad_kernel");
+        AFGB_CUDA(cudaFuncSetAttribute(wgrad_strip_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+        wgrad_strip_kernel<<<dim3((unsigned)ntiles, (unsigned)splits), WG_THREADS, smem, stream()>>>(
+            p, gmap, smap);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("wgrad_strip_kernel");
+    reduce_filter_partials(g0, partial, (int)splits, dw);
+    free_device(partial);
+    return true;
+}
+
 bool tc_filter_grad(const NNGeom &g0, const Array &grad, const Array &sig, Array &dw) {
     if (grad.type != f32) return false;
     // folded taps: the signal operand is the folded image and the problem is
@@ -1330,6 +1603,11 @@ bool tc_filter_grad(const NNGeom &g0, const Array &grad, const Array &sig, Array
     __nv_bfloat16 *x = fold ? fold_taps(sig.ptr<float>(), g0)
                             : to_nhwc(sig.ptr<float>(), (int)g.W, (int)g.H, (int)g.C, (int)g.N, Cpad);
     __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kpad);
+    if (!fold && run_wgrad_strip(g, x, gg, Cpad, Kpad, g0, dw.ptr<float>())) {
+        free_device(gg);
+        free_device(x);
+        return true;
+    }
     WgradParams p;
     std::memset(&p, 0, sizeof(p));
     p.x = x;

@@ -70,6 +70,20 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volati
     return true;
 }
 
+// Bounded wait that spans a whole main loop (the epilogue warps of a kernel
+// that accumulates over all its stages): polls about every half microsecond,
+// leaving the barrier unit and issue slots to the producer and the MMA
+// thread; gives up after about four seconds.
+constexpr unsigned int kSleepLimit = 1u << 23;
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t *bar, uint32_t parity) {
+    unsigned int n = 0;
+    while (!mbar_try_wait(bar, parity)) {
+        if (++n > kSleepLimit) return false;
+        __nanosleep(500);
+    }
+    return true;
+}
+
 // ---------------------------------------------------------------- cp.async
 // 16-byte copy global -> shared; src_bytes == 0 fills the destination with
 // zeros without reading global memory

@@ -30,6 +30,11 @@ TC_CASES = C.NN_CASES + [
     # stride 4 with a 3x3 filter: data-gradient phases that no tap reaches are zero
     ("tc_s4_zero_phases", (21, 18, 16, 2), (3, 3, 16, 24), (4, 4), (1, 1), (1, 1)),
     ("tc_s2x3_c96", (35, 40, 96, 1), (3, 5, 96, 64), (2, 3), (1, 2), (1, 1)),
+    # filter gradients on strips shared by the taps of a filter row
+    ("tc_strip_5x5_d2", (30, 28, 32, 2), (5, 5, 32, 64), (1, 1), (4, 4), (2, 2)),
+    ("tc_strip_7x7", (40, 36, 64, 1), (7, 7, 64, 128), (1, 1), (3, 3), (1, 1)),
+    ("tc_strip_w16", (16, 40, 64, 2), (3, 3, 64, 128), (1, 1), (1, 1), (1, 1)),
+    ("tc_strip_sy2", (33, 40, 64, 1), (3, 3, 64, 64), (1, 2), (1, 1), (1, 1)),
 ]
 
 
