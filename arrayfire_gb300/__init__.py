@@ -301,6 +301,23 @@ def convolve2_gradient_nn(incoming_gradient: Array, original_signal: Array,
                      sn, sp, pn, pp, dn, dp, grad_type, PRECISION[precision])
 
 
+def convolve2_gradients_nn(incoming_gradient: Array, original_signal: Array,
+                           original_filter: Array, stride=(1, 1), padding=(0, 0),
+                           dilation=(1, 1), precision: str = "fp32", data: bool = True,
+                           filter: bool = True, bias: bool = False):
+    """afgb_convolve2_gradients_nn: (data, filter, bias) gradients in one call,
+    None for the ones not requested."""
+    sn, sp = _dimargs(stride)
+    pn, pp = _dimargs(padding)
+    dn, dp = _dimargs(dilation)
+    outs = [af_array() if want else None for want in (data, filter, bias)]
+    _check(lib().afgb_convolve2_gradients_nn(
+        *[ctypes.byref(o) if o is not None else None for o in outs], incoming_gradient.handle,
+        original_signal.handle, original_filter.handle, sn, sp, pn, pp, dn, dp,
+        PRECISION[precision]))
+    return tuple(Array(o.value) if o is not None else None for o in outs)
+
+
 # host-only helpers (no GPU)
 def identify_batch_kind(rank: int, sdims, fdims) -> int:
     return lib().afgb_identify_batch_kind(rank, dims_arg(list(sdims)), dims_arg(list(fdims)))

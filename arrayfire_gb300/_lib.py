@@ -53,6 +53,10 @@ SIGNATURES = [
     ("afgb_convolve2_gradient_nn_ex", af_err, [ctypes.POINTER(af_array), af_array, af_array, af_array,
                                                af_array, ctypes.c_uint, _DP, ctypes.c_uint, _DP,
                                                ctypes.c_uint, _DP, ctypes.c_int, ctypes.c_int]),
+    ("afgb_convolve2_gradients_nn", af_err, [ctypes.POINTER(af_array), ctypes.POINTER(af_array),
+                                             ctypes.POINTER(af_array), af_array, af_array, af_array,
+                                             ctypes.c_uint, _DP, ctypes.c_uint, _DP, ctypes.c_uint,
+                                             _DP, ctypes.c_int]),
     ("afgb_device_array_view", af_err, [ctypes.POINTER(af_array), _P, ctypes.c_uint, _DP, _DP, ctypes.c_int]),
     ("afgb_set_stream", af_err, [_P]),
     ("afgb_get_stream", af_err, [ctypes.POINTER(_P)]),

@@ -6,7 +6,8 @@ forward and af_convolve2_gradient_nn (src/api/c/convolve.cpp:394-477) as the
 backward, exactly as a user of the reference would differentiate a layer:
 the data gradient (AF_CONV_GRADIENT_DATA), the filter gradient
 (AF_CONV_GRADIENT_FILTER) and, through the library's extension, the real bias
-gradient.  Tensors are passed zero-copy: a torch tensor (N, C, H, W) is the
+gradient -- all that are needed in one afgb_convolve2_gradients_nn call, whose
+results equal the per-gradient calls bit for bit.  Tensors are passed zero-copy: a torch tensor (N, C, H, W) is the
 ArrayFire array (W, H, C, N), and the library runs on torch's current stream.
 
 Semantics are ArrayFire's, not torch's: the filter is flipped (a true
@@ -27,8 +28,7 @@ from typing import Optional, Sequence
 
 import torch
 
-from . import (AF_CONV_GRADIENT_BIAS, AF_CONV_GRADIENT_DATA, AF_CONV_GRADIENT_FILTER, Array,
-               convolve2_gradient_nn, convolve2_nn, set_stream)
+from . import Array, convolve2_gradients_nn, convolve2_nn, set_stream
 
 __all__ = ["Conv2NN", "conv2_nn", "cnn_step", "nn_flops"]
 
@@ -66,17 +66,17 @@ class Conv2NN(torch.autograd.Function):
         # the gradient call takes the forward output only for its dims; the
         # incoming gradient has the same dims
         G, X, W = _view(gy), _view(x), _view(w)
+        want = (ctx.needs_input_grad[0], ctx.needs_input_grad[1],
+                has_b and ctx.needs_input_grad[2])
         gx = gw = gb = None
-        if ctx.needs_input_grad[0]:
-            gx = convolve2_gradient_nn(G, X, W, G, stride, padding, dilation,
-                                       AF_CONV_GRADIENT_DATA, precision=gp).to_torch()
-        if ctx.needs_input_grad[1]:
-            gw = convolve2_gradient_nn(G, X, W, G, stride, padding, dilation,
-                                       AF_CONV_GRADIENT_FILTER, precision=gp).to_torch()
-        if has_b and ctx.needs_input_grad[2]:
-            gb = convolve2_gradient_nn(G, X, W, G, stride, padding, dilation,
-                                       AF_CONV_GRADIENT_BIAS, precision=gp,
-                                       real_bias=True).to_torch().reshape(-1)
+        if any(want):
+            # one call for every gradient needed (each equals its
+            # af_convolve2_gradient_nn result; BIAS is the real bias gradient)
+            dX, dW, dB = convolve2_gradients_nn(G, X, W, stride, padding, dilation, precision=gp,
+                                                data=want[0], filter=want[1], bias=want[2])
+            gx = dX.to_torch() if dX is not None else None
+            gw = dW.to_torch() if dW is not None else None
+            gb = dB.to_torch().reshape(-1) if dB is not None else None
         return gx, gw, gb, None, None, None, None
 
 
@@ -139,11 +139,10 @@ def cnn_step(x0: torch.Tensor, weights: Sequence[torch.Tensor], geoms, precision
         # through the ReLU: dL/dz = dL/dh where h > 0 (one fused kernel)
         g = torch.ops.aten.threshold_backward(g, above, 0.0)
         G, X, W = _view(g), _view(x_l), _view(weights[l])
-        grads[l] = convolve2_gradient_nn(G, X, W, G, s, p, d, AF_CONV_GRADIENT_FILTER,
-                                         precision=gp).to_torch()
+        dX, dW, _ = convolve2_gradients_nn(G, X, W, s, p, d, precision=gp, data=l > 0)
+        grads[l] = dW.to_torch()
         if l > 0:
-            g = convolve2_gradient_nn(G, X, W, G, s, p, d, AF_CONV_GRADIENT_DATA,
-                                      precision=gp).to_torch()
+            g = dX.to_torch()
         above = x_l
         del G, X, W
     return loss, grads, rflops

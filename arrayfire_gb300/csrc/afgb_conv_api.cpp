@@ -317,6 +317,46 @@ static af_err convolve2_grad_impl(af_array *out, const af_array incoming_gradien
     return AF_SUCCESS;
 }
 
+static af_err convolve2_grads_impl(af_array *data_grad, af_array *filter_grad, af_array *bias_grad,
+                                   const af_array incoming_gradient, const af_array original_signal,
+                                   const af_array original_filter, unsigned stride_dims,
+                                   const dim_t *strides, unsigned padding_dims,
+                                   const dim_t *paddings, unsigned dilation_dims,
+                                   const dim_t *dilations, afgb_precision prec) {
+    Array *gi = get_array(incoming_gradient);
+    Array *s = get_array(original_signal);
+    Array *f = get_array(original_filter);
+    AFGB_DIM_ASSERT(2, s->dims[2] == f->dims[2]);
+    NNArgs a = nn_args(stride_dims, strides, padding_dims, paddings, dilation_dims, dilations);
+    af_dtype t = s->type;
+    if (t != f32 && t != f64 && t != f16) AFGB_TYPE_ERROR(1, t);
+    require_type(gi, t);
+    require_type(f, t);
+    if (prec != AFGB_PRECISION_FP32 && t != f32) {
+        AFGB_THROW(AF_ERR_TYPE, "tensor-core precisions take f32 arrays");
+    }
+    NNGeom g;
+    nn_geometry(g, s, f, a);
+    AFGB_DIM_ASSERT(1, gi->dims[0] == g.Wo && gi->dims[1] == g.Ho && gi->dims[2] == g.K &&
+                           gi->dims[3] == g.N);
+    Array gd = gi->is_linear() ? *gi : make_dense(*gi);
+    Array sd = s->is_linear() ? *s : make_dense(*s);
+    Array fd = f->is_linear() ? *f : make_dense(*f);
+    Array dx, dw, db;
+    if (data_grad) dx = *create_array(t, s->dims);
+    if (filter_grad) dw = *create_array(t, f->dims);
+    if (bias_grad) {
+        dim_t bd[4] = {1, 1, g.K, 1};
+        db = *create_array(t, bd);
+    }
+    nn_gradients(g, gd, sd, fd, data_grad ? &dx : nullptr, filter_grad ? &dw : nullptr,
+                 bias_grad ? &db : nullptr, prec);
+    if (data_grad) *data_grad = make_handle(&dx);
+    if (filter_grad) *filter_grad = make_handle(&dw);
+    if (bias_grad) *bias_grad = make_handle(&db);
+    return AF_SUCCESS;
+}
+
 }  // namespace afgb
 
 using namespace afgb;
@@ -417,6 +457,22 @@ af_err afgb_convolve2_gradient_nn_ex(af_array *out, const af_array incoming_grad
     return convolve2_grad_impl(out, incoming_gradient, original_signal, original_filter,
                                convolved_output, stride_dims, strides, padding_dims, paddings,
                                dilation_dims, dilations, grad_type, precision, true);
+    AFGB_CATCHALL
+}
+
+af_err afgb_convolve2_gradients_nn(af_array *data_grad, af_array *filter_grad,
+                                   af_array *bias_grad, const af_array incoming_gradient,
+                                   const af_array original_signal, const af_array original_filter,
+                                   const unsigned stride_dims, const dim_t *strides,
+                                   const unsigned padding_dims, const dim_t *paddings,
+                                   const unsigned dilation_dims, const dim_t *dilations,
+                                   afgb_precision precision) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, data_grad != nullptr || filter_grad != nullptr || bias_grad != nullptr);
+    if ((int)precision < 0 || (int)precision > 2) AFGB_THROW(AF_ERR_ARG, "unknown precision");
+    return convolve2_grads_impl(data_grad, filter_grad, bias_grad, incoming_gradient,
+                                original_signal, original_filter, stride_dims, strides,
+                                padding_dims, paddings, dilation_dims, dilations, precision);
     AFGB_CATCHALL
 }
 

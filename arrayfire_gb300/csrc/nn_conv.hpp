@@ -27,6 +27,10 @@ void nn_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array 
 // db[k] = sum_{x,y,n} g[x,y,k,n]  (no reference counterpart: the reference
 // returns the data gradient for AF_CONV_GRADIENT_BIAS, src/api/c/convolve.cpp:401-411)
 void nn_bias_grad(const NNGeom &g, const Array &grad, Array &db);
+// any subset of the three gradients in one call (null outputs are skipped);
+// the reduced precisions share one converted copy of the incoming gradient
+void nn_gradients(const NNGeom &g, const Array &grad, const Array &sig, const Array &filt,
+                  Array *dx, Array *dw, Array *db, afgb_precision prec);
 
 // ---- plain CUDA-core implementations (nn_simt.cu)
 void simt_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out);
@@ -40,6 +44,8 @@ bool tc_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out
                 afgb_precision prec, const Array *scales);
 bool tc_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &dx);
 bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw);
+bool tc_data_filter_grads(const NNGeom &g, const Array &grad, const Array &sig, const Array &filt,
+                          Array &dx, Array &dw);
 
 // fixed-order compensated sum of `splits` fp32 partials R[c + C*tap][k],
 // written flipped into the (fw,fh,C,K) f32 filter gradient

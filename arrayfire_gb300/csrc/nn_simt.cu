@@ -833,6 +833,17 @@ void nn_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array 
         AFGB_THROW(AF_ERR_NOT_SUPPORTED, "tensor-core filter gradient does not cover this shape");
 }
 
+void nn_gradients(const NNGeom &g, const Array &grad, const Array &sig, const Array &filt,
+                  Array *dx, Array *dw, Array *db, afgb_precision prec) {
+    if (dx && dw && prec == AFGB_PRECISION_BF16 && dx->elements() > 0 && dw->elements() > 0 &&
+        tc_data_filter_grads(g, grad, sig, filt, *dx, *dw)) {
+        dx = dw = nullptr;
+    }
+    if (dx) nn_data_grad(g, grad, filt, *dx, prec);
+    if (dw) nn_filter_grad(g, grad, sig, *dw, prec);
+    if (db) nn_bias_grad(g, grad, *db);
+}
+
 }  // namespace afgb
 
 extern "C" af_err afgb_convolve2_filter_grad_noalloc(

@@ -1305,9 +1305,11 @@ static size_t gather_smem() {
 // scales (`user_wscale`, K floats, or amax/448 computed on the device)
 // `unfolded`: g is the folded geometry of *unfolded (bf16 forward only); the
 // image and filter are folded from the f32 operands of *unfolded
+// `img_ready`: the source image already in bf16 NHWC with its channels padded
+// to a multiple of 64 (then img_f32 is not read)
 static void run_gather(const NNGeom &g, int mode, const float *img_f32, const float *w_f32,
                        float *dst, bool fp8 = false, const float *user_wscale = nullptr,
-                       const NNGeom *unfolded = nullptr) {
+                       const NNGeom *unfolded = nullptr, const __nv_bfloat16 *img_ready = nullptr) {
     const int SW = mode == 0 ? (int)g.W : (int)g.Wo;
     const int SH = mode == 0 ? (int)g.H : (int)g.Ho;
     const int SC = mode == 0 ? (int)g.C : (int)g.K;
@@ -1342,7 +1344,8 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
         count_launch();
         AFGB_POST_LAUNCH("weights_fold_bf16_kernel");
     } else if (!fp8) {
-        img = to_nhwc(img_f32, SW, SH, SC, (int)g.N, SCpad);
+        img = img_ready ? const_cast<__nv_bfloat16 *>(img_ready)
+                        : to_nhwc(img_f32, SW, SH, SC, (int)g.N, SCpad);
         wt = alloc_device((size_t)OCpad * taps * SCpad * 2);
         long long total = (long long)OCpad * taps * SCpad;
         unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
@@ -1476,7 +1479,7 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
         AFGB_POST_LAUNCH("gather_conv_kernel");
     }
     free_device(wt);
-    free_device(img);
+    if (img != img_ready) free_device(img);
     if (scales) free_device(scales);
     if (amax) free_device(amax);
 }
@@ -1592,21 +1595,20 @@ static bool run_wgrad_strip(const NNGeom &g, const __nv_bfloat16 *x, const __nv_
     return true;
 }
 
-bool tc_filter_grad(const NNGeom &g0, const Array &grad, const Array &sig, Array &dw) {
-    if (grad.type != f32) return false;
+// filter gradient from the incoming gradient already in bf16 NHWC, its
+// channels padded to Kpad (a multiple of 128)
+static void filter_grad_from(const NNGeom &g0, const __nv_bfloat16 *gg, int Kpad, const Array &sig,
+                             Array &dw) {
     // folded taps: the signal operand is the folded image and the problem is
     // 1x1 on the output grid; its partial rows c + C*tap are the unfolded ones
     const bool fold = foldable(g0);
     const NNGeom g = fold ? folded_geometry(g0) : g0;
     const int Cpad = round_up((int)g.C, 64);
-    const int Kpad = round_up((int)g.K, 128);
     __nv_bfloat16 *x = fold ? fold_taps(sig.ptr<float>(), g0)
                             : to_nhwc(sig.ptr<float>(), (int)g.W, (int)g.H, (int)g.C, (int)g.N, Cpad);
-    __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kpad);
     if (!fold && run_wgrad_strip(g, x, gg, Cpad, Kpad, g0, dw.ptr<float>())) {
-        free_device(gg);
         free_device(x);
-        return true;
+        return;
     }
     WgradParams p;
     std::memset(&p, 0, sizeof(p));
@@ -1701,8 +1703,30 @@ bool tc_filter_grad(const NNGeom &g0, const Array &grad, const Array &sig, Array
     // fixed-order compensated reduction over splits, flipped into (fw,fh,C,K)
     reduce_filter_partials(g0, partial, (int)splits, dw.ptr<float>());
     free_device(partial);
-    free_device(gg);
     free_device(x);
+}
+
+bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw) {
+    if (grad.type != f32) return false;
+    const int Kpad = round_up((int)g.K, 128);
+    __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kpad);
+    filter_grad_from(g, gg, Kpad, sig, dw);
+    free_device(gg);
+    return true;
+}
+
+// data and filter gradients sharing one bf16 copy of the incoming gradient;
+// false (nothing done) when the two would want different channel paddings
+// (K mod 128 in 1..64) or the data-gradient kernel does not cover the shape
+bool tc_data_filter_grads(const NNGeom &g, const Array &grad, const Array &sig, const Array &filt,
+                          Array &dx, Array &dw) {
+    if (grad.type != f32 || !gather_fits(g, 1)) return false;
+    const int Kpad = round_up((int)g.K, 128);
+    if (Kpad != round_up((int)g.K, 64)) return false;
+    __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kpad);
+    run_gather(g, 1, nullptr, filt.ptr<float>(), dx.ptr<float>(), false, nullptr, nullptr, gg);
+    filter_grad_from(g, gg, Kpad, sig, dw);
+    free_device(gg);
     return true;
 }
 

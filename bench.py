@@ -181,11 +181,10 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
         flush_buf.zero_()
 
     def step():
+        # forward, then both input gradients in one call (one shared bf16
+        # copy of the incoming gradient)
         y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
-        dx = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_DATA,
-                                      precision=prec)
-        dw = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_FILTER,
-                                      precision=prec)
+        dx, dw, _ = af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
         return y, dx, dw
 
     # parity of this exact workload against FP64 on sampled points
@@ -259,8 +258,7 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
     if prec != "fp32":
         def step32():
             y = af.convolve2_nn(Xa, Wa, st, pd, dl)
-            dx = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_DATA)
-            dw = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_FILTER)
+            dx, dw, _ = af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl)
             return y, dx, dw
         k32 = max(3, min(args.steps, 5))
         t32, _ = _timed_steps(step32, k32, 3, flush)
@@ -308,10 +306,7 @@ def run_e2e(af, X, Wt, Gd, prec, args) -> dict:
         Wa = mk(pin["w"], Wt.shape)
         Ga = mk(pin["g"], Gd.shape)
         y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
-        dx = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_DATA,
-                                      precision=prec)
-        dw = af.convolve2_gradient_nn(Ga, Xa, Wa, y, st, pd, dl, af.AF_CONV_GRADIENT_FILTER,
-                                      precision=prec)
+        dx, dw, _ = af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
         af._check(L.af_get_data_ptr(ctypes.c_void_p(y_host.data_ptr()), y.handle))
         af._check(L.af_get_data_ptr(ctypes.c_void_p(dx_host.data_ptr()), dx.handle))
         af._check(L.af_get_data_ptr(ctypes.c_void_p(dw_host.data_ptr()), dw.handle))
@@ -657,7 +652,8 @@ def main() -> None:
         run_only(args)
         return
     config = {"workload": "conv2_nn fwd+dgrad+wgrad, signal 128x128x64x32 (W,H,C,N), filter "
-                          "3x3x64x128, stride 1, pad 1, dilation 1",
+                          "3x3x64x128, stride 1, pad 1, dilation 1 (afgb_convolve2_nn_ex + "
+                          "afgb_convolve2_gradients_nn per step)",
               "global_batch": NN_SHAPE["N"] * world, "flops_per_step": 3 * nn_flops() * world,
               "l2": "flushed between timed steps (512 MB write)", "parallelism": "replicas"}
 

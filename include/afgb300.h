@@ -182,6 +182,22 @@ AFGB_API af_err afgb_convolve2_gradient_nn_ex(
     const unsigned dilation_dims, const dim_t *dilations, af_conv_gradient_type grad_type,
     afgb_precision precision);
 
+/* The data, filter and bias gradients of one convolution in one call
+ * (no counterpart in the reference, which computes one per
+ * af_convolve2_gradient_nn call); any of the three outputs may be 0 to skip
+ * it, and each result equals the afgb_convolve2_gradient_nn_ex call for its
+ * type (BIAS as the real bias gradient).  The incoming gradient's dims must
+ * be the forward output's (Wo, Ho, K, N).  In BF16 the data and filter
+ * gradients share one bf16 copy of the incoming gradient. */
+AFGB_API af_err afgb_convolve2_gradients_nn(af_array *data_grad, af_array *filter_grad,
+                                           af_array *bias_grad, const af_array incoming_gradient,
+                                           const af_array original_signal,
+                                           const af_array original_filter,
+                                           const unsigned stride_dims, const dim_t *strides,
+                                           const unsigned padding_dims, const dim_t *paddings,
+                                           const unsigned dilation_dims, const dim_t *dilations,
+                                           afgb_precision precision);
+
 /* Non-owning view of device memory with explicit strides (elements).  The
  * caller keeps ownership; releasing the view never frees `data`.  This is
  * how a framework tensor enters the library without a copy. */

@@ -195,3 +195,42 @@ def test_bf16_strided_tma_paths(af, oracle, case):
         G, S, F, Y, st, pd, dl, af.AF_CONV_GRADIENT_FILTER, precision="bf16"))
     assert n == 1
     check(DW.to_numpy(), oracle.nn_filter_grad_f64(g, s, C.af_shape(fd), st, pd, dl), name + " wgrad")
+
+
+COMBINED = [c for c in TC_CASES if c[0] in ("tc_c64_k128", "tc_c128_k256_s2", "tc_5x5_d2_p4_s2",
+                                            "tc_c200_k130", "tc_rgb_s2", "nn_multi", "tc_strip_7x7")]
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp32"])
+@pytest.mark.parametrize("case", COMBINED, ids=lambda c: c[0])
+def test_combined_gradients_match_separate(af, case, precision):
+    """afgb_convolve2_gradients_nn returns the same bits as one
+    afgb_convolve2_gradient_nn_ex call per gradient (BF16 shares the
+    converted incoming gradient when its channel padding allows)."""
+    name, sd, fd, st, pd, dl = case
+    s, f = C.nn_inputs(case, 6300)
+    g = C.nn_grad(case, 6300)
+    S, F, G = af.Array.from_numpy(s), af.Array.from_numpy(f), af.Array.from_numpy(g)
+    dx, dw, db = af.convolve2_gradients_nn(G, S, F, st, pd, dl, precision=precision, bias=True)
+    sep = [af.convolve2_gradient_nn(G, S, F, G, st, pd, dl, t, precision=precision, real_bias=True)
+           for t in (af.AF_CONV_GRADIENT_DATA, af.AF_CONV_GRADIENT_FILTER, af.AF_CONV_GRADIENT_BIAS)]
+    for a, b in zip((dx, dw, db), sep):
+        assert a.dims == b.dims
+        assert a.to_numpy().tobytes() == b.to_numpy().tobytes()
+    only_w = af.convolve2_gradients_nn(G, S, F, st, pd, dl, precision=precision, data=False)
+    assert only_w[0] is None and only_w[2] is None
+    assert only_w[1].to_numpy().tobytes() == sep[1].to_numpy().tobytes()
+
+
+def test_combined_gradients_validation(af):
+    case = TC_CASES[0]
+    name, sd, fd, st, pd, dl = case
+    s, f = C.nn_inputs(case, 1)
+    S, F = af.Array.from_numpy(s), af.Array.from_numpy(f)
+    bad = af.Array.from_numpy(np.zeros((3, 3, fd[3], sd[3]), np.float32, order="F"))
+    with pytest.raises(af.AfError) as e:
+        af.convolve2_gradients_nn(bad, S, F, st, pd, dl, precision="bf16")
+    assert e.value.code == af.AF_ERR_SIZE
+    with pytest.raises(af.AfError) as e:
+        af.convolve2_gradients_nn(bad, S, F, st, pd, dl, data=False, filter=False, bias=False)
+    assert e.value.code == af.AF_ERR_ARG
