@@ -808,6 +808,7 @@ void launch_convolve_nd(const Array &sig, const Array &filt, Array &out, int kin
         }
         if (done) return;
     }
+    if (rank == 3 && sig.type == f32 && p.nbatch > 0 && dtma::tma_convolve3(p, exact)) return;
     if (rank == 3 && sig.type == f32 && p.fd[0] == 3 && p.fd[1] == 3 && p.fd[2] == 3) {
         const long long nz = (p.od[2] + T3_BZ - 1) / T3_BZ;
         if (p.nbatch * nz <= 65535 && (p.od[1] + T3_BY - 1) / T3_BY <= 65535) {

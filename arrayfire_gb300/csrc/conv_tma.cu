@@ -569,6 +569,116 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
 }
 
 // ===========================================================================
+// 3-D direct convolution, 3x3x3 f32 filter, 64x8x8 output tile per CTA
+// ===========================================================================
+// One 4-D TMA box (x, y, z, volume) brings the haloed input block; the box's
+// x origin is the tile origin minus 4 (16-byte aligned), so the window shift
+// OFF = 4 - (2 - c0) is absorbed by compile-time indices, and coordinates
+// outside the volume read as zero.  Each thread computes 4 x by 4 z outputs
+// of one row: input planes high to low, dim-1 taps ascending, dim-0 taps
+// inside (the reference order, src/backend/cpu/kernel/convolve.hpp:45-73).
+constexpr int C3_BX = 64, C3_BY = 8, C3_BZ = 8;
+constexpr int C3_PF = 76;              // box width: an odd number of 16-byte words
+constexpr int C3_TH = C3_BY + 2, C3_TD = C3_BZ + 2;
+constexpr int C3_BYTES = C3_PF * C3_TH * C3_TD * 4;
+
+struct Conv3Tma {
+    long long ntx, nty, nz;  // tiles along x, y, z
+    long long vstep;         // volume index step per batch
+};
+
+template <bool EXACT, bool EXPAND>
+__global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ CUtensorMap smap,
+                                                        const DirectParams p, const Conv3Tma t3) {
+    constexpr int C0 = EXPAND ? 0 : 1;
+    constexpr int OFF = 4 - (2 - C0);  // window index of tap offset 0
+    constexpr int NW4 = (OFF + 3 + 2 + 4) / 4;
+    static_assert(60 + 4 * NW4 <= C3_PF, "window exceeds the box width");
+    extern __shared__ __align__(128) unsigned char sm3[];
+    float *tile = reinterpret_cast<float *>(sm3);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm3 + C3_BYTES);
+    const long long bz = blockIdx.z;
+    const long long b = bz / t3.nz, zt = bz - b * t3.nz;
+    const long long i0 = (long long)blockIdx.x * C3_BX, j0 = (long long)blockIdx.y * C3_BY,
+                    k0 = zt * C3_BZ;
+    if (threadIdx.x == 0) {
+        tc::mbar_init(bar, 1);
+        tc::fence_barrier_init();
+        tc::mbar_arrive_expect_tx(bar, C3_BYTES);
+        tc::tma_load_4d(smem_u32(tile), &smap, bar, (int)(i0 - 4), (int)(j0 + C0 - 2),
+                        (int)(k0 + C0 - 2), (int)(b * t3.vstep));
+    }
+    // filter taps for this batch (SAME batches: one filter per volume)
+    const float *w = static_cast<const float *>(p.filt) + b * p.filt_step[3];
+    float wr[27];
+#pragma unroll
+    for (int fk = 0; fk < 3; ++fk)
+#pragma unroll
+        for (int fj = 0; fj < 3; ++fj)
+#pragma unroll
+            for (int fi = 0; fi < 3; ++fi)
+                wr[(fk * 3 + fj) * 3 + fi] = __ldg(w + fi * p.fs[0] + fj * p.fs[1] + fk * p.fs[2]);
+    __syncthreads();  // barrier initialised before anyone waits on it
+    if (!wait_tile(bar, 0)) return;
+
+    const int tx = threadIdx.x & 15;
+    const int ty = (threadIdx.x >> 4) & 7;
+    const int tz = threadIdx.x >> 7;  // 0..1, four z each
+    float acc[4][4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
+#pragma unroll
+    for (int q = 5; q >= 0; --q) {      // input plane (relative), high to low
+#pragma unroll
+        for (int fj = 0; fj < 3; ++fj) {  // dim-1 tap, ascending
+            float v[NW4 * 4];
+            const float *row = tile + ((4 * tz + q) * C3_TH + (ty + 2 - fj)) * C3_PF + 4 * tx;
+#pragma unroll
+            for (int u = 0; u < NW4; ++u) {
+                const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
+                v[4 * u] = t4.x;
+                v[4 * u + 1] = t4.y;
+                v[4 * u + 2] = t4.z;
+                v[4 * u + 3] = t4.w;
+            }
+#pragma unroll
+            for (int rz = 0; rz < 4; ++rz) {
+                const int fk = rz + 2 - q;
+                if (fk >= 0 && fk < 3) {
+#pragma unroll
+                    for (int fi = 0; fi < 3; ++fi) {
+                        const float wv = wr[(fk * 3 + fj) * 3 + fi];
+#pragma unroll
+                        for (int cc = 0; cc < 4; ++cc)
+                            acc[rz][cc] = mac<EXACT>(acc[rz][cc], v[OFF + cc + 2 - fi], wv);
+                    }
+                }
+            }
+        }
+    }
+    float *out = static_cast<float *>(p.out) + b * p.out_step[3];
+    const long long x = i0 + 4 * tx, y = j0 + ty;
+    if (y >= p.od[1]) return;
+    const bool vec_ok = (x + 3 < p.od[0]) && ((p.os[1] & 3) == 0) && ((p.os[2] & 3) == 0) &&
+                        ((reinterpret_cast<uintptr_t>(out) & 15) == 0);
+#pragma unroll
+    for (int rz = 0; rz < 4; ++rz) {
+        const long long z = k0 + 4 * tz + rz;
+        if (z >= p.od[2]) break;
+        float *dst = out + x + y * p.os[1] + z * p.os[2];
+        if (vec_ok) {
+            *reinterpret_cast<float4 *>(dst) = make_float4(acc[rz][0], acc[rz][1], acc[rz][2], acc[rz][3]);
+        } else {
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc)
+                if (x + cc < p.od[0]) dst[cc] = acc[rz][cc];
+        }
+    }
+}
+
+// ===========================================================================
 // host side
 // ===========================================================================
 typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
@@ -768,6 +878,62 @@ bool tma_convolve2_sep(const Array &sig, const float *cf, const float *rf, int c
         AFGB_SEPL(int8_t, false)
     }
 #undef AFGB_SEPL
+}
+
+// 3x3x3 f32 volumes: dense, 16-byte rows; false when not applicable
+bool tma_convolve3(const DirectParams &p, bool exact) {
+    if (p.rank != 3 || p.fd[0] != 3 || p.fd[1] != 3 || p.fd[2] != 3) return false;
+    if (p.ss[0] != 1 || p.ss[1] != p.sd[0] || p.ss[2] != p.sd[0] * p.sd[1] ||
+        p.ss[3] != p.sd[0] * p.sd[1] * p.sd[2])
+        return false;
+    if (p.os[0] != 1 || !dense_aligned(p.sig, 4, p.sd[0])) return false;
+    if (p.sd[0] >= (1LL << 30) || p.sd[1] >= (1LL << 30) || p.sd[2] >= (1LL << 30) ||
+        p.sd[3] >= (1LL << 30))
+        return false;
+    const long long vol = p.sd[0] * p.sd[1] * p.sd[2];
+    if (p.in_step[3] % vol != 0) return false;
+    Conv3Tma t3;
+    t3.ntx = (p.od[0] + C3_BX - 1) / C3_BX;
+    t3.nty = (p.od[1] + C3_BY - 1) / C3_BY;
+    t3.nz = (p.od[2] + C3_BZ - 1) / C3_BZ;
+    t3.vstep = p.in_step[3] / vol;
+    if (t3.ntx > 2147483647LL || t3.nty > 65535 || t3.nz * p.nbatch > 65535 || p.nbatch < 1)
+        return false;
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    CUtensorMap m;
+    cuuint64_t dims[4] = {(cuuint64_t)p.sd[0], (cuuint64_t)p.sd[1], (cuuint64_t)p.sd[2],
+                          (cuuint64_t)p.sd[3]};
+    cuuint64_t strides[3] = {(cuuint64_t)(p.sd[0] * 4), (cuuint64_t)(p.sd[0] * p.sd[1] * 4),
+                             (cuuint64_t)(vol * 4)};
+    cuuint32_t box[4] = {(cuuint32_t)C3_PF, (cuuint32_t)C3_TH, (cuuint32_t)C3_TD, 1};
+    cuuint32_t es[4] = {1, 1, 1, 1};
+    if (fn(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, const_cast<void *>(p.sig), dims, strides, box, es,
+           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const size_t smem = C3_BYTES + 16;
+    dim3 grid((unsigned)t3.ntx, (unsigned)t3.nty, (unsigned)(t3.nz * p.nbatch));
+#define AFGB_C3(E, X)                                                                           \
+    do {                                                                                        \
+        AFGB_CUDA(cudaFuncSetAttribute(conv3_tma_kernel<E, X>,                                  \
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+        conv3_tma_kernel<E, X><<<grid, 256, smem, stream()>>>(m, p, t3);                       \
+    } while (0)
+    {
+        KernelTimer kt("conv3_tma_kernel");
+        if (exact) {
+            if (p.expand) AFGB_C3(true, true);
+            else AFGB_C3(true, false);
+        } else {
+            if (p.expand) AFGB_C3(false, true);
+            else AFGB_C3(false, false);
+        }
+    }
+#undef AFGB_C3
+    count_launch();
+    AFGB_POST_LAUNCH("conv3_tma_kernel");
+    return true;
 }
 
 }  // namespace dtma

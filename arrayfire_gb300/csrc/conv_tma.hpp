@@ -10,6 +10,8 @@ namespace afgb {
 namespace dtma {
 
 bool tma_convolve2(const DirectParams &p, af_dtype t, bool exact);
+// 3x3x3 f32 volumes (dense, 16-byte rows)
+bool tma_convolve3(const DirectParams &p, bool exact);
 bool tma_convolve2_sep(const Array &sig, const float *cf, const float *rf, int cl, int rl,
                        Array &out, bool expand, bool exact);
 

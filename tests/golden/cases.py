@@ -95,6 +95,11 @@ DIRECT_SHAPES = [
     ("c_many2one", 3, (9, 8, 7, 2), (3, 3, 3)),
     ("c_one2many", 3, (9, 8, 7), (3, 3, 3, 2)),
     ("c_many2many", 3, (9, 8, 7, 2), (3, 3, 3, 2)),
+    # 16-byte-multiple widths (TMA-staged 3-D path), every batch kind
+    ("c_tma_one", 3, (64, 20, 18), (3, 3, 3)),
+    ("c_tma_lhs", 3, (32, 12, 10, 2), (3, 3, 3)),
+    ("c_tma_same", 3, (36, 10, 9, 2), (3, 3, 3, 2)),
+    ("c_tma_rhs", 3, (40, 9, 11), (3, 3, 3, 2)),
 ]
 
 DIRECT_DTYPES_FULL = [F32, F64, C32, C64, U8, S8, B8, S16, U16, S32, U32, S64, U64]

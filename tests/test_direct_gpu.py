@@ -235,3 +235,23 @@ def test_tma_2d_path_taken(af, oracle, case):
     assert n == 1
     if dt != C.F32:
         assert out["o"].tobytes() == oracle.convolve(s, f, dt, rank, expand).tobytes()
+
+
+TMA_3D = [c for c in CASES if c[0].startswith("c_tma_") and c[1] == C.F32]
+
+
+@pytest.mark.parametrize("case", TMA_3D, ids=lambda c: c[0])
+def test_tma_3d_path_taken(af, oracle, case):
+    """Dense f32 volumes with 16-byte rows and a 3x3x3 filter run on the
+    TMA-staged 3-D kernel in every batch kind, bit-exact in the exact mode."""
+    cid, dt, rank, sd, fd, expand, seed = case
+    s = C.make_signal(dt, sd, seed)
+    f = C.make_filter(dt, fd, seed + 1, rank)
+    out = {}
+    af.set_exact_fp(True)
+    try:
+        n = _ran(af, "conv3_tma_kernel", lambda: out.setdefault("o", run(af, s, f, dt, rank, expand)))
+    finally:
+        af.set_exact_fp(False)
+    assert n == 1
+    assert out["o"].tobytes() == oracle.convolve(s, f, dt, rank, expand).tobytes()
