@@ -569,9 +569,10 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
 }
 
 // ===========================================================================
-// 3-D direct convolution, 3x3x3 f32 filter, 64x8x8 output tile per CTA
+// 3-D direct convolution, 3x3x3 f32 filter, persistent over 64x8x8 tiles
 // ===========================================================================
-// One 4-D TMA box (x, y, z, volume) brings the haloed input block; the box's
+// One 4-D TMA box (x, y, z, volume) brings a tile's haloed input block, the
+// next tile's box in flight while the CTA computes the current one; the box's
 // x origin is the tile origin minus 4 (16-byte aligned), so the window shift
 // OFF = 4 - (2 - c0) is absorbed by compile-time indices, and coordinates
 // outside the volume read as zero.  Each thread computes 4 x by 4 z outputs
@@ -581,9 +582,11 @@ constexpr int C3_BX = 64, C3_BY = 8, C3_BZ = 8;
 constexpr int C3_PF = 76;              // box width: an odd number of 16-byte words
 constexpr int C3_TH = C3_BY + 2, C3_TD = C3_BZ + 2;
 constexpr int C3_BYTES = C3_PF * C3_TH * C3_TD * 4;
+constexpr int C3_BUF = (C3_BYTES + 1023) / 1024 * 1024;  // TMA destinations stay 1024-aligned
 
 struct Conv3Tma {
-    long long ntx, nty, nz;  // tiles along x, y, z
+    FastDiv ntx, nty, nz;    // tiles along x, y, z
+    int ntiles;
     long long vstep;         // volume index step per batch
 };
 
@@ -594,87 +597,114 @@ __global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ 
     constexpr int OFF = 4 - (2 - C0);  // window index of tap offset 0
     constexpr int NW4 = (OFF + 3 + 2 + 4) / 4;
     static_assert(60 + 4 * NW4 <= C3_PF, "window exceeds the box width");
-    extern __shared__ __align__(128) unsigned char sm3[];
-    float *tile = reinterpret_cast<float *>(sm3);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sm3 + C3_BYTES);
-    const long long bz = blockIdx.z;
-    const long long b = bz / t3.nz, zt = bz - b * t3.nz;
-    const long long i0 = (long long)blockIdx.x * C3_BX, j0 = (long long)blockIdx.y * C3_BY,
-                    k0 = zt * C3_BZ;
-    if (threadIdx.x == 0) {
-        tc::mbar_init(bar, 1);
-        tc::fence_barrier_init();
-        tc::mbar_arrive_expect_tx(bar, C3_BYTES);
-        tc::tma_load_4d(smem_u32(tile), &smap, bar, (int)(i0 - 4), (int)(j0 + C0 - 2),
-                        (int)(k0 + C0 - 2), (int)(b * t3.vstep));
-    }
-    // filter taps for this batch (SAME batches: one filter per volume)
-    const float *w = static_cast<const float *>(p.filt) + b * p.filt_step[3];
-    float wr[27];
-#pragma unroll
-    for (int fk = 0; fk < 3; ++fk)
-#pragma unroll
-        for (int fj = 0; fj < 3; ++fj)
-#pragma unroll
-            for (int fi = 0; fi < 3; ++fi)
-                wr[(fk * 3 + fj) * 3 + fi] = __ldg(w + fi * p.fs[0] + fj * p.fs[1] + fk * p.fs[2]);
-    __syncthreads();  // barrier initialised before anyone waits on it
-    if (!wait_tile(bar, 0)) return;
+    extern __shared__ __align__(1024) unsigned char sm3_raw[];
+    unsigned char *sm3 = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(sm3_raw) + 1023) & ~uintptr_t(1023));
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm3 + 2 * C3_BUF);
 
-    const int tx = threadIdx.x & 15;
-    const int ty = (threadIdx.x >> 4) & 7;
-    const int tz = threadIdx.x >> 7;  // 0..1, four z each
-    float acc[4][4];
+    // tile t -> (x tile, y tile, z tile, batch)
+    auto decode = [&](int t, long long &i0, long long &j0, long long &k0, long long &b) {
+        const uint32_t r = fdiv((uint32_t)t, t3.ntx);
+        const uint32_t r2 = fdiv(r, t3.nty);
+        const uint32_t bb = fdiv(r2, t3.nz);
+        i0 = (long long)((uint32_t)t - r * t3.ntx.d) * C3_BX;
+        j0 = (long long)(r - r2 * t3.nty.d) * C3_BY;
+        k0 = (long long)(r2 - bb * t3.nz.d) * C3_BZ;
+        b = bb;
+    };
+    auto issue = [&](int t, int buf) {
+        long long i0, j0, k0, b;
+        decode(t, i0, j0, k0, b);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc::mbar_arrive_expect_tx(&bar[buf], C3_BYTES);
+        tc::tma_load_4d(smem_u32(sm3 + buf * C3_BUF), &smap, &bar[buf], (int)(i0 - 4),
+                        (int)(j0 + C0 - 2), (int)(k0 + C0 - 2), (int)(b * t3.vstep));
+    };
+    if (threadIdx.x == 0) {
+        tc::mbar_init(&bar[0], 1);
+        tc::mbar_init(&bar[1], 1);
+        tc::fence_barrier_init();
+        if ((int)blockIdx.x < t3.ntiles) issue(blockIdx.x, 0);
+    }
+    __syncthreads();  // barriers initialised before anyone waits on them
+
+    int k = 0;
+    for (int t = blockIdx.x; t < t3.ntiles; t += gridDim.x, ++k) {
+        const int buf = k & 1;
+        if (threadIdx.x == 0 && t + (int)gridDim.x < t3.ntiles) issue(t + gridDim.x, buf ^ 1);
+        long long i0, j0, k0, b;
+        decode(t, i0, j0, k0, b);
+        // filter taps for this batch (SAME batches: one filter per volume)
+        const float *w = static_cast<const float *>(p.filt) + b * p.filt_step[3];
+        float wr[27];
 #pragma unroll
-    for (int a = 0; a < 4; ++a)
+        for (int fk = 0; fk < 3; ++fk)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
+            for (int fj = 0; fj < 3; ++fj)
 #pragma unroll
-    for (int q = 5; q >= 0; --q) {      // input plane (relative), high to low
+                for (int fi = 0; fi < 3; ++fi)
+                    wr[(fk * 3 + fj) * 3 + fi] = __ldg(w + fi * p.fs[0] + fj * p.fs[1] + fk * p.fs[2]);
+        if (!wait_tile(&bar[buf], (k >> 1) & 1)) break;
+        const float *tile = reinterpret_cast<const float *>(sm3 + buf * C3_BUF);
+        const int tx = threadIdx.x & 15;
+        const int ty = (threadIdx.x >> 4) & 7;
+        const int tz = threadIdx.x >> 7;  // 0..1, four z each
+        float acc[4][4];
 #pragma unroll
-        for (int fj = 0; fj < 3; ++fj) {  // dim-1 tap, ascending
-            float v[NW4 * 4];
-            const float *row = tile + ((4 * tz + q) * C3_TH + (ty + 2 - fj)) * C3_PF + 4 * tx;
+        for (int a = 0; a < 4; ++a)
 #pragma unroll
-            for (int u = 0; u < NW4; ++u) {
-                const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
-                v[4 * u] = t4.x;
-                v[4 * u + 1] = t4.y;
-                v[4 * u + 2] = t4.z;
-                v[4 * u + 3] = t4.w;
-            }
+            for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
 #pragma unroll
-            for (int rz = 0; rz < 4; ++rz) {
-                const int fk = rz + 2 - q;
-                if (fk >= 0 && fk < 3) {
+        for (int q = 5; q >= 0; --q) {      // input plane (relative), high to low
 #pragma unroll
-                    for (int fi = 0; fi < 3; ++fi) {
-                        const float wv = wr[(fk * 3 + fj) * 3 + fi];
+            for (int fj = 0; fj < 3; ++fj) {  // dim-1 tap, ascending
+                float v[NW4 * 4];
+                const float *row = tile + ((4 * tz + q) * C3_TH + (ty + 2 - fj)) * C3_PF + 4 * tx;
 #pragma unroll
-                        for (int cc = 0; cc < 4; ++cc)
-                            acc[rz][cc] = mac<EXACT>(acc[rz][cc], v[OFF + cc + 2 - fi], wv);
+                for (int u = 0; u < NW4; ++u) {
+                    const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
+                    v[4 * u] = t4.x;
+                    v[4 * u + 1] = t4.y;
+                    v[4 * u + 2] = t4.z;
+                    v[4 * u + 3] = t4.w;
+                }
+#pragma unroll
+                for (int rz = 0; rz < 4; ++rz) {
+                    const int fk = rz + 2 - q;
+                    if (fk >= 0 && fk < 3) {
+#pragma unroll
+                        for (int fi = 0; fi < 3; ++fi) {
+                            const float wv = wr[(fk * 3 + fj) * 3 + fi];
+#pragma unroll
+                            for (int cc = 0; cc < 4; ++cc)
+                                acc[rz][cc] = mac<EXACT>(acc[rz][cc], v[OFF + cc + 2 - fi], wv);
+                        }
                     }
                 }
             }
         }
-    }
-    float *out = static_cast<float *>(p.out) + b * p.out_step[3];
-    const long long x = i0 + 4 * tx, y = j0 + ty;
-    if (y >= p.od[1]) return;
-    const bool vec_ok = (x + 3 < p.od[0]) && ((p.os[1] & 3) == 0) && ((p.os[2] & 3) == 0) &&
-                        ((reinterpret_cast<uintptr_t>(out) & 15) == 0);
+        float *out = static_cast<float *>(p.out) + b * p.out_step[3];
+        const long long x = i0 + 4 * tx, y = j0 + ty;
+        if (y < p.od[1]) {
+            const bool vec_ok = (x + 3 < p.od[0]) && ((p.os[1] & 3) == 0) &&
+                                ((p.os[2] & 3) == 0) &&
+                                ((reinterpret_cast<uintptr_t>(out) & 15) == 0);
 #pragma unroll
-    for (int rz = 0; rz < 4; ++rz) {
-        const long long z = k0 + 4 * tz + rz;
-        if (z >= p.od[2]) break;
-        float *dst = out + x + y * p.os[1] + z * p.os[2];
-        if (vec_ok) {
-            *reinterpret_cast<float4 *>(dst) = make_float4(acc[rz][0], acc[rz][1], acc[rz][2], acc[rz][3]);
-        } else {
+            for (int rz = 0; rz < 4; ++rz) {
+                const long long z = k0 + 4 * tz + rz;
+                if (z >= p.od[2]) break;
+                float *dst = out + x + y * p.os[1] + z * p.os[2];
+                if (vec_ok) {
+                    *reinterpret_cast<float4 *>(dst) =
+                        make_float4(acc[rz][0], acc[rz][1], acc[rz][2], acc[rz][3]);
+                } else {
 #pragma unroll
-            for (int cc = 0; cc < 4; ++cc)
-                if (x + cc < p.od[0]) dst[cc] = acc[rz][cc];
+                    for (int cc = 0; cc < 4; ++cc)
+                        if (x + cc < p.od[0]) dst[cc] = acc[rz][cc];
+                }
+            }
         }
+        __syncthreads();  // every thread is done with this buffer before it is reloaded
     }
 }
 
@@ -892,13 +922,15 @@ bool tma_convolve3(const DirectParams &p, bool exact) {
         return false;
     const long long vol = p.sd[0] * p.sd[1] * p.sd[2];
     if (p.in_step[3] % vol != 0) return false;
+    const long long ntx = (p.od[0] + C3_BX - 1) / C3_BX, nty = (p.od[1] + C3_BY - 1) / C3_BY,
+                    nz = (p.od[2] + C3_BZ - 1) / C3_BZ;
+    if (p.nbatch < 1 || ntx * nty * nz * p.nbatch >= (1LL << 31)) return false;
     Conv3Tma t3;
-    t3.ntx = (p.od[0] + C3_BX - 1) / C3_BX;
-    t3.nty = (p.od[1] + C3_BY - 1) / C3_BY;
-    t3.nz = (p.od[2] + C3_BZ - 1) / C3_BZ;
+    t3.ntx = make_fastdiv((uint32_t)ntx);
+    t3.nty = make_fastdiv((uint32_t)nty);
+    t3.nz = make_fastdiv((uint32_t)nz);
+    t3.ntiles = (int)(ntx * nty * nz * p.nbatch);
     t3.vstep = p.in_step[3] / vol;
-    if (t3.ntx > 2147483647LL || t3.nty > 65535 || t3.nz * p.nbatch > 65535 || p.nbatch < 1)
-        return false;
     EncodeTiledFn fn = encode_fn();
     if (!fn) return false;
     CUtensorMap m;
@@ -912,12 +944,12 @@ bool tma_convolve3(const DirectParams &p, bool exact) {
            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return false;
-    const size_t smem = C3_BYTES + 16;
-    dim3 grid((unsigned)t3.ntx, (unsigned)t3.nty, (unsigned)(t3.nz * p.nbatch));
+    const size_t smem = 1024 + 2 * C3_BUF + 16;
 #define AFGB_C3(E, X)                                                                           \
     do {                                                                                        \
         AFGB_CUDA(cudaFuncSetAttribute(conv3_tma_kernel<E, X>,                                  \
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+        const int grid = persistent_grid(conv3_tma_kernel<E, X>, smem, t3.ntiles);             \
         conv3_tma_kernel<E, X><<<grid, 256, smem, stream()>>>(m, p, t3);                       \
     } while (0)
     {

@@ -255,3 +255,21 @@ def test_tma_3d_path_taken(af, oracle, case):
         af.set_exact_fp(False)
     assert n == 1
     assert out["o"].tobytes() == oracle.convolve(s, f, dt, rank, expand).tobytes()
+
+
+@pytest.mark.parametrize("kind", ["lhs", "same"])
+def test_tma_3d_multi_tile_per_cta(af, oracle, kind):
+    """More tiles than resident CTAs, so each CTA walks several tiles through
+    both of its buffers (256x64x64 x 2 volumes = 512 tiles)."""
+    g = np.random.Generator(np.random.Philox(71))
+    s = np.asfortranarray(g.random((256, 64, 64, 2), dtype=np.float32))
+    fshape = (3, 3, 3) if kind == "lhs" else (3, 3, 3, 2)
+    f = np.asfortranarray(g.standard_normal(fshape).astype(np.float32))
+    out = {}
+    af.set_exact_fp(True)
+    try:
+        n = _ran(af, "conv3_tma_kernel", lambda: out.setdefault("o", run(af, s, f, C.F32, 3, False)))
+    finally:
+        af.set_exact_fp(False)
+    assert n == 1
+    assert out["o"].tobytes() == oracle.convolve(s, f, C.F32, 3, False).tobytes()
