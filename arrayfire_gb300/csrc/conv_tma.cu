@@ -569,6 +569,175 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
 }
 
 // ===========================================================================
+// fused separable convolution on 8-bit images with integer dot products
+// ===========================================================================
+// The reference's 8-bit semantics (src/backend/cpu/kernel/convolve.hpp:233,
+// src/backend/cpu/convolve.cpp:88-97) keep the taps and the intermediate
+// image in the input type, so every product and sum is a small exact
+// integer: each pass is dp4a over four bytes of the window and four reversed
+// taps, and InT(sum) is a clamp to the type's range.  The column pass
+// writes its result transposed (tempT[x][row], bytes) so that the row pass
+// reads its windows as consecutive bytes too.  Unaligned windows come from
+// two aligned words with one byte_perm.
+template <typename T>
+__device__ __forceinline__ int dp4(uint32_t a, uint32_t b, int c) {
+    if constexpr (std::is_same<T, uint8_t>::value) return (int)__dp4a(a, b, (unsigned)c);
+    return __dp4a((int)a, (int)b, c);
+}
+template <typename T>
+__device__ __forceinline__ uint32_t clamp_byte(int v) {
+    if constexpr (std::is_same<T, uint8_t>::value) return (uint32_t)min(v, 255);
+    return (uint32_t)(uint8_t)(int8_t)max(min(v, 127), -128);
+}
+// bytes k..k+3 of the 8-byte little-endian pair (lo, hi), k in 0..3
+__device__ __forceinline__ uint32_t window_word(uint32_t lo, uint32_t hi, int k) {
+    return k == 0 ? lo : __byte_perm(lo, hi, 0x3210u + 0x1111u * (uint32_t)k);
+}
+// reversed taps packed four to a word: word i holds taps L-1-4i .. L-4-4i
+template <typename T, int L>
+__device__ __forceinline__ void pack_taps(const float *f, uint32_t (&w)[(L + 3) / 4]) {
+#pragma unroll
+    for (int i = 0; i < (L + 3) / 4; ++i) {
+        uint32_t v = 0;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int j = 4 * i + e;  // window position; tap index L-1-j
+            const uint32_t b = j < L ? (uint32_t)(uint8_t)from_acc<T>(f[L - 1 - j]) : 0u;
+            v |= b << (8 * e);
+        }
+        w[i] = v;
+    }
+}
+
+// transposed intermediate pitch: every pass-2 word read stays in its row,
+// and an odd word count spreads 32 lanes' rows over the banks
+__host__ __device__ constexpr int sep8_pitch(int nrb, int nrw) {
+    return (((nrb * 4 > 64 + 4 * nrw ? nrb * 4 : 64 + 4 * nrw) + 3) / 4 | 1) * 4;
+}
+
+template <typename T, int CFL, int RFL, bool EXPAND>
+__global__ void __launch_bounds__(THREADS) sep_dp4a_kernel(const __grid_constant__ CUtensorMap smap,
+                                                           const SepTmaParams p,
+                                                           const TileGrid tg) {
+    using H = Halo<T, CFL, RFL, EXPAND>;
+    constexpr int NST = NST_SEP;
+    constexpr int OFF8 = H::LT - H::LX;           // tile byte of output 0's window
+    constexpr int NCW = (CFL + 3) / 4, NRW = (RFL + 3) / 4;
+    constexpr int NA = (OFF8 % 4 + 3) / 4 + NCW + 1;  // aligned words per pass-1 row
+    constexpr int NRB = (H::BH + 3) / 4;          // 4-row blocks of the tile
+    constexpr int TPT = sep8_pitch(NRB, NRW);     // tempT pitch (bytes)
+    // the bytes that meet nonzero taps lie inside the row; the aligned word
+    // loads may run up to 8 bytes past it (into the next row, or the buffer
+    // that follows the last one), where the packed taps are zero
+    static_assert(TILE - 1 + OFF8 + CFL - 1 < H::BW, "window exceeds the tile row");
+    static_assert(4 * (15 + OFF8 / 4 + NA) <= H::BW + 8, "pass-1 words exceed the row by too much");
+    static_assert(4 * (TILE / 4 + NRW) <= TPT, "pass-2 words exceed the transposed pitch");
+    extern __shared__ __align__(128) unsigned char sm[];
+    auto tb = [&](int i) { return sm + i * H::TB_ALIGNED; };
+    unsigned char *tempT = sm + NST * H::TB_ALIGNED;  // TILE rows (x) of TPT bytes (tile rows)
+    uint64_t *full = reinterpret_cast<uint64_t *>(tempT + ((TILE * TPT + 127) / 128) * 128);
+    const int tid = threadIdx.x;
+
+    uint32_t cw[NCW], rw[NRW];
+    pack_taps<T, CFL>(p.cf, cw);
+    pack_taps<T, RFL>(p.rf, rw);
+    if (tid == 0) {
+        for (int i = 0; i < NST; ++i) mbar_init(&full[i], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+
+    auto issue = [&](int t, int buf) {
+        const uint32_t r = fdiv((uint32_t)t, tg.tx);
+        const uint32_t b = fdiv(r, tg.ty);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_arrive_expect_tx(&full[buf], H::TBYTES);
+        tma_load_3d(smem_u32(tb(buf)), &smap, &full[buf], (int)((uint32_t)t - r * tg.tx.d) * TILE - H::LT,
+                    (int)(r - b * tg.ty.d) * TILE - H::LY, (int)b);
+    };
+
+    int tile = blockIdx.x;
+    if (tid == 0)
+        for (int i = 0; i < NST - 1; ++i)
+            if (tile + i * (int)gridDim.x < tg.ntiles) issue(tile + i * (int)gridDim.x, i);
+    for (int k = 0; tile < tg.ntiles; tile += gridDim.x, ++k) {
+        const int buf = k % NST;
+        const int ahead = tile + (NST - 1) * (int)gridDim.x;
+        if (tid == 0 && ahead < tg.ntiles) issue(ahead, (k + NST - 1) % NST);
+        const uint32_t tr_ = fdiv((uint32_t)tile, tg.tx);
+        const uint32_t tb_ = fdiv(tr_, tg.ty);
+        const int ttx = (int)((uint32_t)tile - tr_ * tg.tx.d), tty = (int)(tr_ - tb_ * tg.ty.d);
+        const long long out_off = (long long)tb_ * p.out_slice;
+        if (!wait_tile(&full[buf], (k / NST) & 1)) break;
+        const unsigned char *tile_b = tb(buf);
+
+        // pass 1: a 4-row x 4-column block per item; column blocks fastest
+        for (int it = tid; it < NRB * (TILE / 4); it += THREADS) {
+            const int cb = it % (TILE / 4), rb = it / (TILE / 4);
+            uint32_t res[4] = {0u, 0u, 0u, 0u};  // res[s]: rows 4rb..4rb+3 of column 4cb+s
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int row = 4 * rb + i;
+                if (row >= H::BH) break;
+                const uint32_t *src =
+                    reinterpret_cast<const uint32_t *>(tile_b + row * H::BW) + cb + OFF8 / 4;
+                uint32_t a[NA];
+#pragma unroll
+                for (int w = 0; w < NA; ++w) a[w] = src[w];
+#pragma unroll
+                for (int sidx = 0; sidx < 4; ++sidx) {
+                    constexpr int R0 = OFF8 % 4;
+                    const int q = (R0 + sidx) / 4, sh = (R0 + sidx) % 4;
+                    int acc = 0;
+#pragma unroll
+                    for (int w = 0; w < NCW; ++w) acc = dp4<T>(window_word(a[q + w], a[q + w + 1], sh), cw[w], acc);
+                    res[sidx] |= clamp_byte<T>(acc) << (8 * i);
+                }
+            }
+#pragma unroll
+            for (int sidx = 0; sidx < 4; ++sidx)
+                *reinterpret_cast<uint32_t *>(tempT + (4 * cb + sidx) * TPT + 4 * rb) = res[sidx];
+        }
+        __syncthreads();
+        // pass 2: 4 x by 4 y outputs per thread
+        const int tx = tid & 15, ty = tid >> 4;
+        uint32_t outw[4] = {0u, 0u, 0u, 0u};  // outw[s]: row 4ty+s, columns 4tx..4tx+3
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(tempT + (4 * tx + c) * TPT) + ty;
+            uint32_t a[NRW + 1];
+#pragma unroll
+            for (int w = 0; w <= NRW; ++w) a[w] = src[w];
+#pragma unroll
+            for (int sidx = 0; sidx < 4; ++sidx) {
+                int acc = 0;
+#pragma unroll
+                for (int w = 0; w < NRW; ++w) acc = dp4<T>(window_word(a[w], a[w + 1], sidx), rw[w], acc);
+                outw[sidx] |= clamp_byte<T>(acc) << (8 * c);
+            }
+        }
+        T *out = static_cast<T *>(p.out) + out_off;
+        const long long x = (long long)ttx * TILE + 4 * tx;
+        const bool vec = (x + 3 < p.od0) && ((p.od0 & 3) == 0) &&
+                         ((reinterpret_cast<uintptr_t>(out) & 3) == 0);
+#pragma unroll
+        for (int sidx = 0; sidx < 4; ++sidx) {
+            const long long y = (long long)tty * TILE + 4 * ty + sidx;
+            if (y >= p.od1 || x >= p.od0) continue;
+            T *dst = out + y * p.od0 + x;
+            if (vec) {
+                *reinterpret_cast<uint32_t *>(dst) = outw[sidx];
+            } else {
+#pragma unroll
+                for (int c = 0; c < 4; ++c)
+                    if (x + c < p.od0) dst[c] = (T)(uint8_t)(outw[sidx] >> (8 * c));
+            }
+        }
+        __syncthreads();
+    }
+}
+
+// ===========================================================================
 // 3-D direct convolution, 3x3x3 f32 filter, persistent over 64x8x8 tiles
 // ===========================================================================
 // One 4-D TMA box (x, y, z, volume) brings a tile's haloed input block, the
@@ -862,9 +1031,36 @@ static bool run_sep(SepTmaParams p, const void *sig, long long W, long long Hh, 
     return true;
 }
 
+template <typename T, int CL, int RL, bool EXPAND>
+static bool run_sep_dp4a(SepTmaParams p, const void *sig, long long W, long long Hh,
+                         long long slices) {
+    using H = Halo<T, CL, RL, EXPAND>;
+    TileGrid tg;
+    if (!make_grid(tg, p.tiles_x, p.tiles_y, slices)) return false;
+    CUtensorMap m;
+    if (!make_map(m, sig, 1, W, Hh, slices, H::BW, H::BH)) return false;
+    constexpr int NRB = (H::BH + 3) / 4;
+    constexpr int TPT = sep8_pitch(NRB, (RL + 3) / 4);
+    const size_t smem = NST_SEP * H::TB_ALIGNED + ((TILE * TPT + 127) / 128) * 128 + 8 * NST_SEP;
+    auto kfn = sep_dp4a_kernel<T, CL, RL, EXPAND>;
+    AFGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    const int grid = persistent_grid(kfn, smem, tg.ntiles);
+    {
+        KernelTimer kt("sep_tma_kernel");
+        kfn<<<grid, THREADS, smem, stream()>>>(m, p, tg);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("sep_dp4a_kernel");
+    return true;
+}
+
 template <typename T, int L, bool EXACT>
 static bool sep_len(const SepTmaParams &p, bool expand, const void *sig, long long W, long long Hh,
                     long long slices) {
+    if constexpr (sizeof(T) == 1) {  // exact integer arithmetic: dp4a
+        return expand ? run_sep_dp4a<T, L, L, true>(p, sig, W, Hh, slices)
+                      : run_sep_dp4a<T, L, L, false>(p, sig, W, Hh, slices);
+    }
     return expand ? run_sep<T, L, L, EXACT, true>(p, sig, W, Hh, slices)
                   : run_sep<T, L, L, EXACT, false>(p, sig, W, Hh, slices);
 }
