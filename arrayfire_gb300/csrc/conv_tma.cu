@@ -263,8 +263,9 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
         if constexpr (!EXACT && sizeof(T) == 4) {
             // Fused mode: taps u = 2m, 2m+1 of one output share a packed FMA
             // (even taps accumulate in the low lane, odd taps in the high
-            // lane); the odd filter's last tap takes a scalar FMA into the low
-            // lane, so no lane ever reads a pixel outside the filter window.
+            // lane); the odd filter's last tap takes a scalar FMA into its own
+            // accumulator, so no lane ever reads a pixel outside the filter
+            // window and no accumulator pair is split.
             constexpr int NP = F0 / 2;
             static_assert(H::OFF + F0 + 2 < NW4 * 4, "packed window exceeds the loaded row");
             f2 wp[F1][NP > 0 ? NP : 1];
@@ -274,10 +275,14 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
                 for (int m = 0; m < NP; ++m)
                     wp[fj][m] = pk(wr[fj * F0 + F0 - 1 - 2 * m], wr[fj * F0 + F0 - 2 - 2 * m]);
             f2 acc2[4][4];
+            float acc1[4][4];  // the odd filter's last tap, kept apart (no pair moves)
 #pragma unroll
             for (int a = 0; a < 4; ++a)
 #pragma unroll
-                for (int c = 0; c < 4; ++c) acc2[a][c] = 0ull;
+                for (int c = 0; c < 4; ++c) {
+                    acc2[a][c] = 0ull;
+                    acc1[a][c] = 0.0f;
+                }
 #pragma unroll
             for (int q = 3 + F1 - 1; q >= 0; --q) {
                 float v[NW4 * 4];
@@ -308,12 +313,7 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
                                 const f2 in2 = (j & 1) ? vo[(j - 1) >> 1] : ve[j >> 1];
                                 acc2[rr][cc] = mac2<false>(acc2[rr][cc], in2, wp[fj][m]);
                             }
-                            if (F0 & 1) {
-                                float lo, hi;
-                                upk(acc2[rr][cc], lo, hi);
-                                lo = fmaf(v[b0 + F0 - 1], wr[fj * F0], lo);
-                                acc2[rr][cc] = pk(lo, hi);
-                            }
+                            if (F0 & 1) acc1[rr][cc] = fmaf(v[b0 + F0 - 1], wr[fj * F0], acc1[rr][cc]);
                         }
                     }
                 }
@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
                 for (int c = 0; c < 4; ++c) {
                     float lo, hi;
                     upk(acc2[a][c], lo, hi);
-                    acc[a][c] = lo + hi;
+                    acc[a][c] = (lo + hi) + acc1[a][c];
                 }
         } else {
 #pragma unroll

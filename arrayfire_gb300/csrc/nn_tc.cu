@@ -55,7 +55,8 @@ constexpr int LAG = 2;                // cp.async groups in flight per producer
 constexpr int MAX_PH = 64;
 constexpr int MAX_T = 256;
 constexpr int NUM_THREADS = 320;      // warps 0-3 gather, 4-7 epilogue, 8 MMA, 9 TMA
-constexpr int EP_PITCH = 36;          // epilogue staging row pitch (floats): 32 pixels + 4
+constexpr int EP_PITCH = 20;          // epilogue staging row pitch (floats): 16 pixels + 4
+constexpr int EP_WARPS = 8;           // epilogue warps of the TMA path (two per TMEM quadrant)
 
 struct GatherParams {
     const unsigned char *src;  // [N][SH][SW][SCpad] elements (bf16, or e4m3 bytes)
@@ -174,8 +175,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *a_stage = base;                     // STAGES x 16 KB
     unsigned char *b_stage = base + STAGES * A_BYTES;  // STAGES x 32 KB
-    float *ep_stage = reinterpret_cast<float *>(b_stage + STAGES * B_BYTES);  // 4 x 32 x 36
-    Smem *sm = reinterpret_cast<Smem *>(ep_stage + 4 * 32 * EP_PITCH);
+    float *ep_stage = reinterpret_cast<float *>(b_stage + STAGES * B_BYTES);  // 8 x 32 x 20
+    Smem *sm = reinterpret_cast<Smem *>(ep_stage + EP_WARPS * 32 * EP_PITCH);
     volatile int *abort = &sm->abort;
 
     const int warp = threadIdx.x >> 5;
@@ -188,7 +189,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         }
         for (int b = 0; b < 2; ++b) {
             mbar_init(&sm->tmem_full[b], 1);
-            mbar_init(&sm->tmem_empty[b], 128);
+            mbar_init(&sm->tmem_empty[b], TMA_B ? 32 * EP_WARPS : 128);
         }
         mbar_init(&sm->final_bar, 1);
         sm->abort = 0;
@@ -204,8 +205,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     tc_fence_after();
     const uint32_t tmem_base = sm->tmem_base;
 
-    if (warp < 4) {
-        if (!TMA_B) {
+    if (warp < 4 && !TMA_B) {
+        {
             // ---------------- pixel-row gather (128 threads)
             const int t = threadIdx.x;
             const int j = t & 7;    // 16-byte chunk within the 128-byte row
@@ -271,8 +272,11 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 mbar_arrive(&sm->full[k % STAGES]);
         }
     } else if (warp < 8) {
-        // ---------------- epilogue (128 threads, TMEM lanes 32*(warp%4) ..)
+        // ---------------- epilogue: TMEM lanes 32*(warp%4) ..; on the TMA
+        // path warps 0-3 join warps 4-7 (the gather warps are idle there),
+        // the two warps of a TMEM quadrant taking alternate 16-pixel chunks
         const int q = warp & 3;
+        const int half = TMA_B ? (warp >> 2) : 0;
         uint32_t acc_it = 0;
         const long long plane = (long long)p.DW * p.DH;
         const bool vec_rows = (p.DW & 3) == 0;
@@ -281,7 +285,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             const int och = ti.och0 + 32 * q + lane;
             if (ti.ntaps == 0) {
                 // a stride phase no tap reaches: its gradient is zero
-                if (och < p.DC) {
+                if (och < p.DC && half == 0) {
                     for (int e = 0; e < BN; ++e) {
                         int X, Y, n;
                         if (TMA_B) {
@@ -309,35 +313,33 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             tc_fence_after();
             const uint32_t taddr = tmem_base + (uint32_t)(b * BN) + ((uint32_t)(32 * q) << 16);
             if (TMA_B) {
-                // 32 channels x 32 pixels at a time: TMEM -> registers -> this
-                // warp's shared staging block -> 128-byte rows per channel
-                float *stg = ep_stage + q * (32 * EP_PITCH);
-                const int orow = lane >> 3;         // 0..3: channel within a group of 4
-                const int ocol = (lane & 7) * 4;    // pixel offset within the 32
-                for (int cc = 0; cc < BN / 32; ++cc) {
-                    uint32_t r[32];
-                    tmem_ld16(taddr + cc * 32, *reinterpret_cast<uint32_t(*)[16]>(&r[0]));
-                    tmem_ld16(taddr + cc * 32 + 16, *reinterpret_cast<uint32_t(*)[16]>(&r[16]));
+                // 32 channels x 16 pixels at a time: TMEM -> registers -> this
+                // warp's shared staging block -> 64-byte row pieces per channel
+                float *stg = ep_stage + warp * (32 * EP_PITCH);
+                const int orow = lane >> 2;         // 0..7: channel within a group of 8
+                const int ocol = (lane & 3) * 4;    // pixel offset within the 16
+                const float sc = (FP8 && och < p.DC) ? p.out_scale[och] : 1.0f;
+                const int osx = p.mode == 0 ? 1 : p.sx, osy = p.mode == 0 ? 1 : p.sy;
+                for (int cc = half; cc < BN / 16; cc += 2) {
+                    uint32_t r[16];
+                    tmem_ld16(taddr + cc * 16, r);
                     tmem_ld_wait();
 #pragma unroll
-                    const float sc = (FP8 && och < p.DC) ? p.out_scale[och] : 1.0f;
-#pragma unroll
-                    for (int e = 0; e < 8; ++e)
+                    for (int e = 0; e < 4; ++e)
                         *reinterpret_cast<float4 *>(stg + lane * EP_PITCH + 4 * e) =
                             make_float4(sc * __uint_as_float(r[4 * e]), sc * __uint_as_float(r[4 * e + 1]),
                                         sc * __uint_as_float(r[4 * e + 2]), sc * __uint_as_float(r[4 * e + 3]));
                     __syncwarp();
-                    // BX >= 32 keeps the 32 pixels in one row; (x, y) are
+                    // BX >= 32 keeps the 16 pixels in one row; (x, y) are
                     // coordinates in the phase grid, output (rx + osx*x, ry + osy*y)
-                    const int e0 = cc * 32;
+                    const int e0 = cc * 16;
                     const int x = ti.x0 + (e0 % p.BX) + ocol, y = ti.y0 + e0 / p.BX;
-                    const int osx = p.mode == 0 ? 1 : p.sx, osy = p.mode == 0 ? 1 : p.sy;
                     if (y < ti.MY && x < ti.MX) {
                         const long long xo = ti.rx + (long long)osx * x;
                         const long long yo = ti.ry + (long long)osy * y;
 #pragma unroll
-                        for (int i = 0; i < 8; ++i) {
-                            const int cl = orow + 4 * i;
+                        for (int i = 0; i < 4; ++i) {
+                            const int cl = orow + 8 * i;
                             const int oc = ti.och0 + 32 * q + cl;
                             if (oc >= p.DC) continue;
                             const float4 v = *reinterpret_cast<const float4 *>(stg + cl * EP_PITCH + ocol);
@@ -1297,7 +1299,8 @@ static bool pick_rect(int W, int H, int area, int minx, int &bx, int &by, int sx
 }
 
 static size_t gather_smem() {
-    return 1024 + STAGES * (A_BYTES + B_BYTES) + 4 * 32 * EP_PITCH * sizeof(float) + sizeof(Smem) + 64;
+    return 1024 + STAGES * (A_BYTES + B_BYTES) + EP_WARPS * 32 * EP_PITCH * sizeof(float) +
+           sizeof(Smem) + 64;
 }
 
 // forward (mode 0) or data gradient (mode 1); fp8 (forward only): e4m3
