@@ -7,8 +7,9 @@ backward, exactly as a user of the reference would differentiate a layer:
 the data gradient (AF_CONV_GRADIENT_DATA), the filter gradient
 (AF_CONV_GRADIENT_FILTER) and, through the library's extension, the real bias
 gradient -- all that are needed in one afgb_convolve2_gradients_nn call, whose
-results equal the per-gradient calls bit for bit.  Tensors are passed zero-copy: a torch tensor (N, C, H, W) is the
-ArrayFire array (W, H, C, N), and the library runs on torch's current stream.
+results equal the per-gradient calls bit for bit.  Tensors are passed
+zero-copy: a torch tensor (N, C, H, W) is the ArrayFire array (W, H, C, N),
+and the library runs on torch's current stream.
 
 Semantics are ArrayFire's, not torch's: the filter is flipped (a true
 convolution, src/backend/cpu/convolve.cpp:130-157), and stride, padding and
