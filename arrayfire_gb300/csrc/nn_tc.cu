@@ -57,6 +57,7 @@ constexpr int MAX_T = 256;
 constexpr int NUM_THREADS = 320;      // warps 0-3 gather, 4-7 epilogue, 8 MMA, 9 TMA
 constexpr int EP_PITCH = 20;          // epilogue staging row pitch (floats): 16 pixels + 4
 constexpr int EP_WARPS = 8;           // epilogue warps of the TMA path (two per TMEM quadrant)
+constexpr int EP_SLOT = 768;          // floats of staging per warp: 3 KB, 1024-byte aligned slots
 
 struct GatherParams {
     const unsigned char *src;  // [N][SH][SW][SCpad] elements (bf16, or e4m3 bytes)
@@ -65,6 +66,7 @@ struct GatherParams {
     int SW, SH, SCpad, N;
     int DW, DH, DC;
     int mode;  // 0 forward, 1 data gradient
+    int tma_store;  // epilogue writes by TMA through the output map (unit-stride outputs)
     int sx, sy, px, py, dx, dy, fw;
     int nchunk;       // SCpad / 64
     int n_och_tiles;  // ceil(DC / 128)
@@ -169,14 +171,15 @@ template <bool TMA_B, bool FP8>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     gather_conv_kernel(const __grid_constant__ GatherParams p,
                        const __grid_constant__ CUtensorMap wmap,
-                       const __grid_constant__ CUtensorMap xmap) {
+                       const __grid_constant__ CUtensorMap xmap,
+                       const __grid_constant__ CUtensorMap omap) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     unsigned char *a_stage = base;                     // STAGES x 16 KB
     unsigned char *b_stage = base + STAGES * A_BYTES;  // STAGES x 32 KB
     float *ep_stage = reinterpret_cast<float *>(b_stage + STAGES * B_BYTES);  // 8 x 32 x 20
-    Smem *sm = reinterpret_cast<Smem *>(ep_stage + EP_WARPS * 32 * EP_PITCH);
+    Smem *sm = reinterpret_cast<Smem *>(ep_stage + EP_WARPS * EP_SLOT);
     volatile int *abort = &sm->abort;
 
     const int warp = threadIdx.x >> 5;
@@ -315,7 +318,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             if (TMA_B) {
                 // 32 channels x 16 pixels at a time: TMEM -> registers -> this
                 // warp's shared staging block -> 64-byte row pieces per channel
-                float *stg = ep_stage + warp * (32 * EP_PITCH);
+                float *stg = ep_stage + warp * EP_SLOT;
                 const int orow = lane >> 2;         // 0..7: channel within a group of 8
                 const int ocol = (lane & 3) * 4;    // pixel offset within the 16
                 const float sc = (FP8 && och < p.DC) ? p.out_scale[och] : 1.0f;
@@ -324,6 +327,29 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     uint32_t r[16];
                     tmem_ld16(taddr + cc * 16, r);
                     tmem_ld_wait();
+                    const int e0 = cc * 16;
+                    if (p.tma_store) {
+                        // one 64-byte row per channel, 16-byte chunks swizzled by
+                        // (row >> 1) & 3 (the output map's 64-byte swizzle: conflict-
+                        // free 128-bit stores); one lane stores the 32x16 block by TMA
+                        if (lane == 0) bulk_wait_read();  // the last store has read the buffer
+                        __syncwarp();
+                        unsigned char *row = reinterpret_cast<unsigned char *>(stg) + lane * 64;
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            *reinterpret_cast<float4 *>(row + ((e ^ ((lane >> 1) & 3)) << 4)) =
+                                make_float4(sc * __uint_as_float(r[4 * e]), sc * __uint_as_float(r[4 * e + 1]),
+                                            sc * __uint_as_float(r[4 * e + 2]),
+                                            sc * __uint_as_float(r[4 * e + 3]));
+                        fence_proxy_async_smem();
+                        __syncwarp();
+                        if (lane == 0) {
+                            tma_store_4d(&omap, smem_u32(stg), ti.x0 + (e0 % p.BX), ti.y0 + e0 / p.BX,
+                                         ti.och0 + 32 * q, ti.n);
+                            bulk_commit();
+                        }
+                        continue;
+                    }
 #pragma unroll
                     for (int e = 0; e < 4; ++e)
                         *reinterpret_cast<float4 *>(stg + lane * EP_PITCH + 4 * e) =
@@ -332,7 +358,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     __syncwarp();
                     // BX >= 32 keeps the 16 pixels in one row; (x, y) are
                     // coordinates in the phase grid, output (rx + osx*x, ry + osy*y)
-                    const int e0 = cc * 16;
                     const int x = ti.x0 + (e0 % p.BX) + ocol, y = ti.y0 + e0 / p.BX;
                     if (y < ti.MY && x < ti.MX) {
                         const long long xo = ti.rx + (long long)osx * x;
@@ -391,6 +416,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             mbar_arrive(&sm->tmem_empty[b]);
             ++acc_it;
         }
+        if (TMA_B && p.tma_store && lane == 0) bulk_wait_all();  // stores done before exit
+        __syncwarp();
     } else if (warp == 8) {
         // ---------------- MMA issuer
         if (lane == 0) {
@@ -1299,8 +1326,9 @@ static bool pick_rect(int W, int H, int area, int minx, int &bx, int &by, int sx
 }
 
 static size_t gather_smem() {
-    return 1024 + STAGES * (A_BYTES + B_BYTES) + EP_WARPS * 32 * EP_PITCH * sizeof(float) +
-           sizeof(Smem) + 64;
+    static_assert(32 * EP_PITCH <= EP_SLOT && 32 * 16 <= EP_SLOT, "epilogue staging slot");
+    return 1024 + STAGES * (A_BYTES + B_BYTES) + EP_WARPS * EP_SLOT * sizeof(float) + sizeof(Smem) +
+           64;
 }
 
 // forward (mode 0) or data gradient (mode 1); fp8 (forward only): e4m3
@@ -1462,6 +1490,21 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     if (tma_b) xmap = make_imap(img, SCpad, SW, SH, (int)g.N, p.BX, p.BY, esize, tsx, tsy);
     p.total_tiles = ntile;
 
+    // epilogue by TMA stores for unit-stride outputs with 16-byte rows
+    CUtensorMap omap;
+    std::memset(&omap, 0, sizeof(omap));
+    p.tma_store = 0;
+    if (tma_b && (mode == 0 || (g.sx == 1 && g.sy == 1)) && (DW % 4) == 0 &&
+        (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+        cuuint64_t odims[4] = {(cuuint64_t)DW, (cuuint64_t)DH, (cuuint64_t)DC, (cuuint64_t)g.N};
+        cuuint64_t ostr[3] = {(cuuint64_t)DW * 4, (cuuint64_t)DW * DH * 4, (cuuint64_t)DW * DH * DC * 4};
+        cuuint32_t obox[4] = {16, 1, 32, 1};
+        cuuint32_t oes[4] = {1, 1, 1, 1};
+        if (encode_fn()(&omap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, dst, odims, ostr, obox, oes,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                        CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+            p.tma_store = 1;
+    }
     CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad, esize);
     const size_t smem = gather_smem();
     if (ntile > 0) {
@@ -1471,7 +1514,7 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     do {                                                                                         \
         AFGB_CUDA(cudaFuncSetAttribute(gather_conv_kernel<TB, F8>,                               \
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
-        gather_conv_kernel<TB, F8><<<grid, NUM_THREADS, smem, stream()>>>(p, wmap, xmap);        \
+        gather_conv_kernel<TB, F8><<<grid, NUM_THREADS, smem, stream()>>>(p, wmap, xmap, omap);  \
     } while (0)
         if (tma_b && fp8) AFGB_LAUNCH_GATHER(true, true);
         else if (tma_b) AFGB_LAUNCH_GATHER(true, false);
