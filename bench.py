@@ -47,6 +47,11 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = ("conv2_nn fwd+bwd TFLOP/s BF16-TC vs FP32 (rel err≤2e-2); convolve2 HBM GB/s")
 NN_SHAPE = dict(W=128, H=128, C=64, N=32, fw=3, fh=3, K=128, stride=(1, 1), pad=(1, 1), dil=(1, 1))
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each
+# tensor-core kernel on NN_SHAPE, from one ncu capture of `bench.py --only
+# fwd|dgrad|wgrad` (ncu cannot run inside the timed bench)
+NCU_TRAFFIC = {"tc_fwd_kernel": 67.30e6 + 212.86e6, "tc_dgrad_kernel": 134.60e6 + 90.88e6,
+               "tc_wgrad_kernel": 206.02e6 + 18.06e6}
 
 
 def nn_flops(s=NN_SHAPE) -> float:
@@ -246,7 +251,9 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
         peak = peaks["bf16_tflops"]
         roofline = {"bound": "tensor", "kernel": name, "achieved": round(achieved, 2),
                     "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
-                    "peak_source": peaks["source"] + " bf16 dense", "traffic": None,
+                    "peak_source": peaks["source"] + " bf16 dense",
+                    "traffic": NCU_TRAFFIC.get(name) if prec == "bf16" else None,
+                    "traffic_source": "ncu capture, one launch (bytes)",
                     "launches": cnt, "avg_ms": round(ms / cnt, 4)}
 
     # e2e through the C ABI with pinned host buffers
