@@ -9,6 +9,7 @@ same names, argument meaning and error codes:
     convolve2_separable                    af_convolve2_sep   (include/af/signal.h:1478)
     convolve2_nn                           af_convolve2_nn    (include/af/signal.h:1440)
     convolve2_gradient_nn                  af_convolve2_gradient_nn (include/af/ml.h:84-92)
+    unwrap / wrap / wrap_v2                af_unwrap / af_wrap / af_wrap_v2 (include/af/image.h:1483,1524,1570)
 
 Arrays are ``Array`` handles over device memory with ArrayFire dims
 (d0 fastest).  ``Array.from_numpy`` takes a numpy array laid out in
@@ -316,6 +317,28 @@ def convolve2_gradients_nn(incoming_gradient: Array, original_signal: Array,
         original_signal.handle, original_filter.handle, sn, sp, pn, pp, dn, dp,
         PRECISION[precision]))
     return tuple(Array(o.value) if o is not None else None for o in outs)
+
+
+def unwrap(signal: Array, wx: int, wy: int, sx: int, sy: int, px: int = 0, py: int = 0,
+           is_column: bool = True) -> Array:
+    """af_unwrap: wx x wy patches at strides (sx, sy), zero padding (px, py)."""
+    return _out_call(lib().af_unwrap, signal.handle, wx, wy, sx, sy, px, py, bool(is_column))
+
+
+def wrap(patches: Array, ox: int, oy: int, wx: int, wy: int, sx: int, sy: int, px: int = 0,
+         py: int = 0, is_column: bool = True) -> Array:
+    """af_wrap: accumulate patches into a new (ox, oy, d2, d3) image."""
+    return _out_call(lib().af_wrap, patches.handle, ox, oy, wx, wy, sx, sy, px, py,
+                     bool(is_column))
+
+
+def wrap_v2(out: Optional[Array], patches: Array, ox: int, oy: int, wx: int, wy: int, sx: int,
+            sy: int, px: int = 0, py: int = 0, is_column: bool = True) -> Array:
+    """af_wrap_v2: as wrap, adding into `out` in place when it is given."""
+    h = af_array(out.handle if out is not None else None)
+    _check(lib().af_wrap_v2(ctypes.byref(h), patches.handle, ox, oy, wx, wy, sx, sy, px, py,
+                            bool(is_column)))
+    return out if out is not None else Array(h.value)
 
 
 # host-only helpers (no GPU)

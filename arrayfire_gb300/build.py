@@ -27,6 +27,7 @@ SOURCES = [
     "conv_tma.cu",
     "nn_simt.cu",
     "nn_tc.cu",
+    "unwrap_wrap.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -2,6 +2,7 @@
 // reference's argument checks, batch-kind inference, domain choice and dtype
 // dispatch (src/api/c/convolve.cpp), routed to this library's sm_103a
 // kernels.  No CPU fallback: every path below launches device code.
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -357,6 +358,49 @@ static af_err convolve2_grads_impl(af_array *data_grad, af_array *filter_grad, a
     return AF_SUCCESS;
 }
 
+static bool patch_type(af_dtype t) { return t != f16 && dtype_valid(t); }
+
+// af_wrap_common (src/api/c/wrap.cpp:33-85): argument checks in the
+// reference's order, then out = (allocate ? zeros : *out) + wrap(in); a new
+// output is written once by the kernel, without a zero fill first
+static void wrap_impl(af_array *out, const af_array in, dim_t ox, dim_t oy, dim_t wx, dim_t wy,
+                      dim_t sx, dim_t sy, dim_t px, dim_t py, bool is_column, bool allocate) {
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    AFGB_ARG_ASSERT(1, in != nullptr);
+    Array *a = get_array(in);
+    const dim_t od[4] = {ox, oy, a->dims[2], a->dims[3]};
+    AFGB_ARG_ASSERT(4, wx > 0);
+    AFGB_ARG_ASSERT(5, wy > 0);
+    AFGB_ARG_ASSERT(6, sx > 0);
+    AFGB_ARG_ASSERT(7, sy > 0);
+    const dim_t nx = (ox + 2 * px - wx) / sx + 1;
+    const dim_t ny = (oy + 2 * py - wy) / sy + 1;
+    const dim_t patch_size = is_column ? a->dims[0] : a->dims[1];
+    const dim_t num_patches = is_column ? a->dims[1] : a->dims[0];
+    AFGB_DIM_ASSERT(1, patch_size == wx * wy);
+    AFGB_DIM_ASSERT(1, num_patches == nx * ny);
+    // both counts negative (a window wider than the padded image by a stride or
+    // more) multiply to a positive count; the reference then walks windows at
+    // negative indices.  Rejected here as a size error.
+    AFGB_DIM_ASSERT(1, nx >= 0 && ny >= 0);
+    Array dst;
+    if (allocate) {
+        if (!patch_type(a->type)) AFGB_TYPE_ERROR(1, a->type);
+        for (int i = 0; i < 4; ++i) AFGB_DIM_ASSERT(0, od[i] >= 0);
+        dst = *create_array(a->type, od);  // every pixel is written by the kernel
+    } else {
+        dst = *get_array(*out);
+        bool same = true;
+        for (int i = 0; i < 4; ++i) same &= dst.dims[i] == od[i];
+        AFGB_DIM_ASSERT(0, same);
+        if (!patch_type(a->type)) AFGB_TYPE_ERROR(1, a->type);
+        require_type(&dst, a->type);
+    }
+    Array src = a->is_linear() ? *a : make_dense(*a);
+    patches_wrap(src, dst, wx, wy, sx, sy, px, py, is_column, allocate);
+    if (allocate) *out = make_handle(&dst);
+}
+
 }  // namespace afgb
 
 using namespace afgb;
@@ -473,6 +517,47 @@ af_err afgb_convolve2_gradients_nn(af_array *data_grad, af_array *filter_grad,
     return convolve2_grads_impl(data_grad, filter_grad, bias_grad, incoming_gradient,
                                 original_signal, original_filter, stride_dims, strides,
                                 padding_dims, paddings, dilation_dims, dilations, precision);
+    AFGB_CATCHALL
+}
+
+af_err af_unwrap(af_array *out, const af_array in, const dim_t wx, const dim_t wy, const dim_t sx,
+                 const dim_t sy, const dim_t px, const dim_t py, const bool is_column) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    Array *a = get_array(in);
+    const dim_t *id = a->dims;
+    AFGB_ARG_ASSERT(2, wx > 0 && wx <= id[0] + 2 * px);
+    AFGB_ARG_ASSERT(3, wy > 0 && wy <= id[1] + 2 * py);
+    AFGB_ARG_ASSERT(4, sx > 0);
+    AFGB_ARG_ASSERT(5, sy > 0);
+    AFGB_ARG_ASSERT(6, px >= 0 && px < wx);
+    AFGB_ARG_ASSERT(7, py >= 0 && py < wy);
+    if (!patch_type(a->type)) AFGB_TYPE_ERROR(1, a->type);
+    const dim_t nx = (id[0] + 2 * px - wx) / sx + 1;
+    const dim_t ny = (id[1] + 2 * py - wy) / sy + 1;
+    dim_t od[4] = {wx * wy, nx * ny, id[2], id[3]};
+    if (!is_column) std::swap(od[0], od[1]);
+    Array src = a->is_linear() ? *a : make_dense(*a);
+    Array r = *create_array(a->type, od);
+    patches_unwrap(src, r, wx, wy, sx, sy, px, py, is_column);
+    *out = make_handle(&r);
+    AFGB_CATCHALL
+}
+
+af_err af_wrap(af_array *out, const af_array in, const dim_t ox, const dim_t oy, const dim_t wx,
+               const dim_t wy, const dim_t sx, const dim_t sy, const dim_t px, const dim_t py,
+               const bool is_column) {
+    AFGB_TRY
+    wrap_impl(out, in, ox, oy, wx, wy, sx, sy, px, py, is_column, true);
+    AFGB_CATCHALL
+}
+
+af_err af_wrap_v2(af_array *out, const af_array in, const dim_t ox, const dim_t oy,
+                  const dim_t wx, const dim_t wy, const dim_t sx, const dim_t sy, const dim_t px,
+                  const dim_t py, const bool is_column) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    wrap_impl(out, in, ox, oy, wx, wy, sx, sy, px, py, is_column, *out == nullptr);
     AFGB_CATCHALL
 }
 

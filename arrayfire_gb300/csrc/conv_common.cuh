@@ -160,4 +160,21 @@ __device__ __forceinline__ float int_prod(unsigned long long a, unsigned long lo
     return __ull2float_rn(a * b);
 }
 
+// n / d for 0 <= n < 2^31 by multiply-high (Granlund and Montgomery,
+// "Division by invariant integers using multiplication", PLDI 1994, with
+// l = ceil(log2 d) and m = floor(2^32 (2^l - d) / d) + 1: q = (mulhi(n, m) + n) >> l;
+// n < 2^31 keeps the sum within 32 bits)
+struct FastDiv {
+    uint32_t d, m, s;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+    uint32_t l = 0;
+    while ((1ull << l) < d) ++l;
+    const uint64_t m = ((1ull << 32) * ((1ull << l) - d)) / d + 1;
+    return FastDiv{d, (uint32_t)m, l};
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv &f) {
+    return (__umulhi(n, f.m) + n) >> f.s;
+}
+
 }  // namespace afgb

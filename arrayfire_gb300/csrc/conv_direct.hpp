@@ -25,6 +25,13 @@ Array cast_array(const Array &in, af_dtype to);
 // Dense copy of a strided array (same dtype).
 Array make_dense(const Array &in);
 
+// af_unwrap / af_wrap kernels (unwrap_wrap.cu): `in` dense; wrap adds into
+// `out` (any strides), or overwrites it with the sum alone when zero_init
+void patches_unwrap(const Array &in, Array &out, long long wx, long long wy, long long sx,
+                    long long sy, long long px, long long py, bool is_column);
+void patches_wrap(const Array &in, Array &out, long long wx, long long wy, long long sx,
+                  long long sy, long long px, long long py, bool is_column, bool zero_init);
+
 // out = T( s * (c * r) ) element-wise: the scalar-filter shortcut of
 // af_convolve2_sep (src/api/c/convolve.cpp:57-68).
 void launch_sep_scalar(const Array &sig, const Array &cfilt, const Array &rfilt, Array &out);

@@ -503,6 +503,17 @@ def run_direct_workloads(af, peaks, args) -> dict:
     measure("conv3_3x3x3_f32_256^3_expand",
             lambda: af.convolve3(V, F3, af.AF_CONV_EXPAND, af.AF_CONV_SPATIAL),
             v.numel() * 4 + 258 ** 3 * 4 + 108, ("conv3_tile_kernel", "conv_generic_kernel"))
+    del V, v
+    # af_unwrap / af_wrap of the NN image (128x128x64x32 f32, 3x3 windows,
+    # stride 1, padding 1): the 9x larger patch matrix is written / read once
+    xi = torch.rand(32, 64, 128, 128, device="cuda")
+    XI = af.Array.view_torch(xi)
+    ni = xi.numel()
+    measure("unwrap_3x3_f32_128x128x64x32", lambda: af.unwrap(XI, 3, 3, 1, 1, 1, 1),
+            ni * 4 * 10, ("unwrap_kernel",))
+    U = af.unwrap(XI, 3, 3, 1, 1, 1, 1)
+    measure("wrap_3x3_f32_128x128x64x32", lambda: af.wrap(U, 128, 128, 3, 3, 1, 1, 1, 1),
+            ni * 4 * 10, ("wrap_kernel",))
     return out
 
 
@@ -598,7 +609,13 @@ def run_only(args) -> None:
         t = g.standard_normal(15)
         CF = af.Array.from_numpy((t / t.sum()).astype(np.float32))
         RF = af.Array.from_numpy((t[::-1] / t.sum()).astype(np.float32))
-        if args.only == "conv3":
+        if args.only in ("unwrap", "wrap"):
+            xi = torch.rand(32, 64, 128, 128, device="cuda")
+            XI = af.Array.view_torch(xi)
+            U = af.unwrap(XI, 3, 3, 1, 1, 1, 1)
+            fn = ((lambda: af.unwrap(XI, 3, 3, 1, 1, 1, 1)) if args.only == "unwrap" else
+                  (lambda: af.wrap(U, 128, 128, 3, 3, 1, 1, 1, 1)))
+        elif args.only == "conv3":
             v = torch.rand(256, 256, 256, device="cuda")
             V = af.Array.view_torch(v)
             k3 = g.standard_normal((3, 3, 3))
@@ -646,7 +663,8 @@ def main() -> None:
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--only", default=None,
-                    choices=["fwd", "dgrad", "wgrad", "sep_f32", "sep_u8", "same7", "conv3", "cnn"],
+                    choices=["fwd", "dgrad", "wgrad", "sep_f32", "sep_u8", "same7", "conv3", "cnn",
+                             "unwrap", "wrap"],
                     help="run one operation of the workload --steps times after --warmup "
                          "(for profiler captures); prints its timing, not the bench line")
     args = ap.parse_args()

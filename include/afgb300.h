@@ -17,6 +17,7 @@
 #ifndef AFGB300_H
 #define AFGB300_H
 
+#include <stdbool.h>
 #include <stddef.h>
 
 #ifdef __cplusplus
@@ -148,6 +149,27 @@ AFGB_API af_err af_convolve2_gradient_nn(af_array *out, const af_array incoming_
                                          const unsigned padding_dims, const dim_t *paddings,
                                          const unsigned dilation_dims, const dim_t *dilations,
                                          af_conv_gradient_type grad_type);
+
+/* ---- patch extraction and accumulation (the NN path's unwrap / wrap as
+ * public calls; dilation 1) ----------------------------------------------- */
+
+/* include/af/image.h:1483 (src/api/c/unwrap.cpp:37-103): patches of wx x wy
+ * at strides (sx, sy) with zero padding (px, py); out dims (wx*wy, nx*ny, d2,
+ * d3) with is_column, else (nx*ny, wx*wy, d2, d3); nx = (d0+2px-wx)/sx + 1. */
+AFGB_API af_err af_unwrap(af_array *out, const af_array in, const dim_t wx, const dim_t wy,
+                          const dim_t sx, const dim_t sy, const dim_t px, const dim_t py,
+                          const bool is_column);
+/* include/af/image.h:1524 (src/api/c/wrap.cpp:87-96): the inverse
+ * accumulation into a new (ox, oy, d2, d3) array of zeros; overlapping patch
+ * elements add in the element type. */
+AFGB_API af_err af_wrap(af_array *out, const af_array in, const dim_t ox, const dim_t oy,
+                        const dim_t wx, const dim_t wy, const dim_t sx, const dim_t sy,
+                        const dim_t px, const dim_t py, const bool is_column);
+/* include/af/image.h:1570 (src/api/c/wrap.cpp:98-109): as af_wrap, adding into
+ * *out when it is not 0 (dense, same dims and type). */
+AFGB_API af_err af_wrap_v2(af_array *out, const af_array in, const dim_t ox, const dim_t oy,
+                           const dim_t wx, const dim_t wy, const dim_t sx, const dim_t sy,
+                           const dim_t px, const dim_t py, const bool is_column);
 
 /* ---- extensions (no ArrayFire counterpart) -------------------------- */
 

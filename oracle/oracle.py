@@ -237,6 +237,79 @@ def wrap_dilated(cols: np.ndarray, odims, wx, wy, sx, sy, px, py, dx, dy, which=
 
 
 # ---------------------------------------------------------------------------
+# af_unwrap / af_wrap (public form: dilation 1, is_column, every type)
+# ---------------------------------------------------------------------------
+def patch_grid(W, H, wx, wy, sx, sy, px, py):
+    """Patches across and down, with C's truncating division as the reference
+    computes them (a window wider than the padded image by less than the stride
+    still gives one patch)."""
+    return (_cdiv_trunc(W + 2 * px - wx, sx) + 1, _cdiv_trunc(H + 2 * py - wy, sy) + 1)
+
+
+def _patch_coords(nx, ny, wx, wy, sx, sy, px, py):
+    """(x, y) image coordinates of every patch element, indexed [k, col] with
+    k = kx + wx*ky and col = winx + nx*winy (src/backend/cpu/kernel/unwrap.hpp:40-71)."""
+    k = np.arange(wx * wy)
+    col = np.arange(nx * ny)
+    x = (col % nx)[None, :] * sx - px + (k % wx)[:, None]
+    y = (col // nx)[None, :] * sy - py + (k // wx)[:, None]
+    return x, y
+
+
+def unwrap_patches(sig: np.ndarray, wx, wy, sx, sy, px, py, is_column=True, dtype=None,
+                   which="port") -> np.ndarray:
+    """af_unwrap (src/api/c/unwrap.cpp:37-103, src/backend/cpu/unwrap.cpp:23-41)."""
+    s = as_af(sig)
+    sd = _dims4(s)
+    nx, ny = patch_grid(sd[0], sd[1], wx, wy, sx, sy, px, py)
+    if which == "ref":
+        od = [wx * wy, nx * ny, sd[2], sd[3]] if is_column else [nx * ny, wx * wy, sd[2], sd[3]]
+        out = np.zeros(od, dtype=s.dtype, order="F")
+        rc = lib("ref").ref_unwrap_any(ctypes.c_int(dtype), out.ctypes.data_as(_P),
+                                       s.ctypes.data_as(_P), _ll(sd),
+                                       *[ctypes.c_longlong(v) for v in (wx, wy, sx, sy, px, py)],
+                                       ctypes.c_int(1 if is_column else 0))
+        if rc != 0:
+            raise RuntimeError("ref_unwrap_any failed")
+        return out
+    x, y = _patch_coords(nx, ny, wx, wy, sx, sy, px, py)
+    inside = (x >= 0) & (x < sd[0]) & (y >= 0) & (y < sd[1])
+    cols = np.zeros([wx * wy, nx * ny, sd[2], sd[3]], dtype=s.dtype, order="F")
+    cols[inside] = s[x[inside], y[inside]]
+    return np.asfortranarray(cols if is_column else cols.transpose(1, 0, 2, 3))
+
+
+def wrap_patches(cols: np.ndarray, ox, oy, wx, wy, sx, sy, px, py, is_column=True, out=None,
+                 dtype=None, which="port") -> np.ndarray:
+    """af_wrap / af_wrap_v2 (src/api/c/wrap.cpp:33-109, src/backend/cpu/kernel/wrap.hpp:21-80):
+    out (zeros unless given) += every patch element, patches in increasing col
+    order, each add in the element type."""
+    c = as_af(cols)
+    cd = _dims4(c)
+    od = [ox, oy, cd[2], cd[3]]
+    res = np.zeros(od, dtype=c.dtype, order="F") if out is None else np.array(as_af(out), order="F")
+    nx, ny = patch_grid(ox, oy, wx, wy, sx, sy, px, py)
+    if which == "ref":
+        rc = lib("ref").ref_wrap_any(ctypes.c_int(dtype), res.ctypes.data_as(_P), _ll(od),
+                                     c.ctypes.data_as(_P), _ll(cd),
+                                     *[ctypes.c_longlong(v) for v in (wx, wy, sx, sy, px, py)],
+                                     ctypes.c_int(1 if is_column else 0))
+        if rc != 0:
+            raise RuntimeError("ref_wrap_any failed")
+        return res
+    if nx < 0 or ny < 0:
+        raise ValueError("window exceeds the padded image by a stride or more")
+    km = c if is_column else c.transpose(1, 0, 2, 3)          # [k, col, d2, d3]
+    x, y = _patch_coords(nx, ny, wx, wy, sx, sy, px, py)
+    with np.errstate(over="ignore"):
+        for col in range(nx * ny):
+            m = (x[:, col] >= 0) & (x[:, col] < ox) & (y[:, col] >= 0) & (y[:, col] < oy)
+            xs, ys = x[m, col], y[m, col]
+            res[xs, ys] = res[xs, ys] + km[m, col]
+    return res
+
+
+# ---------------------------------------------------------------------------
 # NN convolution, FP64
 # ---------------------------------------------------------------------------
 def _geom(sd, fd, stride, pad, dil):

@@ -14,12 +14,17 @@
  *                           the temp sized as src/backend/cpu/convolve.cpp:68-99
  *   ref_unwrap_*         -> kernel::unwrap_dim  (src/backend/cpu/kernel/unwrap.hpp:19-80)
  *   ref_wrap_dilated_*   -> kernel::wrap_dim_dilated (src/backend/cpu/kernel/wrap.hpp:166-228)
+ *   ref_unwrap_any       -> kernel::unwrap_dim with dilation 1 and d = is_column
+ *                           (src/backend/cpu/unwrap.cpp:23-41), every af_unwrap type
+ *   ref_wrap_any         -> kernel::wrap_dim<T, is_column> adding into `out`
+ *                           (src/backend/cpu/wrap.cpp:24-37), every af_wrap type
  */
 #include <kernel/convolve.hpp>
 #include <kernel/unwrap.hpp>
 #include <kernel/wrap.hpp>
 
 #include <complex>
+#include <utility>
 #include <cstring>
 #include <vector>
 
@@ -72,6 +77,30 @@ void sep(void *out, const long long *od, const void *sig, const long long *sd, c
     Param<InT> t(temp.data(), d4(td), dense(td));
     if (expand) K::convolve2<InT, AccT, true>(o, s, c, r, t);
     else K::convolve2<InT, AccT, false>(o, s, c, r, t);
+}
+}  // namespace
+
+namespace {
+template <typename T>
+void unwrap_any(void *out, const void *in, const long long *idims, long long wx, long long wy,
+                long long sx, long long sy, long long px, long long py, int is_column) {
+    long long nx = 1 + (idims[0] + 2 * px - wx) / sx;
+    long long ny = 1 + (idims[1] + 2 * py - wy) / sy;
+    long long od[4] = {wx * wy, nx * ny, idims[2], idims[3]};
+    if (!is_column) std::swap(od[0], od[1]);
+    Param<T> o(static_cast<T *>(out), d4(od), dense(od));
+    CParam<T> i(static_cast<const T *>(in), d4(idims), dense(idims));
+    K::unwrap_dim<T>(o, i, wx, wy, sx, sy, px, py, 1, 1, is_column ? 1 : 0);
+}
+
+template <typename T>
+void wrap_any(void *out, const long long *odims, const void *in, const long long *idims,
+              long long wx, long long wy, long long sx, long long sy, long long px, long long py,
+              int is_column) {
+    Param<T> o(static_cast<T *>(out), d4(odims), dense(odims));
+    CParam<T> i(static_cast<const T *>(in), d4(idims), dense(idims));
+    if (is_column) K::wrap_dim<T, 1>(o, i, wx, wy, sx, sy, px, py);
+    else K::wrap_dim<T, 0>(o, i, wx, wy, sx, sy, px, py);
 }
 }  // namespace
 
@@ -149,5 +178,38 @@ REF_UNWRAP(ref_unwrap_f64, double)
     }
 REF_WRAP(ref_wrap_dilated_f32, float)
 REF_WRAP(ref_wrap_dilated_f64, double)
+
+
+#define REF_PATCH_TYPES(FN, ...)                                   \
+    switch (dtype) {                                               \
+        case 0: FN<float>(__VA_ARGS__); break;                     \
+        case 1: FN<std::complex<float>>(__VA_ARGS__); break;       \
+        case 2: FN<double>(__VA_ARGS__); break;                    \
+        case 3: FN<std::complex<double>>(__VA_ARGS__); break;      \
+        case 4: FN<char>(__VA_ARGS__); break;                      \
+        case 5: FN<int>(__VA_ARGS__); break;                       \
+        case 6: FN<unsigned>(__VA_ARGS__); break;                  \
+        case 7: FN<unsigned char>(__VA_ARGS__); break;             \
+        case 8: FN<long long>(__VA_ARGS__); break;                 \
+        case 9: FN<unsigned long long>(__VA_ARGS__); break;        \
+        case 10: FN<short>(__VA_ARGS__); break;                    \
+        case 11: FN<unsigned short>(__VA_ARGS__); break;           \
+        case 13: FN<signed char>(__VA_ARGS__); break;              \
+        default: return -1;                                        \
+    }
+
+int ref_unwrap_any(int dtype, void *out, const void *in, const long long *idims, long long wx,
+                   long long wy, long long sx, long long sy, long long px, long long py,
+                   int is_column) {
+    REF_PATCH_TYPES(unwrap_any, out, in, idims, wx, wy, sx, sy, px, py, is_column)
+    return 0;
+}
+
+int ref_wrap_any(int dtype, void *out, const long long *odims, const void *in,
+                 const long long *idims, long long wx, long long wy, long long sx, long long sy,
+                 long long px, long long py, int is_column) {
+    REF_PATCH_TYPES(wrap_any, out, odims, in, idims, wx, wy, sx, sy, px, py, is_column)
+    return 0;
+}
 
 }  // extern "C"

@@ -232,3 +232,62 @@ def config1b():
     k = np.ones((3, 3), np.float32)
     k[1, 1] = 0
     return sig, np.asfortranarray(k)
+
+
+# af_unwrap / af_wrap: every type x the reference's geometry families
+# (test/unwrap.cpp:104-147, test/wrap.cpp:163-181: window, stride, padding
+# combinations on small images), both layouts, two batch slices each way.
+PATCH_DTYPES = [F32, C32, F64, C64, B8, S32, U32, U8, S64, U64, S16, U16, S8]
+PATCH_GEOMS = [
+    # name,    (W, H),  wx, wy, sx, sy, px, py
+    ("p3s1",   (13, 9),  3, 3, 1, 1, 0, 0),
+    ("p3s1p1", (13, 9),  3, 3, 1, 1, 1, 1),
+    ("p3s2p2", (13, 9),  3, 3, 2, 2, 2, 2),
+    ("p4s2p3", (16, 10), 4, 4, 2, 2, 3, 3),
+    ("p8s8p7", (30, 20), 8, 8, 8, 8, 7, 7),
+    ("p8x12",  (30, 20), 8, 12, 8, 12, 7, 11),
+    ("p15x10", (30, 20), 15, 10, 1, 1, 14, 9),
+    ("p31s8",  (40, 33), 31, 31, 8, 8, 15, 15),
+    ("p5r",    (21, 17), 5, 3, 3, 2, 1, 2),
+]
+
+
+def patch_cases():
+    """(id, dtype, (W, H, d2, d3), wx, wy, sx, sy, px, py, is_column, seed)."""
+    out = []
+    seed = 20000
+    for gname, (W, H), wx, wy, sx, sy, px, py in PATCH_GEOMS:
+        for dt in PATCH_DTYPES:
+            for col in (True, False):
+                seed += 3
+                out.append((f"{gname}_{DT_NAME[dt]}_{'col' if col else 'row'}", dt, (W, H, 2, 2),
+                            wx, wy, sx, sy, px, py, col, seed))
+    return out
+
+
+def patch_values(dtype: int, shape, seed: int) -> np.ndarray:
+    """Values for unwrap inputs and wrap patch matrices: integers large enough
+    that 8- and 16-bit accumulations wrap around."""
+    g = rng(seed)
+    shape = af_shape(shape)
+    if dtype in (F32, F64):
+        a = g.standard_normal(shape) * 4
+    elif dtype in (C32, C64):
+        a = (g.standard_normal(shape) + 1j * g.standard_normal(shape)) * 4
+    elif dtype == B8:
+        a = g.integers(0, 2, shape)
+    elif dtype in (U8, S8):
+        a = g.integers(0, 120, shape)
+    elif dtype in (S16, U16):
+        a = g.integers(0, 30000, shape)
+    else:
+        a = g.integers(0, 1 << 30, shape)
+    return np.asfortranarray(a.astype(NP_OF[dtype]))
+
+
+def patch_dims(case):
+    """unwrap output dims of a patch case."""
+    _, _, (W, H, d2, d3), wx, wy, sx, sy, px, py, col, _ = case
+    nx = (W + 2 * px - wx) // sx + 1
+    ny = (H + 2 * py - wy) // sy + 1
+    return [wx * wy, nx * ny, d2, d3] if col else [nx * ny, wx * wy, d2, d3]

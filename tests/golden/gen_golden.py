@@ -10,6 +10,9 @@ Writes, next to this file:
                convolution case (tests/golden/cases.py:direct_cases) and the
                two full-size configuration-1 images;
   sep.json     the same for af_convolve2_sep cases;
+  patches.json SHA-256 of the reference's af_unwrap output, af_wrap of a
+               seeded patch matrix into zeros, and af_wrap_v2 into a seeded
+               image, for every tests/golden/cases.py:patch_cases case;
   nn.npz       FP64 NN forward / data-gradient / filter-gradient outputs for
                NN_CASES, each cross-checked against the reference's own
                unwrap + GEMM (forward, filter gradient) and wrap_dilated
@@ -39,6 +42,32 @@ import cases as C  # noqa: E402
 
 def digest(a: np.ndarray) -> str:
     return hashlib.sha256(np.asfortranarray(a).tobytes(order="F")).hexdigest()
+
+
+def patches() -> None:
+    """af_unwrap / af_wrap / af_wrap_v2 digests from the reference kernels,
+    with the numpy port asserted bit-identical on every case."""
+    gold = {}
+    for case in C.patch_cases():
+        cid, dt, sd, wx, wy, sx, sy, px, py, col, seed = case
+        img = C.patch_values(dt, sd, seed)
+        geo = (wx, wy, sx, sy, px, py, col)
+        u_ref = O.unwrap_patches(img, *geo, dtype=dt, which="ref")
+        u_port = O.unwrap_patches(img, *geo, dtype=dt, which="port")
+        pm = C.patch_values(dt, C.patch_dims(case), seed + 1)
+        base = C.patch_values(dt, sd, seed + 2)
+        w_ref = O.wrap_patches(pm, sd[0], sd[1], *geo, dtype=dt, which="ref")
+        w_port = O.wrap_patches(pm, sd[0], sd[1], *geo, dtype=dt, which="port")
+        v_ref = O.wrap_patches(pm, sd[0], sd[1], *geo, out=base, dtype=dt, which="ref")
+        v_port = O.wrap_patches(pm, sd[0], sd[1], *geo, out=base, dtype=dt, which="port")
+        for name, a, b in (("unwrap", u_ref, u_port), ("wrap", w_ref, w_port),
+                           ("wrap_v2", v_ref, v_port)):
+            if a.shape != b.shape or a.tobytes(order="F") != b.tobytes(order="F"):
+                raise SystemExit(f"port differs from reference on {cid} {name}")
+        gold[cid] = {"unwrap": digest(u_ref), "unwrap_dims": list(u_ref.shape),
+                     "wrap": digest(w_ref), "wrap_v2": digest(v_ref)}
+    (HERE / "patches.json").write_text(json.dumps(gold, indent=0, sort_keys=True))
+    print(f"patches {len(gold)}")
 
 
 def main() -> None:
@@ -122,4 +151,10 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["patches"]:
+        if O.build_ref() is None:
+            raise SystemExit("reference source tree not found; golden vectors need it")
+        patches()
+    else:
+        main()
+        patches()
