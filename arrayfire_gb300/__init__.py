@@ -335,7 +335,7 @@ def wrap(patches: Array, ox: int, oy: int, wx: int, wy: int, sx: int, sy: int, p
 def wrap_v2(out: Optional[Array], patches: Array, ox: int, oy: int, wx: int, wy: int, sx: int,
             sy: int, px: int = 0, py: int = 0, is_column: bool = True) -> Array:
     """af_wrap_v2: as wrap, adding into `out` in place when it is given."""
-    h = af_array(out.handle if out is not None else None)
+    h = af_array(out.handle.value if out is not None else None)
     _check(lib().af_wrap_v2(ctypes.byref(h), patches.handle, ox, oy, wx, wy, sx, sy, px, py,
                             bool(is_column)))
     return out if out is not None else Array(h.value)

@@ -163,11 +163,11 @@ def test_f16_is_a_type_error(af):
 def test_wrap_v2_existing_output_checks(af):
     pin = af.Array.from_numpy(H_IN)
     wrong_dims = af.Array.from_numpy(np.zeros((5, 4), np.float32))
-    h = af._lib.af_array(wrong_dims.handle)
+    h = af._lib.af_array(wrong_dims.handle.value)
     assert af.lib().af_wrap_v2(ctypes.byref(h), pin.handle, 4, 4, 2, 2, 2, 2, 0, 0, True) \
         == af.AF_ERR_SIZE
     wrong_type = af.Array.from_numpy(np.zeros((4, 4), np.float64))
-    h = af._lib.af_array(wrong_type.handle)
+    h = af._lib.af_array(wrong_type.handle.value)
     assert af.lib().af_wrap_v2(ctypes.byref(h), pin.handle, 4, 4, 2, 2, 2, 2, 0, 0, True) != 0
 
 
