@@ -46,57 +46,97 @@ struct PatchDivs {
     FastDiv wsz, np, nx, wx, W, H, d2;
 };
 
-// one thread per output element; in: image slices of W*H, out: patches
+// elements per 16-byte vector of T (1 for 16-byte complex double)
+template <typename T> constexpr int vec_of() { return sizeof(T) >= 16 ? 1 : 16 / (int)sizeof(T); }
+
+template <typename T> struct alignas(16) VecT { T v[vec_of<T>()]; };
+
+// VEC consecutive output elements per thread: the first element's (k, col,
+// slice) comes from one decomposition, the rest by stepping the counters, and
+// the VEC values leave in one 16-byte store (scalar stores for the tail or an
+// unaligned output)
 template <typename T, bool FAST>
-__global__ void unwrap_kernel(const T *__restrict__ in, T *__restrict__ out, PatchGeom g,
-                              PatchDivs f) {
+__global__ void __launch_bounds__(256) unwrap_kernel(const T *__restrict__ in, T *__restrict__ out,
+                                                     PatchGeom g, PatchDivs f, int vec_store) {
+    constexpr int VEC = vec_of<T>();
     const long long wsz = g.wx * g.wy, np = g.nx * g.ny;
     const long long total = wsz * np * g.slices;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        long long k, col, s, winx, winy, kx, ky;
+    const long long nvec = (total + VEC - 1) / VEC;
+    for (long long v = blockIdx.x * (long long)blockDim.x + threadIdx.x; v < nvec;
+         v += (long long)gridDim.x * blockDim.x) {
+        const long long t0 = v * VEC;
+        long long k, col, s;
         if constexpr (FAST) {
-            const uint32_t u = (uint32_t)t;
-            uint32_t k32, c32, s32;
+            const uint32_t u = (uint32_t)t0;
             if (g.is_column) {  // out[k + wsz*(col + np*s)]
                 const uint32_t r = fdiv(u, f.wsz);
-                k32 = u - r * f.wsz.d;
-                s32 = fdiv(r, f.np);
-                c32 = r - s32 * f.np.d;
+                k = u - r * f.wsz.d;
+                const uint32_t s32 = fdiv(r, f.np);
+                col = r - s32 * f.np.d;
+                s = s32;
             } else {            // out[col + np*(k + wsz*s)]
                 const uint32_t r = fdiv(u, f.np);
-                c32 = u - r * f.np.d;
-                s32 = fdiv(r, f.wsz);
-                k32 = r - s32 * f.wsz.d;
+                col = u - r * f.np.d;
+                const uint32_t s32 = fdiv(r, f.wsz);
+                k = r - s32 * f.wsz.d;
+                s = s32;
             }
-            const uint32_t wy32 = fdiv(c32, f.nx), ky32 = fdiv(k32, f.wx);
-            winy = wy32;
-            winx = c32 - wy32 * f.nx.d;
-            ky = ky32;
-            kx = k32 - ky32 * f.wx.d;
-            s = s32;
         } else {
             if (g.is_column) {
-                k = t % wsz;
-                const long long r = t / wsz;
+                k = t0 % wsz;
+                const long long r = t0 / wsz;
                 col = r % np;
                 s = r / np;
             } else {
-                col = t % np;
-                const long long r = t / np;
+                col = t0 % np;
+                const long long r = t0 / np;
                 k = r % wsz;
                 s = r / wsz;
             }
-            winx = col % g.nx;
-            winy = col / g.nx;
-            kx = k % g.wx;
-            ky = k / g.wx;
         }
-        const long long x = winx * g.sx - g.px + kx;
-        const long long y = winy * g.sy - g.py + ky;
-        T v = pzero<T>();
-        if (x >= 0 && x < g.W && y >= 0 && y < g.H) v = in[x + g.W * (y + g.H * s)];
-        out[t] = v;
+        long long winy = col / g.nx, winx = col - winy * g.nx;
+        long long ky = k / g.wx, kx = k - ky * g.wx;
+        VecT<T> o;
+#pragma unroll
+        for (int j = 0; j < VEC; ++j) {
+            const long long x = winx * g.sx - g.px + kx;
+            const long long y = winy * g.sy - g.py + ky;
+            T val = pzero<T>();
+            if (x >= 0 && x < g.W && y >= 0 && y < g.H && s < g.slices)
+                val = in[x + g.W * (y + g.H * s)];
+            o.v[j] = val;
+            // step to the next output element
+            if (g.is_column) {
+                if (++kx == g.wx) {
+                    kx = 0;
+                    if (++ky == g.wy) {
+                        ky = 0;
+                        if (++winx == g.nx) {
+                            winx = 0;
+                            if (++winy == g.ny) { winy = 0; ++s; }
+                        }
+                    }
+                }
+            } else {
+                if (++winx == g.nx) {
+                    winx = 0;
+                    if (++winy == g.ny) {
+                        winy = 0;
+                        if (++kx == g.wx) {
+                            kx = 0;
+                            if (++ky == g.wy) { ky = 0; ++s; }
+                        }
+                    }
+                }
+            }
+        }
+        if (vec_store && t0 + VEC <= total) {
+            *reinterpret_cast<VecT<T> *>(out + t0) = o;
+        } else {
+#pragma unroll
+            for (int j = 0; j < VEC; ++j)
+                if (t0 + j < total) out[t0 + j] = o.v[j];
+        }
     }
 }
 
@@ -152,6 +192,92 @@ __global__ void wrap_kernel(const T *__restrict__ in, T *__restrict__ out, Patch
     }
 }
 
+// af_wrap with is_column on a TX x TY pixel tile of one slice: the patches
+// covering the tile are, row by row of windows, contiguous runs of
+// wsz * nwx elements; the block stages them in shared memory with 16-byte
+// copies (each row keeps its global 16-byte phase, so the copies stay
+// aligned), then each thread sums its pixels' patch elements in col order
+// from shared memory
+constexpr int WT_X = 32, WT_Y = 32, WT_THREADS = 256;
+
+struct WrapTile {
+    int tiles_x, tiles_y;
+    int nwx_max, nwy_max;
+    int run_pad;          // staged row pitch (elements, a multiple of VEC)
+};
+
+__host__ __device__ inline long long cdiv_pos(long long a, long long b) { return (a + b - 1) / b; }
+
+template <typename T>
+__global__ void __launch_bounds__(WT_THREADS) wrap_tiled_kernel(const T *__restrict__ in,
+                                                                T *__restrict__ out, PatchGeom g,
+                                                                WrapTile wt) {
+    constexpr int VEC = vec_of<T>();
+    extern __shared__ __align__(16) unsigned char wrap_smem[];
+    T *sm = reinterpret_cast<T *>(wrap_smem);
+    const long long wsz = g.wx * g.wy, np = g.nx * g.ny;
+    long long tile = blockIdx.x;
+    const int tx = (int)(tile % wt.tiles_x);
+    tile /= wt.tiles_x;
+    const int ty = (int)(tile % wt.tiles_y);
+    const long long s = tile / wt.tiles_y;
+    const long long x0 = (long long)tx * WT_X, y0 = (long long)ty * WT_Y;
+    const long long x1 = min(x0 + WT_X, g.W) - 1, y1 = min(y0 + WT_Y, g.H) - 1;
+    // windows covering any pixel of the tile
+    const long long ax0 = x0 + g.px, ay0 = y0 + g.py, ax1 = x1 + g.px, ay1 = y1 + g.py;
+    const long long wx_lo = ax0 - g.wx + 1 > 0 ? cdiv_pos(ax0 - g.wx + 1, g.sx) : 0;
+    const long long wy_lo = ay0 - g.wy + 1 > 0 ? cdiv_pos(ay0 - g.wy + 1, g.sy) : 0;
+    const long long wx_hi = min(ax1 >= 0 ? ax1 / g.sx : -1, g.nx - 1);
+    const long long wy_hi = min(ay1 >= 0 ? ay1 / g.sy : -1, g.ny - 1);
+    const int nwx = (int)max(0ll, wx_hi - wx_lo + 1), nwy = (int)max(0ll, wy_hi - wy_lo + 1);
+    const int run = (int)wsz * nwx;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // stage: window row rr of the tile -> sm[rr*run_pad + phase(rr) + e], e < run
+    for (int rr = warp; rr < nwy; rr += WT_THREADS / 32) {
+        const long long gstart = wsz * (wx_lo + g.nx * (wy_lo + rr) + np * s);
+        const int phase = (int)(gstart & (VEC - 1));
+        const T *src = in + (gstart - phase);
+        T *dst = sm + rr * wt.run_pad;
+        const int nchunks = (phase + run + VEC - 1) / VEC;
+        for (int c = lane; c < nchunks; c += 32) {
+            const int e0 = c * VEC - phase;
+            if (e0 >= 0 && e0 + VEC <= run) {
+                *reinterpret_cast<VecT<T> *>(dst + c * VEC) =
+                    *reinterpret_cast<const VecT<T> *>(src + c * VEC);
+            } else {
+#pragma unroll
+                for (int j = 0; j < VEC; ++j)
+                    if (e0 + j >= 0 && e0 + j < run) dst[c * VEC + j] = src[c * VEC + j];
+            }
+        }
+    }
+    __syncthreads();
+    const int lx = threadIdx.x & (WT_X - 1);
+    for (int ly = threadIdx.x / WT_X; ly < WT_Y; ly += WT_THREADS / WT_X) {
+        const long long x = x0 + lx, y = y0 + ly;
+        if (x > x1 || y > y1) continue;
+        const long long ax = x + g.px, ay = y + g.py;
+        const long long px_lo = ax - g.wx + 1 > 0 ? cdiv_pos(ax - g.wx + 1, g.sx) : 0;
+        const long long py_lo = ay - g.wy + 1 > 0 ? cdiv_pos(ay - g.wy + 1, g.sy) : 0;
+        const long long px_hi = min(ax >= 0 ? ax / g.sx : -1, g.nx - 1);
+        const long long py_hi = min(ay >= 0 ? ay / g.sy : -1, g.ny - 1);
+        const long long z = s % g.d2, w = s / g.d2;
+        const long long o = x * g.os[0] + y * g.os[1] + z * g.os[2] + w * g.os[3];
+        T acc = g.zero_init ? pzero<T>() : out[o];
+        for (long long wy_ = py_lo; wy_ <= py_hi; ++wy_) {
+            const int rr = (int)(wy_ - wy_lo);
+            const long long gstart = wsz * (wx_lo + g.nx * wy_ + np * s);
+            const T *row = sm + rr * wt.run_pad + (int)(gstart & (VEC - 1));
+            const int ky = (int)(ay - wy_ * g.sy);
+            for (long long wx_ = px_lo; wx_ <= px_hi; ++wx_) {
+                const int kx = (int)(ax - wx_ * g.sx);
+                acc = padd<T>(acc, row[kx + (int)g.wx * ky + (int)wsz * (int)(wx_ - wx_lo)]);
+            }
+        }
+        out[o] = acc;
+    }
+}
+
 static PatchDivs patch_divs(const PatchGeom &g) {
     auto d = [](long long v) { return make_fastdiv((uint32_t)std::max<long long>(v, 1)); };
     return PatchDivs{d(g.wx * g.wy), d(g.nx * g.ny), d(g.nx), d(g.wx), d(g.W), d(g.H), d(g.d2)};
@@ -161,25 +287,67 @@ static constexpr long long kFastLimit = 1ll << 31;
 
 template <typename T>
 static void launch_unwrap(const Array &in, Array &out, const PatchGeom &g) {
+    constexpr int VEC = vec_of<T>();
     const long long total = g.wx * g.wy * g.nx * g.ny * g.slices;
     if (total == 0) return;
-    const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, (long long)num_sms() * 16);
+    const long long nvec = (total + VEC - 1) / VEC;
+    const unsigned blocks = (unsigned)std::min<long long>((nvec + 255) / 256, (long long)num_sms() * 16);
     const PatchDivs f = patch_divs(g);
+    const int vec_store = ((uintptr_t)out.data() % 16) == 0;
     {
         KernelTimer kt("unwrap_kernel");
         if (total < kFastLimit)
-            unwrap_kernel<T, true><<<blocks, 256, 0, stream()>>>(in.ptr<T>(), out.ptr<T>(), g, f);
+            unwrap_kernel<T, true><<<blocks, 256, 0, stream()>>>(in.ptr<T>(), out.ptr<T>(), g, f,
+                                                                 vec_store);
         else
-            unwrap_kernel<T, false><<<blocks, 256, 0, stream()>>>(in.ptr<T>(), out.ptr<T>(), g, f);
+            unwrap_kernel<T, false><<<blocks, 256, 0, stream()>>>(in.ptr<T>(), out.ptr<T>(), g, f,
+                                                                  vec_store);
     }
     count_launch();
     AFGB_POST_LAUNCH("unwrap_kernel");
+}
+
+// the tiled kernel when the window rows of a tile fit in 64 KB of shared
+// memory, the patch matrix starts on a 16-byte boundary and the tile count
+// fits a grid
+static bool wrap_tiled_plan(const PatchGeom &g, size_t esize, const void *in, WrapTile &wt,
+                            size_t &smem) {
+    if (!g.is_column || ((uintptr_t)in % 16) != 0) return false;
+    const long long vec = esize >= 16 ? 1 : 16 / (long long)esize;
+    wt.tiles_x = (int)((g.W + WT_X - 1) / WT_X);
+    wt.tiles_y = (int)((g.H + WT_Y - 1) / WT_Y);
+    const long long nwx = std::min<long long>((WT_X + g.wx - 2) / g.sx + 1, g.nx);
+    const long long nwy = std::min<long long>((WT_Y + g.wy - 2) / g.sy + 1, g.ny);
+    if (nwx <= 0 || nwy <= 0) return false;
+    const long long run_pad = (g.wx * g.wy * nwx + 2 * vec - 1) / vec * vec;
+    smem = (size_t)(run_pad * nwy) * esize;
+    const long long blocks = (long long)wt.tiles_x * wt.tiles_y * g.slices;
+    if (smem > 64 * 1024 || blocks > 0x7fffffffll || run_pad * nwy > 0x7fffffffll) return false;
+    wt.nwx_max = (int)nwx;
+    wt.nwy_max = (int)nwy;
+    wt.run_pad = (int)run_pad;
+    return true;
 }
 
 template <typename T>
 static void launch_wrap(const Array &in, Array &out, const PatchGeom &g) {
     const long long total = g.W * g.H * g.slices;
     if (total == 0) return;
+    WrapTile wt;
+    size_t smem = 0;
+    if (wrap_tiled_plan(g, sizeof(T), in.data(), wt, smem)) {
+        const unsigned blocks = (unsigned)((long long)wt.tiles_x * wt.tiles_y * g.slices);
+        AFGB_CUDA(cudaFuncSetAttribute(wrap_tiled_kernel<T>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        {
+            KernelTimer kt("wrap_tiled_kernel");
+            wrap_tiled_kernel<T><<<blocks, WT_THREADS, smem, stream()>>>(in.ptr<T>(), out.ptr<T>(),
+                                                                         g, wt);
+        }
+        count_launch();
+        AFGB_POST_LAUNCH("wrap_tiled_kernel");
+        return;
+    }
     const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, (long long)num_sms() * 16);
     const PatchDivs f = patch_divs(g);
     {

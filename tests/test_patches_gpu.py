@@ -60,7 +60,10 @@ def test_kernels_launch(af):
     a = af.Array.from_numpy(np.ones((16, 16), np.float32))
     n, U = _ran(af, "unwrap_kernel", lambda: af.unwrap(a, 3, 3, 1, 1, 1, 1))
     assert n == 1
-    n, _ = _ran(af, "wrap_kernel", lambda: af.wrap(U, 16, 16, 3, 3, 1, 1, 1, 1))
+    n, _ = _ran(af, "wrap_tiled_kernel", lambda: af.wrap(U, 16, 16, 3, 3, 1, 1, 1, 1))
+    assert n == 1
+    R = af.unwrap(a, 3, 3, 1, 1, 1, 1, False)
+    n, _ = _ran(af, "wrap_kernel", lambda: af.wrap(R, 16, 16, 3, 3, 1, 1, 1, 1, False))
     assert n == 1
 
 
