@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 
 #include "afgb_internal.hpp"
 #include "conv_common.cuh"
@@ -43,7 +44,7 @@ template <typename T> __device__ __forceinline__ T pzero() { return T{}; }
 // the index decompositions by multiply-high when every index is below 2^31
 // (FAST), else by 64-bit division
 struct PatchDivs {
-    FastDiv wsz, np, nx, wx, W, H, d2;
+    FastDiv wsz, np, nx, wx, W, H, d2, sx, sy;
 };
 
 // elements per 16-byte vector of T (1 for 16-byte complex double)
@@ -192,49 +193,194 @@ __global__ void wrap_kernel(const T *__restrict__ in, T *__restrict__ out, Patch
     }
 }
 
-// af_wrap with is_column on a TX x TY pixel tile of one slice: the patches
+// asynchronous global -> shared copy of one element (cp.async for 4-, 8- and
+// 16-byte types, zero-filled when !valid; a plain load for 1- and 2-byte types),
+// so a staging loop issues all its loads before waiting on any
+template <typename T>
+__device__ __forceinline__ void stage_elem(T *dst, const T *src, bool valid) {
+    if constexpr (sizeof(T) >= 4) {
+        const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+        const int n = valid ? (int)sizeof(T) : 0;
+        if constexpr (sizeof(T) == 16)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(d), "l"(src), "r"(n)
+                         : "memory");
+        else
+            asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;" ::"r"(d), "l"(src),
+                         "n"((int)sizeof(T)), "r"(n)
+                         : "memory");
+    } else {
+        *dst = valid ? *src : pzero<T>();
+    }
+}
+// 16 bytes at once (both addresses 16-byte aligned)
+__device__ __forceinline__ void stage16(void *dst, const void *src) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void stage_wait() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// af_unwrap by window rows: a unit is one slice, nr <= R consecutive window
+// rows and a chunk of nc <= ncols windows of each.  The block stages the
+// (nr-1)*sy + wy input rows the unit reads (zero outside the image) in shared
+// memory with asynchronous copies, then writes the unit's outputs -- per window
+// row one contiguous run in the column layout, per tap runs of nc in the row
+// layout -- one warp per run, each element read from shared memory through a
+// per-tap offset table.  All per-element arithmetic is 32-bit and incremental.
+struct UnwrapPlan {
+    int ncols, nchunks, rows, nrowgroups, span_pad;
+    long long units;
+};
+
+template <typename T, bool COL>
+__global__ void __launch_bounds__(256) unwrap_rows_kernel(const T *__restrict__ in,
+                                                          T *__restrict__ out, PatchGeom g,
+                                                          UnwrapPlan up) {
+    extern __shared__ __align__(16) unsigned char uw_smem[];
+    const int wx = (int)g.wx, wy = (int)g.wy, sx = (int)g.sx, sy = (int)g.sy, wsz = wx * wy;
+    int *ktab = reinterpret_cast<int *>(uw_smem);
+    T *sm = reinterpret_cast<T *>(uw_smem + ((wsz * 4 + 15) & ~15));
+    for (int k = threadIdx.x; k < wsz; k += blockDim.x) ktab[k] = (k / wx) * up.span_pad + k % wx;
+    const long long np = g.nx * g.ny;
+    const int nthr = blockDim.x;
+    const int rstride = sy * up.span_pad;  // shared-memory step between window rows
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    // (window, tap) of element `lane` of a column-layout run and its 32-element step
+    const int b0 = lane / wsz, k0 = lane - b0 * wsz, db = 32 / wsz, dk = 32 - db * wsz;
+    for (long long u = blockIdx.x; u < up.units; u += gridDim.x) {
+        const int chunk = (int)(u % up.nchunks);
+        const long long r1 = u / up.nchunks;
+        const long long rg = r1 % up.nrowgroups, s = r1 / up.nrowgroups;
+        const long long winy0 = rg * up.rows;
+        const int nr = (int)min((long long)up.rows, g.ny - winy0);
+        const int cx0 = chunk * up.ncols;
+        const int nc = (int)min((long long)up.ncols, g.nx - cx0);
+        const long long xs = (long long)cx0 * g.sx - g.px, ys = winy0 * g.sy - g.py;
+        const int span = (nc - 1) * sx + wx;
+        const int rows_in = (nr - 1) * sy + wy;
+        __syncthreads();  // the previous unit's readers are done (and ktab is written)
+        for (int ry = 0; ry < rows_in; ++ry) {
+            const long long y = ys + ry;
+            const bool yok = y >= 0 && y < g.H;
+            const T *row = in + g.W * ((yok ? y : 0) + g.H * s);
+            for (int xx = threadIdx.x; xx < span; xx += nthr) {
+                const long long x = xs + xx;
+                const bool ok = yok && x >= 0 && x < g.W;
+                stage_elem<T>(sm + ry * up.span_pad + xx, ok ? row + x : in, ok);
+            }
+        }
+        stage_wait();
+        __syncthreads();
+        // one warp per output run: in the column layout a run is one window
+        // row's wsz*nc elements (e = b*wsz + k, the lane's (b, k) stepping by
+        // 32 elements); in the row layout one tap's nc windows of one row
+        if constexpr (COL) {
+            const int L = wsz * nc;
+            for (int a = warp; a < nr; a += nwarps) {
+                T *o = out + wsz * (cx0 + g.nx * (winy0 + a) + np * s);
+                const T *srow = sm + a * rstride;
+                int b = b0, k = k0;
+#pragma unroll 4
+                for (int e = lane; e < L; e += 32) {
+                    o[e] = srow[ktab[k] + b * sx];
+                    k += dk;
+                    b += db;
+                    if (k >= wsz) { k -= wsz; ++b; }
+                }
+            }
+        } else {
+            const int nrun = wsz * nr;
+            for (int rn = warp; rn < nrun; rn += nwarps) {
+                const int k = rn / nr, a = rn - k * nr;
+                T *o = out + (cx0 + g.nx * (winy0 + a)) + np * (k + (long long)wsz * s);
+                const T *src = sm + a * rstride + ktab[k];
+#pragma unroll 4
+                for (int c = lane; c < nc; c += 32) o[c] = src[c * sx];
+            }
+        }
+    }
+}
+
+// Windows covering pixel coordinate a (already offset by the padding) along
+// one axis: lo..hi, empty when hi < lo.  32-bit, divisions by multiply-high;
+// valid while |a| + w + s < 2^31.
+__device__ __forceinline__ void covering(int a, int w, int n, const FastDiv &fs, int &lo, int &hi) {
+    lo = a - w + 1 > 0 ? (int)fdiv((uint32_t)(a - w + fs.d), fs) : 0;
+    hi = a >= 0 ? min((int)fdiv((uint32_t)a, fs), n - 1) : -1;
+}
+
+// acc + the patch elements of one pixel in col order: window rows r = 0..nr-1
+// (first element at p + r*row_step) of cnt windows each (next window at
+// + win_step).  Elements are loaded WB at a time before they are added, so
+// WB loads are in flight per thread; the additions keep their order.
+constexpr int WB = 8;
+template <typename T, typename Off>
+__device__ __forceinline__ T sum_patch_elems(T acc, const T *p, int nr, int cnt, Off row_step,
+                                             Off win_step) {
+    const int total = nr * cnt;
+    int j = 0;
+    const T *rowp = p;
+    for (int t0 = 0; t0 < total; t0 += WB) {
+        T v[WB];
+#pragma unroll
+        for (int i = 0; i < WB; ++i) {
+            if (t0 + i < total) {
+                v[i] = rowp[(Off)j * win_step];
+                if (++j == cnt) {
+                    j = 0;
+                    rowp += row_step;
+                }
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < WB; ++i)
+            if (t0 + i < total) acc = padd<T>(acc, v[i]);
+    }
+    return acc;
+}
+
+// af_wrap, column layout, on a TX x TY pixel tile of one slice.  The patches
 // covering the tile are, row by row of windows, contiguous runs of
-// wsz * nwx elements; the block stages them in shared memory with 16-byte
-// copies (each row keeps its global 16-byte phase, so the copies stay
-// aligned), then each thread sums its pixels' patch elements in col order
-// from shared memory
+// wsz * nwx elements: the block stages them in shared memory with 16-byte
+// asynchronous copies (each row keeps its global 16-byte phase, so the copies
+// stay aligned), then each thread sums its pixels' patch elements in col
+// order from shared memory, with 32-bit incremental indexing.
 constexpr int WT_X = 32, WT_Y = 32, WT_THREADS = 256;
 
 struct WrapTile {
     int tiles_x, tiles_y;
-    int nwx_max, nwy_max;
-    int run_pad;          // staged row pitch (elements, a multiple of VEC)
+    int run_pad;          // staged window-row pitch (elements, a multiple of VEC)
 };
-
-__host__ __device__ inline long long cdiv_pos(long long a, long long b) { return (a + b - 1) / b; }
 
 template <typename T>
 __global__ void __launch_bounds__(WT_THREADS) wrap_tiled_kernel(const T *__restrict__ in,
                                                                 T *__restrict__ out, PatchGeom g,
-                                                                WrapTile wt) {
+                                                                PatchDivs f, WrapTile wt) {
     constexpr int VEC = vec_of<T>();
     extern __shared__ __align__(16) unsigned char wrap_smem[];
     T *sm = reinterpret_cast<T *>(wrap_smem);
-    const long long wsz = g.wx * g.wy, np = g.nx * g.ny;
+    const int wx = (int)g.wx, wy = (int)g.wy, sx = (int)g.sx, sy = (int)g.sy, wsz = wx * wy;
+    const int nx = (int)g.nx, ny = (int)g.ny;
+    const long long np = g.nx * g.ny;
     long long tile = blockIdx.x;
     const int tx = (int)(tile % wt.tiles_x);
     tile /= wt.tiles_x;
     const int ty = (int)(tile % wt.tiles_y);
     const long long s = tile / wt.tiles_y;
-    const long long x0 = (long long)tx * WT_X, y0 = (long long)ty * WT_Y;
-    const long long x1 = min(x0 + WT_X, g.W) - 1, y1 = min(y0 + WT_Y, g.H) - 1;
+    const int x0 = tx * WT_X, y0 = ty * WT_Y;
+    const int x1 = min(x0 + WT_X, (int)g.W) - 1, y1 = min(y0 + WT_Y, (int)g.H) - 1;
+    const int px = (int)g.px, py = (int)g.py;
     // windows covering any pixel of the tile
-    const long long ax0 = x0 + g.px, ay0 = y0 + g.py, ax1 = x1 + g.px, ay1 = y1 + g.py;
-    const long long wx_lo = ax0 - g.wx + 1 > 0 ? cdiv_pos(ax0 - g.wx + 1, g.sx) : 0;
-    const long long wy_lo = ay0 - g.wy + 1 > 0 ? cdiv_pos(ay0 - g.wy + 1, g.sy) : 0;
-    const long long wx_hi = min(ax1 >= 0 ? ax1 / g.sx : -1, g.nx - 1);
-    const long long wy_hi = min(ay1 >= 0 ? ay1 / g.sy : -1, g.ny - 1);
-    const int nwx = (int)max(0ll, wx_hi - wx_lo + 1), nwy = (int)max(0ll, wy_hi - wy_lo + 1);
-    const int run = (int)wsz * nwx;
+    int wx_lo, wx_hi, wy_lo, wy_hi, tmp;
+    covering(x0 + px, wx, nx, f.sx, wx_lo, tmp);
+    covering(x1 + px, wx, nx, f.sx, tmp, wx_hi);
+    covering(y0 + py, wy, ny, f.sy, wy_lo, tmp);
+    covering(y1 + py, wy, ny, f.sy, tmp, wy_hi);
+    const int nwx = max(0, wx_hi - wx_lo + 1), nwy = max(0, wy_hi - wy_lo + 1);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // stage: window row rr of the tile -> sm[rr*run_pad + phase(rr) + e], e < run
+    // window row rr -> sm[rr*run_pad + phase(rr) + e], e < wsz*nwx
+    const int run = wsz * nwx;
     for (int rr = warp; rr < nwy; rr += WT_THREADS / 32) {
-        const long long gstart = wsz * (wx_lo + g.nx * (wy_lo + rr) + np * s);
+        const long long gstart = wsz * (wx_lo + (long long)nx * (wy_lo + rr) + np * s);
         const int phase = (int)(gstart & (VEC - 1));
         const T *src = in + (gstart - phase);
         T *dst = sm + rr * wt.run_pad;
@@ -242,8 +388,7 @@ __global__ void __launch_bounds__(WT_THREADS) wrap_tiled_kernel(const T *__restr
         for (int c = lane; c < nchunks; c += 32) {
             const int e0 = c * VEC - phase;
             if (e0 >= 0 && e0 + VEC <= run) {
-                *reinterpret_cast<VecT<T> *>(dst + c * VEC) =
-                    *reinterpret_cast<const VecT<T> *>(src + c * VEC);
+                stage16(dst + c * VEC, src + c * VEC);
             } else {
 #pragma unroll
                 for (int j = 0; j < VEC; ++j)
@@ -251,45 +396,152 @@ __global__ void __launch_bounds__(WT_THREADS) wrap_tiled_kernel(const T *__restr
             }
         }
     }
+    stage_wait();
     __syncthreads();
+    // row rr of windows starts at sm + rr*run_pad + phase(rr); phase(rr) =
+    // (slice offset + wsz*(wx_lo + nx*(wy_lo + rr))) mod VEC
+    const int phase0 =
+        (int)((np * wsz * s + (long long)wsz * (wx_lo + (long long)nx * wy_lo)) & (VEC - 1));
+    const int phase_step = (int)(((long long)wsz * nx) & (VEC - 1));
+    const int step = wsz - sx;  // next window along x: tap x - sx, window + 1
     const int lx = threadIdx.x & (WT_X - 1);
+    const long long z = s % g.d2, w = s / g.d2;
+    T *oslice = out + z * g.os[2] + w * g.os[3];
+    const int x = x0 + lx;
+    if (x > x1) return;
+    int cx_lo, cx_hi;
+    covering(x + px, wx, nx, f.sx, cx_lo, cx_hi);
+    const int cnt = cx_hi - cx_lo + 1;
+    const int kx0 = x + px - cx_lo * sx, p0 = cx_lo - wx_lo;
     for (int ly = threadIdx.x / WT_X; ly < WT_Y; ly += WT_THREADS / WT_X) {
-        const long long x = x0 + lx, y = y0 + ly;
-        if (x > x1 || y > y1) continue;
-        const long long ax = x + g.px, ay = y + g.py;
-        const long long px_lo = ax - g.wx + 1 > 0 ? cdiv_pos(ax - g.wx + 1, g.sx) : 0;
-        const long long py_lo = ay - g.wy + 1 > 0 ? cdiv_pos(ay - g.wy + 1, g.sy) : 0;
-        const long long px_hi = min(ax >= 0 ? ax / g.sx : -1, g.nx - 1);
-        const long long py_hi = min(ay >= 0 ? ay / g.sy : -1, g.ny - 1);
-        const long long z = s % g.d2, w = s / g.d2;
-        const long long o = x * g.os[0] + y * g.os[1] + z * g.os[2] + w * g.os[3];
-        T acc = g.zero_init ? pzero<T>() : out[o];
-        for (long long wy_ = py_lo; wy_ <= py_hi; ++wy_) {
-            const int rr = (int)(wy_ - wy_lo);
-            const long long gstart = wsz * (wx_lo + g.nx * wy_ + np * s);
-            const T *row = sm + rr * wt.run_pad + (int)(gstart & (VEC - 1));
-            const int ky = (int)(ay - wy_ * g.sy);
-            for (long long wx_ = px_lo; wx_ <= px_hi; ++wx_) {
-                const int kx = (int)(ax - wx_ * g.sx);
-                acc = padd<T>(acc, row[kx + (int)g.wx * ky + (int)wsz * (int)(wx_ - wx_lo)]);
+        const int y = y0 + ly;
+        if (y > y1) break;
+        int cy_lo, cy_hi;
+        covering(y + py, wy, ny, f.sy, cy_lo, cy_hi);
+        T *op = oslice + x * g.os[0] + y * g.os[1];
+        T acc = g.zero_init ? pzero<T>() : *op;
+        if (cnt > 0 && cy_hi >= cy_lo) {
+            // staged rows are run_pad apart plus a per-row phase, so the rows
+            // are summed one at a time unless every row has the same phase
+            if (phase_step == 0) {
+                const int rr = cy_lo - wy_lo;
+                const int base = rr * wt.run_pad + phase0;
+                const int ky = y + py - cy_lo * sy;
+                acc = sum_patch_elems<T, int>(acc, sm + base + kx0 + wx * ky + p0 * wsz,
+                                              cy_hi - cy_lo + 1, cnt, wt.run_pad - wx * sy, step);
+            } else {
+                for (int wy_ = cy_lo; wy_ <= cy_hi; ++wy_) {
+                    const int rr = wy_ - wy_lo;
+                    const int ky = y + py - wy_ * sy;
+                    const int base = rr * wt.run_pad + ((phase0 + rr * phase_step) & (VEC - 1));
+                    acc = sum_patch_elems<T, int>(acc, sm + base + kx0 + wx * ky + p0 * wsz, 1, cnt,
+                                                  0, step);
+                }
             }
         }
-        out[o] = acc;
+        *op = acc;
     }
+}
+
+// af_wrap, row layout: one thread per pixel of a 32 x 8 tile, reading the
+// patch elements straight from global memory -- for a given tap consecutive
+// windows are consecutive elements, so a warp's reads coalesce when sx = 1 --
+// with 32-bit window arithmetic and 64-bit incremental element offsets.
+template <typename T>
+__global__ void __launch_bounds__(256) wrap_rows_kernel(const T *__restrict__ in,
+                                                        T *__restrict__ out, PatchGeom g,
+                                                        PatchDivs f, WrapTile wt) {
+    const int wx = (int)g.wx, wy = (int)g.wy, sx = (int)g.sx, sy = (int)g.sy, wsz = wx * wy;
+    const int nx = (int)g.nx, ny = (int)g.ny;
+    const long long np = g.nx * g.ny;
+    long long tile = blockIdx.x;
+    const int tx = (int)(tile % wt.tiles_x);
+    tile /= wt.tiles_x;
+    const int ty = (int)(tile % wt.tiles_y);
+    const long long s = tile / wt.tiles_y;
+    const int x = tx * 32 + (threadIdx.x & 31), y = ty * 8 + (threadIdx.x >> 5);
+    if (x >= (int)g.W || y >= (int)g.H) return;
+    const int ax = x + (int)g.px, ay = y + (int)g.py;
+    int cx_lo, cx_hi, cy_lo, cy_hi;
+    covering(ax, wx, nx, f.sx, cx_lo, cx_hi);
+    covering(ay, wy, ny, f.sy, cy_lo, cy_hi);
+    const long long z = s % g.d2, w = s / g.d2;
+    T *op = out + x * g.os[0] + y * g.os[1] + z * g.os[2] + w * g.os[3];
+    T acc = g.zero_init ? pzero<T>() : *op;
+    const int cnt = cx_hi - cx_lo + 1;
+    if (cnt > 0 && cy_hi >= cy_lo) {
+        const T *slice = in + np * wsz * s;
+        const int ky = ay - cy_lo * sy, kx = ax - cx_lo * sx;
+        const T *pp = slice + (cx_lo + (long long)nx * cy_lo) + np * (kx + wx * ky);
+        // next window along x: col + 1, tap - sx; next window row: col + nx, tap - wx*sy
+        acc = sum_patch_elems<T, long long>(acc, pp, cy_hi - cy_lo + 1, cnt,
+                                            (long long)nx - np * wx * sy, 1 - (long long)sx * np);
+    }
+    *op = acc;
 }
 
 static PatchDivs patch_divs(const PatchGeom &g) {
     auto d = [](long long v) { return make_fastdiv((uint32_t)std::max<long long>(v, 1)); };
-    return PatchDivs{d(g.wx * g.wy), d(g.nx * g.ny), d(g.nx), d(g.wx), d(g.W), d(g.H), d(g.d2)};
+    return PatchDivs{d(g.wx * g.wy), d(g.nx * g.ny), d(g.nx), d(g.wx), d(g.W), d(g.H), d(g.d2),
+                     d(g.sx), d(g.sy)};
 }
 
 static constexpr long long kFastLimit = 1ll << 31;
+
+// the window-row kernel when a unit's input rows and tap table fit in 48 KB of
+// shared memory: windows per unit halved until one window row fits, then up to
+// 16 window rows per unit while they still fit
+static bool unwrap_rows_plan(const PatchGeom &g, size_t esize, UnwrapPlan &up, size_t &smem) {
+    const long long wsz = g.wx * g.wy;
+    if (wsz > 16384 || g.wx > (1 << 20) || g.sx > (1 << 20) || g.sy > (1 << 20)) return false;
+    const long long budget = 48 * 1024 - ((wsz * 4 + 15) & ~15ll);
+    long long ncols = std::min<long long>(g.nx, 512);
+    while (ncols >= 1) {
+        const long long span = (ncols - 1) * g.sx + g.wx;
+        const long long span_pad = (span + 3) / 4 * 4;
+        if (g.wy * span_pad * (long long)esize <= budget) {
+            long long rows = 1;
+            while (rows < 16 && rows < g.ny &&
+                   (rows * g.sy + g.wy) * span_pad * (long long)esize <= budget)
+                ++rows;
+            up.ncols = (int)ncols;
+            up.nchunks = (int)((g.nx + ncols - 1) / ncols);
+            up.rows = (int)rows;
+            up.nrowgroups = (int)((g.ny + rows - 1) / rows);
+            up.span_pad = (int)span_pad;
+            up.units = (long long)up.nchunks * up.nrowgroups * g.slices;
+            smem = (size_t)(((wsz * 4 + 15) & ~15ll) + ((rows - 1) * g.sy + g.wy) * span_pad *
+                                                           (long long)esize);
+            // per-element counters and offsets stay within 32 bits
+            return wsz * ncols * rows < (1ll << 30) && (rows * g.sy + g.wy) * span_pad < (1ll << 30);
+        }
+        ncols /= 2;
+    }
+    return false;
+}
 
 template <typename T>
 static void launch_unwrap(const Array &in, Array &out, const PatchGeom &g) {
     constexpr int VEC = vec_of<T>();
     const long long total = g.wx * g.wy * g.nx * g.ny * g.slices;
     if (total == 0) return;
+    UnwrapPlan up;
+    size_t smem = 0;
+    if (unwrap_rows_plan(g, sizeof(T), up, smem)) {
+        const unsigned blocks = (unsigned)std::min<long long>(up.units, (long long)num_sms() * 8);
+        {
+            KernelTimer kt("unwrap_rows_kernel");
+            if (g.is_column)
+                unwrap_rows_kernel<T, true><<<blocks, 256, smem, stream()>>>(in.ptr<T>(),
+                                                                             out.ptr<T>(), g, up);
+            else
+                unwrap_rows_kernel<T, false><<<blocks, 256, smem, stream()>>>(in.ptr<T>(),
+                                                                              out.ptr<T>(), g, up);
+        }
+        count_launch();
+        AFGB_POST_LAUNCH("unwrap_rows_kernel");
+        return;
+    }
     const long long nvec = (total + VEC - 1) / VEC;
     const unsigned blocks = (unsigned)std::min<long long>((nvec + 255) / 256, (long long)num_sms() * 16);
     const PatchDivs f = patch_divs(g);
@@ -307,24 +559,32 @@ static void launch_unwrap(const Array &in, Array &out, const PatchGeom &g) {
     AFGB_POST_LAUNCH("unwrap_kernel");
 }
 
-// the tiled kernel when the window rows of a tile fit in 64 KB of shared
-// memory, the patch matrix starts on a 16-byte boundary and the tile count
-// fits a grid
+// the staged / row kernels when every coordinate, window count and offset
+// they form in 32 bits stays below 2^30, and (column layout) the tile's staged
+// windows fit in 64 KB of shared memory with the patch matrix on a 16-byte
+// boundary
 static bool wrap_tiled_plan(const PatchGeom &g, size_t esize, const void *in, WrapTile &wt,
                             size_t &smem) {
-    if (!g.is_column || ((uintptr_t)in % 16) != 0) return false;
+    const long long lim = 1ll << 30;
+    if (g.W + std::llabs(g.px) + g.wx + g.sx >= lim || g.H + std::llabs(g.py) + g.wy + g.sy >= lim ||
+        g.nx >= lim || g.ny >= lim || g.wx * g.wy >= lim)
+        return false;
+    const long long tx = g.is_column ? WT_X : 32, ty = g.is_column ? WT_Y : 8;
+    wt.tiles_x = (int)((g.W + tx - 1) / tx);
+    wt.tiles_y = (int)((g.H + ty - 1) / ty);
+    wt.run_pad = 0;
+    smem = 0;
+    const long long blocks = (long long)wt.tiles_x * wt.tiles_y * g.slices;
+    if (blocks > 0x7fffffffll) return false;
+    if (!g.is_column) return true;
+    if (((uintptr_t)in % 16) != 0) return false;
     const long long vec = esize >= 16 ? 1 : 16 / (long long)esize;
-    wt.tiles_x = (int)((g.W + WT_X - 1) / WT_X);
-    wt.tiles_y = (int)((g.H + WT_Y - 1) / WT_Y);
     const long long nwx = std::min<long long>((WT_X + g.wx - 2) / g.sx + 1, g.nx);
     const long long nwy = std::min<long long>((WT_Y + g.wy - 2) / g.sy + 1, g.ny);
     if (nwx <= 0 || nwy <= 0) return false;
     const long long run_pad = (g.wx * g.wy * nwx + 2 * vec - 1) / vec * vec;
     smem = (size_t)(run_pad * nwy) * esize;
-    const long long blocks = (long long)wt.tiles_x * wt.tiles_y * g.slices;
-    if (smem > 64 * 1024 || blocks > 0x7fffffffll || run_pad * nwy > 0x7fffffffll) return false;
-    wt.nwx_max = (int)nwx;
-    wt.nwy_max = (int)nwy;
+    if (smem > 64 * 1024) return false;
     wt.run_pad = (int)run_pad;
     return true;
 }
@@ -335,21 +595,31 @@ static void launch_wrap(const Array &in, Array &out, const PatchGeom &g) {
     if (total == 0) return;
     WrapTile wt;
     size_t smem = 0;
+    const PatchDivs f = patch_divs(g);
     if (wrap_tiled_plan(g, sizeof(T), in.data(), wt, smem)) {
         const unsigned blocks = (unsigned)((long long)wt.tiles_x * wt.tiles_y * g.slices);
-        AFGB_CUDA(cudaFuncSetAttribute(wrap_tiled_kernel<T>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        {
-            KernelTimer kt("wrap_tiled_kernel");
-            wrap_tiled_kernel<T><<<blocks, WT_THREADS, smem, stream()>>>(in.ptr<T>(), out.ptr<T>(),
-                                                                         g, wt);
+        if (g.is_column) {
+            AFGB_CUDA(cudaFuncSetAttribute(wrap_tiled_kernel<T>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            {
+                KernelTimer kt("wrap_tiled_kernel");
+                wrap_tiled_kernel<T><<<blocks, WT_THREADS, smem, stream()>>>(in.ptr<T>(),
+                                                                             out.ptr<T>(), g, f, wt);
+            }
+            count_launch();
+            AFGB_POST_LAUNCH("wrap_tiled_kernel");
+        } else {
+            {
+                KernelTimer kt("wrap_rows_kernel");
+                wrap_rows_kernel<T><<<blocks, 256, 0, stream()>>>(in.ptr<T>(), out.ptr<T>(), g, f,
+                                                                  wt);
+            }
+            count_launch();
+            AFGB_POST_LAUNCH("wrap_rows_kernel");
         }
-        count_launch();
-        AFGB_POST_LAUNCH("wrap_tiled_kernel");
         return;
     }
     const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, (long long)num_sms() * 16);
-    const PatchDivs f = patch_divs(g);
     {
         KernelTimer kt("wrap_kernel");
         if (total < kFastLimit)

@@ -510,7 +510,7 @@ def run_direct_workloads(af, peaks, args) -> dict:
     XI = af.Array.view_torch(xi)
     ni = xi.numel()
     measure("unwrap_3x3_f32_128x128x64x32", lambda: af.unwrap(XI, 3, 3, 1, 1, 1, 1),
-            ni * 4 * 10, ("unwrap_kernel",))
+            ni * 4 * 10, ("unwrap_rows_kernel", "unwrap_kernel"))
     U = af.unwrap(XI, 3, 3, 1, 1, 1, 1)
     measure("wrap_3x3_f32_128x128x64x32", lambda: af.wrap(U, 128, 128, 3, 3, 1, 1, 1, 1),
             ni * 4 * 10, ("wrap_tiled_kernel", "wrap_kernel"))

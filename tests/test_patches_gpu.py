@@ -58,12 +58,18 @@ def test_patches_match_reference_hash(af, case):
 
 def test_kernels_launch(af):
     a = af.Array.from_numpy(np.ones((16, 16), np.float32))
-    n, U = _ran(af, "unwrap_kernel", lambda: af.unwrap(a, 3, 3, 1, 1, 1, 1))
+    n, U = _ran(af, "unwrap_rows_kernel", lambda: af.unwrap(a, 3, 3, 1, 1, 1, 1))
     assert n == 1
     n, _ = _ran(af, "wrap_tiled_kernel", lambda: af.wrap(U, 16, 16, 3, 3, 1, 1, 1, 1))
     assert n == 1
     R = af.unwrap(a, 3, 3, 1, 1, 1, 1, False)
-    n, _ = _ran(af, "wrap_kernel", lambda: af.wrap(R, 16, 16, 3, 3, 1, 1, 1, 1, False))
+    n, _ = _ran(af, "wrap_rows_kernel", lambda: af.wrap(R, 16, 16, 3, 3, 1, 1, 1, 1, False))
+    assert n == 1
+    # windows too large to stage: the untiled kernels
+    big = af.Array.from_numpy(np.ones((80, 70), np.complex128))
+    n, B = _ran(af, "unwrap_kernel", lambda: af.unwrap(big, 64, 64, 1, 1))
+    assert n == 1
+    n, _ = _ran(af, "wrap_kernel", lambda: af.wrap(B, 80, 70, 64, 64, 1, 1))
     assert n == 1
 
 
@@ -214,3 +220,26 @@ def test_empty_and_strided_input(af):
 
     np.testing.assert_array_equal(got.reshape(-1, order="F"),
                                   O.unwrap_patches(host, 3, 3, 1, 1, 1, 1).reshape(-1, order="F"))
+
+
+@pytest.mark.parametrize("dt", [C.F32, C.U8, C.C64], ids=lambda d: C.DT_NAME[d])
+@pytest.mark.parametrize("col", [True, False])
+@pytest.mark.parametrize("shape,geo", [
+    ((1100, 6, 2, 1), (3, 3, 1, 1, 1, 1)),      # 1100 windows per row: 512-window units
+    ((264, 70, 1, 2), (64, 64, 1, 9, 0, 3)),    # 64x64 windows: 100-window units, short last unit
+    ((90, 40, 3, 1), (5, 4, 3, 2, 2, 1)),
+])
+def test_patch_units_and_tiles_match_oracle(af, oracle, dt, col, shape, geo):
+    """Geometries that split a window row into several units and tiles that
+    fall back to the untiled wrap, bit for bit against the oracle."""
+    wx, wy, sx, sy, px, py = geo
+    x = C.patch_values(dt, shape, 4321)
+    U = af.unwrap(af.Array.from_numpy(x, dt), wx, wy, sx, sy, px, py, col)
+    ref_u = oracle.unwrap_patches(x, wx, wy, sx, sy, px, py, col)
+    got_u = U.to_numpy()
+    assert list(got_u.shape) == list(ref_u.shape)
+    assert got_u.tobytes(order="F") == ref_u.tobytes(order="F")
+    pm = C.patch_values(dt, list(ref_u.shape), 4322)
+    W = af.wrap(af.Array.from_numpy(pm, dt), shape[0], shape[1], wx, wy, sx, sy, px, py, col)
+    ref_w = oracle.wrap_patches(pm, shape[0], shape[1], wx, wy, sx, sy, px, py, col)
+    assert W.to_numpy().tobytes(order="F") == ref_w.tobytes(order="F")
