@@ -514,6 +514,15 @@ def run_direct_workloads(af, peaks, args) -> dict:
     U = af.unwrap(XI, 3, 3, 1, 1, 1, 1)
     measure("wrap_3x3_f32_128x128x64x32", lambda: af.wrap(U, 128, 128, 3, 3, 1, 1, 1, 1),
             ni * 4 * 10, ("wrap_tiled_kernel", "wrap_kernel"))
+    del U
+    # the same with is_column = false (patch elements along dim 1)
+    measure("unwrap_rows_3x3_f32_128x128x64x32",
+            lambda: af.unwrap(XI, 3, 3, 1, 1, 1, 1, False), ni * 4 * 10,
+            ("unwrap_rows_kernel", "unwrap_kernel"))
+    R = af.unwrap(XI, 3, 3, 1, 1, 1, 1, False)
+    measure("wrap_rows_3x3_f32_128x128x64x32",
+            lambda: af.wrap(R, 128, 128, 3, 3, 1, 1, 1, 1, False), ni * 4 * 10,
+            ("wrap_rows_kernel", "wrap_kernel"))
     return out
 
 
