@@ -9,6 +9,7 @@ same names, argument meaning and error codes:
     convolve2_separable                    af_convolve2_sep   (include/af/signal.h:1478)
     convolve2_nn                           af_convolve2_nn    (include/af/signal.h:1440)
     convolve2_gradient_nn                  af_convolve2_gradient_nn (include/af/ml.h:84-92)
+    fft_convolve1 / 2 / 3                  af_fft_convolve1/2/3 (include/af/signal.h:1492,1506,1520)
     unwrap / wrap / wrap_v2                af_unwrap / af_wrap / af_wrap_v2 (include/af/image.h:1483,1524,1570)
 
 Arrays are ``Array`` handles over device memory with ArrayFire dims
@@ -268,6 +269,18 @@ def convolve2_separable(col_filter: Array, row_filter: Array, signal: Array,
                         mode=AF_CONV_DEFAULT) -> Array:
     return _out_call(lib().af_convolve2_sep, col_filter.handle, row_filter.handle, signal.handle,
                      mode)
+
+
+def fft_convolve1(signal: Array, filter: Array, mode=AF_CONV_DEFAULT) -> Array:
+    return _out_call(lib().af_fft_convolve1, signal.handle, filter.handle, mode)
+
+
+def fft_convolve2(signal: Array, filter: Array, mode=AF_CONV_DEFAULT) -> Array:
+    return _out_call(lib().af_fft_convolve2, signal.handle, filter.handle, mode)
+
+
+def fft_convolve3(signal: Array, filter: Array, mode=AF_CONV_DEFAULT) -> Array:
+    return _out_call(lib().af_fft_convolve3, signal.handle, filter.handle, mode)
 
 
 def _dimargs(v: Sequence[int]):

@@ -48,6 +48,9 @@ SIGNATURES = [
     ("af_convolve2_gradient_nn", af_err, [ctypes.POINTER(af_array), af_array, af_array, af_array,
                                           af_array, ctypes.c_uint, _DP, ctypes.c_uint, _DP,
                                           ctypes.c_uint, _DP, ctypes.c_int]),
+    ("af_fft_convolve1", af_err, [ctypes.POINTER(af_array), af_array, af_array, ctypes.c_int]),
+    ("af_fft_convolve2", af_err, [ctypes.POINTER(af_array), af_array, af_array, ctypes.c_int]),
+    ("af_fft_convolve3", af_err, [ctypes.POINTER(af_array), af_array, af_array, ctypes.c_int]),
     ("af_unwrap", af_err, [ctypes.POINTER(af_array), af_array] + [dim_t] * 6 + [ctypes.c_bool]),
     ("af_wrap", af_err, [ctypes.POINTER(af_array), af_array] + [dim_t] * 8 + [ctypes.c_bool]),
     ("af_wrap_v2", af_err, [ctypes.POINTER(af_array), af_array] + [dim_t] * 8 + [ctypes.c_bool]),

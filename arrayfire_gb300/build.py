@@ -28,6 +28,7 @@ SOURCES = [
     "nn_simt.cu",
     "nn_tc.cu",
     "unwrap_wrap.cu",
+    "fft_conv.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -74,7 +75,7 @@ def build(verbose: bool = False) -> Path:
     if LIB.exists() and all(LIB.stat().st_mtime >= o.stat().st_mtime for o in objs):
         return LIB
     cmd = [_nvcc(), "-shared", "-o", str(LIB)] + [str(o) for o in objs] + ARCH + [
-        "-cudart", "static", "-Xcompiler", "-fPIC"]
+        "-cudart", "static", "-Xcompiler", "-fPIC", "-ldl"]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

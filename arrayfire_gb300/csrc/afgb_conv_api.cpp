@@ -120,21 +120,31 @@ static af_err convolve_rank(af_array *out, const af_array signal, const af_array
     return AF_SUCCESS;
 }
 
+// fft_convolve of src/api/c/fftconvolve.cpp:154-237: batch kind of the rank,
+// then the signal's type (f16 is not accepted)
+static af_err fft_convolve_impl(af_array *out, const af_array signal, const af_array filter,
+                                bool expand, int rank) {
+    Array *s = get_array(signal);
+    Array *f = get_array(filter);
+    const int kind = identify_batch_kind(rank, s->dims, f->dims);
+    AFGB_ARG_ASSERT(1, (kind != BATCH_UNSUPPORTED));
+    const af_dtype st = s->type;
+    if (st == f16 || !dtype_valid(st)) AFGB_TYPE_ERROR(1, st);
+    if (f->type == f16 || !dtype_valid(f->type)) AFGB_TYPE_ERROR(2, f->type);
+    Array o = fft_convolve(*s, *f, expand, rank, kind);
+    *out = make_handle(&o);
+    return AF_SUCCESS;
+}
+
 static af_err convolve_domain(af_array *out, const af_array signal, const af_array filter,
                               af_conv_mode mode, af_conv_domain domain, int rank) {
     Array *s = get_array(signal);
     Array *f = get_array(filter);
     if (reference_picks_freq(rank, s->dims, f->dims, domain)) {
-        // The frequency-domain path (af_fft_convolve*) is not part of this
-        // library.  AUTO falls back to the spatial kernels when they accept
-        // the filter (floating results then differ from the reference's FFT
-        // result by rounding only); FREQ, DIFF batches and filters beyond the
-        // spatial limits are reported as not supported.
-        bool diff = identify_batch_kind(rank, s->dims, f->dims) == BATCH_DIFF;
-        if (domain == AF_CONV_FREQ || diff || !spatial_supported(rank, f->dims)) {
-            AFGB_THROW(AF_ERR_NOT_SUPPORTED,
-                       "frequency-domain convolution is not built in this library; "
-                       "use AF_CONV_SPATIAL with a supported filter size");
+        switch (rank) {  // src/api/c/convolve.cpp:220-252
+            case 1: return af_fft_convolve1(out, signal, filter, mode);
+            case 2: return af_fft_convolve2(out, signal, filter, mode);
+            default: return af_fft_convolve3(out, signal, filter, mode);
         }
     }
     return convolve_rank(out, signal, filter, mode, rank);
@@ -517,6 +527,31 @@ af_err afgb_convolve2_gradients_nn(af_array *data_grad, af_array *filter_grad,
     return convolve2_grads_impl(data_grad, filter_grad, bias_grad, incoming_gradient,
                                 original_signal, original_filter, stride_dims, strides,
                                 padding_dims, paddings, dilation_dims, dilations, precision);
+    AFGB_CATCHALL
+}
+
+af_err af_fft_convolve1(af_array *out, const af_array signal, const af_array filter,
+                        const af_conv_mode mode) {
+    AFGB_TRY
+    return fft_convolve_impl(out, signal, filter, mode == AF_CONV_EXPAND, 1);
+    AFGB_CATCHALL
+}
+
+af_err af_fft_convolve2(af_array *out, const af_array signal, const af_array filter,
+                        const af_conv_mode mode) {
+    AFGB_TRY
+    const bool low = dim4_ndims(get_array(signal)->dims) < 2 &&
+                     dim4_ndims(get_array(filter)->dims) < 2;
+    return fft_convolve_impl(out, signal, filter, mode == AF_CONV_EXPAND, low ? 1 : 2);
+    AFGB_CATCHALL
+}
+
+af_err af_fft_convolve3(af_array *out, const af_array signal, const af_array filter,
+                        const af_conv_mode mode) {
+    AFGB_TRY
+    const bool low = dim4_ndims(get_array(signal)->dims) < 3 &&
+                     dim4_ndims(get_array(filter)->dims) < 3;
+    return fft_convolve_impl(out, signal, filter, mode == AF_CONV_EXPAND, low ? 2 : 3);
     AFGB_CATCHALL
 }
 

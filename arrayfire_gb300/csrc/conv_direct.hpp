@@ -32,6 +32,10 @@ void patches_unwrap(const Array &in, Array &out, long long wx, long long wy, lon
 void patches_wrap(const Array &in, Array &out, long long wx, long long wy, long long sx,
                   long long sy, long long px, long long py, bool is_column, bool zero_init);
 
+// Frequency-domain convolution (fft_conv.cu) of rank 1..3 with the batch kind
+// of the rank (not UNSUPPORTED); the reference's af_fft_convolve semantics.
+Array fft_convolve(const Array &sig, const Array &filt, bool expand, int rank, int kind);
+
 // out = T( s * (c * r) ) element-wise: the scalar-filter shortcut of
 // af_convolve2_sep (src/api/c/convolve.cpp:57-68).
 void launch_sep_scalar(const Array &sig, const Array &cfilt, const Array &rfilt, Array &out);

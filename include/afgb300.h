@@ -150,6 +150,23 @@ AFGB_API af_err af_convolve2_gradient_nn(af_array *out, const af_array incoming_
                                          const unsigned dilation_dims, const dim_t *dilations,
                                          af_conv_gradient_type grad_type);
 
+/* ---- frequency-domain convolution ------------------------------------ */
+
+/* include/af/signal.h:1492 (src/api/c/fftconvolve.cpp:239-242): FFT
+ * convolution of rank 1; every batch kind including DIFF; integer types round
+ * the result (DIFF truncates), as the reference's CPU backend. */
+AFGB_API af_err af_fft_convolve1(af_array *out, const af_array signal, const af_array filter,
+                                 const af_conv_mode mode);
+/* include/af/signal.h:1506 (src/api/c/fftconvolve.cpp:244-254): rank 2, or 1
+ * when both inputs have fewer than 2 dims.  af_convolve2 with AF_CONV_FREQ,
+ * or AF_CONV_AUTO where the reference picks the frequency domain, calls this. */
+AFGB_API af_err af_fft_convolve2(af_array *out, const af_array signal, const af_array filter,
+                                 const af_conv_mode mode);
+/* include/af/signal.h:1520 (src/api/c/fftconvolve.cpp:256-266): rank 3, or 2
+ * when both inputs have fewer than 3 dims. */
+AFGB_API af_err af_fft_convolve3(af_array *out, const af_array signal, const af_array filter,
+                                 const af_conv_mode mode);
+
 /* ---- patch extraction and accumulation (the NN path's unwrap / wrap as
  * public calls; dilation 1) ----------------------------------------------- */
 

@@ -237,6 +237,66 @@ def wrap_dilated(cols: np.ndarray, odims, wx, wy, sx, sy, px, py, dx, dy, which=
 
 
 # ---------------------------------------------------------------------------
+# af_fft_convolve1/2/3 (frequency-domain semantics)
+# ---------------------------------------------------------------------------
+def _round_half_away(x):
+    return np.sign(x) * np.floor(np.abs(x) + 0.5)
+
+
+def fft_convolve(sig: np.ndarray, filt: np.ndarray, dtype: int, rank: int, expand: bool):
+    """What the reference's frequency-domain path returns, computed exactly in
+    FP64 (src/api/c/fftconvolve.cpp:38-152 and src/backend/cpu/fftconvolve.cpp:
+    38-200, kernel/fftconvolve.hpp:179-250):
+
+    * real signal, batch kind NONE/LHS/RHS/SAME: the filter is converted to
+      the signal type first (castArray<T>: integer signals truncate the taps);
+      integer outputs are rounded half away from zero (roundf);
+    * complex signal or DIFF batch (fftconvolve_fallback): the filter keeps its
+      values; the real part (complex value) is converted without rounding;
+    * EXPAND: the full s+f-1 window of the rank dims, DEFAULT: from f//2;
+      batch dims max(s, f).
+    The linear convolution itself is exact here (FP64); the library's FP32
+    transforms agree within rounding."""
+    s = as_af(sig)
+    f = as_af(filt)
+    sd, fd = _dims4(s), _dims4(f)
+    kind = identify_batch_kind(rank, sd, fd)
+    if kind == BATCH_UNSUPPORTED:
+        raise ValueError("unsupported batch")
+    t = NP_OF[dtype]
+    cplx = dtype in (C32, C64)
+    fallback = cplx or kind == BATCH_DIFF
+    if not fallback:
+        f = f.astype(t)  # castArray<T>: C conversion, truncating toward zero
+    sw = s.astype(np.complex128 if cplx else np.float64)
+    fw = f.astype(np.complex128 if (cplx or np.iscomplexobj(f)) else np.float64)
+    full = [sd[k] + fd[k] - 1 for k in range(rank)]
+    axes = tuple(range(rank))
+    Sf = np.fft.fftn(sw, s=full, axes=axes)
+    Ff = np.fft.fftn(fw, s=full, axes=axes)
+    # broadcast batch dims (each is 1 on one side or equal)
+    res = np.fft.ifftn(Sf * Ff, axes=axes)
+    if not (cplx or np.iscomplexobj(fw)):
+        res = res.real
+    elif not cplx:
+        res = res.real
+    sl = []
+    for k in range(4):
+        if k < rank:
+            sl.append(slice(0, full[k]) if expand else slice(fd[k] // 2, fd[k] // 2 + sd[k]))
+        else:
+            sl.append(slice(None))
+    res = res[tuple(sl)]
+    if dtype in (F32, F64, C32, C64):
+        out = res.astype(t)
+    elif fallback:
+        out = np.trunc(res).astype(t)
+    else:
+        out = _round_half_away(res).astype(t)
+    return np.asfortranarray(out)
+
+
+# ---------------------------------------------------------------------------
 # af_unwrap / af_wrap (public form: dilation 1, is_column, every type)
 # ---------------------------------------------------------------------------
 def patch_grid(W, H, wx, wy, sx, sy, px, py):
