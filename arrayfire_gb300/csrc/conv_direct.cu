@@ -589,9 +589,21 @@ __device__ __forceinline__ double real_of(__half v) { return (double)__half2floa
 __device__ __forceinline__ double mag_of(cf32 v) { return (double)hypotf(v.x, v.y); }
 __device__ __forceinline__ double mag_of(cf64 v) { return hypot(v.x, v.y); }
 
+// b8 target: char(v != 0) (src/backend/cpu/cast.hpp:140-155)
+struct BoolByte {
+    signed char v;
+};
+
 template <typename F, typename To> struct CastOp {
     __device__ static To run(F v) {
-        if constexpr (std::is_same<To, float>::value) {
+        if constexpr (std::is_same<To, BoolByte>::value) {
+            if constexpr (std::is_same<F, __half>::value) return BoolByte{(signed char)(__half2float(v) != 0.f)};
+            else return BoolByte{(signed char)(v != F(0))};
+        } else if constexpr (std::is_integral<To>::value) {
+            // C conversion: truncation toward zero for floating sources
+            if constexpr (std::is_same<F, __half>::value) return (To)__half2float(v);
+            else return (To)v;
+        } else if constexpr (std::is_same<To, float>::value) {
             if constexpr (std::is_same<F, __half>::value) return __half2float(v);
             else return (float)v;
         } else if constexpr (std::is_same<To, double>::value) {
@@ -608,14 +620,16 @@ template <typename F, typename To> struct CastOp {
 };
 template <typename To> struct CastOp<cf32, To> {
     __device__ static To run(cf32 v) {
-        if constexpr (std::is_same<To, cf32>::value) return v;
+        if constexpr (std::is_same<To, BoolByte>::value) return BoolByte{(signed char)(v.x != 0.f || v.y != 0.f)};
+        else if constexpr (std::is_same<To, cf32>::value) return v;
         else if constexpr (std::is_same<To, cf64>::value) return cf64{(double)v.x, (double)v.y};
         else return (To)mag_of(v);
     }
 };
 template <typename To> struct CastOp<cf64, To> {
     __device__ static To run(cf64 v) {
-        if constexpr (std::is_same<To, cf64>::value) return v;
+        if constexpr (std::is_same<To, BoolByte>::value) return BoolByte{(signed char)(v.x != 0.0 || v.y != 0.0)};
+        else if constexpr (std::is_same<To, cf64>::value) return v;
         else if constexpr (std::is_same<To, cf32>::value) return cf32{(float)v.x, (float)v.y};
         else return (To)mag_of(v);
     }
@@ -996,6 +1010,15 @@ Array cast_array(const Array &in, af_dtype to) {
         case f64: cast_from<double>(in, out); break;
         case c32: cast_from<cf32>(in, out); break;
         case c64: cast_from<cf64>(in, out); break;
+        case s32: cast_from<int32_t>(in, out); break;
+        case u32: cast_from<uint32_t>(in, out); break;
+        case s64: cast_from<long long>(in, out); break;
+        case u64: cast_from<unsigned long long>(in, out); break;
+        case s16: cast_from<int16_t>(in, out); break;
+        case u16: cast_from<uint16_t>(in, out); break;
+        case s8: cast_from<int8_t>(in, out); break;
+        case u8: cast_from<uint8_t>(in, out); break;
+        case b8: cast_from<BoolByte>(in, out); break;
         default: AFGB_TYPE_ERROR(1, to);
     }
     return out;

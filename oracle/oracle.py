@@ -267,7 +267,9 @@ def fft_convolve(sig: np.ndarray, filt: np.ndarray, dtype: int, rank: int, expan
     cplx = dtype in (C32, C64)
     fallback = cplx or kind == BATCH_DIFF
     if not fallback:
-        f = f.astype(t)  # castArray<T>: C conversion, truncating toward zero
+        # castArray<T>: C conversion, truncating toward zero; b8 is (v != 0)
+        # (src/backend/cpu/cast.hpp:140-155)
+        f = (f != 0).astype(t) if dtype == B8 else f.astype(t)
     sw = s.astype(np.complex128 if cplx else np.float64)
     fw = f.astype(np.complex128 if (cplx or np.iscomplexobj(f)) else np.float64)
     full = [sd[k] + fd[k] - 1 for k in range(rank)]

@@ -41,7 +41,7 @@ def values(dt, shape, seed):
     return np.asfortranarray(g.integers(0, hi, C.af_shape(shape)).astype(C.NP_OF[dt]))
 
 
-@pytest.mark.parametrize("dt", [C.F32, C.F64, C.C32, C.C64, C.S32, C.U8, C.S16, C.U64],
+@pytest.mark.parametrize("dt", [C.F32, C.F64, C.C32, C.C64, C.S32, C.U8, C.S16, C.U64, C.B8],
                          ids=lambda d: C.DT_NAME[d])
 @pytest.mark.parametrize("rank,sd,fd", SHAPES, ids=lambda v: str(v).replace(" ", ""))
 @pytest.mark.parametrize("expand", [False, True])
