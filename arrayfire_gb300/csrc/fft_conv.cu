@@ -487,6 +487,7 @@ Array fft_convolve(const Array &sig, const Array &filt, bool expand, int rank, i
 
     const bool integral = !(T == f32 || T == f64 || is_cplx(T));
     const int mode = integral ? (fallback ? CROP_TRUNC : CROP_ROUND) : CROP_PLAIN;
+    KernelTimer kt("fft_pipeline");  // pads, transforms, product and crop
     if (complex_path) {
         if (dbl) run_complex<cf64>(s, f, out, g, expand, mode, CUFFT_Z2Z);
         else run_complex<cf32>(s, f, out, g, expand, mode, CUFFT_C2C);

@@ -491,6 +491,13 @@ def run_direct_workloads(af, peaks, args) -> dict:
     measure("same7x7_f32_64x2048x2048",
             lambda: af.convolve2(S, F7, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL),
             n * 8 + f7.size * 4, ("conv2_tma_kernel", "conv2_tile_kernel"))
+    # a 31x31 filter: AUTO takes the frequency-domain route (the whole
+    # pipeline is timed: pads, cuFFT transforms, spectrum product, crop)
+    f31 = g.standard_normal((31, 31))
+    F31 = af.Array.from_numpy(np.asfortranarray((f31 / f31.sum()).astype(np.float32)))
+    measure("fft31x31_f32_64x2048x2048",
+            lambda: af.convolve2(S, F31, af.AF_CONV_DEFAULT, af.AF_CONV_AUTO),
+            n * 8 + 31 * 31 * 4, ("fft_pipeline",))
     del S, xs
     # 256^3 volume, 3x3x3
     v = torch.rand(256, 256, 256, device="cuda")
