@@ -116,26 +116,55 @@ void cufft_check(cufftResult r, const char *what) {
                    std::string("cuFFT ") + what + " failed (" + std::to_string((int)r) + ")");
 }
 
-// plans by (rank, sizes, batch, type), kept for reuse
+// plans by (rank, sizes, batch, type), kept for reuse.  Each convolution
+// starts a new epoch; when the cache is full, plans not used in the current
+// epoch are destroyed (never one the running convolution already holds).
+struct PlanEntry {
+    cufftHandle h;
+    unsigned long long epoch;
+};
 std::mutex plan_mu;
-std::map<std::tuple<int, int, int, int, int, int>, cufftHandle> plans;
+std::map<std::tuple<int, int, int, int, int, int>, PlanEntry> plans;
+unsigned long long plan_epoch = 0;
+constexpr size_t kMaxPlans = 16;
 
-cufftHandle get_plan(int rank, const int *n_fast_first, int batch, cufftType type) {
+// one frequency-domain convolution at a time per process: a plan's stream
+// binding and its execution stay together, and no other call evicts the plans
+// a running convolution holds (the work itself is asynchronous, so this only
+// serialises host-side enqueueing)
+std::mutex fft_call_mu;
+
+unsigned long long begin_plan_epoch() {
+    std::lock_guard<std::mutex> lk(plan_mu);
+    return ++plan_epoch;
+}
+
+cufftHandle get_plan(int rank, const int *n_fast_first, int batch, cufftType type,
+                     unsigned long long epoch) {
     std::lock_guard<std::mutex> lk(plan_mu);
     auto key = std::make_tuple(rank, n_fast_first[0], n_fast_first[1], n_fast_first[2], batch,
                                (int)type);
     auto it = plans.find(key);
-    if (it != plans.end()) return it->second;
+    if (it != plans.end()) {
+        it->second.epoch = epoch;
+        return it->second.h;
+    }
     CufftApi &api = cufft();
-    if (plans.size() >= 32) {  // bounded: drop every cached plan
-        for (auto &kv : plans) api.destroy(kv.second);
-        plans.clear();
+    if (plans.size() >= kMaxPlans) {
+        for (auto e = plans.begin(); e != plans.end();) {
+            if (e->second.epoch != epoch) {
+                api.destroy(e->second.h);
+                e = plans.erase(e);
+            } else {
+                ++e;
+            }
+        }
     }
     int n[3];
     for (int k = 0; k < rank; ++k) n[k] = n_fast_first[rank - 1 - k];  // cuFFT: slowest first
     cufftHandle h;
     cufft_check(api.plan_many(&h, rank, n, nullptr, 1, 0, nullptr, 1, 0, type, batch), "plan");
-    plans[key] = h;
+    plans[key] = PlanEntry{h, epoch};
     return h;
 }
 
@@ -271,6 +300,7 @@ struct Scratch {
 namespace {
 
 struct FftGeom {
+    unsigned long long epoch;  // plan-cache epoch of this convolution
     int rank;
     long long n[3];       // transform sizes, fastest first (1 beyond rank)
     long long nreal, ncplx;  // elements per slice: real input, spectrum
@@ -357,8 +387,8 @@ void run_real(const Array &s, const Array &f, Array &out, const FftGeom &g, bool
     pad_into<R>(s, sreal.as<R>(), g, g.sb);
     pad_into<R>(f, freal.as<R>(), g, g.fb);
     const int nf[3] = {(int)g.n[0], (int)g.n[1], (int)g.n[2]};
-    cufftHandle ps = get_plan(g.rank, nf, (int)g.sb, fwd);
-    cufftHandle pf = get_plan(g.rank, nf, (int)g.fb, fwd);
+    cufftHandle ps = get_plan(g.rank, nf, (int)g.sb, fwd, g.epoch);
+    cufftHandle pf = get_plan(g.rank, nf, (int)g.fb, fwd, g.epoch);
     cufft_check(api.set_stream(ps, stream()), "set stream");
     cufft_check(api.set_stream(pf, stream()), "set stream");
     if constexpr (std::is_same<R, float>::value) {
@@ -381,7 +411,7 @@ void run_real(const Array &s, const Array &f, Array &out, const FftGeom &g, bool
     C *P = s_is_out ? sspec.as<C>() : (f_is_out ? fspec.as<C>() : pspec.as<C>());
     R *oreal = s_is_out ? sreal.as<R>() : (f_is_out ? freal.as<R>() : obuf.as<R>());
     multiply<C>(sspec.as<C>(), fspec.as<C>(), P, g);
-    cufftHandle po = get_plan(g.rank, nf, (int)g.ob, inv);
+    cufftHandle po = get_plan(g.rank, nf, (int)g.ob, inv, g.epoch);
     cufft_check(api.set_stream(po, stream()), "set stream");
     if constexpr (std::is_same<R, float>::value)
         cufft_check(api.c2r(po, reinterpret_cast<cufftComplex *>(P), reinterpret_cast<cufftReal *>(oreal)),
@@ -404,8 +434,8 @@ void run_complex(const Array &s, const Array &f, Array &out, const FftGeom &g, b
     pad_into<C>(s, sspec.as<C>(), g, g.sb);
     pad_into<C>(f, fspec.as<C>(), g, g.fb);
     const int nf[3] = {(int)g.n[0], (int)g.n[1], (int)g.n[2]};
-    cufftHandle ps = get_plan(g.rank, nf, (int)g.sb, type);
-    cufftHandle pf = get_plan(g.rank, nf, (int)g.fb, type);
+    cufftHandle ps = get_plan(g.rank, nf, (int)g.sb, type, g.epoch);
+    cufftHandle pf = get_plan(g.rank, nf, (int)g.fb, type, g.epoch);
     cufft_check(api.set_stream(ps, stream()), "set stream");
     cufft_check(api.set_stream(pf, stream()), "set stream");
     auto exec = [&](cufftHandle h, C *in, C *o, int dir) {
@@ -426,7 +456,7 @@ void run_complex(const Array &s, const Array &f, Array &out, const FftGeom &g, b
     Scratch pspec(s_is_out || f_is_out ? 0 : sizeof(C) * g.ncplx * g.ob);
     C *P = s_is_out ? sspec.as<C>() : (f_is_out ? fspec.as<C>() : pspec.as<C>());
     multiply<C>(sspec.as<C>(), fspec.as<C>(), P, g);
-    cufftHandle po = get_plan(g.rank, nf, (int)g.ob, type);
+    cufftHandle po = get_plan(g.rank, nf, (int)g.ob, type, g.epoch);
     cufft_check(api.set_stream(po, stream()), "set stream");
     exec(po, P, P, CUFFT_INVERSE);
     if (mode == CROP_TRUNC) crop_to<C, CROP_TRUNC>(P, out, g, expand, f.dims);
@@ -447,7 +477,9 @@ Array fft_convolve(const Array &sig, const Array &filt, bool expand, int rank, i
     Array s = cast_array(sig, work);
     Array f = fallback ? cast_array(filt, work) : cast_array(cast_array(filt, T), work);
 
+    std::lock_guard<std::mutex> call_lock(fft_call_mu);
     FftGeom g{};
+    g.epoch = begin_plan_epoch();
     g.rank = rank;
     for (int k = 0; k < 3; ++k) g.n[k] = 1;
     for (int k = 0; k < rank; ++k)
