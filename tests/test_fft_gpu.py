@@ -168,3 +168,15 @@ def test_fft_strided_input_and_launches(af, oracle):
     host = np.asfortranarray(base.cpu().numpy().T[::2, :])
     ref = oracle.fft_convolve(host, f, C.F32, 2, False)
     assert np.abs(got - ref).max() <= 1e-5 * bound(host, f, 2, False, oracle)
+
+
+def test_fft_plan_cache_eviction(af, oracle):
+    """More distinct transform shapes than the plan cache holds, twice over:
+    every call keeps the plans it uses while older ones are evicted."""
+    for rep in range(2):
+        for n in range(20, 60, 2):
+            s = C.make_signal(C.F32, (n, 3), n)
+            f = C.make_filter(C.F32, (5,), n + 1, 1)
+            got = af.fft_convolve1(af.Array.from_numpy(s), af.Array.from_numpy(f)).to_numpy()
+            ref = oracle.fft_convolve(s, f, C.F32, 1, False)
+            assert np.abs(got - ref).max() <= 1e-5 * bound(s, f, 1, False, oracle)
