@@ -625,12 +625,13 @@ def run_only(args) -> None:
         t = g.standard_normal(15)
         CF = af.Array.from_numpy((t / t.sum()).astype(np.float32))
         RF = af.Array.from_numpy((t[::-1] / t.sum()).astype(np.float32))
-        if args.only in ("unwrap", "wrap"):
+        if args.only in ("unwrap", "wrap", "unwrap_rows", "wrap_rows"):
             xi = torch.rand(32, 64, 128, 128, device="cuda")
             XI = af.Array.view_torch(xi)
-            U = af.unwrap(XI, 3, 3, 1, 1, 1, 1)
-            fn = ((lambda: af.unwrap(XI, 3, 3, 1, 1, 1, 1)) if args.only == "unwrap" else
-                  (lambda: af.wrap(U, 128, 128, 3, 3, 1, 1, 1, 1)))
+            col = not args.only.endswith("_rows")
+            U = af.unwrap(XI, 3, 3, 1, 1, 1, 1, col)
+            fn = ((lambda: af.unwrap(XI, 3, 3, 1, 1, 1, 1, col)) if args.only.startswith("unwrap")
+                  else (lambda: af.wrap(U, 128, 128, 3, 3, 1, 1, 1, 1, col)))
         elif args.only == "conv3":
             v = torch.rand(256, 256, 256, device="cuda")
             V = af.Array.view_torch(v)
@@ -680,7 +681,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--only", default=None,
                     choices=["fwd", "dgrad", "wgrad", "sep_f32", "sep_u8", "same7", "conv3", "cnn",
-                             "unwrap", "wrap"],
+                             "unwrap", "wrap", "unwrap_rows", "wrap_rows"],
                     help="run one operation of the workload --steps times after --warmup "
                          "(for profiler captures); prints its timing, not the bench line")
     args = ap.parse_args()
