@@ -11,6 +11,7 @@ same names, argument meaning and error codes:
     convolve2_gradient_nn                  af_convolve2_gradient_nn (include/af/ml.h:84-92)
     fft_convolve1 / 2 / 3                  af_fft_convolve1/2/3 (include/af/signal.h:1492,1506,1520)
     unwrap / wrap / wrap_v2                af_unwrap / af_wrap / af_wrap_v2 (include/af/image.h:1483,1524,1570)
+    gaussian_kernel / dog / sobel_operator af_gaussian_kernel, af_dog, af_sobel_operator
 
 Arrays are ``Array`` handles over device memory with ArrayFire dims
 (d0 fastest).  ``Array.from_numpy`` takes a numpy array laid out in
@@ -330,6 +331,22 @@ def convolve2_gradients_nn(incoming_gradient: Array, original_signal: Array,
         original_signal.handle, original_filter.handle, sn, sp, pn, pp, dn, dp,
         PRECISION[precision]))
     return tuple(Array(o.value) if o is not None else None for o in outs)
+
+
+def gaussian_kernel(rows: int, cols: int, sigma_r: float = 0.0, sigma_c: float = 0.0) -> Array:
+    out = af_array()
+    _check(lib().af_gaussian_kernel(ctypes.byref(out), rows, cols, sigma_r, sigma_c))
+    return Array(out.value)
+
+
+def dog(image: Array, radius1: int, radius2: int) -> Array:
+    return _out_call(lib().af_dog, image.handle, radius1, radius2)
+
+
+def sobel_operator(image: Array, ker_size: int = 3):
+    dx, dy = af_array(), af_array()
+    _check(lib().af_sobel_operator(ctypes.byref(dx), ctypes.byref(dy), image.handle, ker_size))
+    return Array(dx.value), Array(dy.value)
 
 
 def unwrap(signal: Array, wx: int, wy: int, sx: int, sy: int, px: int = 0, py: int = 0,

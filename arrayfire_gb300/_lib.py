@@ -51,6 +51,11 @@ SIGNATURES = [
     ("af_fft_convolve1", af_err, [ctypes.POINTER(af_array), af_array, af_array, ctypes.c_int]),
     ("af_fft_convolve2", af_err, [ctypes.POINTER(af_array), af_array, af_array, ctypes.c_int]),
     ("af_fft_convolve3", af_err, [ctypes.POINTER(af_array), af_array, af_array, ctypes.c_int]),
+    ("af_gaussian_kernel", af_err, [ctypes.POINTER(af_array), ctypes.c_int, ctypes.c_int,
+                                    ctypes.c_double, ctypes.c_double]),
+    ("af_dog", af_err, [ctypes.POINTER(af_array), af_array, ctypes.c_int, ctypes.c_int]),
+    ("af_sobel_operator", af_err, [ctypes.POINTER(af_array), ctypes.POINTER(af_array), af_array,
+                                   ctypes.c_uint]),
     ("af_unwrap", af_err, [ctypes.POINTER(af_array), af_array] + [dim_t] * 6 + [ctypes.c_bool]),
     ("af_wrap", af_err, [ctypes.POINTER(af_array), af_array] + [dim_t] * 8 + [ctypes.c_bool]),
     ("af_wrap_v2", af_err, [ctypes.POINTER(af_array), af_array] + [dim_t] * 8 + [ctypes.c_bool]),

@@ -29,6 +29,7 @@ SOURCES = [
     "nn_tc.cu",
     "unwrap_wrap.cu",
     "fft_conv.cu",
+    "image_ops.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

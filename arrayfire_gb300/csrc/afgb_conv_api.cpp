@@ -555,6 +555,60 @@ af_err af_fft_convolve3(af_array *out, const af_array signal, const af_array fil
     AFGB_CATCHALL
 }
 
+af_err af_gaussian_kernel(af_array *out, const int rows, const int cols, const double sigma_r,
+                          const double sigma_c) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    AFGB_DIM_ASSERT(1, rows >= 0);
+    AFGB_DIM_ASSERT(2, cols >= 0);
+    Array g = gaussian_kernel(rows, cols, sigma_r, sigma_c);
+    *out = make_handle(&g);
+    AFGB_CATCHALL
+}
+
+// src/api/c/dog.cpp:56-85
+af_err af_dog(af_array *out, const af_array in, const int radius1, const int radius2) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    Array *a = get_array(in);
+    const dim_t nd = dim4_ndims(a->dims);
+    AFGB_ARG_ASSERT(1, (nd >= 2));
+    AFGB_ARG_ASSERT(1, (nd <= 3));
+    switch (a->type) {
+        case f32: case f64: case b8: case s32: case u32: case s16: case u16: case s8: case u8:
+            break;
+        default: AFGB_TYPE_ERROR(1, a->type);
+    }
+    AFGB_DIM_ASSERT(2, radius1 >= 0);
+    AFGB_DIM_ASSERT(3, radius2 >= 0);
+    Array o = dog(*a, radius1, radius2);
+    *out = make_handle(&o);
+    AFGB_CATCHALL
+}
+
+// src/api/c/sobel.cpp:38-87: dx, dy of the input's type for f32/f64/s32,
+// s32 for the other integer types
+af_err af_sobel_operator(af_array *dx, af_array *dy, const af_array img, const unsigned ker_size) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(4, (ker_size == 3));
+    AFGB_ARG_ASSERT(0, dx != nullptr && dy != nullptr);
+    Array *a = get_array(img);
+    AFGB_DIM_ASSERT(3, (dim4_ndims(a->dims) >= 2));
+    af_dtype ot;
+    switch (a->type) {
+        case f32: ot = f32; break;
+        case f64: ot = f64; break;
+        case s32: case u32: case s16: case u16: case b8: case s8: case u8: ot = s32; break;
+        default: AFGB_TYPE_ERROR(1, a->type);
+    }
+    Array ox = *create_array(ot, a->dims);
+    Array oy = *create_array(ot, a->dims);
+    sobel_3x3(*a, ox, oy);
+    *dx = make_handle(&ox);
+    *dy = make_handle(&oy);
+    AFGB_CATCHALL
+}
+
 af_err af_unwrap(af_array *out, const af_array in, const dim_t wx, const dim_t wy, const dim_t sx,
                  const dim_t sy, const dim_t px, const dim_t py, const bool is_column) {
     AFGB_TRY

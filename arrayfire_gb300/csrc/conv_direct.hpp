@@ -36,6 +36,13 @@ void patches_wrap(const Array &in, Array &out, long long wx, long long wy, long 
 // of the rank (not UNSUPPORTED); the reference's af_fft_convolve semantics.
 Array fft_convolve(const Array &sig, const Array &filt, bool expand, int rank, int kind);
 
+// Image-processing callers (image_ops.cu): the (rows x cols) f32 Gaussian of
+// af_gaussian_kernel; af_dog's difference of Gaussian-blurred images; the 3x3
+// Sobel derivatives of af_sobel_operator into dense dx, dy of the output type.
+Array gaussian_kernel(int rows, int cols, double sigma_r, double sigma_c);
+Array dog(const Array &in, int radius1, int radius2);
+void sobel_3x3(const Array &img, Array &dx, Array &dy);
+
 // out = T( s * (c * r) ) element-wise: the scalar-filter shortcut of
 // af_convolve2_sep (src/api/c/convolve.cpp:57-68).
 void launch_sep_scalar(const Array &sig, const Array &cfilt, const Array &rfilt, Array &out);

@@ -167,6 +167,22 @@ AFGB_API af_err af_fft_convolve2(af_array *out, const af_array signal, const af_
 AFGB_API af_err af_fft_convolve3(af_array *out, const af_array signal, const af_array filter,
                                  const af_conv_mode mode);
 
+/* ---- image-processing callers of the convolution path ------------------ */
+
+/* include/af/image.h:1404 (src/api/c/gaussian_kernel.cpp:29-99): rows x cols
+ * f32 Gaussian, sigma <= 0 meaning a quarter of the size, normalised to unit
+ * sum. */
+AFGB_API af_err af_gaussian_kernel(af_array *out, const int rows, const int cols,
+                                   const double sigma_r, const double sigma_c);
+/* include/af/vision.h:635 (src/api/c/dog.cpp:30-85): difference of the input
+ * convolved with the (2r1+1)^2 and (2r2+1)^2 Gaussians (DEFAULT mode); 2-D or
+ * 3-D input (LHS batch), f32 result (f64 for f64). */
+AFGB_API af_err af_dog(af_array *out, const af_array in, const int radius1, const int radius2);
+/* include/af/image.h:1340 (src/api/c/sobel.cpp:38-87): 3x3 Sobel derivatives
+ * with reflect-101 borders; ker_size must be 3. */
+AFGB_API af_err af_sobel_operator(af_array *dx, af_array *dy, const af_array img,
+                                  const unsigned ker_size);
+
 /* ---- patch extraction and accumulation (the NN path's unwrap / wrap as
  * public calls; dilation 1) ----------------------------------------------- */
 

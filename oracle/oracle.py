@@ -299,6 +299,78 @@ def fft_convolve(sig: np.ndarray, filt: np.ndarray, dtype: int, rank: int, expan
 
 
 # ---------------------------------------------------------------------------
+# image-processing callers: af_gaussian_kernel, af_dog, af_sobel_operator
+# ---------------------------------------------------------------------------
+SOBEL_OUT = {F32: F32, F64: F64, S32: S32, U32: S32, S16: S32, U16: S32, B8: S32, S8: S32,
+             U8: S32}
+
+
+def gaussian_kernel(rows: int, cols: int, sigma_r: float = 0.0, sigma_c: float = 0.0):
+    """src/api/c/gaussian_kernel.cpp:29-88, in FP64: exp(-((j - (cols-1)/2)/sc)^2/2
+    - ((i - (rows-1)/2)/sr)^2/2) normalised to unit sum, sc = sigma_c or cols/4."""
+    i = np.arange(rows, dtype=np.float64)[:, None]
+    j = np.arange(cols, dtype=np.float64)[None, :]
+    tmp = np.zeros((rows, cols))
+    if cols > 1:
+        sc = sigma_c if sigma_c > 0 else 0.25 * cols
+        tmp = tmp + ((j - (cols - 1) / 2.0) / sc) ** 2
+    if rows > 1:
+        sr = sigma_r if sigma_r > 0 else 0.25 * rows
+        tmp = tmp + ((i - (rows - 1) / 2.0) / sr) ** 2
+    g = np.exp(-0.5 * tmp)
+    return np.asfortranarray(g / g.sum())
+
+
+def dog(img: np.ndarray, dtype: int, r1: int, r2: int):
+    """src/api/c/dog.cpp:30-54: convolve2 DEFAULT with the two Gaussians in the
+    accumulator type (f64 for f64, else f32), then the difference."""
+    acc = F64 if dtype == F64 else F32
+    x = as_af(img).astype(NP_OF[acc])
+    g1 = gaussian_kernel(2 * r1 + 1, 2 * r1 + 1).astype(NP_OF[acc])
+    g2 = gaussian_kernel(2 * r2 + 1, 2 * r2 + 1).astype(NP_OF[acc])
+    a = convolve(np.asfortranarray(x), np.asfortranarray(g1), acc, 2, False)
+    b = convolve(np.asfortranarray(x), np.asfortranarray(g2), acc, 2, False)
+    return np.asfortranarray(a - b)
+
+
+def _reflect101(idx, end):
+    return np.abs(end - np.abs(end - idx)) if end > 0 else np.zeros_like(idx)
+
+
+def sobel(img: np.ndarray, dtype: int, which: str = "port"):
+    """af_sobel_operator, ker_size 3 (src/backend/cpu/kernel/sobel.hpp:19-75):
+    returns (dx, dy) in the output type, each operation rounded in the
+    reference's order."""
+    a = as_af(img)
+    d = _dims4(a)
+    ot = NP_OF[SOBEL_OUT[dtype]]
+    if which == "ref":
+        dx = np.zeros(d, dtype=ot, order="F")
+        dy = np.zeros(d, dtype=ot, order="F")
+        rc = lib("ref").ref_sobel(ctypes.c_int(dtype), dx.ctypes.data_as(_P),
+                                  dy.ctypes.data_as(_P), a.ctypes.data_as(_P), _ll(d))
+        if rc != 0:
+            raise RuntimeError("ref_sobel failed")
+        return dx, dy
+    x = a.astype(ot)
+    i = np.arange(d[0])
+    j = np.arange(d[1])
+    im, ip = _reflect101(i - 1, d[0] - 1), _reflect101(i + 1, d[0] - 1)
+    jm, jp = _reflect101(j - 1, d[1] - 1), _reflect101(j + 1, d[1] - 1)
+
+    def at(ii, jj):
+        return x[ii][:, jj]
+
+    NW, SW, NE, SE = at(im, jm), at(ip, jm), at(im, jp), at(ip, jp)
+    N, S, W, E = at(im, j), at(ip, j), at(i, jm), at(i, jp)
+    two = ot(2)
+    with np.errstate(over="ignore"):
+        dx = ((SW + SE) - (NW + NE)) + two * (S - N)
+        dy = ((NE + SE) - (NW + SW)) + two * (E - W)
+    return np.asfortranarray(dx.astype(ot)), np.asfortranarray(dy.astype(ot))
+
+
+# ---------------------------------------------------------------------------
 # af_unwrap / af_wrap (public form: dilation 1, is_column, every type)
 # ---------------------------------------------------------------------------
 def patch_grid(W, H, wx, wy, sx, sy, px, py):

@@ -18,8 +18,12 @@
  *                           (src/backend/cpu/unwrap.cpp:23-41), every af_unwrap type
  *   ref_wrap_any         -> kernel::wrap_dim<T, is_column> adding into `out`
  *                           (src/backend/cpu/wrap.cpp:24-37), every af_wrap type
+ *   ref_sobel            -> kernel::derivative<Ti, To, isDX> for dx and dy
+ *                           (src/backend/cpu/kernel/sobel.hpp:19-75), every
+ *                           af_sobel_operator type
  */
 #include <kernel/convolve.hpp>
+#include <kernel/sobel.hpp>
 #include <kernel/unwrap.hpp>
 #include <kernel/wrap.hpp>
 
@@ -104,6 +108,17 @@ void wrap_any(void *out, const long long *odims, const void *in, const long long
 }
 }  // namespace
 
+namespace {
+template <typename Ti, typename To>
+void sobel_any(void *dx, void *dy, const void *in, const long long *dims) {
+    Param<To> ox(static_cast<To *>(dx), d4(dims), dense(dims));
+    Param<To> oy(static_cast<To *>(dy), d4(dims), dense(dims));
+    CParam<Ti> i(static_cast<const Ti *>(in), d4(dims), dense(dims));
+    K::derivative<Ti, To, true>(ox, i);
+    K::derivative<Ti, To, false>(oy, i);
+}
+}  // namespace
+
 extern "C" {
 
 // dtype numbering: include/af/defines.h af_dtype
@@ -179,6 +194,25 @@ REF_UNWRAP(ref_unwrap_f64, double)
 REF_WRAP(ref_wrap_dilated_f32, float)
 REF_WRAP(ref_wrap_dilated_f64, double)
 
+
+
+// dtype numbering: include/af/defines.h af_dtype; outputs as af_sobel_operator
+// (src/api/c/sobel.cpp:52-80)
+int ref_sobel(int dtype, void *dx, void *dy, const void *in, const long long *dims) {
+    switch (dtype) {
+        case 0: sobel_any<float, float>(dx, dy, in, dims); break;
+        case 2: sobel_any<double, double>(dx, dy, in, dims); break;
+        case 5: sobel_any<int, int>(dx, dy, in, dims); break;
+        case 6: sobel_any<unsigned, int>(dx, dy, in, dims); break;
+        case 10: sobel_any<short, int>(dx, dy, in, dims); break;
+        case 11: sobel_any<unsigned short, int>(dx, dy, in, dims); break;
+        case 4: sobel_any<char, int>(dx, dy, in, dims); break;
+        case 13: sobel_any<signed char, int>(dx, dy, in, dims); break;
+        case 7: sobel_any<unsigned char, int>(dx, dy, in, dims); break;
+        default: return -1;
+    }
+    return 0;
+}
 
 #define REF_PATCH_TYPES(FN, ...)                                   \
     switch (dtype) {                                               \

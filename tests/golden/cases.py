@@ -291,3 +291,25 @@ def patch_dims(case):
     nx = (W + 2 * px - wx) // sx + 1
     ny = (H + 2 * py - wy) // sy + 1
     return [wx * wy, nx * ny, d2, d3] if col else [nx * ny, wx * wy, d2, d3]
+
+
+# af_sobel_operator: every accepted type on images, batches and small sizes
+SOBEL_DTYPES = [F32, F64, S32, U32, S16, U16, B8, S8, U8]
+SOBEL_SHAPES = [(17, 13), (16, 9, 3), (2, 2), (64, 3, 2, 2), (3, 40)]
+
+
+def sobel_cases():
+    out = []
+    seed = 30000
+    for shape in SOBEL_SHAPES:
+        for dt in SOBEL_DTYPES:
+            seed += 1
+            out.append((f"sobel_{'x'.join(map(str, shape))}_{DT_NAME[dt]}", dt, shape, seed))
+    return out
+
+
+def sobel_input(dt: int, shape, seed: int) -> np.ndarray:
+    x = make_signal(dt, shape, seed)
+    if dt in (F32, F64):
+        x = (x * 10).astype(x.dtype)
+    return np.asfortranarray(x)

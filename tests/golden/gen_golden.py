@@ -13,6 +13,8 @@ Writes, next to this file:
   patches.json SHA-256 of the reference's af_unwrap output, af_wrap of a
                seeded patch matrix into zeros, and af_wrap_v2 into a seeded
                image, for every tests/golden/cases.py:patch_cases case;
+  image.json   SHA-256 of the reference's Sobel derivatives (dx, dy) for every
+               tests/golden/cases.py:sobel_cases case;
   nn.npz       FP64 NN forward / data-gradient / filter-gradient outputs for
                NN_CASES, each cross-checked against the reference's own
                unwrap + GEMM (forward, filter gradient) and wrap_dilated
@@ -68,6 +70,22 @@ def patches() -> None:
                      "wrap": digest(w_ref), "wrap_v2": digest(v_ref)}
     (HERE / "patches.json").write_text(json.dumps(gold, indent=0, sort_keys=True))
     print(f"patches {len(gold)}")
+
+
+def images() -> None:
+    """af_sobel_operator digests from the reference's CPU kernel, with the
+    numpy port asserted bit-identical on every case."""
+    gold = {}
+    for cid, dt, shape, seed in C.sobel_cases():
+        x = C.sobel_input(dt, shape, seed)
+        rx, ry = O.sobel(x, dt, which="ref")
+        px, py = O.sobel(x, dt, which="port")
+        if rx.tobytes(order="F") != px.tobytes(order="F") or \
+                ry.tobytes(order="F") != py.tobytes(order="F"):
+            raise SystemExit(f"port differs from reference on {cid}")
+        gold[cid] = {"dx": digest(rx), "dy": digest(ry)}
+    (HERE / "image.json").write_text(json.dumps(gold, indent=0, sort_keys=True))
+    print(f"image {len(gold)}")
 
 
 def main() -> None:
@@ -151,10 +169,13 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] == ["patches"]:
+    parts = {"patches": patches, "images": images}
+    if sys.argv[1:] and all(a in parts for a in sys.argv[1:]):
         if O.build_ref() is None:
             raise SystemExit("reference source tree not found; golden vectors need it")
-        patches()
+        for a in sys.argv[1:]:
+            parts[a]()
     else:
         main()
         patches()
+        images()
