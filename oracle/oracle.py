@@ -326,8 +326,9 @@ def dog(img: np.ndarray, dtype: int, r1: int, r2: int):
     accumulator type (f64 for f64, else f32), then the difference."""
     acc = F64 if dtype == F64 else F32
     x = as_af(img).astype(NP_OF[acc])
-    g1 = gaussian_kernel(2 * r1 + 1, 2 * r1 + 1).astype(NP_OF[acc])
-    g2 = gaussian_kernel(2 * r2 + 1, 2 * r2 + 1).astype(NP_OF[acc])
+    # af_gaussian_kernel is always f32 (gaussian_kernel.cpp:90-99), cast after
+    g1 = gaussian_kernel(2 * r1 + 1, 2 * r1 + 1).astype(np.float32).astype(NP_OF[acc])
+    g2 = gaussian_kernel(2 * r2 + 1, 2 * r2 + 1).astype(np.float32).astype(NP_OF[acc])
     a = convolve(np.asfortranarray(x), np.asfortranarray(g1), acc, 2, False)
     b = convolve(np.asfortranarray(x), np.asfortranarray(g2), acc, 2, False)
     return np.asfortranarray(a - b)
