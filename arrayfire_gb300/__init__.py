@@ -290,10 +290,19 @@ def _dimargs(v: Sequence[int]):
 
 
 def convolve2_nn(signal: Array, filter: Array, stride=(1, 1), padding=(0, 0), dilation=(1, 1),
-                 precision: str = "fp32", scales: Optional[Array] = None) -> Array:
+                 precision: str = "fp32", scales: Optional[Array] = None,
+                 bias: Optional[Array] = None, relu: bool = False) -> Array:
+    """af_convolve2_nn; `precision`/`scales` select afgb_convolve2_nn_ex, and
+    `bias`/`relu` the fused epilogue of afgb_convolve2_nn_fused."""
     sn, sp = _dimargs(stride)
     pn, pp = _dimargs(padding)
     dn, dp = _dimargs(dilation)
+    if bias is not None or relu:
+        if scales is not None:
+            raise ValueError("scales and a fused epilogue are separate entry points")
+        return _out_call(lib().afgb_convolve2_nn_fused, signal.handle, filter.handle, sn, sp, pn,
+                         pp, dn, dp, PRECISION[precision],
+                         bias.handle if bias is not None else None, 1 if relu else 0)
     if precision == "fp32" and scales is None:
         return _out_call(lib().af_convolve2_nn, signal.handle, filter.handle, sn, sp, pn, pp, dn, dp)
     return _out_call(lib().afgb_convolve2_nn_ex, signal.handle, filter.handle, sn, sp, pn, pp, dn,

@@ -61,6 +61,9 @@ SIGNATURES = [
     ("af_wrap_v2", af_err, [ctypes.POINTER(af_array), af_array] + [dim_t] * 8 + [ctypes.c_bool]),
     ("afgb_convolve2_nn_ex", af_err, [ctypes.POINTER(af_array), af_array, af_array, ctypes.c_uint, _DP,
                                       ctypes.c_uint, _DP, ctypes.c_uint, _DP, ctypes.c_int, af_array]),
+    ("afgb_convolve2_nn_fused", af_err, [ctypes.POINTER(af_array), af_array, af_array, ctypes.c_uint,
+                                         _DP, ctypes.c_uint, _DP, ctypes.c_uint, _DP, ctypes.c_int,
+                                         af_array, ctypes.c_int]),
     ("afgb_convolve2_gradient_nn_ex", af_err, [ctypes.POINTER(af_array), af_array, af_array, af_array,
                                                af_array, ctypes.c_uint, _DP, ctypes.c_uint, _DP,
                                                ctypes.c_uint, _DP, ctypes.c_int, ctypes.c_int]),

@@ -98,9 +98,9 @@ def nn_flops(x_shape, w_shape, stride, padding, dilation) -> float:
 
 
 def _layer(h, w, geom, precision):
+    """conv2_nn + ReLU, the ReLU fused into the convolution's epilogue."""
     s, p, d = geom
-    out = convolve2_nn(_view(h), _view(w), s, p, d, precision=precision).to_torch()
-    return out.relu_()
+    return convolve2_nn(_view(h), _view(w), s, p, d, precision=precision, relu=True).to_torch()
 
 
 def cnn_step(x0: torch.Tensor, weights: Sequence[torch.Tensor], geoms, precision: str = "bf16",

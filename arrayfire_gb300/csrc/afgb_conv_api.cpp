@@ -246,7 +246,8 @@ static af_err convolve2_nn_impl(af_array *out, const af_array signal, const af_a
                                 unsigned stride_dims, const dim_t *strides, unsigned padding_dims,
                                 const dim_t *paddings, unsigned dilation_dims,
                                 const dim_t *dilations, afgb_precision prec,
-                                const af_array scales) {
+                                const af_array scales, const af_array bias = nullptr,
+                                int activation = 0) {
     Array *s = get_array(signal);
     Array *f = get_array(filter);
     NNArgs a = nn_args(stride_dims, strides, padding_dims, paddings, dilation_dims, dilations);
@@ -272,7 +273,19 @@ static af_err convolve2_nn_impl(af_array *out, const af_array signal, const af_a
         scd = sa->is_linear() ? *sa : make_dense(*sa);
         sc = &scd;
     }
-    nn_forward(g, sd, fd, o, prec, sc);
+    NNEpilogue ep;
+    Array bd;
+    if (bias) {
+        Array *ba = get_array(bias);
+        require_type(ba, f32);
+        AFGB_DIM_ASSERT(10, ba->elements() == g.K);
+        if (t != f32) AFGB_TYPE_ERROR(1, t);
+        bd = ba->is_linear() ? *ba : make_dense(*ba);
+        ep.bias = bd.ptr<float>();
+    }
+    ep.relu = activation;
+    if (activation && t != f32) AFGB_TYPE_ERROR(1, t);
+    nn_forward(g, sd, fd, o, prec, sc, (bias || activation) ? &ep : nullptr);
     *out = make_handle(&o);
     return AF_SUCCESS;
 }
@@ -467,6 +480,20 @@ af_err af_convolve2_nn(af_array *out, const af_array signal, const af_array filt
     AFGB_ARG_ASSERT(0, out != nullptr);
     return convolve2_nn_impl(out, signal, filter, stride_dims, strides, padding_dims, paddings,
                              dilation_dims, dilations, AFGB_PRECISION_FP32, nullptr);
+    AFGB_CATCHALL
+}
+
+af_err afgb_convolve2_nn_fused(af_array *out, const af_array signal, const af_array filter,
+                               const unsigned stride_dims, const dim_t *strides,
+                               const unsigned padding_dims, const dim_t *paddings,
+                               const unsigned dilation_dims, const dim_t *dilations,
+                               afgb_precision precision, const af_array bias, int activation) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    if ((int)precision < 0 || (int)precision > 2) AFGB_THROW(AF_ERR_ARG, "unknown precision");
+    AFGB_ARG_ASSERT(11, activation == 0 || activation == 1);
+    return convolve2_nn_impl(out, signal, filter, stride_dims, strides, padding_dims, paddings,
+                             dilation_dims, dilations, precision, nullptr, bias, activation);
     AFGB_CATCHALL
 }
 

@@ -16,8 +16,14 @@ struct NNGeom {
 
 // out[x,y,k,n] = sum_{c,u,v} in[x*sx-px+u*dx, y*sy-py+v*dy, c, n] *
 //                w[fw-1-u, fh-1-v, c, k]   (src/backend/cpu/convolve.cpp:123-158)
+// optional forward epilogue (afgb_convolve2_nn_fused): out = act(conv + bias[k])
+struct NNEpilogue {
+    const float *bias = nullptr;  // K floats on the device, or none
+    int relu = 0;
+};
+
 void nn_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out,
-                afgb_precision prec, const Array *scales);
+                afgb_precision prec, const Array *scales, const NNEpilogue *ep = nullptr);
 // dX = col2im(G * flip(W)^T)   (src/backend/cpu/convolve.cpp:179-211)
 void nn_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &dx,
                   afgb_precision prec);
@@ -41,7 +47,7 @@ void simt_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Arra
 // is outside what the tcgen05 kernels cover (the caller then reports
 // AF_ERR_NOT_SUPPORTED; there is no silent fallback to another precision)
 bool tc_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out,
-                afgb_precision prec, const Array *scales);
+                afgb_precision prec, const Array *scales, const NNEpilogue *ep = nullptr);
 bool tc_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &dx);
 bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw);
 bool tc_data_filter_grads(const NNGeom &g, const Array &grad, const Array &sig, const Array &filt,

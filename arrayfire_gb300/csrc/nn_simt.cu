@@ -805,11 +805,37 @@ static void filter_grad_noalloc(const NNGeom &g, const float *grad, const float 
 // ---------------------------------------------------------------------------
 // precision routing
 // ---------------------------------------------------------------------------
+// out = act(out + bias[k]) over (Wo, Ho, K, N): the epilogue of the SIMT
+// forward, which does not fuse it
+__global__ void bias_act_kernel(float *out, long long plane, long long K, long long total,
+                                const float *bias, int relu) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+         t += (long long)gridDim.x * blockDim.x) {
+        float v = out[t];
+        if (bias) v += bias[(t / plane) % K];
+        if (relu && v < 0.0f) v = 0.0f;
+        out[t] = v;
+    }
+}
+
 void nn_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out,
-                afgb_precision prec, const Array *scales) {
-    if (prec == AFGB_PRECISION_FP32) return simt_forward(g, sig, filt, out);
+                afgb_precision prec, const Array *scales, const NNEpilogue *ep) {
+    if (prec == AFGB_PRECISION_FP32) {
+        simt_forward(g, sig, filt, out);
+        const long long total = out.elements();
+        if (ep && (ep->bias || ep->relu) && total) {
+            if (out.type != f32) AFGB_THROW(AF_ERR_TYPE, "fused epilogues take f32 arrays");
+            const unsigned blocks =
+                (unsigned)std::min<long long>((total + 255) / 256, (long long)num_sms() * 32);
+            bias_act_kernel<<<blocks, 256, 0, stream()>>>(out.ptr<float>(), g.Wo * g.Ho, g.K,
+                                                          total, ep->bias, ep->relu);
+            count_launch();
+            AFGB_POST_LAUNCH("bias_act_kernel");
+        }
+        return;
+    }
     if (out.elements() == 0) return;
-    if (!tc_forward(g, sig, filt, out, prec, scales))
+    if (!tc_forward(g, sig, filt, out, prec, scales, ep))
         AFGB_THROW(AF_ERR_NOT_SUPPORTED, "tensor-core forward does not cover this shape");
 }
 

@@ -63,6 +63,8 @@ struct GatherParams {
     const unsigned char *src;  // [N][SH][SW][SCpad] elements (bf16, or e4m3 bytes)
     float *dst;                // ArrayFire layout (DW, DH, DC, N)
     const float *out_scale;    // FP8: per-output-channel dequantisation factor
+    const float *bias;         // forward: per-output-channel bias added in the epilogue
+    int relu;                  // forward: max(v, 0) in the epilogue
     int SW, SH, SCpad, N;
     int DW, DH, DC;
     int mode;  // 0 forward, 1 data gradient
@@ -322,6 +324,14 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 const int orow = lane >> 2;         // 0..7: channel within a group of 8
                 const int ocol = (lane & 3) * 4;    // pixel offset within the 16
                 const float sc = (FP8 && och < p.DC) ? p.out_scale[och] : 1.0f;
+                const float bi = (p.bias && och < p.DC) ? p.bias[och] : 0.0f;
+                // scale, then the fused bias and ReLU (forward only)
+                auto fin = [&](uint32_t raw) {
+                    float v = sc * __uint_as_float(raw);
+                    if (p.bias) v += bi;
+                    if (p.relu && v < 0.0f) v = 0.0f;
+                    return v;
+                };
                 const int osx = p.mode == 0 ? 1 : p.sx, osy = p.mode == 0 ? 1 : p.sy;
                 for (int cc = half; cc < BN / 16; cc += 2) {
                     uint32_t r[16];
@@ -338,9 +348,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
                         for (int e = 0; e < 4; ++e)
                             *reinterpret_cast<float4 *>(row + ((e ^ ((lane >> 1) & 3)) << 4)) =
-                                make_float4(sc * __uint_as_float(r[4 * e]), sc * __uint_as_float(r[4 * e + 1]),
-                                            sc * __uint_as_float(r[4 * e + 2]),
-                                            sc * __uint_as_float(r[4 * e + 3]));
+                                make_float4(fin(r[4 * e]), fin(r[4 * e + 1]), fin(r[4 * e + 2]),
+                                            fin(r[4 * e + 3]));
                         fence_proxy_async_smem();
                         __syncwarp();
                         if (lane == 0) {
@@ -353,8 +362,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 #pragma unroll
                     for (int e = 0; e < 4; ++e)
                         *reinterpret_cast<float4 *>(stg + lane * EP_PITCH + 4 * e) =
-                            make_float4(sc * __uint_as_float(r[4 * e]), sc * __uint_as_float(r[4 * e + 1]),
-                                        sc * __uint_as_float(r[4 * e + 2]), sc * __uint_as_float(r[4 * e + 3]));
+                            make_float4(fin(r[4 * e]), fin(r[4 * e + 1]), fin(r[4 * e + 2]),
+                                        fin(r[4 * e + 3]));
                     __syncwarp();
                     // BX >= 32 keeps the 16 pixels in one row; (x, y) are
                     // coordinates in the phase grid, output (rx + osx*x, ry + osy*y)
@@ -399,8 +408,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         if (pix0 + e >= ti.npix) break;
                         const long long xo = p.mode == 0 ? X : ti.rx + (long long)p.sx * X;
                         const long long yo = p.mode == 0 ? Y : ti.ry + (long long)p.sy * Y;
-                        p.dst[xo + p.DW * yo + plane * (och + (long long)p.DC * n)] =
-                            (FP8 ? p.out_scale[och] : 1.0f) * __uint_as_float(r[e]);
+                        float v = (FP8 ? p.out_scale[och] : 1.0f) * __uint_as_float(r[e]);
+                        if (p.bias) v += p.bias[och];
+                        if (p.relu && v < 0.0f) v = 0.0f;
+                        p.dst[xo + p.DW * yo + plane * (och + (long long)p.DC * n)] = v;
                         if (++X == ti.MX) {
                             X = 0;
                             if (++Y == ti.MY) {
@@ -1340,7 +1351,8 @@ static size_t gather_smem() {
 // to a multiple of 64 (then img_f32 is not read)
 static void run_gather(const NNGeom &g, int mode, const float *img_f32, const float *w_f32,
                        float *dst, bool fp8 = false, const float *user_wscale = nullptr,
-                       const NNGeom *unfolded = nullptr, const __nv_bfloat16 *img_ready = nullptr) {
+                       const NNGeom *unfolded = nullptr, const __nv_bfloat16 *img_ready = nullptr,
+                       const NNEpilogue *ep = nullptr) {
     const int SW = mode == 0 ? (int)g.W : (int)g.Wo;
     const int SH = mode == 0 ? (int)g.H : (int)g.Ho;
     const int SC = mode == 0 ? (int)g.C : (int)g.K;
@@ -1430,6 +1442,10 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     p.src = static_cast<const unsigned char *>(img);
     p.dst = dst;
     p.out_scale = fp8 ? scales + 1 + g.K : nullptr;
+    if (ep && mode == 0) {
+        p.bias = ep->bias;
+        p.relu = ep->relu;
+    }
     p.SW = SW;
     p.SH = SH;
     p.SCpad = SCpad;
@@ -1553,20 +1569,22 @@ unsigned int tc_take_error() {
 }
 
 bool tc_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out,
-                afgb_precision prec, const Array *scales) {
+                afgb_precision prec, const Array *scales, const NNEpilogue *ep) {
     if (sig.type != f32 || !gather_fits(g, 0)) return false;
     if (prec == AFGB_PRECISION_FP8_E4M3) {
         run_gather(g, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>(), true,
-                   scales ? scales->ptr<float>() : nullptr);
+                   scales ? scales->ptr<float>() : nullptr, nullptr, nullptr, ep);
         return true;
     }
     if (prec != AFGB_PRECISION_BF16) return false;
     if (foldable(g)) {
         const NNGeom f = folded_geometry(g);
-        run_gather(f, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>(), false, nullptr, &g);
+        run_gather(f, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>(), false, nullptr, &g,
+                   nullptr, ep);
         return true;
     }
-    run_gather(g, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>());
+    run_gather(g, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>(), false, nullptr,
+               nullptr, nullptr, ep);
     return true;
 }
 

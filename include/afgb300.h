@@ -227,6 +227,19 @@ AFGB_API af_err afgb_convolve2_nn_ex(af_array *out, const af_array signal, const
                                      const unsigned dilation_dims, const dim_t *dilations,
                                      afgb_precision precision, const af_array out_channel_scales);
 
+/* Extension: afgb_convolve2_nn_ex without scales, with a fused
+ * epilogue: out = act(conv + bias[k]).  `bias` is 0 or an f32 array of K
+ * elements; `activation` is 0 (none) or 1 (ReLU, max(v, 0) leaving NaN).  On
+ * the tensor-core paths the bias and ReLU are applied in the kernel epilogue
+ * before the output is stored; the FP32 path applies them in one extra pass.
+ * f32 arrays only. */
+AFGB_API af_err afgb_convolve2_nn_fused(af_array *out, const af_array signal,
+                                       const af_array filter, const unsigned stride_dims,
+                                       const dim_t *strides, const unsigned padding_dims,
+                                       const dim_t *paddings, const unsigned dilation_dims,
+                                       const dim_t *dilations, afgb_precision precision,
+                                       const af_array bias, int activation);
+
 /* af_convolve2_gradient_nn with a precision knob and a real bias gradient:
  * AF_CONV_GRADIENT_BIAS returns db[k] = sum_{x,y,n} g[x,y,k,n] as a
  * 1x1xKx1 array (FP32 compensated pairwise sum in a fixed order). */
