@@ -35,7 +35,6 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
-#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -70,7 +69,6 @@ struct GatherParams {
     int DW, DH, DC;
     int mode;  // 0 forward, 1 data gradient
     int tma_store;  // epilogue writes by TMA through the output map (unit-stride outputs)
-    int swap;       // data gradient with DC <= 64: pixels on the MMA's M, channels on N
     int sx, sy, px, py, dx, dy, fw;
     int nchunk;       // SCpad / 64
     int n_och_tiles;  // ceil(DC / 128)
@@ -319,30 +317,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
             if (!mbar_wait(&sm->tmem_full[b], (acc_it >> 1) & 1, abort, 2u)) break;
             tc_fence_after();
             const uint32_t taddr = tmem_base + (uint32_t)(b * BN) + ((uint32_t)(32 * q) << 16);
-            if (TMA_B && p.swap) {
-                // TMEM lane = pixel 128*half + 32*q + lane of the rectangle,
-                // columns 64*half + channel: each store instruction writes 32
-                // consecutive pixels of one channel row
-                const int rpix = 128 * half + 32 * q + lane;
-                const int X = ti.x0 + rpix % p.BX, Y = ti.y0 + rpix / p.BX;
-                const bool valid = X < ti.MX && Y < ti.MY;
-                const long long xo = ti.rx + (long long)p.sx * X;
-                const long long yo = ti.ry + (long long)p.sy * Y;
-                float *d0 = p.dst + xo + (long long)p.DW * yo + plane * ((long long)p.DC * ti.n);
-#pragma unroll 1
-                for (int cc = 0; cc < 4; ++cc) {
-                    uint32_t r[16];
-                    tmem_ld16(taddr + (uint32_t)(64 * half + 16 * cc), r);
-                    tmem_ld_wait();
-                    if (valid) {
-#pragma unroll
-                        for (int e = 0; e < 16; ++e) {
-                            const int c = 16 * cc + e;
-                            if (c < p.DC) d0[plane * c] = __uint_as_float(r[e]);
-                        }
-                    }
-                }
-            } else if (TMA_B) {
+            if (TMA_B) {
                 // 32 channels x 16 pixels at a time: TMEM -> registers -> this
                 // warp's shared staging block -> 64-byte row pieces per channel
                 float *stg = ep_stage + warp * EP_SLOT;
@@ -457,10 +432,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     } else if (warp == 8) {
         // ---------------- MMA issuer
         if (lane == 0) {
-            // swapped roles (p.swap): two M=128 pixel halves of the B tile
-            // against the first 64 rows of the weight tile, N = 64 channels
-            const uint32_t idesc = FP8 ? idesc_e4m3(BM, BN)
-                                       : (p.swap ? idesc_bf16(128, 64, 0, 0) : idesc_bf16(BM, BN, 0, 0));
+            const uint32_t idesc = FP8 ? idesc_e4m3(BM, BN) : idesc_bf16(BM, BN, 0, 0);
             // descriptors: precomputed bases plus 16-byte-unit offsets (the
             // issuing thread is latency-bound on its scalar work)
             const uint64_t a0 = smem_desc(smem_u32(a_stage), 16, 1024);
@@ -489,15 +461,10 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                     for (int k = 0; k < 4; ++k) {  // 4 x 32 bytes of K per stage
                         const uint64_t ad = as + (uint32_t)(2 * k);
                         const uint64_t bd = bs + (uint32_t)(2 * k);
-                        if (FP8) {
+                        if (FP8)
                             mma_f8(d_tmem, ad, bd, idesc, (kb | k) != 0);
-                        } else if (p.swap) {
-                            mma_f16(d_tmem, bd, ad, idesc, (kb | k) != 0);
-                            mma_f16(d_tmem + 64, bd + (uint32_t)((128 * 128) >> 4), ad, idesc,
-                                    (kb | k) != 0);
-                        } else {
+                        else
                             mma_f16(d_tmem, ad, bd, idesc, (kb | k) != 0);
-                        }
                     }
                     mma_commit(&sm->empty[s]);
                     issued = true;
@@ -1382,16 +1349,6 @@ static size_t gather_smem() {
 // image and filter are folded from the f32 operands of *unfolded
 // `img_ready`: the source image already in bf16 NHWC with its channels padded
 // to a multiple of 64 (then img_f32 is not read)
-// AFGB_TC_NO_SWAP=1 keeps the data gradient on the channel-M form (for
-// comparisons of the two forms)
-static bool swap_disabled() {
-    static const bool off = [] {
-        const char *e = std::getenv("AFGB_TC_NO_SWAP");
-        return e && e[0] == '1';
-    }();
-    return off;
-}
-
 static void run_gather(const NNGeom &g, int mode, const float *img_f32, const float *w_f32,
                        float *dst, bool fp8 = false, const float *user_wscale = nullptr,
                        const NNGeom *unfolded = nullptr, const __nv_bfloat16 *img_ready = nullptr,
@@ -1564,9 +1521,6 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
                         CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
             p.tma_store = 1;
     }
-    // data gradients into at most 64 channels: pixels on M (no padded half of M)
-    p.swap = (mode == 1 && tma_b && !fp8 && DC <= 64 && !swap_disabled()) ? 1 : 0;
-    if (p.swap) p.tma_store = 0;
     CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad, esize);
     const size_t smem = gather_smem();
     if (ntile > 0) {
