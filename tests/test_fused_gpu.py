@@ -17,6 +17,7 @@ SHAPES = [
     ((57, 41, 32, 2), (3, 3, 64), (2, 2), (1, 1), (1, 1)),     # strided: manual stores
     ((96, 80, 3, 2), (3, 3, 32), (2, 2), (1, 1), (1, 1)),      # RGB: taps folded
     ((40, 36, 16, 1), (5, 5, 200), (1, 1), (4, 4), (2, 2)),    # two output-channel tiles
+    ((128, 10, 64, 2), (3, 3, 96), (1, 1), (1, 1), (1, 1)),    # 128-pixel rows
 ]
 
 

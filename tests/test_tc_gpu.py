@@ -35,6 +35,13 @@ TC_CASES = C.NN_CASES + [
     ("tc_strip_7x7", (40, 36, 64, 1), (7, 7, 64, 128), (1, 1), (3, 3), (1, 1)),
     ("tc_strip_w16", (16, 40, 64, 2), (3, 3, 64, 128), (1, 1), (1, 1), (1, 1)),
     ("tc_strip_sy2", (33, 40, 64, 1), (3, 3, 64, 64), (1, 2), (1, 1), (1, 1)),
+    # wide rows and edge rows at stride 1
+    ("tc_w128_c64_k128", (128, 12, 64, 2), (3, 3, 64, 128), (1, 1), (1, 1), (1, 1)),
+    ("tc_w120_c96_k96", (120, 9, 96, 1), (3, 3, 96, 96), (1, 1), (1, 1), (1, 1)),
+    ("tc_1x5_w256", (256, 6, 64, 1), (5, 1, 64, 128), (1, 1), (2, 0), (1, 1)),
+    ("tc_nopad_k32", (130, 10, 64, 1), (3, 3, 64, 32), (1, 1), (0, 0), (1, 1)),
+    ("tc_fold_rgb_w128", (128, 10, 3, 2), (3, 3, 3, 64), (1, 1), (1, 1), (1, 1)),
+    ("tc_d2_c16_k48", (124, 8, 16, 2), (3, 3, 16, 48), (1, 1), (2, 2), (2, 2)),
 ]
 
 
