@@ -670,6 +670,26 @@ def run_only(args) -> None:
 
 
 # ---------------------------------------------------------------------------
+def replica_reduce(ms: float, world: int) -> float:
+    """The slowest rank's time per step: a MAX all-reduce over the replicas
+    (NCCL with a device tensor, gloo with a host tensor)."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([ms], device=dev, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ms: float, world: int) -> float:
+    """Whole-job TFLOP/s of `world` replicas of the headline step that each
+    took `ms` (the slowest rank's time) per step."""
+    return 3 * nn_flops() * world / (ms / 1e3) / 1e12
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -722,13 +742,8 @@ def main() -> None:
     value = res["value"]
     ms = res["ms_per_step"]
     if world > 1:
-        import torch
-        import torch.distributed as dist
-
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        value = 3 * nn_flops() * world / (ms / 1e3) / 1e12
+        ms = replica_reduce(ms, world)
+        value = replica_value(ms, world)
     if rank != 0:
         return
     cpu = cpu_nn_sample(args.cpu_seconds)
