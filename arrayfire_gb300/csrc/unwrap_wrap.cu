@@ -338,6 +338,33 @@ __device__ __forceinline__ T sum_patch_elems(T acc, const T *p, int nr, int cnt,
     return acc;
 }
 
+// the same for at most 4 x 4 covering windows (every stride >= window/4, so
+// 3x3 at stride 1 included): a fully unrolled, predicated 4 x 4 loop, all
+// loads issued before the adds, offsets from precomputed row and window steps
+template <typename T, typename Off>
+__device__ __forceinline__ T sum_patch_small(T acc, const T *p, int nr, int cnt, Off row_step,
+                                             Off win_step) {
+    T v[16];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (r < nr && j < cnt) v[4 * r + j] = p[(Off)r * row_step + (Off)j * win_step];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+            if (r < nr && j < cnt) acc = padd<T>(acc, v[4 * r + j]);
+    return acc;
+}
+
+template <typename T, typename Off>
+__device__ __forceinline__ T sum_patch(T acc, const T *p, int nr, int cnt, Off row_step,
+                                       Off win_step) {
+    if (nr <= 4 && cnt <= 4) return sum_patch_small<T, Off>(acc, p, nr, cnt, row_step, win_step);
+    return sum_patch_elems<T, Off>(acc, p, nr, cnt, row_step, win_step);
+}
+
 // af_wrap, column layout, on a TX x TY pixel tile of one slice.  The patches
 // covering the tile are, row by row of windows, contiguous runs of
 // wsz * nwx elements: the block stages them in shared memory with 16-byte
@@ -427,14 +454,14 @@ __global__ void __launch_bounds__(WT_THREADS) wrap_tiled_kernel(const T *__restr
                 const int rr = cy_lo - wy_lo;
                 const int base = rr * wt.run_pad + phase0;
                 const int ky = y + py - cy_lo * sy;
-                acc = sum_patch_elems<T, int>(acc, sm + base + kx0 + wx * ky + p0 * wsz,
-                                              cy_hi - cy_lo + 1, cnt, wt.run_pad - wx * sy, step);
+                acc = sum_patch<T, int>(acc, sm + base + kx0 + wx * ky + p0 * wsz,
+                                        cy_hi - cy_lo + 1, cnt, wt.run_pad - wx * sy, step);
             } else {
                 for (int wy_ = cy_lo; wy_ <= cy_hi; ++wy_) {
                     const int rr = wy_ - wy_lo;
                     const int ky = y + py - wy_ * sy;
                     const int base = rr * wt.run_pad + ((phase0 + rr * phase_step) & (VEC - 1));
-                    acc = sum_patch_elems<T, int>(acc, sm + base + kx0 + wx * ky + p0 * wsz, 1, cnt,
+                    acc = sum_patch<T, int>(acc, sm + base + kx0 + wx * ky + p0 * wsz, 1, cnt,
                                                   0, step);
                 }
             }
@@ -474,8 +501,8 @@ __global__ void __launch_bounds__(256) wrap_rows_kernel(const T *__restrict__ in
         const int ky = ay - cy_lo * sy, kx = ax - cx_lo * sx;
         const T *pp = slice + (cx_lo + (long long)nx * cy_lo) + np * (kx + wx * ky);
         // next window along x: col + 1, tap - sx; next window row: col + nx, tap - wx*sy
-        acc = sum_patch_elems<T, long long>(acc, pp, cy_hi - cy_lo + 1, cnt,
-                                            (long long)nx - np * wx * sy, 1 - (long long)sx * np);
+        acc = sum_patch<T, long long>(acc, pp, cy_hi - cy_lo + 1, cnt,
+                                      (long long)nx - np * wx * sy, 1 - (long long)sx * np);
     }
     *op = acc;
 }
