@@ -19,9 +19,10 @@
 //
 // How it runs here: the reference halves the signal's dim 0 into a complex
 // vector and uses complex transforms of power-of-two sizes.  This library
-// uses real-to-complex transforms for real data, of the smallest 2^a 3^b 5^c
-// 7^d sizes that hold s+f-1 (about half the work and memory of the
-// power-of-two packing), all on the library's stream:
+// uses real-to-complex transforms for real data, of the smallest 2^a 3^b sizes
+// that hold s+f-1 (about half the work and memory of the power-of-two packing;
+// measured faster than sizes with factors 5 and 7 as well), all on the
+// library's stream:
 //   pad      signal and filter -> zero-padded real (or complex) batches
 //   forward  cuFFT R2C / D2Z / C2C / Z2Z, batched over the slices
 //   multiply one kernel, broadcasting the batch dims per batch kind
@@ -38,6 +39,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <map>
 #include <mutex>
 #include <string>
@@ -168,14 +170,24 @@ cufftHandle get_plan(int rank, const int *n_fast_first, int batch, cufftType typ
     return h;
 }
 
-// smallest 2^a 3^b 5^c 7^d >= n (even when `even`)
+// smallest n' >= n whose prime factors are all in the allowed set (even when
+// `even`): 2 and 3 by default; AFGB_FFT_RADICES=2357, 235 or 2 changes the set
+// (for comparing transform sizes)
 long long good_size(long long n, bool even) {
+    static const int radices = [] {
+        const char *e = std::getenv("AFGB_FFT_RADICES");
+        return e ? std::atoi(e) : 23;
+    }();
     if (n <= 1) return 1;
     for (long long m = n;; ++m) {
         if (even && (m & 1)) continue;
         long long r = m;
-        for (long long p : {2ll, 3ll, 5ll, 7ll})
-            while (r % p == 0) r /= p;
+        for (long long p : {2ll, 3ll, 5ll, 7ll}) {
+            const bool ok = radices == 2 ? p == 2
+                                         : (radices == 23 ? p <= 3 : (radices == 235 ? p <= 5 : true));
+            if (ok)
+                while (r % p == 0) r /= p;
+        }
         if (r == 1) return m;
     }
 }
