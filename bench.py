@@ -512,10 +512,10 @@ def run_direct_workloads(af, peaks, args) -> dict:
     F3 = af.Array.from_numpy(np.asfortranarray((k3 / k3.sum()).astype(np.float32)))
     measure("conv3_3x3x3_f32_256^3_default",
             lambda: af.convolve3(V, F3, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL),
-            v.numel() * 8 + 108, ("conv3_tile_kernel", "conv_generic_kernel"))
+            v.numel() * 8 + 108, ("conv3_tma_kernel", "conv3_tile_kernel", "conv_generic_kernel"))
     measure("conv3_3x3x3_f32_256^3_expand",
             lambda: af.convolve3(V, F3, af.AF_CONV_EXPAND, af.AF_CONV_SPATIAL),
-            v.numel() * 4 + 258 ** 3 * 4 + 108, ("conv3_tile_kernel", "conv_generic_kernel"))
+            v.numel() * 4 + 258 ** 3 * 4 + 108, ("conv3_tma_kernel", "conv3_tile_kernel", "conv_generic_kernel"))
     del V, v
     # af_unwrap / af_wrap of the NN image (128x128x64x32 f32, 3x3 windows,
     # stride 1, padding 1): the 9x larger patch matrix is written / read once
