@@ -422,6 +422,7 @@ static void wrap_impl(af_array *out, const af_array in, dim_t ox, dim_t oy, dim_
     Array src = a->is_linear() ? *a : make_dense(*a);
     patches_wrap(src, dst, wx, wy, sx, sy, px, py, is_column, allocate);
     if (allocate) *out = make_handle(&dst);
+    else mark_written(dst);  // written in place
 }
 
 }  // namespace afgb

@@ -72,6 +72,14 @@ struct Buffer {
     size_t bytes = 0;
     BufKind kind = BufKind::Pool;
     int device = 0;
+    // host transfers run on the library's copy streams so that they overlap
+    // compute: `uploaded` completes the af_create_array copy (the compute
+    // stream waits on it once, at the first use); `written` is recorded on the
+    // compute stream after the last operation that wrote the buffer, and
+    // af_get_data_ptr's copy waits on it instead of on the whole stream
+    cudaEvent_t uploaded = nullptr;
+    std::atomic<bool> upload_pending{false};
+    cudaEvent_t written = nullptr;
     ~Buffer();
 };
 
@@ -98,7 +106,10 @@ struct Array {
 void dim4_from(dim_t out[4], unsigned n, const dim_t *vals);
 dim_t dim4_ndims(const dim_t d[4]);
 
-Array *get_array(const af_array a);       // validates the handle
+Array *get_array(const af_array a);       // validates the handle; orders a pending upload
+// record that the compute stream has just enqueued the last write of `a`'s
+// buffer (pool buffers only; af_get_data_ptr then copies after that point)
+void mark_written(const Array &a);
 af_array make_handle(Array *a);
 // a new dense array on the current device/stream
 Array *create_array(af_dtype t, const dim_t dims[4]);

@@ -113,6 +113,8 @@ bool dtype_valid(af_dtype t) { return (int)t >= 0 && (int)t <= (int)s8; }
 namespace {
 struct DevState {
     cudaStream_t own = nullptr;
+    cudaStream_t h2d = nullptr;  // af_create_array uploads
+    cudaStream_t d2h = nullptr;  // af_get_data_ptr downloads
     bool pool_ready = false;
     int sms = 0;
 };
@@ -138,6 +140,8 @@ static DevState &dev_state(int d) {
         std::lock_guard<std::mutex> lk(g_mu);
         if (!s.pool_ready) {
             AFGB_CUDA(cudaStreamCreateWithFlags(&s.own, cudaStreamNonBlocking));
+            AFGB_CUDA(cudaStreamCreateWithFlags(&s.h2d, cudaStreamNonBlocking));
+            AFGB_CUDA(cudaStreamCreateWithFlags(&s.d2h, cudaStreamNonBlocking));
             cudaMemPool_t pool;
             AFGB_CUDA(cudaDeviceGetDefaultMemPool(&pool, d));
             uint64_t thr = UINT64_MAX;
@@ -223,7 +227,16 @@ void free_device(void *p) {
     (void)cudaFreeAsync(p, stream());
 }
 
+static cudaEvent_t new_event() {
+    cudaEvent_t e = nullptr;
+    AFGB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    return e;
+}
+
 Buffer::~Buffer() {
+    if (ptr && upload_pending.load()) (void)cudaStreamWaitEvent(stream(), uploaded, 0);
+    if (uploaded) (void)cudaEventDestroy(uploaded);
+    if (written) (void)cudaEventDestroy(written);
     if (!ptr) return;
     if (kind == BufKind::Pool) {
         free_device(ptr);
@@ -273,12 +286,23 @@ Array *get_array(const af_array a) {
     if (!a) AFGB_THROW(AF_ERR_ARG, "Invalid (null) af_array handle");
     Handle *h = static_cast<Handle *>(a);
     if (h->magic != kMagic) AFGB_THROW(AF_ERR_ARG, "Invalid af_array handle");
+    Buffer *b = h->arr.buf.get();
+    if (b && b->upload_pending.exchange(false))
+        AFGB_CUDA(cudaStreamWaitEvent(stream(), b->uploaded, 0));  // its upload first
     return &h->arr;
+}
+
+void mark_written(const Array &a) {
+    Buffer *b = a.buf.get();
+    if (!b || b->kind != BufKind::Pool) return;
+    if (!b->written) b->written = new_event();
+    AFGB_CUDA(cudaEventRecord(b->written, stream()));
 }
 
 af_array make_handle(Array *a) {
     Handle *h = new Handle();
     h->arr = *a;
+    mark_written(*a);  // every operation hands its outputs out through here
     return static_cast<af_array>(h);
 }
 
@@ -364,7 +388,18 @@ af_err af_create_array(af_array *arr, const void *const data, const unsigned ndi
     Array *a = create_array(type, d);
     size_t bytes = (size_t)a->elements() * dtype_size(type);
     if (bytes && data) {
-        AFGB_CUDA(cudaMemcpyAsync(a->data(), data, bytes, cudaMemcpyHostToDevice, stream()));
+        // upload on the copy stream, after the stream-ordered allocation; the
+        // compute stream waits for it at the array's first use (get_array)
+        DevState &ds = dev_state(device());
+        cudaEvent_t allocated = new_event();
+        AFGB_CUDA(cudaEventRecord(allocated, stream()));
+        AFGB_CUDA(cudaStreamWaitEvent(ds.h2d, allocated, 0));
+        (void)cudaEventDestroy(allocated);
+        AFGB_CUDA(cudaMemcpyAsync(a->data(), data, bytes, cudaMemcpyHostToDevice, ds.h2d));
+        Buffer *b = a->buf.get();
+        b->uploaded = new_event();
+        AFGB_CUDA(cudaEventRecord(b->uploaded, ds.h2d));
+        b->upload_pending.store(true);
     }
     *arr = make_handle(a);
     AFGB_CATCHALL
@@ -422,6 +457,19 @@ af_err af_get_data_ptr(void *data, const af_array arr) {
     AFGB_ARG_ASSERT(0, data != nullptr);
     size_t es = dtype_size(a->type);
     if (a->elements() == 0) return AF_SUCCESS;
+    Buffer *b = a->buf.get();
+    if (a->is_linear() && b && b->kind == BufKind::Pool && b->written) {
+        // on the download stream, after the last write only: the copy
+        // overlaps whatever the compute stream has queued since
+        DevState &ds = dev_state(device());
+        AFGB_CUDA(cudaStreamWaitEvent(ds.d2h, b->written, 0));
+        if (b->uploaded) AFGB_CUDA(cudaStreamWaitEvent(ds.d2h, b->uploaded, 0));
+        AFGB_CUDA(cudaMemcpyAsync(data, a->data(), (size_t)a->elements() * es,
+                                  cudaMemcpyDeviceToHost, ds.d2h));
+        AFGB_CUDA(cudaStreamSynchronize(ds.d2h));
+        check_device_errors();
+        return AF_SUCCESS;
+    }
     if (a->is_linear()) {
         AFGB_CUDA(cudaMemcpyAsync(data, a->data(), (size_t)a->elements() * es,
                                   cudaMemcpyDeviceToHost, stream()));
@@ -448,7 +496,14 @@ af_err af_get_data_ptr(void *data, const af_array arr) {
 af_err af_get_device_ptr(void **ptr, const af_array arr) {
     AFGB_TRY
     AFGB_ARG_ASSERT(0, ptr != nullptr);
-    *ptr = get_array(arr)->data();
+    Array *a = get_array(arr);
+    // the caller may now write through the pointer on a stream of its own:
+    // later downloads of this buffer go back to waiting on the whole stream
+    if (Buffer *b = a->buf.get()) {
+        if (b->written) (void)cudaEventDestroy(b->written);
+        b->written = nullptr;
+    }
+    *ptr = a->data();
     AFGB_CATCHALL
 }
 
@@ -507,17 +562,23 @@ af_err af_get_strides(dim_t *s0, dim_t *s1, dim_t *s2, dim_t *s3, const af_array
     AFGB_CATCHALL
 }
 
+static void sync_current_device() {
+    DevState &ds = dev_state(device());
+    AFGB_CUDA(cudaStreamSynchronize(ds.h2d));
+    AFGB_CUDA(cudaStreamSynchronize(stream()));
+    AFGB_CUDA(cudaStreamSynchronize(ds.d2h));
+    check_device_errors();
+}
+
 af_err af_sync(const int dev) {
     AFGB_TRY
     if (dev >= 0) {
         int cur = device();
         if (dev != cur) AFGB_CUDA(cudaSetDevice(dev));
-        AFGB_CUDA(cudaStreamSynchronize(stream()));
-        check_device_errors();
+        sync_current_device();
         if (dev != cur) AFGB_CUDA(cudaSetDevice(cur));
     } else {
-        AFGB_CUDA(cudaStreamSynchronize(stream()));
-        check_device_errors();
+        sync_current_device();
     }
     AFGB_CATCHALL
 }
