@@ -389,7 +389,10 @@ af_err af_create_array(af_array *arr, const void *const data, const unsigned ndi
     size_t bytes = (size_t)a->elements() * dtype_size(type);
     if (bytes && data) {
         // upload on the copy stream, after the stream-ordered allocation; the
-        // compute stream waits for it at the array's first use (get_array)
+        // compute stream waits for it at the array's first use (get_array).
+        // As in ArrayFire (src/backend/cuda/Array.cpp:107-111) the call
+        // returns once the host buffer has been read, so the caller may reuse
+        // it; work already queued on the compute stream keeps running meanwhile
         DevState &ds = dev_state(device());
         cudaEvent_t allocated = new_event();
         AFGB_CUDA(cudaEventRecord(allocated, stream()));
@@ -400,6 +403,7 @@ af_err af_create_array(af_array *arr, const void *const data, const unsigned ndi
         b->uploaded = new_event();
         AFGB_CUDA(cudaEventRecord(b->uploaded, ds.h2d));
         b->upload_pending.store(true);
+        AFGB_CUDA(cudaEventSynchronize(b->uploaded));
     }
     *arr = make_handle(a);
     AFGB_CATCHALL
