@@ -259,30 +259,30 @@ template <typename V> struct ScalarOf { using type = V; };
 template <> struct ScalarOf<cf32> { using type = float; };
 template <> struct ScalarOf<cf64> { using type = double; };
 
-// out[i0, i1, i2, b] = convert( buf[b][(i0+off0) + n0*((i1+off1) + n1*(i2+off2))] / scale )
+// out[i0, i1, i2, b] = convert( buf[b][(i0+off0) + n0*((i1+off1) + n1*(i2+off2))] / scale ),
+// one output row (i1, i2, b) per block iteration, threads along i0
 template <typename V, typename To, int MODE>
 __global__ void fft_crop_kernel(const V *__restrict__ buf, To *__restrict__ out, long long o0,
                                 long long o1, long long o2, long long n0, long long n1,
                                 long long n2, long long off0, long long off1, long long off2,
-                                long long total, typename ScalarOf<V>::type scale) {
+                                long long rows, typename ScalarOf<V>::type scale) {
     const long long nslice = n0 * n1 * n2;
-    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-         t += (long long)gridDim.x * blockDim.x) {
-        const long long i0 = t % o0;
-        long long r = t / o0;
-        const long long i1 = r % o1;
-        r /= o1;
-        const long long i2 = r % o2, b = r / o2;
-        const V v = buf[b * nslice + (i0 + off0) + n0 * ((i1 + off1) + n1 * (i2 + off2))];
-        if constexpr (std::is_same<V, cf32>::value || std::is_same<V, cf64>::value) {
-            if constexpr (std::is_same<To, cf32>::value || std::is_same<To, cf64>::value) {
-                using OS = decltype(To{}.x);
-                out[t] = To{(OS)(v.x / scale), (OS)(v.y / scale)};
+    for (long long row = blockIdx.x; row < rows; row += gridDim.x) {
+        const long long i1 = row % o1, r = row / o1, i2 = r % o2, b = r / o2;
+        const V *src = buf + b * nslice + off0 + n0 * ((i1 + off1) + n1 * (i2 + off2));
+        To *dst = out + row * o0;
+        for (long long i0 = threadIdx.x; i0 < o0; i0 += blockDim.x) {
+            const V v = src[i0];
+            if constexpr (std::is_same<V, cf32>::value || std::is_same<V, cf64>::value) {
+                if constexpr (std::is_same<To, cf32>::value || std::is_same<To, cf64>::value) {
+                    using OS = decltype(To{}.x);
+                    dst[i0] = To{(OS)(v.x / scale), (OS)(v.y / scale)};
+                } else {
+                    dst[i0] = to_out<To, MODE>(v.x / scale);  // the real part
+                }
             } else {
-                out[t] = to_out<To, MODE>(v.x / scale);  // the real part
+                dst[i0] = to_out<To, MODE>(v / scale);
             }
-        } else {
-            out[t] = to_out<To, MODE>(v / scale);
         }
     }
 }
@@ -356,8 +356,10 @@ void crop(const V *buf, Array &out, const FftGeom &g, bool expand, const dim_t *
         for (int k = 0; k < g.rank; ++k) off[k] = fd[k] / 2;
     using S = typename ScalarOf<V>::type;
     const S scale = (S)((double)g.n[0] * (double)g.n[1] * (double)g.n[2]);
-    fft_crop_kernel<V, To, MODE><<<blocks_for(total, 256), 256, 0, stream()>>>(
-        buf, out.ptr<To>(), o0, o1, o2, g.n[0], g.n[1], g.n[2], off[0], off[1], off[2], total,
+    const long long rows = total / o0;
+    const int threads = o0 >= 256 ? 256 : (o0 >= 64 ? 64 : 32);
+    fft_crop_kernel<V, To, MODE><<<blocks_for(rows, 1), threads, 0, stream()>>>(
+        buf, out.ptr<To>(), o0, o1, o2, g.n[0], g.n[1], g.n[2], off[0], off[1], off[2], rows,
         scale);
     count_launch();
     AFGB_POST_LAUNCH("fft_crop_kernel");
