@@ -52,12 +52,13 @@ int main(int argc, char **argv) {
         }
         sum += out[i];
     }
-    /* a reference error code: a 1-D signal for the NN call (ARG) */
+    /* a reference error code: three stride dims for the NN call (ARG,
+     * src/api/c/convolve.cpp:358-360) */
     af_array bad = 0;
-    dim_t st[2] = {1, 1}, pd[2] = {0, 0}, dl[2] = {1, 1};
-    af_err e = af_convolve2_nn(&bad, s, f, 0, st, 2, pd, 2, dl);
+    dim_t st[3] = {1, 1, 2}, pd[2] = {0, 0}, dl[2] = {1, 1};
+    af_err e = af_convolve2_nn(&bad, s, f, 3, st, 2, pd, 2, dl);
     if (e != AF_ERR_ARG) {
-        fprintf(stderr, "af_convolve2_nn with 0 stride dims returned %d\n", (int)e);
+        fprintf(stderr, "af_convolve2_nn with 3 stride dims returned %d\n", (int)e);
         return 1;
     }
     af_release_array(o);
