@@ -53,7 +53,7 @@ int main(int argc, char **argv) {
         sum += out[i];
     }
     /* a reference error code: three stride dims for the NN call (ARG,
-     * src/api/c/convolve.cpp:358-360) */
+     * src/api/c/convolve.cpp:365) */
     af_array bad = 0;
     dim_t st[3] = {1, 1, 2}, pd[2] = {0, 0}, dl[2] = {1, 1};
     af_err e = af_convolve2_nn(&bad, s, f, 3, st, 2, pd, 2, dl);
