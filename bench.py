@@ -419,7 +419,8 @@ def run_cnn(af, args) -> dict:
 
 
 def run_direct_workloads(af, peaks, args) -> dict:
-    """Bandwidth-bound direct convolutions (configuration 2), GB/s of
+    """Bandwidth-bound direct convolutions (64 x 2048^2 separable and 7x7,
+    256^3 volume) and the patch / FFT lines, GB/s of
     algorithmic traffic (each input and output counted once)."""
     import ctypes
 

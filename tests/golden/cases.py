@@ -214,7 +214,8 @@ def nn_grad(case, seed: int, dtype=np.float32):
     return np.asfortranarray(g.standard_normal(od).astype(dtype))
 
 
-# BASELINE config 1 (full size; outputs stored as SHA-256 of the reference's bytes)
+# the two full-size f32 image workloads (512x512 Gaussian blur, 1024x1024 neighbour
+# count); outputs stored as SHA-256 of the reference's bytes
 def config1a():
     """512x512 f32 U[0,1) (Philox seed 0) with the 5x5 Gaussian sigma=1,
     normalised to unit sum (src/api/c/gaussian_kernel.cpp:36-88)."""

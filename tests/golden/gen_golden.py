@@ -8,7 +8,8 @@ Run here (where the ArrayFire v3.10.0 source tree is available):
 Writes, next to this file:
   direct.json  SHA-256 of the reference output bytes for every direct
                convolution case (tests/golden/cases.py:direct_cases) and the
-               two full-size configuration-1 images;
+               two full-size image workloads (512x512 Gaussian, 1024x1024
+               neighbour count);
   sep.json     the same for af_convolve2_sep cases;
   patches.json SHA-256 of the reference's af_unwrap output, af_wrap of a
                seeded patch matrix into zeros, and af_wrap_v2 into a seeded

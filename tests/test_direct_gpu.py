@@ -81,7 +81,8 @@ def test_direct_fused_within_tolerance(af, oracle, case):
 @pytest.mark.parametrize("name,fn", [("config1a_gauss5_512", C.config1a),
                                      ("config1b_neighbour3_1024", C.config1b)])
 def test_config1_full_size(af, oracle, name, fn):
-    """BASELINE configuration 1 at full size: bit-exact in the exact mode,
+    """The 512x512 Gaussian and 1024x1024 neighbour-count images at full
+    size: bit-exact in the exact mode,
     within 1e-6 relative in the default mode."""
     s, f = fn()
     af.set_exact_fp(True)

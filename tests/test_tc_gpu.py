@@ -104,7 +104,7 @@ def test_bf16_filter_grad_deterministic(af):
     assert a.tobytes() == b.tobytes()
 
 
-def test_bf16_config3a_sampled(af, oracle):
+def test_bf16_bench_shape_sampled(af, oracle):
     """The benchmark forward shape (128x128x64x32 * 3x3x64x128) against FP64
     on 512 sampled outputs."""
     g = C.rng(33)
