@@ -525,262 +525,6 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 }
 
 // ===========================================================================
-// stride-1 forward / data gradient: one source strip per channel chunk,
-// shared by every tap
-// ===========================================================================
-// A tile is SG_BY output rows of SG_BX = 128 pixels and 128 output channels.
-// Per 64 source channels the producer loads ONE strip of (128 + span_x) x
-// (SG_BY + span_y) source pixels (128 bytes each, 128-byte swizzle) instead of
-// one shifted 256-pixel tile per tap: tap t's B operand (N = the 128 pixels of
-// output row r) starts at strip row (r + sy_t) * SWp + sx_t, any 128-byte row
-// (the swizzle is keyed on address bits, as the TMA wrote the strip).  A is
-// the tap's 128-channel weight tile, as in the gather kernel; FP32
-// accumulators in TMEM (lane = output channel, SG_BY x 128 pixel columns per
-// buffer, double-buffered).  For a 3x3 filter the pixel operand traffic from
-// L2 drops from 9 x 32 KB to one 65 KB strip per channel chunk and tile.
-constexpr int SG_BX = 128;
-constexpr int SG_BY = 2;
-constexpr int SG_SST = 2;          // strip stages
-constexpr int SG_WST_MAX = 8;      // weight-tile stages at most (as many as fit)
-constexpr int SG_THREADS = 384;    // warp 0 TMA, warp 1 MMA + TMEM, warps 4-11 epilogue
-
-struct StripConvParams {
-    float *dst;          // ArrayFire layout (DW, DH, DC, N)
-    const float *bias;   // forward epilogue: per-channel bias, or none
-    int relu;
-    int DW, DH, DC, N;
-    int SCpad, nchunk;   // source channels (multiple of 64), 64-channel chunks
-    int n_och_tiles;     // 128-channel output tiles
-    int ntx, nty, total_tiles;
-    int ox_min, oy_min;  // strip origin relative to the tile origin
-    int SWp;             // strip width in pixels
-    int strip_bytes;     // strip stage size (a multiple of 1024)
-    int strip_tx;        // bytes one strip load writes (SWp * SHp * 128)
-    int wst;             // weight-tile stages
-    int ntaps, fw;
-    short tap_u[MAX_T], tap_v[MAX_T];    // weight column block u + fw*v
-    short tap_sx[MAX_T], tap_sy[MAX_T];  // tap offset inside the strip
-};
-
-struct StripConvSmem {
-    uint64_t sfull[SG_SST], sempty[SG_SST];
-    uint64_t wfull[SG_WST_MAX], wempty[SG_WST_MAX];
-    uint64_t tmem_full[2], tmem_empty[2];
-    uint64_t final_bar;
-    uint32_t tmem_base;
-    int abort;
-};
-
-__device__ __forceinline__ void strip_tile(const StripConvParams &p, int tile, int &tx, int &ty,
-                                           int &n, int &och0) {
-    int t = tile;
-    och0 = (t % p.n_och_tiles) * 128;
-    t /= p.n_och_tiles;
-    tx = t % p.ntx;
-    t /= p.ntx;
-    ty = t % p.nty;
-    n = t / p.nty;
-}
-
-__global__ void __launch_bounds__(SG_THREADS, 1)
-    strip_conv_kernel(const __grid_constant__ StripConvParams p,
-                      const __grid_constant__ CUtensorMap wmap,
-                      const __grid_constant__ CUtensorMap smap) {
-    extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char *base = reinterpret_cast<unsigned char *>(
-        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    unsigned char *strips = base;                            // SG_SST x strip_bytes
-    unsigned char *wtiles = base + SG_SST * p.strip_bytes;   // wst x A_BYTES
-    StripConvSmem *sm = reinterpret_cast<StripConvSmem *>(wtiles + p.wst * A_BYTES);
-    volatile int *abort = &sm->abort;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-    if (threadIdx.x == 0) {
-        for (int i = 0; i < SG_SST; ++i) {
-            mbar_init(&sm->sfull[i], 1);
-            mbar_init(&sm->sempty[i], 1);
-        }
-        for (int i = 0; i < p.wst; ++i) {
-            mbar_init(&sm->wfull[i], 1);
-            mbar_init(&sm->wempty[i], 1);
-        }
-        for (int b = 0; b < 2; ++b) {
-            mbar_init(&sm->tmem_full[b], 1);
-            mbar_init(&sm->tmem_empty[b], 256);  // 8 epilogue warps
-        }
-        mbar_init(&sm->final_bar, 1);
-        sm->abort = 0;
-        fence_barrier_init();
-    }
-    if (warp == 1) tmem_alloc(&sm->tmem_base, 512);
-    if (warp == 0 && lane == 0) {
-        prefetch_tmap(&wmap);
-        prefetch_tmap(&smap);
-    }
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
-    const uint32_t tmem_base = sm->tmem_base;
-
-    if (warp == 0) {
-        // ---------------- TMA producer: per chunk one strip, then the taps'
-        // weight tiles (128 output channels x 64 source channels)
-        if (lane == 0) {
-            uint32_t sit = 0, wit = 0;
-            bool stop = false;
-            for (int tile = blockIdx.x; tile < p.total_tiles && !stop && !*abort;
-                 tile += gridDim.x) {
-                int tx, ty, n, och0;
-                strip_tile(p, tile, tx, ty, n, och0);
-                const int x0 = tx * SG_BX, y0 = ty * SG_BY;
-                for (int c = 0; c < p.nchunk && !stop; ++c, ++sit) {
-                    const int ss = sit % SG_SST;
-                    if (!mbar_wait(&sm->sempty[ss], ((sit / SG_SST) & 1) ^ 1, abort, 1u)) {
-                        stop = true;
-                        break;
-                    }
-                    mbar_arrive_expect_tx(&sm->sfull[ss], (uint32_t)p.strip_tx);
-                    tma_load_4d(smem_u32(strips + ss * p.strip_bytes), &smap, &sm->sfull[ss], c * 64,
-                                x0 + p.ox_min, y0 + p.oy_min, n);
-                    for (int tq = 0; tq < p.ntaps; ++tq, ++wit) {
-                        const int ws = wit % p.wst;
-                        if (!mbar_wait(&sm->wempty[ws], ((wit / p.wst) & 1) ^ 1, abort, 2u)) {
-                            stop = true;
-                            break;
-                        }
-                        mbar_arrive_expect_tx(&sm->wfull[ws], (uint32_t)A_BYTES);
-                        tma_load_2d(smem_u32(wtiles + ws * A_BYTES), &wmap, &sm->wfull[ws],
-                                    (p.tap_u[tq] + p.fw * p.tap_v[tq]) * p.SCpad + c * 64, och0);
-                    }
-                }
-            }
-        }
-        __syncwarp();
-    } else if (warp == 1) {
-        // ---------------- MMA issue: per tap, SG_BY MMAs (M = 128 channels,
-        // N = the 128 pixels of one output row) per 16-channel K step
-        if (lane == 0) {
-            const uint32_t idesc = idesc_bf16(128, 128, 0, 0);
-            const uint64_t s0 = smem_desc(smem_u32(strips), 16, 1024);
-            const uint64_t w0 = smem_desc(smem_u32(wtiles), 16, 1024);
-            const uint32_t sstep = (uint32_t)p.strip_bytes >> 4, wstep = (uint32_t)A_BYTES >> 4;
-            const uint32_t rstep = (uint32_t)p.SWp * 8u;  // one strip row of pixels
-            uint32_t sit = 0, wit = 0, acc_it = 0;
-            bool issued = false, ok = true;
-            for (int tile = blockIdx.x; tile < p.total_tiles && ok && !*abort; tile += gridDim.x) {
-                const int b = acc_it & 1;
-                if (!mbar_wait(&sm->tmem_empty[b], ((acc_it >> 1) & 1) ^ 1, abort, 4u)) break;
-                tc_fence_after();
-                const uint32_t d0 = tmem_base + (uint32_t)(b * 256);
-                for (int c = 0; c < p.nchunk && ok; ++c, ++sit) {
-                    const int ss = sit % SG_SST;
-                    if (!mbar_wait(&sm->sfull[ss], (sit / SG_SST) & 1, abort, 8u)) {
-                        ok = false;
-                        break;
-                    }
-                    tc_fence_after();
-                    const uint64_t sa = s0 + (uint32_t)ss * sstep;
-                    for (int tq = 0; tq < p.ntaps; ++tq, ++wit) {
-                        const int ws = wit % p.wst;
-                        if (!mbar_wait(&sm->wfull[ws], (wit / p.wst) & 1, abort, 16u)) {
-                            ok = false;
-                            break;
-                        }
-                        tc_fence_after();
-                        const uint64_t wa = w0 + (uint32_t)ws * wstep;
-                        const uint32_t toff = (uint32_t)(p.tap_sy[tq] * p.SWp + p.tap_sx[tq]) * 8u;
-#pragma unroll
-                        for (int r = 0; r < SG_BY; ++r) {
-#pragma unroll
-                            for (int k = 0; k < 4; ++k)
-                                mma_f16(d0 + (uint32_t)(r * 128), wa + 2u * k,
-                                        sa + toff + (uint32_t)r * rstep + 2u * k, idesc,
-                                        (c | tq | k) != 0);
-                        }
-                        mma_commit(&sm->wempty[ws]);
-                        issued = true;
-                    }
-                    if (!ok) break;
-                    mma_commit(&sm->sempty[ss]);
-                }
-                if (!ok) break;
-                mma_commit(&sm->tmem_full[b]);
-                ++acc_it;
-            }
-            if (issued) {
-                mma_commit(&sm->final_bar);
-                unsigned spins = 0;
-                while (!mbar_try_wait(&sm->final_bar, 0) && ++spins < kSpinLimit) {
-                }
-            }
-        }
-        __syncwarp();
-    } else if (warp >= 4) {
-        // ---------------- epilogue: TMEM lane = output channel 32*q + lane,
-        // columns r*128 + pixel; the two warps of a quadrant take the left and
-        // right 64 pixels; each lane writes 16 consecutive pixels at a time
-        const int q = warp & 3;
-        const int half = (warp - 4) >> 2;
-        const long long plane = (long long)p.DW * p.DH;
-        const bool vec = (p.DW & 3) == 0;
-        uint32_t acc_it = 0;
-        for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
-            int tx, ty, n, och0;
-            strip_tile(p, tile, tx, ty, n, och0);
-            const int b = acc_it & 1;
-            if (!mbar_wait(&sm->tmem_full[b], (acc_it >> 1) & 1, abort, 32u)) break;
-            tc_fence_after();
-            const int ch = och0 + 32 * q + lane;
-            const float bi = (p.bias && ch < p.DC) ? p.bias[ch] : 0.0f;
-#pragma unroll 1
-            for (int r = 0; r < SG_BY; ++r) {
-                const int y = ty * SG_BY + r;
-                float *drow = p.dst + (long long)p.DW * y + plane * ((long long)ch + (long long)p.DC * n);
-#pragma unroll 1
-                for (int cc = 4 * half; cc < 4 * half + 4; ++cc) {
-                    uint32_t v[16];
-                    tmem_ld16(tmem_base + (uint32_t)(b * 256 + r * 128 + 16 * cc) +
-                                  ((uint32_t)(32 * q) << 16),
-                              v);
-                    tmem_ld_wait();
-                    const int xs = tx * SG_BX + 16 * cc;
-                    if (ch < p.DC && y < p.DH && xs < p.DW) {
-                        float o[16];
-#pragma unroll
-                        for (int e = 0; e < 16; ++e) {
-                            float t = __uint_as_float(v[e]);
-                            if (p.bias) t += bi;
-                            if (p.relu && t < 0.0f) t = 0.0f;
-                            o[e] = t;
-                        }
-                        float *d = drow + xs;
-                        if (vec && xs + 16 <= p.DW) {
-#pragma unroll
-                            for (int e = 0; e < 16; e += 4)
-                                *reinterpret_cast<float4 *>(d + e) = make_float4(o[e], o[e + 1], o[e + 2], o[e + 3]);
-                        } else {
-#pragma unroll
-                            for (int e = 0; e < 16; ++e)
-                                if (xs + e < p.DW) d[e] = o[e];
-                        }
-                    }
-                }
-            }
-            tc_fence_before();
-            mbar_arrive(&sm->tmem_empty[b]);
-            ++acc_it;
-        }
-    }
-
-    tc_fence_before();
-    __syncthreads();
-    if (warp == 1) {
-        tc_fence_after();
-        tmem_dealloc(tmem_base, 512);
-    }
-}
-
-// ===========================================================================
 // filter gradient kernel
 // ===========================================================================
 constexpr int WG_STAGES = 4;
@@ -1598,92 +1342,6 @@ static size_t gather_smem() {
            64;
 }
 
-// the strip kernel for stride-1 bf16 forwards and data gradients, when two
-// strips and at least three weight stages fit in shared memory and rows of
-// 128 pixels waste at most an eighth of the output width; returns false
-// (nothing launched) otherwise.  AFGB_TC_NO_STRIP=1 turns it off.
-static bool run_strip_conv(const NNGeom &g, int mode, const void *img, const void *wt, float *dst,
-                           int SW, int SH, int DW, int DH, int DC, int SCpad, int OCpad, int taps,
-                           const NNEpilogue *ep) {
-    static const bool off = [] {
-        const char *e = std::getenv("AFGB_TC_NO_STRIP");
-        return e && e[0] == '1';
-    }();
-    if (off || g.sx != 1 || g.sy != 1 || taps > MAX_T || DW <= 0 || DH <= 0 || g.N <= 0)
-        return false;
-    StripConvParams p;
-    std::memset(&p, 0, sizeof(p));
-    int oxmin = 1 << 30, oxmax = -(1 << 30), oymin = 1 << 30, oymax = -(1 << 30);
-    int nt = 0;
-    for (int v = 0; v < g.fh; ++v)
-        for (int u = 0; u < g.fw; ++u) {
-            // the gather kernel's tap offsets at stride 1 (phase 0)
-            const int ox = (int)(mode == 0 ? u * g.dx - g.px : g.px - u * g.dx);
-            const int oy = (int)(mode == 0 ? v * g.dy - g.py : g.py - v * g.dy);
-            p.tap_u[nt] = (short)u;
-            p.tap_v[nt] = (short)v;
-            p.tap_sx[nt] = (short)ox;  // made strip-relative below
-            p.tap_sy[nt] = (short)oy;
-            oxmin = std::min(oxmin, ox);
-            oxmax = std::max(oxmax, ox);
-            oymin = std::min(oymin, oy);
-            oymax = std::max(oymax, oy);
-            ++nt;
-        }
-    const int SWp = SG_BX + (oxmax - oxmin), SHp = SG_BY + (oymax - oymin);
-    if (SWp > 256 || SHp > 256) return false;
-    const long long tx_bytes = (long long)SWp * SHp * 128;
-    const long long strip_bytes = (tx_bytes + 1023) / 1024 * 1024;
-    const long long budget = 227 * 1024 - 1024 - SG_SST * strip_bytes - (long long)sizeof(StripConvSmem);
-    const long long wst = std::min<long long>(SG_WST_MAX, budget / A_BYTES);
-    if (wst < 3) return false;
-    const long long smem = 1024 + SG_SST * strip_bytes + wst * A_BYTES + (long long)sizeof(StripConvSmem);
-    const int ntx = (DW + SG_BX - 1) / SG_BX, nty = (DH + SG_BY - 1) / SG_BY;
-    if ((long long)ntx * SG_BX * 8 > 9LL * DW) return false;
-    const int n_och = OCpad / 128;
-    const long long tiles = (long long)n_och * ntx * nty * g.N;
-    if (tiles >= (1LL << 30)) return false;
-    for (int t = 0; t < nt; ++t) {
-        p.tap_sx[t] = (short)(p.tap_sx[t] - oxmin);
-        p.tap_sy[t] = (short)(p.tap_sy[t] - oymin);
-    }
-    p.dst = dst;
-    if (ep && mode == 0) {
-        p.bias = ep->bias;
-        p.relu = ep->relu;
-    }
-    p.DW = DW;
-    p.DH = DH;
-    p.DC = DC;
-    p.N = (int)g.N;
-    p.SCpad = SCpad;
-    p.nchunk = SCpad / 64;
-    p.n_och_tiles = n_och;
-    p.ntx = ntx;
-    p.nty = nty;
-    p.total_tiles = (int)tiles;
-    p.ox_min = oxmin;
-    p.oy_min = oymin;
-    p.SWp = SWp;
-    p.strip_bytes = (int)strip_bytes;
-    p.strip_tx = (int)tx_bytes;
-    p.wst = (int)wst;
-    p.ntaps = nt;
-    p.fw = (int)g.fw;
-    CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad);
-    CUtensorMap smap = make_imap(img, SCpad, SW, SH, (int)g.N, SWp, SHp);
-    AFGB_CUDA(cudaFuncSetAttribute(strip_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                   (int)smem));
-    const int grid = (int)std::min<long long>(tiles, num_sms());
-    {
-        KernelTimer kt(mode == 0 ? "tc_fwd_kernel" : "tc_dgrad_kernel");
-        strip_conv_kernel<<<grid, SG_THREADS, (size_t)smem, stream()>>>(p, wmap, smap);
-    }
-    count_launch();
-    AFGB_POST_LAUNCH("strip_conv_kernel");
-    return true;
-}
-
 // forward (mode 0) or data gradient (mode 1); fp8 (forward only): e4m3
 // operands with a per-tensor activation scale and per-output-channel weight
 // scales (`user_wscale`, K floats, or amax/448 computed on the device)
@@ -1777,12 +1435,6 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
                                                           static_cast<unsigned char *>(wt));
         count_launch();
         AFGB_POST_LAUNCH("weights_e4m3_kernel");
-    }
-
-    if (!fp8 && run_strip_conv(g, mode, img, wt, dst, SW, SH, DW, DH, DC, SCpad, OCpad, taps, ep)) {
-        free_device(wt);
-        if (img != img_ready) free_device(img);
-        return;
     }
 
     GatherParams p;
