@@ -786,6 +786,72 @@ static bool try_tile2(const DirectParams &p) {
     return false;
 }
 
+// ---- 1-D, f32: a block stages C1_BX outputs' worth of input (zero outside
+// the signal, as the reference's loop reads zeros there) and the taps in
+// shared memory; thread t computes outputs t + 256r, taps in the reference's
+// order (wi = 0..f0-1), one shared load and one multiply-add per tap
+constexpr int C1_BX = 1024;
+
+template <bool EXACT>
+__global__ void __launch_bounds__(256) conv1_tile_kernel(DirectParams p, long long ntx) {
+    extern __shared__ float c1_smem[];
+    const int f0 = (int)p.fd[0];
+    const int span = C1_BX + f0 - 1;
+    float *tin = c1_smem;
+    float *tw = c1_smem + span;
+    const float *sig = static_cast<const float *>(p.sig);
+    const float *filt = static_cast<const float *>(p.filt);
+    float *out = static_cast<float *>(p.out);
+    const long long c0 = p.expand ? 0 : f0 / 2;
+    for (long long blk = blockIdx.x; blk < ntx * p.nbatch; blk += gridDim.x) {
+        const long long b = blk / ntx, tx = blk - b * ntx;
+        const BatchOff bo = batch_offsets(p, b);
+        const long long x0 = tx * C1_BX;
+        const long long lo = x0 + c0 - (f0 - 1);  // input index of tin[0]
+        __syncthreads();                          // the previous tile's readers are done
+        for (int e = threadIdx.x; e < span; e += blockDim.x) {
+            const long long ii = lo + e;
+            tin[e] = (ii >= 0 && ii < p.sd[0]) ? sig[bo.in + ii * p.ss[0]] : 0.0f;
+        }
+        for (int e = threadIdx.x; e < f0; e += blockDim.x) tw[e] = filt[bo.filt + e * p.fs[0]];
+        __syncthreads();
+        float acc[C1_BX / 256];
+#pragma unroll
+        for (int r = 0; r < C1_BX / 256; ++r) acc[r] = 0.0f;
+        // output li reads input index li + c0 - wi, i.e. tin[li + f0 - 1 - wi]
+        for (int wi = 0; wi < f0; ++wi) {
+            const float w = tw[wi];
+#pragma unroll
+            for (int r = 0; r < C1_BX / 256; ++r)
+                acc[r] = mac<EXACT>(acc[r], tin[threadIdx.x + 256 * r + f0 - 1 - wi], w);
+        }
+#pragma unroll
+        for (int r = 0; r < C1_BX / 256; ++r) {
+            const long long i = x0 + threadIdx.x + 256 * r;
+            if (i < p.od[0]) out[bo.out + i * p.os[0]] = acc[r];
+        }
+    }
+}
+
+// f32 1-D convolutions (filters up to 129 taps: the spatial limit)
+static bool try_conv1_tile(const DirectParams &p, bool exact) {
+    if (p.rank != 1 || p.nbatch <= 0 || p.fd[0] < 1 || p.fd[0] > 129) return false;
+    const long long ntx = (p.od[0] + C1_BX - 1) / C1_BX;
+    if (ntx * p.nbatch <= 0) return false;
+    const size_t smem = (size_t)(C1_BX + 2 * p.fd[0]) * sizeof(float);
+    const unsigned grid = (unsigned)std::min<long long>(ntx * p.nbatch, (long long)num_sms() * 8);
+    {
+        KernelTimer kt("conv1_tile_kernel");
+        if (exact)
+            conv1_tile_kernel<true><<<grid, 256, smem, stream()>>>(p, ntx);
+        else
+            conv1_tile_kernel<false><<<grid, 256, smem, stream()>>>(p, ntx);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("conv1_tile_kernel");
+    return true;
+}
+
 template <typename T>
 static void run_generic(const DirectParams &p, bool exact) {
     long long slice = p.od[0];
@@ -822,6 +888,7 @@ void launch_convolve_nd(const Array &sig, const Array &filt, Array &out, int kin
         }
         if (done) return;
     }
+    if (rank == 1 && sig.type == f32 && try_conv1_tile(p, exact)) return;
     if (rank == 3 && sig.type == f32 && p.nbatch > 0 && dtma::tma_convolve3(p, exact)) return;
     if (rank == 3 && sig.type == f32 && p.fd[0] == 3 && p.fd[1] == 3 && p.fd[2] == 3) {
         const long long nz = (p.od[2] + T3_BZ - 1) / T3_BZ;

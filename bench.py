@@ -518,6 +518,15 @@ def run_direct_workloads(af, peaks, args) -> dict:
             lambda: af.convolve3(V, F3, af.AF_CONV_EXPAND, af.AF_CONV_SPATIAL),
             v.numel() * 4 + 258 ** 3 * 4 + 108, ("conv3_tma_kernel", "conv3_tile_kernel", "conv_generic_kernel"))
     del V, v
+    # 1-D: 64 signals of 2^20 samples, a 31-tap filter (LHS batch)
+    s1 = torch.rand(64, 1 << 20, device="cuda")
+    S1 = af.Array.view_torch(s1)
+    k1 = g.standard_normal(31)
+    F1 = af.Array.from_numpy((k1 / k1.sum()).astype(np.float32))
+    measure("conv1_31tap_f32_64x1M", lambda: af.convolve1(S1, F1, af.AF_CONV_DEFAULT,
+                                                          af.AF_CONV_SPATIAL),
+            s1.numel() * 8 + 124, ("conv1_tile_kernel", "conv_generic_kernel"))
+    del S1, s1
     # af_unwrap / af_wrap of the NN image (128x128x64x32 f32, 3x3 windows,
     # stride 1, padding 1): the 9x larger patch matrix is written / read once
     xi = torch.rand(32, 64, 128, 128, device="cuda")
