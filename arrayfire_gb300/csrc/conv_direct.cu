@@ -790,7 +790,7 @@ static bool try_tile2(const DirectParams &p) {
 // the signal, as the reference's loop reads zeros there) and the taps in
 // shared memory; thread t computes outputs t + 256r, taps in the reference's
 // order (wi = 0..f0-1), one shared load and one multiply-add per tap
-constexpr int C1_BX = 1024;
+constexpr int C1_BX = 4096;
 
 template <bool EXACT>
 __global__ void __launch_bounds__(256) conv1_tile_kernel(DirectParams p, long long ntx) {
