@@ -118,7 +118,8 @@ void cufft_check(cufftResult r, const char *what) {
                    std::string("cuFFT ") + what + " failed (" + std::to_string((int)r) + ")");
 }
 
-// plans by (rank, sizes, batch, type), kept for reuse.  Each convolution
+// plans by (device, rank, sizes, batch, type), kept for reuse (a cuFFT plan
+// belongs to the device that was current when it was made).  Each convolution
 // starts a new epoch; when the cache is full, plans not used in the current
 // epoch are destroyed (never one the running convolution already holds).
 struct PlanEntry {
@@ -126,7 +127,7 @@ struct PlanEntry {
     unsigned long long epoch;
 };
 std::mutex plan_mu;
-std::map<std::tuple<int, int, int, int, int, int>, PlanEntry> plans;
+std::map<std::tuple<int, int, int, int, int, int, int>, PlanEntry> plans;
 unsigned long long plan_epoch = 0;
 constexpr size_t kMaxPlans = 16;
 
@@ -144,7 +145,9 @@ unsigned long long begin_plan_epoch() {
 cufftHandle get_plan(int rank, const int *n_fast_first, int batch, cufftType type,
                      unsigned long long epoch) {
     std::lock_guard<std::mutex> lk(plan_mu);
-    auto key = std::make_tuple(rank, n_fast_first[0], n_fast_first[1], n_fast_first[2], batch,
+    int dev = 0;
+    AFGB_CUDA(cudaGetDevice(&dev));
+    auto key = std::make_tuple(dev, rank, n_fast_first[0], n_fast_first[1], n_fast_first[2], batch,
                                (int)type);
     auto it = plans.find(key);
     if (it != plans.end()) {

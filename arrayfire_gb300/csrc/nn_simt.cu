@@ -725,13 +725,14 @@ static float *noalloc_scratch_ptr(int dev) {
     return ptrs[dev];
 }
 
+// the launch error of the kernel just enqueued: the caller clears the
+// thread's error state (cudaGetLastError) right before the launch, so an
+// earlier, unrelated non-sticky error is not reported against this call
 static void noalloc_check_launch(const char *what) {
-    cudaError_t e = cudaPeekAtLastError();
-    if (e != cudaSuccess) {
-        (void)cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
         AFGB_THROW(AF_ERR_RUNTIME, std::string("kernel launch failed: ") + what + ": " +
                                        cudaGetErrorString(e));
-    }
 }
 
 static void filter_grad_noalloc(const NNGeom &g, const float *grad, const float *sig, float *dw,
@@ -784,19 +785,20 @@ static void filter_grad_noalloc(const NNGeom &g, const float *grad, const float 
     const size_t smem = (size_t)(WG_K * WG_M + WG_K * WG_N) * sizeof(float) + WG_M * (8 + 4 + 4);
     AFGB_CUDA(cudaFuncSetAttribute(wgrad_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
-    if (p.Q > 0) {
-        // every split writes its whole rows x K slice, so the scratch left
-        // by an earlier call needs no clearing
-        wgrad_kernel<float><<<dim3((unsigned)mt, (unsigned)nt, (unsigned)splits), WG_THREADS, smem,
-                              st>>>(p);
-        count_launch();
-        noalloc_check_launch("wgrad_kernel");
-    } else {
-        // no output pixels: the gradient is zero (cudaMemsetAsync allocates nothing)
-        AFGB_CUDA(cudaMemsetAsync(scratch, 0, (size_t)total * sizeof(float), st));
-        splits = 1;
-    }
-    wgrad_reduce_kernel<float, float><<<grid_cap(total, 256), 256, 0, st>>>(
+    // p.Q > 0: the entry point rejects empty signals and output grids.  Every
+    // split writes its whole rows x K slice, so the scratch left by an
+    // earlier call needs no clearing.
+    (void)cudaGetLastError();
+    wgrad_kernel<float><<<dim3((unsigned)mt, (unsigned)nt, (unsigned)splits), WG_THREADS, smem,
+                          st>>>(p);
+    count_launch();
+    noalloc_check_launch("wgrad_kernel");
+    // the reduce grid from the SM count read above (grid_cap would go through
+    // the library's per-device state, which creates its streams on first use)
+    const unsigned rgrid =
+        (unsigned)std::max(1LL, std::min((total + 255) / 256, (long long)sms * 16));
+    (void)cudaGetLastError();
+    wgrad_reduce_kernel<float, float><<<rgrid, 256, 0, st>>>(
         scratch, (int)splits, p.rows, g.K, g.C, g.fw, g.fh, dw);
     count_launch();
     noalloc_check_launch("wgrad_reduce_kernel");

@@ -329,13 +329,20 @@ AFGB_API unsigned long long afgb_kernel_launch_count(void);
  * buffers in ArrayFire layout: incoming_gradient (Wo,Ho,K,N), signal
  * (W,H,C,N) = signal_dims, filter_grad (fw,fh,C,K) = filter_dims; strides,
  * paddings and dilations hold two values each.  Work runs on `stream`
- * (0: the library's current stream).
+ * (0: the library's current stream, which the library creates on its first
+ * use of the device — pass the caller's own stream to avoid that set-up).
  * Scratch: a fixed 8 MiB device array inside the library (2,097,152 floats;
- * fw*fh*C*K must not exceed that, else AF_ERR_SIZE), present on every GPU
- * that loads the library until the process exits.  The first call on a
- * device looks up that array's device address, so make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU (other
- * streams, other host threads) race and give wrong results. */
+ * fw*fh*C*K must not exceed that, else AF_ERR_SIZE).  CUDA loads a library's
+ * kernel modules lazily by default (CUDA_MODULE_LOADING=LAZY since CUDA
+ * 12.2), so the array, with the code of the module that holds it, is placed
+ * in device memory by the FIRST call on each device, which also looks up the
+ * array's device address; from then on it stays until the process exits.
+ * Make that first call (a warm-up on small buffers will do) before the
+ * caller's allocator reserves the device's memory and before any stream
+ * capture, or run with CUDA_MODULE_LOADING=EAGER to place it when the
+ * library is loaded.  Later calls allocate nothing.  All calls share the
+ * array and leave their partial sums in it: calls that overlap on the GPU
+ * (other streams, other host threads) race and give wrong results. */
 AFGB_API af_err afgb_convolve2_filter_grad_noalloc(float *filter_grad, const float *incoming_gradient,
                                                    const float *signal, const dim_t *signal_dims,
                                                    const dim_t *filter_dims, const dim_t *strides,

@@ -58,7 +58,8 @@ def build_port() -> Path:
 
 def build_ref(reference: str | None = None) -> Path | None:
     """Compile the reference's CPU kernels in place, when its tree exists."""
-    ref = reference or os.environ.get("AF_REFERENCE_SRC", "/root/reference")
+    # AF_REFERENCE_SRC, else an ArrayFire checkout named `reference` beside this repository
+    ref = reference or os.environ.get("AF_REFERENCE_SRC") or str(HERE.parent.parent / "reference")
     if not Path(ref, "src", "backend", "cpu", "kernel", "convolve.hpp").exists():
         return None
     subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REFERENCE={ref}"], check=True)
