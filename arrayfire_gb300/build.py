@@ -23,6 +23,7 @@ LIB = PKG / "libafgb300.so"
 SOURCES = [
     "afgb_runtime.cpp",
     "afgb_conv_api.cpp",
+    "afgb_foreign.cpp",
     "conv_direct.cu",
     "conv_tma.cu",
     "nn_simt.cu",

@@ -7,6 +7,7 @@
 #include <atomic>
 #include <cstdint>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 
@@ -80,6 +81,17 @@ struct Buffer {
     cudaEvent_t uploaded = nullptr;
     std::atomic<bool> upload_pending{false};
     cudaEvent_t written = nullptr;
+    // a device copy derived from this buffer's contents (the bf16
+    // channels-last operand of the tensor-core kernels), made on
+    // `derived_stream` and keyed by the layout it was made for; it stays
+    // valid until the buffer is written (mark_written), handed to the caller
+    // for writing (af_get_device_ptr) or freed.  Pool buffers only: the
+    // library sees every write to those.
+    std::mutex derived_mu;
+    void *derived = nullptr;
+    unsigned long long derived_key = 0;
+    cudaStream_t derived_stream = nullptr;
+    void drop_derived();
     ~Buffer();
 };
 

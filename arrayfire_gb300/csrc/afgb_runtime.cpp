@@ -161,6 +161,8 @@ cudaStream_t stream() {
 int num_sms() { return dev_state(device()).sms; }
 
 unsigned int tma_take_error();
+void tma_set_wait_limit(unsigned int polls, int skip_block0);
+void tc_set_wait_limit(unsigned int polls);
 
 void check_device_errors() {
     unsigned int w = tc_take_error() | tma_take_error();
@@ -233,7 +235,16 @@ static cudaEvent_t new_event() {
     return e;
 }
 
+void Buffer::drop_derived() {
+    std::lock_guard<std::mutex> lk(derived_mu);
+    if (derived) free_device(derived);
+    derived = nullptr;
+    derived_key = 0;
+    derived_stream = nullptr;
+}
+
 Buffer::~Buffer() {
+    if (derived) free_device(derived);
     if (ptr && upload_pending.load()) (void)cudaStreamWaitEvent(stream(), uploaded, 0);
     if (uploaded) (void)cudaEventDestroy(uploaded);
     if (written) (void)cudaEventDestroy(written);
@@ -295,6 +306,7 @@ Array *get_array(const af_array a) {
 void mark_written(const Array &a) {
     Buffer *b = a.buf.get();
     if (!b || b->kind != BufKind::Pool) return;
+    if (b->derived) b->drop_derived();  // new contents: the derived copy is stale
     if (!b->written) b->written = new_event();
     AFGB_CUDA(cudaEventRecord(b->written, stream()));
 }
@@ -449,7 +461,14 @@ af_err afgb_device_array_view(af_array *arr, void *data, const unsigned ndims,
     auto b = std::make_shared<Buffer>();
     b->ptr = data;
     b->kind = BufKind::View;
-    b->device = device();
+    // a view reads and writes nothing here; without a usable device (host-side
+    // binding tests) it is recorded against device 0
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        dev = 0;
+    }
+    b->device = dev;
     a.buf = b;
     *arr = make_handle(&a);
     AFGB_CATCHALL
@@ -506,6 +525,7 @@ af_err af_get_device_ptr(void **ptr, const af_array arr) {
     if (Buffer *b = a->buf.get()) {
         if (b->written) (void)cudaEventDestroy(b->written);
         b->written = nullptr;
+        b->drop_derived();  // nor can a copy derived from its contents be kept
     }
     *ptr = a->data();
     AFGB_CATCHALL
@@ -702,6 +722,13 @@ af_err afgb_set_exact_fp(int exact) {
 }
 
 void afgb_debug_fail_alloc_after(int n) { g_fail_after.store(n > 0 ? n : 0); }
+
+af_err afgb_debug_wait_limit(unsigned int polls, int skip_first_block_copies) {
+    AFGB_TRY
+    tma_set_wait_limit(polls, skip_first_block_copies ? 1 : 0);
+    tc_set_wait_limit(polls);
+    AFGB_CATCHALL
+}
 
 unsigned long long afgb_kernel_launch_count(void) { return g_launches.load(); }
 

@@ -25,6 +25,7 @@
 #include <algorithm>
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 #include <type_traits>
 
 #include "conv_common.cuh"
@@ -833,9 +834,270 @@ __global__ void __launch_bounds__(256) conv1_tile_kernel(DirectParams p, long lo
     }
 }
 
+// ---- 1-D, f32, unit-stride signal and output rows: persistent blocks walk
+// tiles of C1P_T outputs through a C1P_NST-stage ring filled by 16-byte
+// cp.async copies (zero-filled outside the signal).  Thread t owns outputs
+// 16t .. 16t+15 of a tile and slides a register window over the input: the
+// taps run in chunks of eight, each chunk loading 24 inputs with six 128-bit
+// shared loads for 128 multiply-adds.
+//
+// The copy grid is aligned to the absolute address, so a tile's staged span
+// starts `mis` (0..3) elements before its first needed input.  Chunk k of
+// the padded tap range [0, 8M) holds tap wi = W_hi - k with
+// W_hi = F - 1 + mis, which makes every thread's window start on a 16-byte
+// boundary; k outside [mis, W_hi] is no tap and is skipped (never multiplied
+// by zero, so an inf or NaN next to the window cannot leak in).
+// Shared layout: 16-float groups at a pitch of 20 floats, so eight lanes
+// reading 128 bits at the same offset of consecutive groups hit eight
+// different bank quads.
+constexpr int C1P_T = 4096;
+constexpr int C1P_THREADS = 256;
+constexpr int C1P_NST = 3;
+constexpr int C1P_MAXF = 129;
+// the last thread's window of the last chunk ends at element
+// 16*255 + 8*(M-1) + 23 with M <= (C1P_MAXF + 2) / 8 + 1
+constexpr int C1P_GROUPS = (16 * 255 + 8 * ((C1P_MAXF + 2) / 8) + 24 + 15) / 16;
+constexpr int C1P_STAGE = C1P_GROUPS * 20;                        // floats
+constexpr int C1P_WMAX = 8 * ((C1P_MAXF + 2) / 8 + 1);            // padded taps
+constexpr size_t C1P_SMEM = (size_t)C1P_NST * C1P_STAGE * 4 + (size_t)C1P_WMAX * 4;
+
+__device__ __forceinline__ void c1p_copy16(float *dst, const float *src, int bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(bytes)
+                 : "memory");
+}
+
+// one chunk of eight taps for the 16 outputs of a thread.  gb points at the
+// thread's group for this chunk pair; ODD selects the second chunk of the
+// pair (window starting 8 floats into the group).  wk holds the chunk's
+// eight taps; k0 is the chunk's first padded tap index and [klo, khi] the
+// real taps.
+template <bool ODD>
+__device__ __forceinline__ void c1p_window(float (&win)[24], const float *gb) {
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const int x = ODD ? q + 2 : q;
+        const float4 v = *reinterpret_cast<const float4 *>(gb + (x >> 2) * 20 + (x & 3) * 4);
+        win[4 * q] = v.x;
+        win[4 * q + 1] = v.y;
+        win[4 * q + 2] = v.z;
+        win[4 * q + 3] = v.w;
+    }
+}
+
+// fused mode: one fused multiply-add per tap and output from the register
+// window (packing output pairs into f32x2 FMAs needs a register-pair move
+// per misaligned window pair, which cost more issue slots than it saved)
+template <bool ODD, bool FULL>
+__device__ __forceinline__ void c1p_chunk_fused(float (&acc)[16], const float *gb, const float *wk,
+                                                int k0, int klo, int khi) {
+    float win[24];
+    c1p_window<ODD>(win, gb);
+    const float4 wa = *reinterpret_cast<const float4 *>(wk);
+    const float4 wb = *reinterpret_cast<const float4 *>(wk + 4);
+    const float w[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+        if (FULL || (k0 + r >= klo && k0 + r <= khi)) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) acc[j] = __fmaf_rn(win[j + r], w[r], acc[j]);
+        }
+    }
+}
+
+// exact mode: taps in ascending wi, i.e. descending k, each product and sum
+// rounded separately
+template <bool ODD, bool FULL>
+__device__ __forceinline__ void c1p_chunk_exact(float (&acc)[16], const float *gb, const float *wk,
+                                                int k0, int klo, int khi) {
+    float win[24];
+    c1p_window<ODD>(win, gb);
+#pragma unroll
+    for (int r = 7; r >= 0; --r) {
+        if (FULL || (k0 + r >= klo && k0 + r <= khi)) {
+            const float w = wk[r];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) acc[j] = mac<true>(acc[j], win[j + r], w);
+        }
+    }
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(C1P_THREADS, 2)
+    conv1_pipe_kernel(const DirectParams p, long long ntx, long long ntiles) {
+    extern __shared__ __align__(16) float c1p_smem[];
+    float *wbuf = c1p_smem + C1P_NST * C1P_STAGE;
+    const int F = (int)p.fd[0];
+    const long long len = p.sd[0], od = p.od[0];
+    const long long c0 = p.expand ? 0 : F / 2;
+    const float *sig = static_cast<const float *>(p.sig);
+    const float *filt = static_cast<const float *>(p.filt);
+    float *out = static_cast<float *>(p.out);
+    const int tid = threadIdx.x;
+
+    // the tile's batch slice, first output and staging misalignment,
+    // decoded with 32-bit divisions (the launcher keeps tile counts and
+    // batch extents below 2^31) when the tile is issued, and kept in shared
+    // memory for the iteration that computes it
+    struct Tile {
+        BatchOff bo;
+        long long x0, lo;
+        int mis;
+    };
+    __shared__ Tile tinfo[C1P_NST];
+    const unsigned untx = (unsigned)ntx, nb1 = (unsigned)p.batch[1], nb2 = (unsigned)p.batch[2];
+    auto decode = [&](long long tile) {
+        Tile t;
+        const unsigned b = (unsigned)tile / untx;
+        t.x0 = (long long)((unsigned)tile - b * untx) * C1P_T;
+        const unsigned r = b / nb1, b1 = b - r * nb1, b3 = r / nb2, b2 = r - b3 * nb2;
+        t.bo.in = b1 * p.in_step[1] + b2 * p.in_step[2] + b3 * p.in_step[3];
+        t.bo.out = b1 * p.out_step[1] + b2 * p.out_step[2] + b3 * p.out_step[3];
+        t.bo.filt = b1 * p.filt_step[1] + b2 * p.filt_step[2] + b3 * p.filt_step[3];
+        const long long first = t.x0 + c0 - (F - 1);  // first input index any output reads
+        const long long abs_first = (long long)(reinterpret_cast<uintptr_t>(sig + t.bo.in) >> 2) + first;
+        t.mis = (int)(abs_first & 3);
+        t.lo = first - t.mis;  // signal index of staged element 0 (16-byte aligned address)
+        return t;
+    };
+    auto issue = [&](long long tile, int buf) {
+        const Tile t = decode(tile);
+        if (tid == 0) tinfo[buf] = t;
+        const float *sp = sig + t.bo.in;
+        const long long nout = min((long long)C1P_T, od - t.x0);
+        const int nch = (int)((t.mis + nout + F - 1 + 3) / 4);
+        float *st = c1p_smem + buf * C1P_STAGE;
+        for (int c = tid; c < nch; c += C1P_THREADS) {
+            const long long ci = t.lo + 4LL * c;
+            int bytes = 0;
+            const float *src = sp;
+            if (ci < len && ci + 4 > 0) {
+                bytes = (int)min(4LL, len - ci) * 4;
+                src = sp + ci;  // up to 3 elements before the slice: zeroed after landing
+            }
+            c1p_copy16(st + (c >> 2) * 20 + (c & 3) * 4, src, bytes);
+        }
+    };
+
+#pragma unroll 1
+    for (int i = 0; i < C1P_NST - 1; ++i) {
+        const long long t = blockIdx.x + (long long)i * gridDim.x;
+        if (t < ntiles) issue(t, i);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    __syncthreads();  // the prologue's tile records
+    long long k = 0;
+#pragma unroll 1
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++k) {
+        const int buf = (int)(k % C1P_NST);
+        const long long ahead = tile + (long long)(C1P_NST - 1) * gridDim.x;
+        if (ahead < ntiles) issue(ahead, (int)((k + C1P_NST - 1) % C1P_NST));
+        asm volatile("cp.async.commit_group;" ::: "memory");
+        asm volatile("cp.async.wait_group %0;" ::"n"(C1P_NST - 1) : "memory");
+        // tinfo[buf] was written when this tile was issued, at least one
+        // barrier ago (the prologue's, or an earlier iteration's last)
+        const Tile t = tinfo[buf];
+        const int whi = F - 1 + t.mis;
+        const int M = whi / 8 + 1;
+        for (int kk = tid; kk < 8 * M; kk += C1P_THREADS) {
+            const int wi = whi - kk;
+            const float w = (wi >= 0 && wi < F) ? filt[t.bo.filt + wi * p.fs[0]] : 0.0f;
+            wbuf[kk] = w;
+        }
+        __syncthreads();
+        float *st = c1p_smem + buf * C1P_STAGE;
+        if (t.lo < 0) {  // staged elements before the signal start read as zero
+            const int nz = (int)min(-t.lo, (long long)C1P_STAGE);
+            for (int e = tid; e < nz; e += C1P_THREADS) st[(e >> 4) * 20 + (e & 15)] = 0.0f;
+            __syncthreads();
+        }
+        const long long i0 = t.x0 + 16LL * tid;
+        float res[16];
+        if (EXACT) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) res[j] = 0.0f;
+#pragma unroll 1
+            for (int m = M - 1; m >= 0; --m) {
+                const float *gb = st + (tid + (m >> 1)) * 20;
+                const bool full = 8 * m >= t.mis && 8 * m + 7 <= whi;
+                if (m & 1) {
+                    if (full) c1p_chunk_exact<true, true>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
+                    else c1p_chunk_exact<true, false>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
+                } else {
+                    if (full) c1p_chunk_exact<false, true>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
+                    else c1p_chunk_exact<false, false>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) res[j] = 0.0f;
+#pragma unroll 1
+            for (int m = 0; m < M; ++m) {
+                const float *gb = st + (tid + (m >> 1)) * 20;
+                const bool full = 8 * m >= t.mis && 8 * m + 7 <= whi;
+                if (m & 1) {
+                    if (full) c1p_chunk_fused<true, true>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
+                    else c1p_chunk_fused<true, false>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
+                } else {
+                    if (full) c1p_chunk_fused<false, true>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
+                    else c1p_chunk_fused<false, false>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
+                }
+            }
+        }
+        if (i0 < od) {
+            float *op = out + t.bo.out + i0;
+            if (i0 + 15 < od && (reinterpret_cast<uintptr_t>(op) & 15) == 0) {
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    reinterpret_cast<float4 *>(op)[q] =
+                        make_float4(res[4 * q], res[4 * q + 1], res[4 * q + 2], res[4 * q + 3]);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    if (i0 + j < od) op[j] = res[j];
+            }
+        }
+        __syncthreads();  // this stage and the taps are rewritten next
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+}
+
+static bool try_conv1_pipe(const DirectParams &p, bool exact) {
+    if (p.ss[0] != 1 || p.os[0] != 1) return false;
+    const long long ntx = (p.od[0] + C1P_T - 1) / C1P_T;
+    const long long ntiles = ntx * p.nbatch;
+    if (ntiles <= 0 || ntiles >= (1LL << 31) || p.batch[1] >= (1LL << 31) ||
+        p.batch[2] >= (1LL << 31))
+        return false;
+    static int per_sm[2] = {0, 0};
+    static std::once_flag once[2];
+    std::call_once(once[exact ? 1 : 0], [&] {
+        auto fn = exact ? conv1_pipe_kernel<true> : conv1_pipe_kernel<false>;
+        AFGB_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)C1P_SMEM));
+        int n = 0;
+        AFGB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, C1P_THREADS, C1P_SMEM));
+        per_sm[exact ? 1 : 0] = std::max(1, n);
+    });
+    const unsigned grid = (unsigned)std::min<long long>(
+        ntiles, (long long)num_sms() * per_sm[exact ? 1 : 0]);
+    {
+        KernelTimer kt("conv1_pipe_kernel");
+        if (exact)
+            conv1_pipe_kernel<true><<<grid, C1P_THREADS, C1P_SMEM, stream()>>>(p, ntx, ntiles);
+        else
+            conv1_pipe_kernel<false><<<grid, C1P_THREADS, C1P_SMEM, stream()>>>(p, ntx, ntiles);
+    }
+    count_launch();
+    AFGB_POST_LAUNCH("conv1_pipe_kernel");
+    return true;
+}
+
 // f32 1-D convolutions (filters up to 129 taps: the spatial limit)
 static bool try_conv1_tile(const DirectParams &p, bool exact) {
     if (p.rank != 1 || p.nbatch <= 0 || p.fd[0] < 1 || p.fd[0] > 129) return false;
+    if (try_conv1_pipe(p, exact)) return true;
     const long long ntx = (p.od[0] + C1_BX - 1) / C1_BX;
     if (ntx * p.nbatch <= 0) return false;
     const size_t smem = (size_t)(C1_BX + 2 * p.fd[0]) * sizeof(float);

@@ -114,11 +114,17 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map
         : "memory");
 }
 
+// test hook (afgb_debug_wait_limit): when set, block 0 of the 2-D kernel
+// issues no tile copies, so its consumers' bounded waits run out with no copy
+// in flight
+__device__ int g_debug_skip_block0 = 0;
+
 // bounded wait on a TMA barrier; false (and the error word raised) on timeout
 __device__ __forceinline__ bool wait_tile(uint64_t *bar, uint32_t parity) {
     unsigned n = 0;
+    const unsigned limit = tc::g_spin_limit;
     while (!mbar_try_wait(bar, parity)) {
-        if (++n > tc::kSpinLimit) {
+        if (++n > limit) {
             atomicOr(&tc::g_tc_error, 256u);
             return false;
         }
@@ -206,7 +212,9 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
     }
     __syncthreads();
 
+    const bool skip_copies = g_debug_skip_block0 && blockIdx.x == 0;
     auto issue = [&](int t, int buf) {
+        if (skip_copies) return;
         const TileRec tr = decode_tile(t, tg, p.out_step, p.filt_step);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive_expect_tx(&full[buf], H::TBYTES);
@@ -1149,6 +1157,12 @@ bool tma_convolve3(const DirectParams &p, bool exact) {
 }
 
 }  // namespace dtma
+
+void tma_set_wait_limit(unsigned int polls, int skip_block0) {
+    const unsigned int v = polls ? polls : tc::kSpinLimit;
+    AFGB_CUDA(cudaMemcpyToSymbol(tc::g_spin_limit, &v, sizeof(v)));
+    AFGB_CUDA(cudaMemcpyToSymbol(dtma::g_debug_skip_block0, &skip_block0, sizeof(skip_block0)));
+}
 
 unsigned int tma_take_error() {
     unsigned int v = 0, zero = 0;

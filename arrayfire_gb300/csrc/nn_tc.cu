@@ -35,6 +35,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -525,6 +526,275 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
 }
 
 // ===========================================================================
+// stride-1 forward and data gradient with pixels on M (strip kernel)
+// ===========================================================================
+// For images whose rows hold at least 128 output pixels.  A tile is SC_R
+// output rows x 128 output pixels (one row segment) x all output channels
+// (the MMA's N, a multiple of 16 up to 128).  For each 64-channel chunk of the
+// source the producer loads one strip per source row the tile touches:
+// SL = 128 + (ox_max - ox_min) pixels of 64 channels, zero outside the image
+// (the convolution's padding).  Tap t of output row r reads strip
+// r + oy(t) - oy_min from row ox(t) - ox_min on: its A operand (128 pixels x
+// 64 channels, K-major, 128-byte swizzle) is a view into the strip, so a
+// source pixel is loaded once per chunk and source row instead of once per
+// tap.  The 128-byte swizzle is keyed on the shared-memory address bits, as
+// the TMA wrote the strip, so a view may start at any 128-byte row.  The
+// weights of one tap and chunk (N x 64, K-major) stream through their own
+// ring.  MMA M=128 x N x K=16 with FP32 accumulators in TMEM (SC_R*N columns,
+// double-buffered).  Every output channel is a real MMA column: nothing is
+// padding when the output has 64 channels (the weights-on-M gather kernel
+// pads such a data gradient to M=128).  The epilogue warps own 32 pixels
+// each (their TMEM lanes) and store a channel's 32 consecutive pixels as one
+// 128-byte piece.
+constexpr int SC_R = 2;
+constexpr int SC_MAXS = 4;                  // strips per chunk: SC_R + oy range
+constexpr int SC_MAXSL = 136;               // strip pixels
+constexpr int SC_STRIP = SC_MAXSL * 128;    // 17 KB, a multiple of 1024
+constexpr int SC_NA = 2;                    // strip-set buffers
+constexpr int SC_B_AREA = 64 * 1024;        // weight-tile ring
+constexpr int SC_MAXN = 128;
+constexpr int SC_MAXNB = 8;
+constexpr int SC_THREADS = 320;             // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+
+struct StripConvParams {
+    float *dst;          // ArrayFire layout (DW, DH, DC, N)
+    const float *bias;   // forward: per-output-channel bias, or 0
+    int relu;
+    int SW, SH, SCpad, N;
+    int DW, DH, DC;
+    int nmma;            // MMA N (output channels rounded up to 16)
+    int nchunk, ntaps, S, SL;
+    int ox_min, oy_min;
+    int nb;              // weight-tile buffers
+    int nseg, nrg, total_tiles;
+    int strip16;         // SC_STRIP in 16-byte units
+    uint32_t a_off[MAX_T];  // per tap: offset of its A view within a strip set (16-byte units)
+};
+
+struct StripConvSmem {
+    uint64_t a_full[SC_NA], a_empty[SC_NA];
+    uint64_t b_full[SC_MAXNB], b_empty[SC_MAXNB];
+    uint64_t tmem_full[2], tmem_empty[2];
+    uint64_t final_bar;
+    uint32_t tmem_base;
+    int abort;
+};
+
+__global__ void __launch_bounds__(SC_THREADS, 1)
+    strip_conv_kernel(const __grid_constant__ StripConvParams p,
+                      const __grid_constant__ CUtensorMap wmap,
+                      const __grid_constant__ CUtensorMap smap) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    unsigned char *a_area = base;                                   // SC_NA x SC_MAXS strips
+    unsigned char *b_area = base + SC_NA * SC_MAXS * SC_STRIP;      // weight tiles
+    StripConvSmem *sm = reinterpret_cast<StripConvSmem *>(b_area + SC_B_AREA);
+    volatile int *abort = &sm->abort;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t b_bytes = (uint32_t)p.nmma * 128u;
+    const int tiles_per_img = p.nseg * p.nrg;
+
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < SC_NA; ++i) {
+            mbar_init(&sm->a_full[i], 1);
+            mbar_init(&sm->a_empty[i], 1);
+        }
+        for (int i = 0; i < p.nb; ++i) {
+            mbar_init(&sm->b_full[i], 1);
+            mbar_init(&sm->b_empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&sm->tmem_full[i], 1);
+            mbar_init(&sm->tmem_empty[i], 256);
+        }
+        mbar_init(&sm->final_bar, 1);
+        sm->abort = 0;
+        fence_barrier_init();
+    }
+    if (warp == 1) tmem_alloc(&sm->tmem_base, 512);
+    if (warp == 0 && lane == 0) {
+        prefetch_tmap(&wmap);
+        prefetch_tmap(&smap);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = sm->tmem_base;
+
+    if (warp == 0) {
+        // ---------------- TMA producer: strip sets and weight tiles
+        if (lane == 0) {
+            int a = 0, b = 0;
+            uint32_t aph = 1, bph = 1;
+            bool stop = false;
+            for (int tile = blockIdx.x; tile < p.total_tiles && !stop; tile += gridDim.x) {
+                const int n = tile / tiles_per_img;
+                const int rem = tile - n * tiles_per_img;
+                const int rg = rem / p.nseg, seg = rem - rg * p.nseg;
+                const int x0 = seg * 128, y0 = rg * SC_R;
+                for (int ch = 0; ch < p.nchunk && !stop; ++ch) {
+                    if (!mbar_wait(&sm->a_empty[a], aph, abort, 1u)) {
+                        stop = true;
+                        break;
+                    }
+                    mbar_arrive_expect_tx(&sm->a_full[a], (uint32_t)(p.S * p.SL * 128));
+                    unsigned char *set = a_area + a * (SC_MAXS * SC_STRIP);
+                    for (int s = 0; s < p.S; ++s)
+                        tma_load_4d(smem_u32(set + s * SC_STRIP), &smap, &sm->a_full[a], ch * 64,
+                                    x0 + p.ox_min, y0 + p.oy_min + s, n);
+                    if (++a == SC_NA) {
+                        a = 0;
+                        aph ^= 1u;
+                    }
+                    for (int t = 0; t < p.ntaps; ++t) {
+                        if (!mbar_wait(&sm->b_empty[b], bph, abort, 2u)) {
+                            stop = true;
+                            break;
+                        }
+                        mbar_arrive_expect_tx(&sm->b_full[b], b_bytes);
+                        tma_load_2d(smem_u32(b_area + b * b_bytes), &wmap, &sm->b_full[b],
+                                    t * p.SCpad + ch * 64, 0);
+                        if (++b == p.nb) {
+                            b = 0;
+                            bph ^= 1u;
+                        }
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer: descriptors are precomputed bases plus
+        // 16-byte-unit offsets; stage indices and phases advance without
+        // division
+        if (lane == 0) {
+            const uint32_t idesc = idesc_bf16(128, (uint32_t)p.nmma, 0, 0);
+            const uint64_t a0 = smem_desc(smem_u32(a_area), 16, 1024);
+            const uint64_t b0 = smem_desc(smem_u32(b_area), 16, 1024);
+            const uint32_t set16 = (uint32_t)(SC_MAXS * SC_STRIP) >> 4;
+            const uint32_t b16 = b_bytes >> 4;
+            int a = 0, b = 0;
+            uint32_t aph = 0, bph = 0, aoff = 0, boff = 0, acc_it = 0;
+            bool issued = false, stop = false;
+            for (int tile = blockIdx.x; tile < p.total_tiles && !stop; tile += gridDim.x) {
+                const int acc = acc_it & 1;
+                if (!mbar_wait(&sm->tmem_empty[acc], ((acc_it >> 1) & 1) ^ 1, abort, 4u)) break;
+                tc_fence_after();
+                const uint32_t d0 = tmem_base + (uint32_t)(acc * SC_R * p.nmma);
+                for (int ch = 0; ch < p.nchunk && !stop; ++ch) {
+                    if (!mbar_wait(&sm->a_full[a], aph, abort, 8u)) {
+                        stop = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    for (int t = 0; t < p.ntaps; ++t) {
+                        if (!mbar_wait(&sm->b_full[b], bph, abort, 16u)) {
+                            stop = true;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint64_t ad = a0 + aoff + p.a_off[t];
+                        const uint64_t bd = b0 + boff;
+#pragma unroll
+                        for (int r = 0; r < SC_R; ++r)
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                mma_f16(d0 + (uint32_t)(r * p.nmma),
+                                        ad + (uint32_t)(r * p.strip16 + 2 * k),
+                                        bd + (uint32_t)(2 * k), idesc, (ch | t | k) != 0);
+                        mma_commit(&sm->b_empty[b]);
+                        issued = true;
+                        if (++b == p.nb) {
+                            b = 0;
+                            boff = 0;
+                            bph ^= 1u;
+                        } else {
+                            boff += b16;
+                        }
+                    }
+                    if (stop) break;
+                    mma_commit(&sm->a_empty[a]);
+                    if (++a == SC_NA) {
+                        a = 0;
+                        aoff = 0;
+                        aph ^= 1u;
+                    } else {
+                        aoff += set16;
+                    }
+                }
+                if (stop) break;
+                mma_commit(&sm->tmem_full[acc]);
+                ++acc_it;
+            }
+            if (issued) {
+                mma_commit(&sm->final_bar);
+                unsigned n = 0;
+                while (!mbar_try_wait(&sm->final_bar, 0) && ++n < kSpinLimit) {
+                }
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue: warp w reads TMEM lanes 32*(w % 4) ..,
+        // i.e. pixels x0 + 32*(w % 4) + lane of each output row; the two
+        // warps of a lane quadrant take alternate groups of 64 channels.
+        // Up to four 16-column TMEM loads are in flight per wait.
+        const int q = warp & 3, half = (warp - 2) >> 2;
+        const long long plane = (long long)p.DW * p.DH;
+        uint32_t acc_it = 0;
+        for (int tile = blockIdx.x; tile < p.total_tiles && !*abort; tile += gridDim.x) {
+            const int n = tile / tiles_per_img;
+            const int rem = tile - n * tiles_per_img;
+            const int rg = rem / p.nseg, seg = rem - rg * p.nseg;
+            const int x = seg * 128 + 32 * q + lane, y0 = rg * SC_R;
+            const int acc = acc_it & 1;
+            if (!mbar_wait(&sm->tmem_full[acc], (acc_it >> 1) & 1, abort, 32u)) break;
+            tc_fence_after();
+            const uint32_t tq = tmem_base + (uint32_t)(acc * SC_R * p.nmma) + ((uint32_t)(32 * q) << 16);
+            for (int r = 0; r < SC_R; ++r) {
+                const int y = y0 + r;
+                float *drow = p.dst + (long long)n * p.DC * plane + (long long)y * p.DW + x;
+                const bool ok = y < p.DH && x < p.DW;
+                for (int c0 = 64 * half; c0 < p.nmma; c0 += 128) {
+                    const int ng = min(4, (p.nmma - c0) / 16);  // 16-column groups here
+                    uint32_t v[4][16];
+#pragma unroll
+                    for (int g = 0; g < 4; ++g)
+                        if (g < ng) tmem_ld16(tq + (uint32_t)(r * p.nmma + c0 + 16 * g), v[g]);
+                    tmem_ld_wait();
+                    if (!ok) continue;
+#pragma unroll
+                    for (int g = 0; g < 4; ++g) {
+                        if (g >= ng) break;
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) {
+                            const int c = c0 + 16 * g + e;
+                            if (c < p.DC) {
+                                float val = __uint_as_float(v[g][e]);
+                                if (p.bias) val += __ldg(p.bias + c);
+                                if (p.relu && val < 0.0f) val = 0.0f;
+                                drow[(long long)c * plane] = val;
+                            }
+                        }
+                    }
+                }
+            }
+            tc_fence_before();
+            mbar_arrive(&sm->tmem_empty[acc]);
+            ++acc_it;
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem_base, 512);
+    }
+}
+
+// ===========================================================================
 // filter gradient kernel
 // ===========================================================================
 constexpr int WG_STAGES = 4;
@@ -1006,6 +1276,75 @@ __global__ void __launch_bounds__(256) to_nhwc_bf16_kernel(const float *__restri
     }
 }
 
+// f32 ArrayFire (W,H,C,N) -> bf16 [N][H*W][Cpad], over the flattened pixel
+// plane P = W*H (NCHW and NHWC both keep pixels in y*W + x order, so the
+// conversion is a transpose of [C][P] per image, independent of W).  A block
+// converts 128 pixels x 64 channels:
+//   phase 1: a thread reads four pixels of two channels (two 16-byte loads;
+//            eight lanes cover 128 contiguous bytes of a channel row) and
+//            stores one bf16x2 word per pixel into [pixel][32 words], word
+//            column c2 ^ 4*((pixel >> 2) & 7) (conflict-free for the 32
+//            lanes of a warp);
+//   phase 2: a thread reads one pixel's eight channels (16 bytes: the
+//            swizzle keeps each aligned group of four words contiguous) and
+//            stores them to the pixel's 128-byte row.
+// Pixels beyond P and channels beyond C are zero.  Needs P % 4 == 0 and a
+// 16-byte aligned source; to_nhwc_bf16_kernel covers the rest.
+constexpr int CV_PIX = 128;
+__global__ void __launch_bounds__(256) to_nhwc_flat_bf16_kernel(const float *__restrict__ in,
+                                                                long long P, int C, int Cpad,
+                                                                long long tiles_p,
+                                                                long long ntiles,
+                                                                __nv_bfloat16 *__restrict__ out) {
+    __shared__ __align__(16) uint32_t tile[CV_PIX * 32];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int nck = Cpad / 64;
+    for (long long bt = blockIdx.x; bt < ntiles; bt += gridDim.x) {
+        const long long ck = bt % nck;
+        const long long r = bt / nck;
+        const long long pt = r % tiles_p;
+        const long long n = r / tiles_p;
+        const long long p0 = pt * CV_PIX;
+        const int c0 = (int)ck * 64;
+        // phase 1: item = (c2 in 0..31, p4 in 0..31); lane -> p4 low 3 bits, c2 low 2 bits
+#pragma unroll
+        for (int it = 0; it < 4; ++it) {
+            const int combo = warp * 4 + it;  // 0..31: (c2_hi 0..7, p4_hi 0..3)
+            const int p4 = (combo & 3) * 8 + (lane & 7);
+            const int c2 = (combo >> 2) * 4 + (lane >> 3);
+            const int c = c0 + 2 * c2;
+            const long long px = p0 + 4 * p4;
+            float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+            if (px < P) {
+                const float *src = in + (n * C + c) * P + px;
+                if (c < C) a = __ldg(reinterpret_cast<const float4 *>(src));
+                if (c + 1 < C) b = __ldg(reinterpret_cast<const float4 *>(src + P));
+            }
+            const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int pl = 4 * p4 + i;
+                __nv_bfloat162 h = __floats2bfloat162_rn(av[i], bv[i]);
+                tile[pl * 32 + (c2 ^ (4 * (p4 & 7)))] = *reinterpret_cast<uint32_t *>(&h);
+            }
+        }
+        __syncthreads();
+        // phase 2: item = (pixel 0..127, 16-byte chunk j 0..7)
+#pragma unroll
+        for (int it = 0; it < 4; ++it) {
+            const int item = it * 256 + t;
+            const int pl = item >> 3, j = item & 7;
+            const long long px = p0 + pl;
+            if (px < P) {
+                const uint4 w = *reinterpret_cast<const uint4 *>(
+                    &tile[pl * 32 + 4 * (j ^ ((pl >> 2) & 7))]);
+                *reinterpret_cast<uint4 *>(out + (n * P + px) * Cpad + c0 + 8 * j) = w;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // weights (fw,fh,C,K) f32 -> bf16 GEMM operand with the reference's flip:
 // forward  Wt[och=k][tap*Cpad + c];  data grad Wt[och=c][tap*Kpad + k]
 // with tap = u + fw*v multiplying w[fw-1-u, fh-1-v, c, k]; padded rows and
@@ -1232,11 +1571,12 @@ static EncodeTiledFn encode_fn() {
 
 // 2-D tensor [rows][cols] (cols contiguous) of bf16 (esize 2) or e4m3 bytes
 // (esize 1), box 128 bytes x 128 rows, 128B swizzle
-static CUtensorMap make_wmap(const void *ptr, long long rows, long long cols, int esize = 2) {
+static CUtensorMap make_wmap(const void *ptr, long long rows, long long cols, int esize = 2,
+                             int box_rows = 128) {
     CUtensorMap m;
     cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
     cuuint64_t strides[1] = {(cuuint64_t)cols * esize};
-    cuuint32_t box[2] = {(cuuint32_t)(128 / esize), 128};
+    cuuint32_t box[2] = {(cuuint32_t)(128 / esize), (cuuint32_t)box_rows};
     cuuint32_t es[2] = {1, 1};
     CUresult r = encode_fn()(&m, esize == 2 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_UINT8,
                              2, (void *)ptr, dims, strides, box,
@@ -1271,6 +1611,20 @@ static int round_up(int v, int m) { return (v + m - 1) / m * m; }
 static __nv_bfloat16 *to_nhwc(const float *src, int W, int H, int C, int N, int Cpad) {
     __nv_bfloat16 *out =
         static_cast<__nv_bfloat16 *>(alloc_device((size_t)W * H * N * Cpad * sizeof(__nv_bfloat16)));
+    const long long P = (long long)W * H;
+    if ((P & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+        const long long tiles_p = (P + CV_PIX - 1) / CV_PIX;
+        const long long ntiles = tiles_p * N * (Cpad / 64);
+        const unsigned grid = (unsigned)std::min<long long>(ntiles, (long long)num_sms() * 8);
+        {
+            KernelTimer kt("tc_convert_kernel");
+            to_nhwc_flat_bf16_kernel<<<grid, 256, 0, stream()>>>(src, P, C, Cpad, tiles_p, ntiles,
+                                                                 out);
+        }
+        count_launch();
+        AFGB_POST_LAUNCH("to_nhwc_flat_bf16_kernel");
+        return out;
+    }
     dim3 grid((unsigned)((W + 63) / 64), (unsigned)(H * N), (unsigned)(Cpad / 64));
     {
         KernelTimer kt("tc_convert_kernel");
@@ -1279,6 +1633,34 @@ static __nv_bfloat16 *to_nhwc(const float *src, int W, int H, int C, int N, int 
     count_launch();
     AFGB_POST_LAUNCH("to_nhwc_bf16_kernel");
     return out;
+}
+
+// The signal in bf16 channels-last form for the tensor-core kernels.  A
+// dense f32 array in library-owned memory keeps its converted copy on its
+// buffer, so the forward and the filter gradient of one training step
+// convert the signal once; the copy is dropped as soon as anything writes
+// the buffer (or hands it out for writing), and it is reused only on the
+// stream it was made on.  Other arrays are converted per call; `owned` then
+// tells the caller to free the copy.
+static const __nv_bfloat16 *signal_nhwc(const Array &sig, int W, int H, int C, int N, int Cpad,
+                                        bool &owned) {
+    Buffer *b = sig.buf.get();
+    const bool cacheable = b && b->kind == BufKind::Pool && sig.type == f32 && sig.is_linear();
+    owned = !cacheable;
+    if (!cacheable) return to_nhwc(sig.ptr<float>(), W, H, C, N, Cpad);
+    unsigned long long key = (unsigned long long)sig.offset;
+    for (long long v : {(long long)W, (long long)H, (long long)C, (long long)N, (long long)Cpad})
+        key = key * 0x100000001B3ull ^ (unsigned long long)v;
+    key |= 1ull;  // never 0 (no copy)
+    std::lock_guard<std::mutex> lk(b->derived_mu);
+    if (b->derived && b->derived_key == key && b->derived_stream == stream())
+        return static_cast<const __nv_bfloat16 *>(b->derived);
+    __nv_bfloat16 *x = to_nhwc(sig.ptr<float>(), W, H, C, N, Cpad);
+    if (b->derived) free_device(b->derived);
+    b->derived = x;
+    b->derived_key = key;
+    b->derived_stream = stream();
+    return x;
 }
 
 static bool foldable(const NNGeom &g) { return g.C * g.fw * g.fh <= 64; }
@@ -1546,6 +1928,109 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     if (amax) free_device(amax);
 }
 
+// Stride-1 forward (mode 0) or data gradient (mode 1) by the strip kernel,
+// from the source already in bf16 NHWC with channels padded to 64.  False
+// (nothing launched) when the shape is outside its limits: unit strides, at
+// most 128 output channels, strips of at most SC_MAXSL pixels and SC_MAXS
+// rows per chunk, and rows long enough that 128-pixel segments waste at most
+// a quarter of the MMA rows.  The gather kernel is measured faster on the
+// shapes both cover, so the strip kernel runs only when AFGB_NN_KERNEL=strip
+// selects it (its parity tests run that way).
+static bool strip_conv_fits(const NNGeom &g, int mode) {
+    static const int wanted = [] {
+        const char *e = std::getenv("AFGB_NN_KERNEL");
+        return e && std::strcmp(e, "strip") == 0 ? 1 : 0;
+    }();
+    if (!wanted) return false;
+    if (g.sx != 1 || g.sy != 1 || g.fw * g.fh > MAX_T) return false;
+    const long long DW = mode == 0 ? g.Wo : g.W, DC = mode == 0 ? g.K : g.C;
+    if (DC > SC_MAXN || DW < 96) return false;
+    const long long nseg = (DW + 127) / 128;
+    if ((nseg * 128 - DW) * 4 > nseg * 128) return false;
+    if ((g.fw - 1) * g.dx > SC_MAXSL - 128) return false;
+    if (SC_R + (g.fh - 1) * g.dy > SC_MAXS) return false;
+    const long long SW = mode == 0 ? g.W : g.Wo, SH = mode == 0 ? g.H : g.Ho;
+    return SW < (1 << 24) && SH < (1 << 24) && g.N < (1 << 24);
+}
+
+static void run_strip_conv(const NNGeom &g, int mode, const __nv_bfloat16 *img, const float *w_f32,
+                           float *dst, const NNEpilogue *ep) {
+    const int SW = mode == 0 ? (int)g.W : (int)g.Wo;
+    const int SH = mode == 0 ? (int)g.H : (int)g.Ho;
+    const int SC = mode == 0 ? (int)g.C : (int)g.K;
+    const int DW = mode == 0 ? (int)g.Wo : (int)g.W;
+    const int DH = mode == 0 ? (int)g.Ho : (int)g.H;
+    const int DC = mode == 0 ? (int)g.K : (int)g.C;
+    const int SCpad = round_up(SC, 64);
+    const int OCpad = round_up(DC, 64);
+    const int taps = (int)(g.fw * g.fh);
+    __nv_bfloat16 *wt =
+        static_cast<__nv_bfloat16 *>(alloc_device((size_t)OCpad * taps * SCpad * 2));
+    {
+        const long long total = (long long)OCpad * taps * SCpad;
+        const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
+        weights_bf16_kernel<<<blocks, 256, 0, stream()>>>(w_f32, (int)g.fw, (int)g.fh, (int)g.C,
+                                                          (int)g.K, mode, OCpad, SCpad, wt);
+        count_launch();
+        AFGB_POST_LAUNCH("weights_bf16_kernel");
+    }
+    StripConvParams p;
+    std::memset(&p, 0, sizeof(p));
+    p.dst = dst;
+    if (ep && mode == 0) {
+        p.bias = ep->bias;
+        p.relu = ep->relu;
+    }
+    p.SW = SW;
+    p.SH = SH;
+    p.SCpad = SCpad;
+    p.N = (int)g.N;
+    p.DW = DW;
+    p.DH = DH;
+    p.DC = DC;
+    p.nmma = round_up(DC, 16);
+    p.nchunk = SCpad / 64;
+    p.ntaps = taps;
+    // per-tap source offsets of an output pixel: forward (u*dx - px, v*dy - py),
+    // data gradient (px - u*dx, py - v*dy)
+    int oxs[MAX_T], oys[MAX_T];
+    int oxmin = 1 << 30, oxmax = -(1 << 30), oymin = 1 << 30, oymax = -(1 << 30);
+    for (int t = 0; t < taps; ++t) {
+        const int u = t % (int)g.fw, v = t / (int)g.fw;
+        oxs[t] = mode == 0 ? u * (int)g.dx - (int)g.px : (int)g.px - u * (int)g.dx;
+        oys[t] = mode == 0 ? v * (int)g.dy - (int)g.py : (int)g.py - v * (int)g.dy;
+        oxmin = std::min(oxmin, oxs[t]);
+        oxmax = std::max(oxmax, oxs[t]);
+        oymin = std::min(oymin, oys[t]);
+        oymax = std::max(oymax, oys[t]);
+    }
+    p.ox_min = oxmin;
+    p.oy_min = oymin;
+    p.SL = 128 + (oxmax - oxmin);
+    p.S = SC_R + (oymax - oymin);
+    p.strip16 = SC_STRIP >> 4;
+    for (int t = 0; t < taps; ++t)
+        p.a_off[t] = (uint32_t)(((oys[t] - oymin) * SC_STRIP + (oxs[t] - oxmin) * 128) >> 4);
+    p.nb = std::min(SC_MAXNB, SC_B_AREA / (p.nmma * 128));
+    p.nseg = (DW + 127) / 128;
+    p.nrg = (DH + SC_R - 1) / SC_R;
+    p.total_tiles = p.nseg * p.nrg * (int)g.N;
+    CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad, 2, p.nmma);
+    CUtensorMap smap = make_imap(img, SCpad, SW, SH, (int)g.N, p.SL, 1);
+    const size_t smem = 1024 + (size_t)SC_NA * SC_MAXS * SC_STRIP + SC_B_AREA +
+                        sizeof(StripConvSmem) + 64;
+    if (p.total_tiles > 0) {
+        const int grid = std::min(p.total_tiles, num_sms());
+        KernelTimer kt(mode == 0 ? "tc_fwd_kernel" : "tc_dgrad_kernel");
+        AFGB_CUDA(cudaFuncSetAttribute(strip_conv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)smem));
+        strip_conv_kernel<<<grid, SC_THREADS, smem, stream()>>>(p, wmap, smap);
+        count_launch();
+        AFGB_POST_LAUNCH("strip_conv_kernel");
+    }
+    free_device(wt);
+}
+
 // the gather kernel's limits: phases and taps fit the parameter block,
 // 32-bit pixel coordinates
 static bool gather_fits(const NNGeom &g, int mode) {
@@ -1560,6 +2045,11 @@ static bool gather_fits(const NNGeom &g, int mode) {
 }  // namespace tc
 
 using namespace tc;
+
+void tc_set_wait_limit(unsigned int polls) {
+    const unsigned int v = polls ? polls : kSpinLimit;
+    AFGB_CUDA(cudaMemcpyToSymbol(g_spin_limit, &v, sizeof(v)));
+}
 
 unsigned int tc_take_error() {
     unsigned int v = 0, zero = 0;
@@ -1583,13 +2073,27 @@ bool tc_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out
                    nullptr, ep);
         return true;
     }
-    run_gather(g, 0, sig.ptr<float>(), filt.ptr<float>(), out.ptr<float>(), false, nullptr,
-               nullptr, nullptr, ep);
+    bool owned = false;
+    const __nv_bfloat16 *x = signal_nhwc(sig, (int)g.W, (int)g.H, (int)g.C, (int)g.N,
+                                         round_up((int)g.C, 64), owned);
+    if (strip_conv_fits(g, 0))
+        run_strip_conv(g, 0, x, filt.ptr<float>(), out.ptr<float>(), ep);
+    else
+        run_gather(g, 0, nullptr, filt.ptr<float>(), out.ptr<float>(), false, nullptr, nullptr, x,
+                   ep);
+    if (owned) free_device(const_cast<__nv_bfloat16 *>(x));
     return true;
 }
 
 bool tc_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &dx) {
     if (grad.type != f32 || !gather_fits(g, 1)) return false;
+    if (strip_conv_fits(g, 1)) {
+        const int Kp = round_up((int)g.K, 64);
+        __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kp);
+        run_strip_conv(g, 1, gg, filt.ptr<float>(), dx.ptr<float>(), nullptr);
+        free_device(gg);
+        return true;
+    }
     run_gather(g, 1, grad.ptr<float>(), filt.ptr<float>(), dx.ptr<float>());
     return true;
 }
@@ -1668,10 +2172,15 @@ static void filter_grad_from(const NNGeom &g0, const __nv_bfloat16 *gg, int Kpad
     const bool fold = foldable(g0);
     const NNGeom g = fold ? folded_geometry(g0) : g0;
     const int Cpad = round_up((int)g.C, 64);
-    __nv_bfloat16 *x = fold ? fold_taps(sig.ptr<float>(), g0)
-                            : to_nhwc(sig.ptr<float>(), (int)g.W, (int)g.H, (int)g.C, (int)g.N, Cpad);
+    bool owned = true;
+    const __nv_bfloat16 *x =
+        fold ? fold_taps(sig.ptr<float>(), g0)
+             : signal_nhwc(sig, (int)g.W, (int)g.H, (int)g.C, (int)g.N, Cpad, owned);
+    auto release = [&] {
+        if (owned) free_device(const_cast<__nv_bfloat16 *>(x));
+    };
     if (!fold && run_wgrad_strip(g, x, gg, Cpad, Kpad, g0, dw.ptr<float>())) {
-        free_device(x);
+        release();
         return;
     }
     WgradParams p;
@@ -1767,7 +2276,7 @@ static void filter_grad_from(const NNGeom &g0, const __nv_bfloat16 *gg, int Kpad
     // fixed-order compensated reduction over splits, flipped into (fw,fh,C,K)
     reduce_filter_partials(g0, partial, (int)splits, dw.ptr<float>());
     free_device(partial);
-    free_device(x);
+    release();
 }
 
 bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw) {
@@ -1788,7 +2297,10 @@ bool tc_data_filter_grads(const NNGeom &g, const Array &grad, const Array &sig, 
     const int Kpad = round_up((int)g.K, 128);
     if (Kpad != round_up((int)g.K, 64)) return false;
     __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kpad);
-    run_gather(g, 1, nullptr, filt.ptr<float>(), dx.ptr<float>(), false, nullptr, nullptr, gg);
+    if (strip_conv_fits(g, 1))
+        run_strip_conv(g, 1, gg, filt.ptr<float>(), dx.ptr<float>(), nullptr);
+    else
+        run_gather(g, 1, nullptr, filt.ptr<float>(), dx.ptr<float>(), false, nullptr, nullptr, gg);
     filter_grad_from(g, gg, Kpad, sig, dw);
     free_device(gg);
     return true;

@@ -21,6 +21,9 @@ namespace tc {
 __device__ unsigned int g_tc_error = 0;
 
 constexpr unsigned int kSpinLimit = 1u << 26;  // ~seconds of polling
+// polls before a bounded wait gives up: kSpinLimit unless the host lowered it
+// (afgb_debug_wait_limit, so that a test can make a wait run out quickly)
+__device__ unsigned int g_spin_limit = kSpinLimit;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
     return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -59,9 +62,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort,
                                           unsigned code) {
     unsigned int n = 0;
+    const unsigned int limit = g_spin_limit;
     while (!mbar_try_wait(bar, parity)) {
         if (*abort) return false;
-        if (++n > kSpinLimit) {
+        if (++n > limit) {
             *abort = 1;
             atomicOr(&g_tc_error, code);
             return false;

@@ -1,29 +1,35 @@
 """Benchmark of the spatial-convolution hot path on GB300.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--precision bf16|fp32] [--no-secondary]
+                    [--precision bf16|fp32|fp8] [--no-secondary]
 
 Headline (`value`): af_convolve2_nn forward + data gradient + filter
 gradient TFLOP/s on the 128x128x64x32 signal / 3x3x64x128 filter workload
 (stride 1, padding 1, dilation 1; 3 x 77.31 GFLOP per step), inputs resident
 in HBM, each step one pass of forward and both gradients.  Inputs are
 seeded synthetic N(0,1) / He-normal arrays (no dataset).  Timing: CUDA events
-on the launching stream around each step; between steps a 512 MB buffer is
-written to flush the 126 MB L2.
-
-`secondary` reports the bandwidth-bound direct convolutions (64 images of
-2048x2048 with the 15-tap separable filter in f32 and u8, 64 distinct 7x7
-filters in SAME batch mode, a 256^3 volume with a 3x3x3 filter) as HBM GB/s
-against the measured copy bandwidth.
+on the launching stream around each step, with the library's per-kernel
+timers off; between steps a 512 MB buffer is written to flush the 126 MB L2.
+Per-kernel times (the roofline) come from a separate pass with the kernel
+timers on.
 
 `e2e` is the same headline metric through the C ABI with host buffers:
 af_create_array from pinned host memory, the three calls, af_get_data_ptr
 back to host, all inside the timed region.
 
-`--impl reference` times the reference's CPU algorithm for the same metric
-(the oracle's C restatement of unwrap/wrap plus the BLAS sgemm bundled with
-numpy, as the reference CPU backend's unwrap + CBLAS path) on a bounded
-sample, with all host threads the BLAS can use.
+`cudnn` times cuDNN (through torch) on the same shapes, in BF16 and in FP32
+with TF32 off: the reference's CUDA backend calls cuDNN for this operation.
+`nn_workloads` adds the 56x56x256x64 1x1 workload, the FP8-E4M3 forward and
+the strided / dilated backward shapes, each with errors against FP64.
+`secondary` reports the bandwidth-bound direct convolutions and the patch /
+FFT lines as HBM GB/s against the measured copy bandwidth, each with its
+error against the oracle on a sampled slice and the reference CPU kernel's
+single-thread rate on a bounded sample of the same workload.
+
+`--impl reference` times the reference's CPU algorithm for the headline
+metric on full 32-image steps (the oracle's C restatement of unwrap/wrap plus
+the BLAS sgemm bundled with numpy, as the reference CPU backend's unwrap +
+CBLAS path), with all host threads the BLAS can use.
 
 Multi-GPU: the path does not shard (replicas only): each rank runs the same
 workload on its own GPU; `value` sums the ranks' work over the slowest rank's
@@ -32,6 +38,7 @@ time.
 from __future__ import annotations
 
 import argparse
+import concurrent.futures as cf
 import json
 import os
 import subprocess
@@ -47,16 +54,37 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = ("conv2_nn fwd+bwd TFLOP/s BF16-TC vs FP32 (rel err≤2e-2); convolve2 HBM GB/s")
 NN_SHAPE = dict(W=128, H=128, C=64, N=32, fw=3, fh=3, K=128, stride=(1, 1), pad=(1, 1), dil=(1, 1))
+# the other NN workloads: (W, H, C, N), (fw, fh, C, K), stride, padding, dilation
+NN_OTHER = {
+    "56x56x256x64_1x1x256x512": ((56, 56, 256, 64), (1, 1, 256, 512), (1, 1), (0, 0), (1, 1)),
+    "64x64x128x16_3x3x128x256_s2p1": ((64, 64, 128, 16), (3, 3, 128, 256), (2, 2), (1, 1),
+                                      (1, 1)),
+    "64x64x128x16_5x5x128x256_s2p4d2": ((64, 64, 128, 16), (5, 5, 128, 256), (2, 2), (4, 4),
+                                        (2, 2)),
+}
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each
 # tensor-core kernel on NN_SHAPE, from one ncu capture of `bench.py --only
 # fwd|dgrad|wgrad` (ncu cannot run inside the timed bench)
 NCU_TRAFFIC = {"tc_fwd_kernel": 67.30e6 + 212.86e6, "tc_dgrad_kernel": 134.60e6 + 90.88e6,
                "tc_wgrad_kernel": 206.02e6 + 18.06e6}
+MAIN_KERNELS = ("simt_fwd_kernel", "simt_dgrad_kernel", "simt_wgrad_kernel", "tc_fwd_kernel",
+                "tc_fwd_fp8_kernel", "tc_dgrad_kernel", "tc_wgrad_kernel", "tc_convert_kernel",
+                "wgrad_reduce_kernel")
+
+
+def shape_dict(sd, fd, st, pd, dl) -> dict:
+    return dict(W=sd[0], H=sd[1], C=sd[2], N=sd[3], fw=fd[0], fh=fd[1], K=fd[3], stride=st,
+                pad=pd, dil=dl)
+
+
+def nn_out_hw(s) -> tuple[int, int]:
+    Wo = 1 + (s["W"] + 2 * s["pad"][0] - ((s["fw"] - 1) * s["dil"][0] + 1)) // s["stride"][0]
+    Ho = 1 + (s["H"] + 2 * s["pad"][1] - ((s["fh"] - 1) * s["dil"][1] + 1)) // s["stride"][1]
+    return Wo, Ho
 
 
 def nn_flops(s=NN_SHAPE) -> float:
-    Wo = 1 + (s["W"] + 2 * s["pad"][0] - ((s["fw"] - 1) * s["dil"][0] + 1)) // s["stride"][0]
-    Ho = 1 + (s["H"] + 2 * s["pad"][1] - ((s["fh"] - 1) * s["dil"][1] + 1)) // s["stride"][1]
+    Wo, Ho = nn_out_hw(s)
     return 2.0 * Wo * Ho * s["N"] * s["K"] * s["fw"] * s["fh"] * s["C"]
 
 
@@ -69,6 +97,18 @@ def load_peaks() -> dict:
                 "source": "measured"}
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0,
             "source": "fallback"}
+
+
+def cpu_model() -> str:
+    try:
+        for ln in Path("/proc/cpuinfo").read_text().splitlines():
+            if ln.lower().startswith(("model name", "cpu part")):
+                return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+
+    return platform.machine()
 
 
 # ---------------------------------------------------------------------------
@@ -132,13 +172,15 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# our implementation
+# timing helpers
 # ---------------------------------------------------------------------------
-def _timed_steps(step_fn, steps: int, warmup: int, flush) -> tuple[float, list[float]]:
+def _timed(fn, steps: int, warmup: int, flush) -> list[float]:
+    """CUDA-event milliseconds of `steps` calls of fn after `warmup` calls,
+    with `flush` (an L2-sized write) before each timed call."""
     import torch
 
     for _ in range(warmup):
-        step_fn()
+        fn()
     torch.cuda.synchronize()
     times = []
     for _ in range(steps):
@@ -146,13 +188,236 @@ def _timed_steps(step_fn, steps: int, warmup: int, flush) -> tuple[float, list[f
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record()
-        step_fn()
+        fn()
         b.record()
         b.synchronize()
         times.append(a.elapsed_time(b))
-    return sum(times), times
+    return times
 
 
+def _kernel_times(af, fn, reps: int, flush) -> dict:
+    """Average device ms per launch of the library's main kernels over `reps`
+    calls of fn, with the kernel timers on (a pass apart from the timed one)."""
+    import ctypes
+
+    import torch
+
+    L = af.lib()
+    fn()
+    torch.cuda.synchronize()
+    L.afgb_kernel_timing(1)
+    for _ in range(reps):
+        flush()
+        fn()
+    torch.cuda.synchronize()
+    kt = {}
+    for name in MAIN_KERNELS:
+        c = ctypes.c_ulonglong()
+        ms = ctypes.c_double()
+        L.afgb_kernel_time(name.encode(), ctypes.byref(c), ctypes.byref(ms))
+        if c.value:
+            kt[name] = {"launches": int(c.value), "avg_ms": ms.value / c.value,
+                        "per_call": c.value / reps}
+    L.afgb_kernel_timing(0)
+    return kt
+
+
+def _err(got, ref) -> dict:
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    return {"rel": float(np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-300)),
+            "maxabs": float(np.abs(got - ref).max()),
+            "maxabs_over_max_ref": float(np.abs(got - ref).max() / max(np.abs(ref).max(), 1e-300))}
+
+
+def make_flush():
+    import torch
+
+    buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    return lambda: buf.zero_()
+
+
+# ---------------------------------------------------------------------------
+# NN workloads
+# ---------------------------------------------------------------------------
+def nn_inputs(s, seed):
+    g = np.random.Generator(np.random.Philox(seed))
+    X = np.asfortranarray(g.standard_normal((s["W"], s["H"], s["C"], s["N"]), dtype=np.float32))
+    std = np.sqrt(2.0 / (s["fw"] * s["fh"] * s["C"]))
+    Wt = np.asfortranarray((g.standard_normal((s["fw"], s["fh"], s["C"], s["K"])) * std
+                            ).astype(np.float32))
+    Wo, Ho = nn_out_hw(s)
+    Gd = np.asfortranarray(g.standard_normal((Wo, Ho, s["K"], s["N"]), dtype=np.float32))
+    return X, Wt, Gd, g
+
+
+def nn_errors(af, O, s, X, Wt, Gd, prec, g, grads=True) -> dict:
+    """Errors of one forward (and gradient) call against FP64 on sampled points."""
+    st, pd, dl = s["stride"], s["pad"], s["dil"]
+    Xa, Wa, Ga = af.Array.from_numpy(X), af.Array.from_numpy(Wt), af.Array.from_numpy(Gd)
+    y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec).to_numpy().ravel(order="F")
+    idx = g.integers(0, y.size, 256)
+    out = {"fwd": _err(y[idx], O.nn_forward_points_f64(X, Wt, st, pd, dl, idx))}
+    if grads:
+        dx, dw, _ = af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
+        dxn = dx.to_numpy().ravel(order="F")
+        i2 = g.integers(0, X.size, 128)
+        out["dgrad"] = _err(dxn[i2], O.nn_data_grad_points_f64(Gd, list(X.shape), Wt, st, pd, dl,
+                                                                i2))
+        dwn = dw.to_numpy().ravel(order="F")
+        i3 = g.integers(0, Wt.size, 64)
+        out["wgrad"] = _err(dwn[i3], O.nn_filter_grad_points_f64(Gd, X, list(Wt.shape), st, pd, dl,
+                                                                  i3))
+    out["points"] = [256, 128, 64] if grads else [256]
+    return out
+
+
+def nn_workload(af, O, s, prec, steps, flush, seed, grads=True) -> dict:
+    """Device time of forward (+ both gradients) per step on one NN shape,
+    per-kernel times from a separate pass, and errors against FP64."""
+    X, Wt, Gd, g = nn_inputs(s, seed)
+    st, pd, dl = s["stride"], s["pad"], s["dil"]
+    Xa, Wa, Ga = af.Array.from_numpy(X), af.Array.from_numpy(Wt), af.Array.from_numpy(Gd)
+
+    def step():
+        Xa.device_ptr()  # a new signal each step (drops the converted copy)
+        af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
+        if grads:
+            af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
+
+    times = _timed(step, steps, 3, flush)
+    ms = float(np.median(times))
+    fl = nn_flops(s) * (3 if grads else 1)
+    kt = _kernel_times(af, step, 3, flush)
+    errs = nn_errors(af, O, s, X, Wt, Gd, prec, g, grads)
+    return {"precision": prec, "ops": "fwd+dgrad+wgrad" if grads else "fwd",
+            "gflop_per_step": round(fl / 1e9, 2), "ms_per_step": round(ms, 4),
+            "TFLOP/s": round(fl / (ms / 1e3) / 1e12, 1),
+            "kernel_ms": {k: round(v["avg_ms"], 4) for k, v in kt.items()},
+            "errors_vs_fp64": errs}
+
+
+def cudnn_bar(s, steps, flush) -> dict:
+    """cuDNN through torch on one NN shape: forward (conv2d with the filter
+    flipped, since af_convolve2_nn is a true convolution) and the backward of
+    data and filter (aten.convolution_backward), BF16 and FP32 with TF32 off,
+    in NCHW and channels-last; the faster layout is kept per precision.
+    Inputs are already in the timed precision and layout (the library's own
+    times include its f32 -> bf16 conversions)."""
+    import torch
+    import torch.nn.functional as F
+
+    torch.backends.cudnn.benchmark = True
+    torch.backends.cudnn.allow_tf32 = False
+    torch.backends.cuda.matmul.allow_tf32 = False
+    gen = torch.Generator(device="cuda").manual_seed(3)
+    Wo, Ho = nn_out_hw(s)
+    x0 = torch.randn((s["N"], s["C"], s["H"], s["W"]), device="cuda", generator=gen)
+    w0 = torch.randn((s["K"], s["C"], s["fh"], s["fw"]), device="cuda", generator=gen) * 0.05
+    g0 = torch.randn((s["N"], s["K"], Ho, Wo), device="cuda", generator=gen)
+    stv = (s["stride"][1], s["stride"][0])
+    pdv = (s["pad"][1], s["pad"][0])
+    dlv = (s["dil"][1], s["dil"][0])
+    fl = nn_flops(s)
+    res = {}
+    for name, dt in (("bf16", torch.bfloat16), ("fp32_no_tf32", torch.float32)):
+        best = None
+        for layout in ("nchw", "channels_last"):
+            mf = torch.channels_last if layout == "channels_last" else torch.contiguous_format
+            x = x0.to(dt).contiguous(memory_format=mf)
+            w = w0.flip([2, 3]).to(dt).contiguous(memory_format=mf)
+            gg = g0.to(dt).contiguous(memory_format=mf)
+
+            def fwd():
+                return F.conv2d(x, w, None, stv, pdv, dlv)
+
+            def bwd():
+                return torch.ops.aten.convolution_backward(gg, x, w, None, stv, pdv, dlv, False,
+                                                           [0, 0], 1, [True, True, False])
+
+            def dgr():
+                return torch.ops.aten.convolution_backward(gg, x, w, None, stv, pdv, dlv, False,
+                                                           [0, 0], 1, [True, False, False])
+
+            def wgr():
+                return torch.ops.aten.convolution_backward(gg, x, w, None, stv, pdv, dlv, False,
+                                                           [0, 0], 1, [False, True, False])
+
+            def step():
+                fwd()
+                bwd()
+
+            t = {k: float(np.median(_timed(f, steps, 3, flush)))
+                 for k, f in (("fwd", fwd), ("dgrad", dgr), ("wgrad", wgr), ("bwd", bwd),
+                              ("step", step))}
+            rec = {"layout": layout, **{k + "_ms": round(v, 4) for k, v in t.items()},
+                   "step_TFLOP/s": round(3 * fl / (t["step"] / 1e3) / 1e12, 1)}
+            if best is None or t["step"] < best["step_ms"]:
+                best = rec
+        res[name] = best
+    # the reference's own call: f32 NCHW arrays, cuDNN's default math type
+    # (src/backend/cuda/convolveNN.cpp sets none), which lets FP32
+    # convolutions run on TF32 tensor cores
+    torch.backends.cudnn.allow_tf32 = True
+    x, w, gg = x0.contiguous(), w0.flip([2, 3]).contiguous(), g0.contiguous()
+
+    def step_ref():
+        F.conv2d(x, w, None, stv, pdv, dlv)
+        torch.ops.aten.convolution_backward(gg, x, w, None, stv, pdv, dlv, False, [0, 0], 1,
+                                            [True, True, False])
+    t = float(np.median(_timed(step_ref, steps, 3, flush)))
+    res["fp32_default_math_nchw"] = {"layout": "nchw", "step_ms": round(t, 4),
+                                     "step_TFLOP/s": round(3 * fl / (t / 1e3) / 1e12, 1),
+                                     "note": "TF32 tensor cores allowed, as in the reference"}
+    torch.backends.cudnn.allow_tf32 = False
+    # BF16 cuDNN for a caller holding f32 NCHW arrays (this library's
+    # interface): casts to bf16 channels-last in, f32 NCHW out, inside the step
+    cl = torch.channels_last
+
+    def step_cast():
+        xb = x0.to(torch.bfloat16).contiguous(memory_format=cl)
+        wb = w0.flip([2, 3]).to(torch.bfloat16).contiguous(memory_format=cl)
+        gb = g0.to(torch.bfloat16).contiguous(memory_format=cl)
+        y = F.conv2d(xb, wb, None, stv, pdv, dlv)
+        y.float().contiguous()
+        dx, dw, _ = torch.ops.aten.convolution_backward(gb, xb, wb, None, stv, pdv, dlv, False,
+                                                        [0, 0], 1, [True, True, False])
+        dx.float().contiguous()
+        dw.float().contiguous()
+    t = float(np.median(_timed(step_cast, steps, 3, flush)))
+    res["bf16_from_f32_arrays"] = {"layout": "channels_last", "step_ms": round(t, 4),
+                                   "step_TFLOP/s": round(3 * fl / (t / 1e3) / 1e12, 1),
+                                   "note": "casts of signal, filter and incoming gradient to bf16 "
+                                           "channels-last and of the three results to f32 NCHW "
+                                           "inside the step"}
+    torch.backends.cudnn.benchmark = False
+    return res
+
+
+def ours_split(af, s, prec, steps, flush, seed) -> dict:
+    """The library's forward call and gradients call timed apart (same events
+    and flush as the cuDNN bar)."""
+    X, Wt, Gd, _ = nn_inputs(s, seed)
+    st, pd, dl = s["stride"], s["pad"], s["dil"]
+    Xa, Wa, Ga = af.Array.from_numpy(X), af.Array.from_numpy(Wt), af.Array.from_numpy(Gd)
+    def fwd():
+        Xa.device_ptr()  # a new signal each call (drops the converted copy)
+        af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
+
+    def step():
+        fwd()
+        af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
+
+    t = {k: float(np.median(_timed(f, steps, 3, flush))) for k, f in (("fwd", fwd), ("step", step))}
+    t["bwd"] = t["step"] - t["fwd"]  # the gradients after a forward of the same signal
+    fl = nn_flops(s)
+    return {**{k + "_ms": round(v, 4) for k, v in t.items()},
+            "step_TFLOP/s": round(3 * fl / (t["step"] / 1e3) / 1e12, 1)}
+
+
+# ---------------------------------------------------------------------------
+# our implementation
+# ---------------------------------------------------------------------------
 def run_ours(args, peaks, rank: int, world: int) -> dict:
     import torch
 
@@ -162,56 +427,38 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
     torch.cuda.set_device(dev)
     af.set_stream(torch.cuda.current_stream())
     L = af.lib()
+    L.afgb_kernel_timing(0)
     s = NN_SHAPE
-    g = np.random.Generator(np.random.Philox(1234 + rank))
-    X = np.asfortranarray(g.standard_normal((s["W"], s["H"], s["C"], s["N"]), dtype=np.float32))
-    std = np.sqrt(2.0 / (s["fw"] * s["fh"] * s["C"]))
-    Wt = np.asfortranarray((g.standard_normal((s["fw"], s["fh"], s["C"], s["K"])) * std
-                            ).astype(np.float32))
+    X, Wt, Gd, g = nn_inputs(s, 1234 + rank)
     Xa, Wa = af.Array.from_numpy(X), af.Array.from_numpy(Wt)
     st, pd, dl = s["stride"], s["pad"], s["dil"]
     prec = args.precision
     try:
-        Y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
+        af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
     except af.AfError as e:
         if prec == "fp32" or e.code != af.AF_ERR_NOT_SUPPORTED:
             raise
         prec = "fp32"
-        Y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
-    Gd = np.asfortranarray(g.standard_normal(Y.dims, dtype=np.float32))
     Ga = af.Array.from_numpy(Gd)
-    flush_buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-
-    def flush():
-        flush_buf.zero_()
+    flush = make_flush()
+    grads = prec != "fp8"  # FP8 is provided for the forward only
 
     def step():
-        # forward, then both input gradients in one call (one shared bf16
-        # copy of the incoming gradient)
+        # a new signal each step, as in training: handing the buffer out for
+        # writing (af_get_device_ptr) drops the library's bf16 copy of the
+        # previous signal, so the forward converts it again.  The forward,
+        # then both input gradients in one call (one shared bf16 copy of the
+        # incoming gradient; the signal's copy from the forward reused)
+        Xa.device_ptr()
         y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
-        dx, dw, _ = af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
-        return y, dx, dw
+        if grads:
+            af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
+        return y
 
-    # parity of this exact workload against FP64 on sampled points
-    y, dx, dw = step()
     import oracle.oracle as O  # checker only
 
-    idx = g.integers(0, int(np.prod(Y.dims)), 256)
-    ref = O.nn_forward_points_f64(X, Wt, st, pd, dl, idx)
-    got = y.to_numpy().ravel(order="F")[idx].astype(np.float64)
-    rel_fwd = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
-    maxabs_fwd = float(np.abs(got - ref).max())
-    idx2 = g.integers(0, X.size, 128)
-    ref2 = O.nn_data_grad_points_f64(Gd, list(X.shape), Wt, st, pd, dl, idx2)
-    got2 = dx.to_numpy().ravel(order="F")[idx2].astype(np.float64)
-    rel_dx = float(np.linalg.norm(got2 - ref2) / np.linalg.norm(ref2))
-    idx3 = g.integers(0, Wt.size, 64)
-    ref3 = O.nn_filter_grad_points_f64(Gd, X, list(Wt.shape), st, pd, dl, idx3)
-    got3 = dw.to_numpy().ravel(order="F")[idx3].astype(np.float64)
-    rel_dw = float(np.linalg.norm(got3 - ref3) / np.linalg.norm(ref3))
-    del y, dx, dw
+    errs = nn_errors(af, O, s, X, Wt, Gd, prec, g, grads)
 
-    L.afgb_kernel_timing(1)
     launches0 = af.launch_count()
     if world > 1:
         import torch.distributed as dist
@@ -220,41 +467,31 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
     torch.cuda.synchronize()
     clock = ClockSampler(dev)
     clock.start()
-    total_ms, times = _timed_steps(step, args.steps, args.warmup, flush)
+    times = _timed(step, args.steps, args.warmup, flush)
     clocks = clock.stop()
-    launches = af.launch_count() - launches0
     torch.cuda.synchronize()
+    launches = (af.launch_count() - launches0) * args.steps // (args.steps + args.warmup)
+    total_ms = sum(times)
+    flops = nn_flops() * (3 if grads else 1)
+    value = flops * args.steps / (total_ms / 1e3) / 1e12
 
-    # dominant kernel timing (events around each launch, same stream)
-    import ctypes
-
-    kt = {}
-    for name in ("simt_fwd_kernel", "simt_dgrad_kernel", "simt_wgrad_kernel", "tc_fwd_kernel",
-                 "tc_dgrad_kernel", "tc_wgrad_kernel", "tc_convert_kernel", "wgrad_reduce_kernel"):
-        c = ctypes.c_ulonglong()
-        ms = ctypes.c_double()
-        L.afgb_kernel_time(name.encode(), ctypes.byref(c), ctypes.byref(ms))
-        if c.value:
-            kt[name] = (c.value, ms.value)
-    L.afgb_kernel_timing(0)
-    flops = nn_flops()
-    steps_total = args.warmup + args.steps
-    value = 3 * flops * args.steps / (total_ms / 1e3) / 1e12
-
-    mains = {k: v for k, v in kt.items() if k.endswith(("fwd_kernel", "dgrad_kernel", "wgrad_kernel"))}
-    dom = max(mains.items(), key=lambda kv: kv[1][1]) if mains else None
+    # per-kernel device times: a separate pass with the kernel timers on
+    kt = _kernel_times(af, step, 5, flush)
+    mains = {k: v for k, v in kt.items() if k.endswith(("fwd_kernel", "fwd_fp8_kernel",
+                                                       "dgrad_kernel", "wgrad_kernel"))}
+    dom = max(mains.items(), key=lambda kv: kv[1]["avg_ms"]) if mains else None
     roofline = None
     if dom:
-        name, (cnt, ms) = dom
-        avg_s = ms / cnt / 1e3
-        achieved = flops / avg_s / 1e12
+        name, v = dom
+        achieved = nn_flops() / (v["avg_ms"] / 1e3) / 1e12
         peak = peaks["bf16_tflops"]
         roofline = {"bound": "tensor", "kernel": name, "achieved": round(achieved, 2),
                     "peak": peak, "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
-                    "peak_source": peaks["source"] + " bf16 dense",
+                    "peak_source": peaks["source"] + " bf16 dense (burst)",
                     "traffic": NCU_TRAFFIC.get(name) if prec == "bf16" else None,
                     "traffic_source": "ncu capture, one launch (bytes)",
-                    "launches": cnt, "avg_ms": round(ms / cnt, 4)}
+                    "avg_ms": round(v["avg_ms"], 4),
+                    "algorithmic_gflop_per_launch": round(nn_flops() / 1e9, 2)}
 
     # e2e through the C ABI with pinned host buffers
     e2e = run_e2e(af, X, Wt, Gd, prec, args)
@@ -262,29 +499,75 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
     # the plain FP32 CUDA-core path on the same workload (the >= 5x target's
     # denominator), fewer steps
     fp32 = None
-    if prec != "fp32":
+    if prec == "bf16":
         def step32():
-            y = af.convolve2_nn(Xa, Wa, st, pd, dl)
-            dx, dw, _ = af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl)
-            return y, dx, dw
+            af.convolve2_nn(Xa, Wa, st, pd, dl)
+            af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl)
         k32 = max(3, min(args.steps, 5))
-        t32, _ = _timed_steps(step32, k32, 3, flush)
-        v32 = 3 * flops * k32 / (t32 / 1e3) / 1e12
+        t32 = sum(_timed(step32, k32, 3, flush))
+        v32 = 3 * nn_flops() * k32 / (t32 / 1e3) / 1e12
         fp32 = {"value": v32, "ms_per_step": t32 / k32, "unit": "TFLOP/s",
                 "speedup_of_" + prec: value / v32}
 
     res = {
         "value": value, "ms_per_step": total_ms / args.steps, "precision": prec,
-        "errors_vs_fp64": {"fwd_rel": rel_fwd, "fwd_maxabs": maxabs_fwd, "dgrad_rel": rel_dx,
-                           "wgrad_rel": rel_dw, "points": [256, 128, 64]},
-        "kernel_times_ms": {k: round(v[1] / v[0], 4) for k, v in kt.items()},
+        "errors_vs_fp64": errs,
+        "kernel_times_ms": {k: round(v["avg_ms"], 4) for k, v in kt.items()},
+        "kernel_launches_per_step": {k: v["per_call"] for k, v in kt.items()},
         "roofline": roofline, "clocks": clocks, "e2e": e2e, "fp32_path": fp32,
         "gpu_launches": int(launches), "step_times_ms": [round(t, 4) for t in times],
     }
+    del Xa, Wa, Ga
+    if not args.no_secondary and prec == "bf16":
+        res["cudnn"] = run_cudnn_comparison(af, args, flush)
+        res["nn_workloads"] = run_nn_workloads(af, O, args, flush)
     if not args.no_secondary:
-        res["secondary"] = run_direct_workloads(af, peaks, args)
+        res["secondary"] = run_direct_workloads(af, O, peaks, args)
         res["cnn4"] = run_cnn(af, args)
     return res
+
+
+def run_cudnn_comparison(af, args, flush) -> dict:
+    steps = max(5, min(args.steps, 10))
+    out = {"note": "cuDNN via torch " + __import__("torch").__version__ + ", cudnn.benchmark on; "
+                   "inputs pre-converted to the timed precision/layout (ours: f32 arrays in, "
+                   "conversions inside the timed calls)"}
+    for key, shp in (("128x128x64x32_3x3x64x128", NN_SHAPE),
+                     ("56x56x256x64_1x1x256x512", shape_dict(*NN_OTHER["56x56x256x64_1x1x256x512"]))):
+        c = cudnn_bar(shp, steps, flush)
+        o = ours_split(af, shp, "bf16", steps, flush, 21)
+        o32 = ours_split(af, shp, "fp32", 3, flush, 21)
+        out[key] = {"cudnn": c, "ours_bf16": o, "ours_fp32": o32,
+                    "ours_bf16_speedup_over_cudnn_bf16": {
+                        "fwd": round(c["bf16"]["fwd_ms"] / o["fwd_ms"], 3),
+                        "bwd": round(c["bf16"]["bwd_ms"] / o["bwd_ms"], 3),
+                        "step": round(c["bf16"]["step_ms"] / o["step_ms"], 3)},
+                    "ours_bf16_speedup_over_cudnn_bf16_from_f32_arrays": round(
+                        c["bf16_from_f32_arrays"]["step_ms"] / o["step_ms"], 3),
+                    "ours_bf16_speedup_over_reference_cudnn_call": round(
+                        c["fp32_default_math_nchw"]["step_ms"] / o["step_ms"], 3),
+                    "ours_fp32_speedup_over_cudnn_fp32": round(
+                        c["fp32_no_tf32"]["step_ms"] / o32["step_ms"], 3)}
+    return out
+
+
+def run_nn_workloads(af, O, args, flush) -> dict:
+    steps = max(5, min(args.steps, 10))
+    out = {}
+    s3b = shape_dict(*NN_OTHER["56x56x256x64_1x1x256x512"])
+    out["56x56x256x64_1x1x256x512_bf16"] = nn_workload(af, O, s3b, "bf16", steps, flush, 31)
+    out["56x56x256x64_1x1x256x512_fp32"] = nn_workload(af, O, s3b, "fp32", 3, flush, 31)
+    out["128x128x64x32_3x3x64x128_fp8_fwd"] = nn_workload(af, O, NN_SHAPE, "fp8", steps, flush, 32,
+                                                           grads=False)
+    out["56x56x256x64_1x1x256x512_fp8_fwd"] = nn_workload(af, O, s3b, "fp8", steps, flush, 33,
+                                                          grads=False)
+    out["128x128x64x32_3x3x64x128_bf16_fwd"] = nn_workload(af, O, NN_SHAPE, "bf16", steps, flush,
+                                                           32, grads=False)
+    for key in ("64x64x128x16_3x3x128x256_s2p1", "64x64x128x16_5x5x128x256_s2p4d2"):
+        sh = shape_dict(*NN_OTHER[key])
+        out[key + "_bf16"] = nn_workload(af, O, sh, "bf16", steps, flush, 41)
+        out[key + "_fp32"] = nn_workload(af, O, sh, "fp32", 3, flush, 41)
+    return out
 
 
 def run_e2e(af, X, Wt, Gd, prec, args) -> dict:
@@ -295,9 +578,10 @@ def run_e2e(af, X, Wt, Gd, prec, args) -> dict:
     L = af.lib()
     s = NN_SHAPE
     st, pd, dl = s["stride"], s["pad"], s["dil"]
+    grads = prec != "fp8"
     pin = {k: torch.from_numpy(np.ascontiguousarray(v.ravel(order="F"))).pin_memory()
            for k, v in (("x", X), ("w", Wt), ("g", Gd))}
-    Wo, Ho = X.shape[0], X.shape[1]
+    Wo, Ho = nn_out_hw(s)
     y_host = torch.empty(Wo * Ho * s["K"] * s["N"], dtype=torch.float32).pin_memory()
     dx_host = torch.empty(X.size, dtype=torch.float32).pin_memory()
     dw_host = torch.empty(Wt.size, dtype=torch.float32).pin_memory()
@@ -311,12 +595,13 @@ def run_e2e(af, X, Wt, Gd, prec, args) -> dict:
     def step():
         Xa = mk(pin["x"], X.shape)
         Wa = mk(pin["w"], Wt.shape)
-        Ga = mk(pin["g"], Gd.shape)
         y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
-        dx, dw, _ = af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
         af._check(L.af_get_data_ptr(ctypes.c_void_p(y_host.data_ptr()), y.handle))
-        af._check(L.af_get_data_ptr(ctypes.c_void_p(dx_host.data_ptr()), dx.handle))
-        af._check(L.af_get_data_ptr(ctypes.c_void_p(dw_host.data_ptr()), dw.handle))
+        if grads:
+            Ga = mk(pin["g"], Gd.shape)
+            dx, dw, _ = af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
+            af._check(L.af_get_data_ptr(ctypes.c_void_p(dx_host.data_ptr()), dx.handle))
+            af._check(L.af_get_data_ptr(ctypes.c_void_p(dw_host.data_ptr()), dw.handle))
 
     for _ in range(max(1, args.warmup)):
         step()
@@ -326,9 +611,9 @@ def run_e2e(af, X, Wt, Gd, prec, args) -> dict:
         step()
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
-    h2d = (X.size + Wt.size + Gd.size) * 4
-    d2h = (y_host.numel() + dx_host.numel() + dw_host.numel()) * 4
-    return {"value": 3 * nn_flops() * args.steps / dt / 1e12, "unit": "TFLOP/s",
+    h2d = (X.size + Wt.size + (Gd.size if grads else 0)) * 4
+    d2h = (y_host.numel() + ((dx_host.numel() + dw_host.numel()) if grads else 0)) * 4
+    return {"value": (3 if grads else 1) * nn_flops() * args.steps / dt / 1e12, "unit": "TFLOP/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "ms_per_step": dt * 1e3 / args.steps}
 
@@ -418,37 +703,66 @@ def run_cnn(af, args) -> dict:
     return out
 
 
-def run_direct_workloads(af, peaks, args) -> dict:
+# ---------------------------------------------------------------------------
+# bandwidth-bound lines: GPU GB/s, error on a sampled slice, CPU baseline
+# ---------------------------------------------------------------------------
+def cpu_direct_baseline(slice_fn, slices, bytes_per_slice, par_slices=None) -> dict:
+    """The reference CPU kernel (the oracle's C restatement of
+    src/backend/cpu/kernel/convolve.hpp, bit-identical to it) on a bounded
+    sample: `slices` run one after another on one thread, as libafcpu runs
+    each call on its one worker thread (src/backend/cpu/queue.hpp:79-118);
+    then, informational and not the reference's behaviour, `par_slices`
+    slices at once on all host threads.  Returns the first slice's output."""
+    t0 = time.perf_counter()
+    first = None
+    for b in slices:
+        r = slice_fn(b)
+        if first is None:
+            first = r
+    dt = time.perf_counter() - t0
+    out = {"value": round(bytes_per_slice * len(slices) / dt / 1e9, 3), "unit": "GB/s", "cores": 1,
+           "kind": "port", "sample": f"{len(slices)} slice(s), {bytes_per_slice} bytes each, "
+                                     "oracle C kernel on one thread"}
+    if par_slices:
+        n = len(par_slices)
+        with cf.ThreadPoolExecutor(max_workers=n) as ex:
+            t0 = time.perf_counter()
+            list(ex.map(slice_fn, par_slices))
+            dt = time.perf_counter() - t0
+        out["all_threads_informational"] = {
+            "value": round(bytes_per_slice * n / dt / 1e9, 3), "threads": n,
+            "note": "slices in parallel; libafcpu itself runs one call on one thread"}
+    return out, first
+
+
+def run_direct_workloads(af, O, peaks, args) -> dict:
     """Bandwidth-bound direct convolutions (64 x 2048^2 separable and 7x7,
-    256^3 volume) and the patch / FFT lines, GB/s of
-    algorithmic traffic (each input and output counted once)."""
+    256^3 volume, 64 x 2^20 1-D, the two small image workloads) and the
+    patch / FFT lines: GB/s of algorithmic traffic (each input and output
+    counted once), kernel time, error against the oracle on a sampled slice
+    of the same output, and the CPU baseline."""
     import ctypes
 
     import torch
 
     L = af.lib()
     g = np.random.Generator(np.random.Philox(77))
-    flush_buf = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    flush = make_flush()
+    nthreads = min(16, os.cpu_count() or 1)
     out = {}
 
-    def measure(name, fn, nbytes, kernel):
+    def measure(name, fn, nbytes, kernel, check=None):
         for _ in range(3):
             r = fn()
         del r
         torch.cuda.synchronize()
-        L.afgb_kernel_timing(1)
-        tot = 0.0
         steps = max(3, min(args.steps, 10))
-        for _ in range(steps):
-            flush_buf.zero_()
-            a = torch.cuda.Event(enable_timing=True)
-            b = torch.cuda.Event(enable_timing=True)
-            a.record()
-            r = fn()
-            b.record()
-            b.synchronize()
-            tot += a.elapsed_time(b)
-            del r
+        times = _timed(fn, steps, 0, flush)
+        L.afgb_kernel_timing(1)
+        for _ in range(3):
+            flush()
+            fn()
+        torch.cuda.synchronize()
         c = ctypes.c_ulonglong()
         ms = ctypes.c_double()
         for cand in kernel:  # the first candidate that ran is the one reported
@@ -459,7 +773,7 @@ def run_direct_workloads(af, peaks, args) -> dict:
         else:
             kernel = kernel[0]
         L.afgb_kernel_timing(0)
-        call_ms = tot / steps
+        call_ms = float(np.median(times))
         k_ms = ms.value / c.value if c.value else None
         gbs = nbytes / (call_ms / 1e3) / 1e9
         kgbs = nbytes / (k_ms / 1e3) / 1e9 if k_ms else None
@@ -468,37 +782,100 @@ def run_direct_workloads(af, peaks, args) -> dict:
                      "kernel_GB/s": round(kgbs, 1) if kgbs else None,
                      "frac_of_hbm": round((kgbs or gbs) / peaks["hbm_gbs"], 4),
                      "bytes": int(nbytes)}
+        if check is not None:
+            res = fn()
+            torch.cuda.synchronize()
+            out[name].update(check(res))
 
-    # 64 x 2048 x 2048 separable 15-tap, f32 and u8, LHS batch
+    def err_vs(got, ref):
+        got = np.asarray(got).ravel(order="F")
+        ref = np.asarray(ref).ravel(order="F")
+        assert got.size == ref.size, (got.size, ref.size)
+        e = _err(got, ref)
+        return {"max_err_vs_oracle": {"maxabs": e["maxabs"], "maxabs_over_max_ref":
+                                      e["maxabs_over_max_ref"],
+                                      "bit_exact": bool(np.asarray(got).tobytes() ==
+                                                        np.asarray(ref).tobytes())}}
+
+    def slice2(t, b):  # torch (B, H, W) slice b -> AF (W, H) Fortran
+        return np.asfortranarray(t[b].cpu().numpy().T)
+
+    # ---- the two small image workloads (fit in L2: flushed between calls)
+    sig1a = np.asfortranarray(np.random.Generator(np.random.Philox(0)).random((512, 512),
+                                                                             dtype=np.float32))
+    xg = np.arange(5) - 2
+    k1a = np.exp(-0.5 * (xg[:, None] ** 2 + xg[None, :] ** 2))
+    k1a = np.asfortranarray((k1a / k1a.sum()).astype(np.float32))
+    sig1b = np.asfortranarray((np.random.Generator(np.random.Philox(1)).random((1024, 1024)) < 0.5)
+                              .astype(np.float32))
+    k1b = np.ones((3, 3), np.float32)
+    k1b[1, 1] = 0
+    for name, sg, kk in (("gauss5x5_f32_512x512", sig1a, k1a),
+                         ("neighbour3x3_f32_1024x1024", sig1b, np.asfortranarray(k1b))):
+        S, F = af.Array.from_numpy(sg), af.Array.from_numpy(kk)
+
+        def chk(res, sg=sg, kk=kk):
+            cpu, ref = cpu_direct_baseline(lambda b: O.convolve(sg, kk, O.F32, 2, False), range(20),
+                                           sg.nbytes * 2 + kk.nbytes)
+            return {**err_vs(res.to_numpy(), ref), "cpu_baseline": cpu}
+        measure(name, lambda: af.convolve2(S, F, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL),
+                sg.nbytes * 2 + kk.nbytes, ("conv2_tma_kernel", "conv2_tile_kernel"), chk)
+
+    # ---- 64 x 2048 x 2048 separable 15-tap, f32 and u8, LHS batch
     t = g.standard_normal(15)
-    cf = (t / t.sum()).astype(np.float32)
+    cf_ = (t / t.sum()).astype(np.float32)
     t = g.standard_normal(15)
-    rf = (t / t.sum()).astype(np.float32)
-    CF, RF = af.Array.from_numpy(cf), af.Array.from_numpy(rf)
+    rf_ = (t / t.sum()).astype(np.float32)
+    CF, RF = af.Array.from_numpy(cf_), af.Array.from_numpy(rf_)
     xs = torch.rand(64, 2048, 2048, device="cuda")
     S = af.Array.view_torch(xs)
     n = xs.numel()
+    slice_bytes_f32 = 2048 * 2048 * 8
+
+    def chk_sep(res, x=xs, dt=O.F32, bpp=8):
+        o = res.to_torch().reshape(64, 2048, 2048)
+        cpu, ref = cpu_direct_baseline(
+            lambda b: O.convolve2_sep(slice2(x, b), cf_, rf_, dt, False), range(3),
+            2048 * 2048 * bpp, par_slices=list(range(nthreads)))
+        return {**err_vs(slice2(o, 0), ref), "cpu_baseline": cpu}
     measure("sep15_f32_64x2048x2048", lambda: af.convolve2_separable(CF, RF, S), n * 8 + 120,
-            ("sep_tma_kernel", "sep_fused_kernel"))
+            ("sep_tma_kernel", "sep_fused_kernel"), chk_sep)
     xu = torch.randint(0, 256, (64, 2048, 2048), dtype=torch.uint8, device="cuda")
     SU = af.Array.view_torch(xu)
     measure("sep15_u8_64x2048x2048", lambda: af.convolve2_separable(CF, RF, SU), n * 2 + 120,
-            ("sep_tma_kernel", "sep_fused_kernel"))
+            ("sep_tma_kernel", "sep_fused_kernel"),
+            lambda r: chk_sep(r, xu, O.U8, 2))
     del SU, xu
-    # SAME batch, 64 distinct 7x7 filters (AF_CONV_SPATIAL: AUTO would pick FFT)
+    # ---- SAME batch, 64 distinct 7x7 filters (AF_CONV_SPATIAL: AUTO would pick FFT)
     f7 = g.standard_normal((7, 7, 64))
-    f7 = (f7 / f7.sum(axis=(0, 1), keepdims=True)).astype(np.float32)
-    F7 = af.Array.from_numpy(np.asfortranarray(f7))
+    f7 = np.asfortranarray((f7 / f7.sum(axis=(0, 1), keepdims=True)).astype(np.float32))
+    F7 = af.Array.from_numpy(f7)
+
+    def chk7(res):
+        o = res.to_torch().reshape(64, 2048, 2048)
+        cpu, ref = cpu_direct_baseline(
+            lambda b: O.convolve(slice2(xs, b), np.asfortranarray(f7[:, :, b]), O.F32, 2, False),
+            range(2), slice_bytes_f32 + 196, par_slices=list(range(nthreads)))
+        return {**err_vs(slice2(o, 0), ref), "cpu_baseline": cpu}
     measure("same7x7_f32_64x2048x2048",
             lambda: af.convolve2(S, F7, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL),
-            n * 8 + f7.size * 4, ("conv2_tma_kernel", "conv2_tile_kernel"))
-    # a 31x31 filter: AUTO takes the frequency-domain route (the whole
+            n * 8 + f7.size * 4, ("conv2_tma_kernel", "conv2_tile_kernel"), chk7)
+    # ---- a 31x31 filter: AUTO takes the frequency-domain route (the whole
     # pipeline is timed: pads, cuFFT transforms, spectrum product, crop)
     f31 = g.standard_normal((31, 31))
-    F31 = af.Array.from_numpy(np.asfortranarray((f31 / f31.sum()).astype(np.float32)))
+    f31 = np.asfortranarray((f31 / f31.sum()).astype(np.float32))
+    F31 = af.Array.from_numpy(f31)
+
+    def chk31(res):
+        o = res.to_torch().reshape(64, 2048, 2048)
+        cpu, ref = cpu_direct_baseline(
+            lambda b: O.fft_convolve(slice2(xs, b), f31, O.F32, 2, False), range(2),
+            slice_bytes_f32 + f31.nbytes)
+        cpu["sample"] += " (numpy pocketfft in FP64 standing in for FFTW)"
+        return {**err_vs(slice2(o, 0), ref), "cpu_baseline": cpu}
     measure("fft31x31_f32_64x2048x2048",
             lambda: af.convolve2(S, F31, af.AF_CONV_DEFAULT, af.AF_CONV_AUTO),
-            n * 8 + 31 * 31 * 4, ("fft_pipeline",))
+            n * 8 + 31 * 31 * 4, ("fft_pipeline",), chk31)
     # several transform passes over 2304x2187 padded slices: its GB/s above
     # counts input + output once; the direct-convolution work it replaces is
     # 2*31*31 flops per output
@@ -506,77 +883,115 @@ def run_direct_workloads(af, peaks, args) -> dict:
     e["equivalent_direct_TFLOP/s"] = round(2 * 31 * 31 * n / (e["ms"] / 1e3) / 1e12, 1)
     e["bound"] = "cuFFT transforms (multi-pass), not one HBM pass"
     del S, xs
-    # 256^3 volume, 3x3x3
+    # ---- 256^3 volume, 3x3x3
     v = torch.rand(256, 256, 256, device="cuda")
     V = af.Array.view_torch(v)
     k3 = g.standard_normal((3, 3, 3))
     F3 = af.Array.from_numpy(np.asfortranarray((k3 / k3.sum()).astype(np.float32)))
-    measure("conv3_3x3x3_f32_256^3_default",
-            lambda: af.convolve3(V, F3, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL),
-            v.numel() * 8 + 108, ("conv3_tma_kernel", "conv3_tile_kernel", "conv_generic_kernel"))
-    measure("conv3_3x3x3_f32_256^3_expand",
-            lambda: af.convolve3(V, F3, af.AF_CONV_EXPAND, af.AF_CONV_SPATIAL),
-            v.numel() * 4 + 258 ** 3 * 4 + 108, ("conv3_tma_kernel", "conv3_tile_kernel", "conv_generic_kernel"))
-    del V, v
-    # 1-D: 64 signals of 2^20 samples, a 31-tap filter (LHS batch)
+    vh = np.asfortranarray(v.cpu().numpy().transpose(2, 1, 0))
+    k3f = np.asfortranarray((k3 / k3.sum()).astype(np.float32))
+    for expand in (False, True):
+        def chk3(res, expand=expand):
+            cpu, ref = cpu_direct_baseline(lambda b: O.convolve(vh, k3f, O.F32, 3, expand), range(1),
+                                           v.numel() * 4 + (258 ** 3 if expand else v.numel()) * 4)
+            return {**err_vs(res.to_numpy(), ref), "cpu_baseline": cpu}
+        measure("conv3_3x3x3_f32_256^3_" + ("expand" if expand else "default"),
+                lambda expand=expand: af.convolve3(V, F3, af.AF_CONV_EXPAND if expand else
+                                                   af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL),
+                v.numel() * 4 + (258 ** 3 if expand else v.numel()) * 4 + 108,
+                ("conv3_tma_kernel", "conv3_tile_kernel", "conv_generic_kernel"), chk3)
+    del V, v, vh
+    # ---- 1-D: 64 signals of 2^20 samples, a 31-tap filter (LHS batch)
     s1 = torch.rand(64, 1 << 20, device="cuda")
     S1 = af.Array.view_torch(s1)
     k1 = g.standard_normal(31)
-    F1 = af.Array.from_numpy((k1 / k1.sum()).astype(np.float32))
+    k1 = (k1 / k1.sum()).astype(np.float32)
+    F1 = af.Array.from_numpy(k1)
+
+    def chk1(res):
+        o = res.to_torch().reshape(64, -1)
+        cpu, ref = cpu_direct_baseline(
+            lambda b: O.convolve(s1[b].cpu().numpy(), k1, O.F32, 1, False), range(4),
+            (1 << 20) * 8, par_slices=list(range(nthreads)))
+        return {**err_vs(o[0].cpu().numpy(), ref), "cpu_baseline": cpu}
     measure("conv1_31tap_f32_64x1M", lambda: af.convolve1(S1, F1, af.AF_CONV_DEFAULT,
                                                           af.AF_CONV_SPATIAL),
-            s1.numel() * 8 + 124, ("conv1_tile_kernel", "conv_generic_kernel"))
+            s1.numel() * 8 + 124, ("conv1_pipe_kernel", "conv1_tile_kernel", "conv_generic_kernel"), chk1)
     del S1, s1
-    # af_unwrap / af_wrap of the NN image (128x128x64x32 f32, 3x3 windows,
-    # stride 1, padding 1): the 9x larger patch matrix is written / read once
+    # ---- af_unwrap / af_wrap of the NN image (128x128x64x32 f32, 3x3
+    # windows, stride 1, padding 1): the 9x larger patch matrix is written /
+    # read once
     xi = torch.rand(32, 64, 128, 128, device="cuda")
     XI = af.Array.view_torch(xi)
     ni = xi.numel()
+    img0 = np.asfortranarray(xi[0].cpu().numpy().transpose(2, 1, 0))[..., None]  # (W,H,C,1)
+    img_bytes = 128 * 128 * 64 * 4 * 10
+
+    def chk_unwrap(res, col=True):
+        o = res.to_numpy()
+        cpu, ref = cpu_direct_baseline(lambda b: O.unwrap(img0, 3, 3, 1, 1, 1, 1, 1, 1), range(2),
+                                       img_bytes, par_slices=list(range(nthreads)))
+        got = o[..., 0:1] if col else np.asfortranarray(o[..., 0:1].transpose(1, 0, 2, 3))
+        return {**err_vs(got, ref), "cpu_baseline": cpu}
     measure("unwrap_3x3_f32_128x128x64x32", lambda: af.unwrap(XI, 3, 3, 1, 1, 1, 1),
-            ni * 4 * 10, ("unwrap_rows_kernel", "unwrap_kernel"))
+            ni * 4 * 10, ("unwrap_rows_kernel", "unwrap_kernel"), chk_unwrap)
     U = af.unwrap(XI, 3, 3, 1, 1, 1, 1)
+    u0 = np.asfortranarray(U.to_numpy()[..., 0:1])
+
+    def chk_wrap(res):
+        cpu, ref = cpu_direct_baseline(
+            lambda b: O.wrap_dilated(u0, [128, 128, 64, 1], 3, 3, 1, 1, 1, 1, 1, 1), range(2),
+            img_bytes, par_slices=list(range(nthreads)))
+        return {**err_vs(res.to_numpy()[..., 0:1], ref), "cpu_baseline": cpu}
     measure("wrap_3x3_f32_128x128x64x32", lambda: af.wrap(U, 128, 128, 3, 3, 1, 1, 1, 1),
-            ni * 4 * 10, ("wrap_tiled_kernel", "wrap_kernel"))
-    del U
+            ni * 4 * 10, ("wrap_tiled_kernel", "wrap_kernel"), chk_wrap)
+    del U, u0
     # the same with is_column = false (patch elements along dim 1)
     measure("unwrap_rows_3x3_f32_128x128x64x32",
             lambda: af.unwrap(XI, 3, 3, 1, 1, 1, 1, False), ni * 4 * 10,
-            ("unwrap_rows_kernel", "unwrap_kernel"))
+            ("unwrap_rows_kernel", "unwrap_kernel"), lambda r: chk_unwrap(r, False))
     R = af.unwrap(XI, 3, 3, 1, 1, 1, 1, False)
+    r0 = np.asfortranarray(R.to_numpy()[..., 0:1].transpose(1, 0, 2, 3))
+
+    def chk_wrap_rows(res):
+        cpu, ref = cpu_direct_baseline(
+            lambda b: O.wrap_dilated(r0, [128, 128, 64, 1], 3, 3, 1, 1, 1, 1, 1, 1), range(2),
+            img_bytes)
+        return {**err_vs(res.to_numpy()[..., 0:1], ref), "cpu_baseline": cpu}
     measure("wrap_rows_3x3_f32_128x128x64x32",
             lambda: af.wrap(R, 128, 128, 3, 3, 1, 1, 1, 1, False), ni * 4 * 10,
-            ("wrap_rows_kernel", "wrap_kernel"))
+            ("wrap_rows_kernel", "wrap_kernel"), chk_wrap_rows)
     return out
 
 
 # ---------------------------------------------------------------------------
 # CPU baseline: the reference's algorithm on the host cores
 # ---------------------------------------------------------------------------
-def cpu_nn_sample(seconds_budget: float = 20.0) -> dict:
-    """Forward + both gradients of the headline workload for a subset of the
-    batch (images of the same 128x128x64 shape), timed on the host:
-    oracle unwrap/wrap (C restatement of the reference CPU kernels) + numpy's
-    BLAS sgemm in place of CBLAS (src/backend/cpu/convolve.cpp:123-243)."""
+def cpu_nn_steps(steps: int, warmup: int, seconds_budget: float) -> dict:
+    """Forward + both gradients of the headline workload, full 32-image
+    steps, timed on the host: oracle unwrap/wrap (C restatement of the
+    reference CPU kernels) + numpy's BLAS sgemm in place of CBLAS
+    (src/backend/cpu/convolve.cpp:123-243: unwrap of the whole batch, one
+    GEMM per operation, wrap_dilated for the data gradient).  Runs `warmup`
+    untimed and up to `steps` timed steps; stops early (at least one timed
+    step) when the next step would exceed `seconds_budget`, and reports the
+    counts it ran."""
     import oracle.oracle as O
 
     s = NN_SHAPE
     st, pd, dl = s["stride"], s["pad"], s["dil"]
-    g = np.random.Generator(np.random.Philox(99))
-    nimg = 1
-    X = np.asfortranarray(g.standard_normal((s["W"], s["H"], s["C"], nimg), dtype=np.float32))
-    Wt = np.asfortranarray((g.standard_normal((s["fw"], s["fh"], s["C"], s["K"])) * 0.06
-                            ).astype(np.float32))
-    Gd = np.asfortranarray(g.standard_normal((s["W"], s["H"], s["K"], nimg), dtype=np.float32))
+    X, Wt, Gd, _ = nn_inputs(s, 99)
     fd = Wt.shape
     wsz = fd[0] * fd[1]
+    nimg = s["N"]
 
     def one():
         y = O.nn_forward_unwrap_gemm_f32(X, Wt, st, pd, dl)
         cols = O.unwrap(X, fd[0], fd[1], st[0], st[1], pd[0], pd[1], dl[0], dl[1])
         npix = cols.shape[1]
         A = np.ascontiguousarray(cols.transpose(1, 3, 2, 0)).reshape(npix * nimg, s["C"] * wsz)
-        G2 = np.asfortranarray(Gd).reshape(npix, s["K"], nimg, order="F").transpose(2, 0, 1
-                                                                                     ).reshape(-1, s["K"])
+        G2 = np.asfortranarray(Gd).reshape(npix, s["K"], nimg, order="F").transpose(
+            2, 0, 1).reshape(-1, s["K"])
         wflip = Wt[::-1, ::-1, :, :]
         B = np.ascontiguousarray(wflip.reshape(wsz, s["C"], s["K"], order="F").transpose(1, 0, 2)
                                  ).reshape(s["C"] * wsz, s["K"])
@@ -586,20 +1001,29 @@ def cpu_nn_sample(seconds_budget: float = 20.0) -> dict:
                             pd[0], pd[1], dl[0], dl[1])
         return y, dx, dw
 
-    one()
-    t0 = time.perf_counter()
-    reps = 0
-    while True:
+    t_start = time.perf_counter()
+    w_run = 0
+    for _ in range(max(1, warmup)):
         one()
-        reps += 1
-        if time.perf_counter() - t0 > seconds_budget or reps >= 20:
+        w_run += 1
+        if time.perf_counter() - t_start > seconds_budget / 3:
             break
-    dt = (time.perf_counter() - t0) / reps
-    flops = 3 * nn_flops() * nimg / s["N"]
+    per = (time.perf_counter() - t_start) / w_run
+    times = []
+    for _ in range(max(1, steps)):
+        if times and time.perf_counter() - t_start + per > seconds_budget:
+            break
+        t0 = time.perf_counter()
+        one()
+        times.append(time.perf_counter() - t0)
+        per = float(np.mean(times))
+    dt = float(np.mean(times))
+    flops = 3 * nn_flops()
     return {"value": flops / dt / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(),
-            "kind": "port",
-            "sample": f"{nimg} of {s['N']} images per step (fwd+dgrad+wgrad), {reps} reps; "
-                      "oracle unwrap/wrap + numpy BLAS sgemm",
+            "kind": "port", "steps": len(times), "warmup": w_run,
+            "sample": f"full {nimg}-image steps (fwd+dgrad+wgrad): {w_run} warm-up + {len(times)} "
+                      f"timed; oracle unwrap/wrap (1 thread) + numpy BLAS sgemm (all threads); "
+                      f"host CPU {cpu_model()}",
             "seconds_per_step": dt}
 
 
@@ -623,7 +1047,7 @@ def run_only(args) -> None:
               for c, k in CNN_CHANNELS]
         prec = "fp32" if args.precision == "fp32" else "bf16"
         fn = lambda: cnn_step(x0, ws, CNN_GEOMS, precision=prec, recompute=True)  # noqa: E731
-    elif args.only in ("fwd", "dgrad", "wgrad"):
+    elif args.only in ("fwd", "dgrad", "wgrad", "step"):
         X = np.asfortranarray(g.standard_normal((s["W"], s["H"], s["C"], s["N"]), dtype=np.float32))
         Wt = np.asfortranarray((g.standard_normal((s["fw"], s["fh"], s["C"], s["K"])) * 0.06
                                 ).astype(np.float32))
@@ -631,12 +1055,16 @@ def run_only(args) -> None:
         Y = af.convolve2_nn(Xa, Wa, st, pd, dl)
         Ga = af.Array.from_numpy(np.asfortranarray(g.standard_normal(Y.dims, dtype=np.float32)))
         prec = args.precision
+
+        def step():
+            af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
+            af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
         fn = {"fwd": lambda: af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec),
               "dgrad": lambda: af.convolve2_gradient_nn(Ga, Xa, Wa, Y, st, pd, dl,
                                                         af.AF_CONV_GRADIENT_DATA, precision=prec),
               "wgrad": lambda: af.convolve2_gradient_nn(Ga, Xa, Wa, Y, st, pd, dl,
-                                                        af.AF_CONV_GRADIENT_FILTER, precision=prec)
-              }[args.only]
+                                                        af.AF_CONV_GRADIENT_FILTER, precision=prec),
+              "step": step}[args.only]
     else:
         t = g.standard_normal(15)
         CF = af.Array.from_numpy((t / t.sum()).astype(np.float32))
@@ -648,12 +1076,19 @@ def run_only(args) -> None:
             U = af.unwrap(XI, 3, 3, 1, 1, 1, 1, col)
             fn = ((lambda: af.unwrap(XI, 3, 3, 1, 1, 1, 1, col)) if args.only.startswith("unwrap")
                   else (lambda: af.wrap(U, 128, 128, 3, 3, 1, 1, 1, 1, col)))
-        elif args.only == "conv3":
+        elif args.only in ("conv3", "conv3_expand"):
             v = torch.rand(256, 256, 256, device="cuda")
             V = af.Array.view_torch(v)
             k3 = g.standard_normal((3, 3, 3))
             F3 = af.Array.from_numpy(np.asfortranarray((k3 / k3.sum()).astype(np.float32)))
-            fn = lambda: af.convolve3(V, F3, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL)  # noqa: E731
+            mode = af.AF_CONV_EXPAND if args.only == "conv3_expand" else af.AF_CONV_DEFAULT
+            fn = lambda: af.convolve3(V, F3, mode, af.AF_CONV_SPATIAL)  # noqa: E731
+        elif args.only == "conv1":
+            s1 = torch.rand(64, 1 << 20, device="cuda")
+            S1 = af.Array.view_torch(s1)
+            k1 = g.standard_normal(31)
+            F1 = af.Array.from_numpy((k1 / k1.sum()).astype(np.float32))
+            fn = lambda: af.convolve1(S1, F1, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL)  # noqa: E731
         elif args.only == "sep_u8":
             xu = torch.randint(0, 256, (64, 2048, 2048), dtype=torch.uint8, device="cuda")
             S = af.Array.view_torch(xu)
@@ -714,10 +1149,12 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="bf16", choices=["bf16", "fp32", "fp8"])
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--cpu-seconds", type=float, default=150.0,
+                    help="time budget of the reference arm's full-batch CPU steps")
     ap.add_argument("--only", default=None,
-                    choices=["fwd", "dgrad", "wgrad", "sep_f32", "sep_u8", "same7", "conv3", "cnn",
-                             "unwrap", "wrap", "unwrap_rows", "wrap_rows"],
+                    choices=["fwd", "dgrad", "wgrad", "step", "sep_f32", "sep_u8", "same7", "conv3",
+                             "conv3_expand", "conv1", "cnn", "unwrap", "wrap", "unwrap_rows",
+                             "wrap_rows"],
                     help="run one operation of the workload --steps times after --warmup "
                          "(for profiler captures); prints its timing, not the bench line")
     args = ap.parse_args()
@@ -738,12 +1175,13 @@ def main() -> None:
     if args.impl == "reference":
         if rank != 0:
             return
-        cpu = cpu_nn_sample(args.cpu_seconds)
+        cpu = cpu_nn_steps(args.steps, args.warmup, args.cpu_seconds)
         line = {"impl": "reference", "metric": METRIC, "value": cpu["value"], "unit": "TFLOP/s",
-                "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-                "ms_per_step": cpu["seconds_per_step"] * 1e3 * NN_SHAPE["N"],
+                "n_gpus": args.gpus, "steps": cpu["steps"], "warmup": cpu["warmup"],
+                "ms_per_step": cpu["seconds_per_step"] * 1e3,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32", "data": "synthetic", "config": config,
+                "steps_requested": args.steps, "warmup_requested": args.warmup,
                 "cpu_baseline": {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")},
                 "e2e": {"value": cpu["value"], "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                         "d2h_bytes_per_step": 0}}
@@ -762,7 +1200,7 @@ def main() -> None:
         value = replica_value(ms, world)
     if rank != 0:
         return
-    cpu = cpu_nn_sample(args.cpu_seconds)
+    cpu = cpu_nn_steps(2, 1, 30.0)
     line = {
         "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -773,7 +1211,9 @@ def main() -> None:
                                                       ("value", "unit", "cores", "kind", "sample")},
         "e2e": res["e2e"], "clocks": res["clocks"], "gpu_launches": res["gpu_launches"],
         "errors_vs_fp64": res["errors_vs_fp64"], "kernel_times_ms": res["kernel_times_ms"],
-        "fp32_path": res["fp32_path"],
+        "kernel_launches_per_step": res["kernel_launches_per_step"],
+        "fp32_path": res["fp32_path"], "cudnn": res.get("cudnn"),
+        "nn_workloads": res.get("nn_workloads"),
         "secondary": res.get("secondary"), "cnn4": res.get("cnn4"), "peaks": peaks,
     }
     print(json.dumps(line))

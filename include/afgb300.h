@@ -273,6 +273,29 @@ AFGB_API af_err afgb_device_array_view(af_array *arr, void *data, const unsigned
                                        const dim_t *const dims, const dim_t *const strides,
                                        const af_dtype type);
 
+/* Interop with another ArrayFire backend library in the same process
+ * (libafcuda, or the unified libaf forwarding to it; its af_array handles are
+ * opaque objects of that library, src/api/c/handle.hpp:50-83, passed through
+ * unchanged by src/api/unified/symbol_manager.hpp:144-165).  `foreign_lib`
+ * is that library's dlopen handle; its entry points are looked up with
+ * dlsym (AF_ERR_LOAD_SYM when one is missing).
+ *   afgb_import_foreign_array: a non-owning view of this library over the
+ *     foreign array's device memory, without a copy.  Pointer, dims, strides
+ *     and type come from the foreign af_get_device_ptr (src/api/c/
+ *     memory.cpp:121: ArrayFire makes the array linear and locks its
+ *     buffer), af_get_dims, af_get_strides and af_get_type; its af_sync, when
+ *     exported, runs before the view is made.  Keep the foreign
+ *     array alive while the view is used; release the view, then call the
+ *     foreign af_unlock_array.
+ *   afgb_export_foreign_array: a new af_array of the foreign library (its
+ *     af_create_handle) holding a copy of `arr`, filled through its
+ *     af_get_device_ptr and unlocked with its af_unlock_array when exported;
+ *     the copy has completed when the call returns. */
+AFGB_API af_err afgb_import_foreign_array(af_array *out, const af_array foreign,
+                                          void *foreign_lib);
+AFGB_API af_err afgb_export_foreign_array(af_array *foreign_out, const af_array arr,
+                                          void *foreign_lib);
+
 /* Route all subsequent work of the calling process to `stream`
  * (a cudaStream_t; 0 restores the library's own non-blocking stream). */
 AFGB_API af_err afgb_set_stream(void *stream);
@@ -316,6 +339,15 @@ AFGB_API af_err afgb_device_mem_peak(size_t *peak_bytes, int reset);
 /* Fault injection for tests: the n-th device allocation from now fails with
  * AF_ERR_NO_MEM (n <= 0 disables).  Host-side only. */
 AFGB_API void afgb_debug_fail_alloc_after(int n);
+
+/* Failure-path test hook: the bounded waits of the TMA and tensor-core
+ * kernels give up after `polls` polls (0 restores the default, about
+ * seconds), raising the device error word that af_sync / af_get_data_ptr
+ * report as AF_ERR_RUNTIME and clear.  With skip_first_block_copies != 0,
+ * block 0 of the TMA 2-D direct kernel issues no tile copies, so its waits
+ * run out with nothing in flight and the kernel returns.  Call it while no
+ * work of this library is in flight, on the current device. */
+AFGB_API af_err afgb_debug_wait_limit(unsigned int polls, int skip_first_block_copies);
 
 /* Number of kernels this library has launched since load (all devices). */
 AFGB_API unsigned long long afgb_kernel_launch_count(void);

@@ -46,6 +46,20 @@ def _exact(af, fn):
         af.set_exact_fp(False)
 
 
+def assert_same(got, ref, what=""):
+    """Bit-for-bit equality of two float arrays of the same size, reported
+    as the number of differing elements and the first few (a plain
+    `assert a.tobytes() == b.tobytes()` makes pytest diff megabytes)."""
+    g = np.ascontiguousarray(np.asarray(got)).ravel(order="K").view(np.uint32)
+    r = np.ascontiguousarray(np.asarray(ref)).ravel(order="K").view(np.uint32)
+    assert g.size == r.size, f"{what}: {g.size} vs {r.size} elements"
+    bad = np.nonzero(g != r)[0]
+    if bad.size:
+        gf, rf = g.view(np.float32), r.view(np.float32)
+        first = [(int(i), float(gf[i]), float(rf[i])) for i in bad[:6]]
+        raise AssertionError(f"{what}: {bad.size} of {g.size} differ; first (index, got, ref): {first}")
+
+
 def _fused_ok(oracle, out, s, f, rank, expand):
     ref = oracle.convolve(s, f, C.F32, rank, expand)
     bound = oracle.convolve(np.abs(s.astype(np.float64)), np.abs(f.astype(np.float64)), C.F64,
@@ -71,7 +85,7 @@ def test_conv1_64x1M(af, oracle, taps, expand):
     f = (k / k.sum()).astype(np.float32)
     S, F = af.Array.view_torch(s), af.Array.from_numpy(f)
     mode = af.AF_CONV_EXPAND if expand else af.AF_CONV_DEFAULT
-    n, out = _exact(af, lambda: _ran(af, "conv1_tile_kernel",
+    n, out = _exact(af, lambda: _ran(af, "conv1_pipe_kernel",
                                      lambda: af.convolve1(S, F, mode, af.AF_CONV_SPATIAL)))
     assert n == 1
     assert out.dims == [(1 << 20) + (taps - 1 if expand else 0), 64, 1, 1]
@@ -79,7 +93,7 @@ def test_conv1_64x1M(af, oracle, taps, expand):
     for b in (0, 29, 63):
         sb = s[b].cpu().numpy()
         ref = oracle.convolve(sb, f, C.F32, 1, expand)
-        assert o[b].cpu().numpy().tobytes() == ref.tobytes(), f"slice {b}"
+        assert_same(o[b].cpu().numpy(), ref, f"slice {b}")
     fused = af.convolve1(S, F, mode, af.AF_CONV_SPATIAL).to_torch().reshape(64, -1)
     sb = s[17].cpu().numpy()
     assert _fused_ok(oracle, fused[17].cpu().numpy(), sb, f, 1, expand) <= 1e-6
@@ -97,11 +111,11 @@ def test_conv1_ragged_many_tiles(af, oracle, taps, expand):
     f = (k / k.sum()).astype(np.float32)
     S, F = af.Array.from_numpy(s), af.Array.from_numpy(f)
     mode = af.AF_CONV_EXPAND if expand else af.AF_CONV_DEFAULT
-    n, out = _exact(af, lambda: _ran(af, "conv1_tile_kernel",
+    n, out = _exact(af, lambda: _ran(af, "conv1_pipe_kernel",
                                      lambda: af.convolve1(S, F, mode, af.AF_CONV_SPATIAL)))
     assert n == 1
     ref = oracle.convolve(s, f, C.F32, 1, expand)
-    assert out.to_numpy().tobytes() == ref.tobytes()
+    assert_same(out.to_numpy(), ref)
 
 
 def test_conv1_many2one_filter_batch(af, oracle):
@@ -111,11 +125,28 @@ def test_conv1_many2one_filter_batch(af, oracle):
     s = g.random(50000, dtype=np.float32)
     f = np.asfortranarray(g.standard_normal((31, 12)).astype(np.float32))
     S, F = af.Array.from_numpy(s), af.Array.from_numpy(f)
-    n, out = _exact(af, lambda: _ran(af, "conv1_tile_kernel",
+    n, out = _exact(af, lambda: _ran(af, "conv1_pipe_kernel",
                                      lambda: af.convolve1(S, F, af.AF_CONV_DEFAULT,
                                                           af.AF_CONV_SPATIAL)))
     assert n == 1
-    assert out.to_numpy().tobytes() == oracle.convolve(s, f, C.F32, 1, False).tobytes()
+    assert_same(out.to_numpy(), oracle.convolve(s, f, C.F32, 1, False))
+
+
+def test_conv1_strided_signal_takes_tile_kernel(af, oracle):
+    """A signal read with a stride (every other sample of a torch tensor)
+    runs the shared-memory tile kernel; bit for bit in the exact mode."""
+    import torch
+
+    base = torch.rand(3, 2 * 9000, device="cuda")
+    view = af.Array.view_device(base.data_ptr(), [9000, 3], af.f32, strides=[2, 18000], keep=base)
+    f = C.rng(5).standard_normal(31).astype(np.float32)
+    F = af.Array.from_numpy(f)
+    n, out = _exact(af, lambda: _ran(af, "conv1_tile_kernel",
+                                     lambda: af.convolve1(view, F, af.AF_CONV_EXPAND,
+                                                          af.AF_CONV_SPATIAL)))
+    assert n == 1
+    dense = np.asfortranarray(base.cpu().numpy()[:, ::2].T)
+    assert_same(out.to_numpy(), oracle.convolve(dense, f, C.F32, 1, True))
 
 
 # ---------------------------------------------------------------------------
@@ -140,8 +171,8 @@ def test_same7x7_64x2048sq(af, oracle):
     for b in (0, 40, 63):
         sb = np.asfortranarray(x[b].cpu().numpy().T)
         ref = oracle.convolve(sb, f7[:, :, b], C.F32, 2, False)
-        assert np.asfortranarray(o[b].cpu().numpy().T).tobytes(order="F") == \
-            ref.tobytes(order="F"), f"slice {b}"
+        assert_same(np.asfortranarray(o[b].cpu().numpy().T).ravel(order="F"), ref.ravel(order="F"),
+                    f"slice {b}")
     fused = run().to_torch().reshape(64, 2048, 2048)
     sb = np.asfortranarray(x[5].cpu().numpy().T)
     got = np.asfortranarray(fused[5].cpu().numpy().T)
@@ -167,7 +198,7 @@ def test_conv2_tma_many_tiles_per_cta(af, oracle, fsz, expand, kind):
     n, out = _exact(af, lambda: _ran(af, "conv2_tma_kernel",
                                      lambda: af.convolve2(S, F, mode, af.AF_CONV_SPATIAL)))
     assert n == 1
-    assert out.to_numpy().tobytes() == oracle.convolve(s, f, C.F32, 2, expand).tobytes()
+    assert_same(out.to_numpy(), oracle.convolve(s, f, C.F32, 2, expand))
 
 
 def test_sep15_f32_64x2048sq(af, oracle):
@@ -191,8 +222,8 @@ def test_sep15_f32_64x2048sq(af, oracle):
     for b in (0, 33, 63):
         sb = np.asfortranarray(x[b].cpu().numpy().T)
         ref = oracle.convolve2_sep(sb, cf, rf, C.F32, False)
-        assert np.asfortranarray(o[b].cpu().numpy().T).tobytes(order="F") == \
-            ref.tobytes(order="F"), f"slice {b}"
+        assert_same(np.asfortranarray(o[b].cpu().numpy().T).ravel(order="F"), ref.ravel(order="F"),
+                    f"slice {b}")
     fused = af.convolve2_separable(CF, RF, S).to_torch().reshape(64, 2048, 2048)
     sb = np.asfortranarray(x[9].cpu().numpy().T)
     ref = oracle.convolve2_sep(sb, cf, rf, C.F32, False)
@@ -217,7 +248,7 @@ def test_sep_tma_many_tiles_per_cta(af, oracle, expand):
     n, out = _exact(af, lambda: _ran(af, "sep_tma_kernel",
                                      lambda: af.convolve2_separable(CF, RF, S, mode)))
     assert n == 1
-    assert out.to_numpy().tobytes() == oracle.convolve2_sep(s, cf, rf, C.F32, expand).tobytes()
+    assert_same(out.to_numpy(), oracle.convolve2_sep(s, cf, rf, C.F32, expand))
 
 
 # ---------------------------------------------------------------------------
@@ -237,7 +268,7 @@ def test_conv3_256cube(af, oracle, expand):
                                      lambda: af.convolve3(V, F, mode, af.AF_CONV_SPATIAL)))
     assert n == 1
     ref = oracle.convolve(v, f, C.F32, 3, expand)
-    assert out.to_numpy().tobytes() == ref.tobytes()
+    assert_same(out.to_numpy(), ref)
     fused = af.convolve3(V, F, mode, af.AF_CONV_SPATIAL).to_numpy()
     assert _fused_ok(oracle, fused, v, f, 3, expand) <= 1e-6
 
@@ -324,4 +355,4 @@ def test_nn_gradients_bench_shape(af, oracle, key, prec):
     Y = af.convolve2_nn(X, W, st, pd, dl)
     dw1 = af.convolve2_gradient_nn(G, X, W, Y, st, pd, dl, af.AF_CONV_GRADIENT_FILTER,
                                    precision=prec).to_numpy().ravel(order="F")
-    assert dw1.tobytes() == dwn.tobytes()
+    assert_same(dw1, dwn, "per-gradient call")

@@ -42,6 +42,14 @@ TC_CASES = C.NN_CASES + [
     ("tc_nopad_k32", (130, 10, 64, 1), (3, 3, 64, 32), (1, 1), (0, 0), (1, 1)),
     ("tc_fold_rgb_w128", (128, 10, 3, 2), (3, 3, 3, 64), (1, 1), (1, 1), (1, 1)),
     ("tc_d2_c16_k48", (124, 8, 16, 2), (3, 3, 16, 48), (1, 1), (2, 2), (2, 2)),
+    # pixels-on-M strip kernel (stride 1, rows of 96+ pixels): two 128-pixel
+    # segments with a ragged second, odd heights, N = 16 / 80 channels,
+    # dilated and rectangular filters, four source chunks
+    ("tc_strip_w200_k80", (200, 7, 48, 2), (3, 3, 48, 80), (1, 1), (1, 1), (1, 1)),
+    ("tc_strip_w256_1x1", (256, 5, 128, 1), (1, 1, 128, 16), (1, 1), (0, 0), (1, 1)),
+    ("tc_strip_5x3_dx2", (160, 9, 64, 1), (5, 3, 64, 32), (1, 1), (4, 1), (2, 1)),
+    ("tc_strip_c256_k64", (128, 6, 256, 1), (3, 3, 256, 64), (1, 1), (1, 1), (1, 1)),
+    ("tc_strip_w100_nopad", (100, 9, 64, 2), (3, 3, 64, 128), (1, 1), (0, 0), (1, 1)),
 ]
 
 
@@ -241,3 +249,39 @@ def test_combined_gradients_validation(af):
     with pytest.raises(af.AfError) as e:
         af.convolve2_gradients_nn(bad, S, F, st, pd, dl, data=False, filter=False, bias=False)
     assert e.value.code == af.AF_ERR_ARG
+
+
+# ---- the signal's converted copy kept on its array --------------------------
+def test_signal_copy_shared_and_invalidated(af, oracle):
+    """A library-owned signal keeps its bf16 channels-last copy between the
+    forward and the gradients of one step (same bits as a fresh array), and
+    drops it when the buffer is written: through af_get_device_ptr (here a
+    torch view writing new data) and by a library call writing in place
+    (af_wrap_v2)."""
+    import torch
+
+    case = ("tc_c64_k128", (24, 20, 64, 2), (3, 3, 64, 128), (1, 1), (1, 1), (1, 1))
+    name, sd, fd, st, pd, dl = case
+    s1, f = C.nn_inputs(case, 91)
+    s2, _ = C.nn_inputs(case, 92)
+    g = C.nn_grad(case, 91)
+    S, F, G = af.Array.from_numpy(s1), af.Array.from_numpy(f), af.Array.from_numpy(g)
+    y1 = af.convolve2_nn(S, F, st, pd, dl, precision="bf16").to_numpy()
+    dx, dw, _ = af.convolve2_gradients_nn(G, S, F, st, pd, dl, precision="bf16")
+    S_fresh = af.Array.from_numpy(s1)
+    dx0, dw0, _ = af.convolve2_gradients_nn(G, S_fresh, F, st, pd, dl, precision="bf16")
+    assert dw.to_numpy().tobytes() == dw0.to_numpy().tobytes()
+    assert dx.to_numpy().tobytes() == dx0.to_numpy().tobytes()
+    # new contents through the device pointer
+    t = torch.as_tensor(S, device="cuda")
+    t.copy_(torch.from_numpy(np.ascontiguousarray(s2.transpose(3, 2, 1, 0))).cuda())
+    torch.cuda.synchronize()
+    y2 = af.convolve2_nn(S, F, st, pd, dl, precision="bf16").to_numpy()
+    check(y2, oracle.nn_forward_f64(s2, f, st, pd, dl), "fwd after external write")
+    assert np.abs(y2 - y1).max() > 0
+    # new contents from a library call writing in place: wrap_v2 adds the
+    # patches of s1 back into S (S becomes s2 + wrap(unwrap(s1)))
+    U = af.unwrap(af.Array.from_numpy(s1), 1, 1, 1, 1, 0, 0)
+    af.wrap_v2(S, U, sd[0], sd[1], 1, 1, 1, 1, 0, 0)
+    y3 = af.convolve2_nn(S, F, st, pd, dl, precision="bf16").to_numpy()
+    check(y3, oracle.nn_forward_f64(s1 + s2, f, st, pd, dl), "fwd after in-place library write")
