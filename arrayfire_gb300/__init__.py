@@ -241,6 +241,17 @@ def device_mem_peak(reset: bool = False) -> int:
     return v.value
 
 
+def device_mem_peak_breakdown() -> dict:
+    """Bytes per allocation purpose at the peak of device_mem_peak."""
+    buf = ctypes.create_string_buffer(4096)
+    _check(lib().afgb_device_mem_peak_breakdown(buf, len(buf)))
+    out = {}
+    for ln in buf.value.decode().splitlines():
+        k, _, v = ln.rpartition("=")
+        out[k] = int(v)
+    return out
+
+
 def version() -> str:
     return lib().afgb_version().decode()
 

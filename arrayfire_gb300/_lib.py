@@ -74,6 +74,7 @@ SIGNATURES = [
     ("afgb_device_array_view", af_err, [ctypes.POINTER(af_array), _P, ctypes.c_uint, _DP, _DP, ctypes.c_int]),
     ("afgb_set_stream", af_err, [_P]),
     ("afgb_debug_wait_limit", af_err, [ctypes.c_uint, ctypes.c_int]),
+    ("afgb_device_mem_peak_breakdown", af_err, [ctypes.c_char_p, ctypes.c_size_t]),
     ("afgb_import_foreign_array", af_err, [ctypes.POINTER(af_array), _P, _P]),
     ("afgb_export_foreign_array", af_err, [ctypes.POINTER(af_array), _P, _P]),
     ("afgb_get_stream", af_err, [ctypes.POINTER(_P)]),

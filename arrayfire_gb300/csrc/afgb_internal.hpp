@@ -128,6 +128,14 @@ Array *create_array(af_dtype t, const dim_t dims[4]);
 // raw stream-ordered scratch (freed with free_scratch on the same stream)
 void *alloc_device(size_t bytes);
 void free_device(void *p);
+// the purpose recorded with the allocations this thread makes while the
+// object lives (reported by afgb_device_mem_peak_breakdown); `tag` must be a
+// string literal
+struct MemTag {
+    const char *prev;
+    explicit MemTag(const char *tag);
+    ~MemTag();
+};
 
 // ---------------------------------------------------------------------------
 // execution state

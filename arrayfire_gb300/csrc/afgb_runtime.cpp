@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <string>
@@ -175,12 +176,20 @@ bool exact_fp() { return g_exact.load() != 0; }
 void count_launch(unsigned n) { g_launches += n; }
 
 // ---------------------------------------------------------------- memory
-// Every pool allocation is recorded with its size so that af_device_mem_info
-// can report the bytes and buffers in use and the peak since the last reset.
+// Every pool allocation is recorded with its size and the purpose tag that
+// was current on the allocating thread (MemTag), so that af_device_mem_info
+// can report the bytes and buffers in use, and afgb_device_mem_peak the peak
+// since the last reset together with the bytes each purpose held at it.
 namespace {
+thread_local const char *t_mem_tag = "scratch";
+struct LiveBuf {
+    size_t bytes;
+    const char *tag;
+};
 struct MemBook {
     std::mutex mu;
-    std::unordered_map<void *, size_t> live;
+    std::unordered_map<void *, LiveBuf> live;
+    std::map<std::string, size_t> by_tag, peak_by_tag;
     size_t bytes = 0, peak = 0;
 };
 MemBook &mem_book() {
@@ -190,19 +199,27 @@ MemBook &mem_book() {
 void book_alloc(void *p, size_t bytes) {
     MemBook &b = mem_book();
     std::lock_guard<std::mutex> lk(b.mu);
-    b.live[p] = bytes;
+    b.live[p] = LiveBuf{bytes, t_mem_tag};
     b.bytes += bytes;
-    if (b.bytes > b.peak) b.peak = b.bytes;
+    b.by_tag[t_mem_tag] += bytes;
+    if (b.bytes > b.peak) {
+        b.peak = b.bytes;
+        b.peak_by_tag = b.by_tag;
+    }
 }
 void book_free(void *p) {
     MemBook &b = mem_book();
     std::lock_guard<std::mutex> lk(b.mu);
     auto it = b.live.find(p);
     if (it == b.live.end()) return;
-    b.bytes -= it->second;
+    b.bytes -= it->second.bytes;
+    b.by_tag[it->second.tag] -= it->second.bytes;
     b.live.erase(it);
 }
 }  // namespace
+
+MemTag::MemTag(const char *tag) : prev(t_mem_tag) { t_mem_tag = tag; }
+MemTag::~MemTag() { t_mem_tag = prev; }
 
 void *alloc_device(size_t bytes) {
     int fa = g_fail_after.load();
@@ -329,7 +346,10 @@ Array *create_array(af_dtype t, const dim_t dims[4]) {
     dense_strides(&scratch);
     auto b = std::make_shared<Buffer>();
     b->bytes = (size_t)scratch.elements() * dtype_size(t);
-    b->ptr = alloc_device(b->bytes);
+    {
+        MemTag tag("arrays");
+        b->ptr = alloc_device(b->bytes);
+    }
     b->kind = BufKind::Pool;
     b->device = device();
     scratch.buf = b;
@@ -651,7 +671,26 @@ af_err afgb_device_mem_peak(size_t *peak_bytes, int reset) {
     MemBook &b = mem_book();
     std::lock_guard<std::mutex> lk(b.mu);
     *peak_bytes = b.peak;
-    if (reset) b.peak = b.bytes;
+    if (reset) {
+        b.peak = b.bytes;
+        b.peak_by_tag = b.by_tag;
+    }
+    AFGB_CATCHALL
+}
+
+af_err afgb_device_mem_peak_breakdown(char *buf, size_t len) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, buf != nullptr && len > 0);
+    std::string out;
+    {
+        MemBook &b = mem_book();
+        std::lock_guard<std::mutex> lk(b.mu);
+        for (const auto &kv : b.peak_by_tag)
+            if (kv.second) out += kv.first + "=" + std::to_string(kv.second) + "\n";
+    }
+    const size_t n = std::min(len - 1, out.size());
+    std::memcpy(buf, out.data(), n);
+    buf[n] = 0;
     AFGB_CATCHALL
 }
 

@@ -924,7 +924,7 @@ __device__ __forceinline__ void c1p_chunk_exact(float (&acc)[16], const float *g
 }
 
 template <bool EXACT>
-__global__ void __launch_bounds__(C1P_THREADS, 2)
+__global__ void __launch_bounds__(C1P_THREADS, 3)
     conv1_pipe_kernel(const DirectParams p, long long ntx, long long ntiles) {
     extern __shared__ __align__(16) float c1p_smem[];
     float *wbuf = c1p_smem + C1P_NST * C1P_STAGE;
@@ -1207,7 +1207,11 @@ static void run_sep_generic(const Array &sig, const Array &cfilt, const Array &r
     long long tw = sig.dims[0] + (expand ? cfl - 1 : 0);
     long long th = sig.dims[1];
     size_t tbytes = (size_t)(tw * th * n2 * n3) * sizeof(T);
-    T *temp = static_cast<T *>(alloc_device(tbytes));
+    T *temp;
+    {
+        MemTag tag("separable intermediates");
+        temp = static_cast<T *>(alloc_device(tbytes));
+    }
     long long total1 = tw * th * n2 * n3;
     long long total2 = out.elements();
     const T *in = sig.ptr<T>();

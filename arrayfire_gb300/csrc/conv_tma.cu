@@ -12,9 +12,13 @@
 //
 // Arithmetic is the reference's (src/backend/cpu/kernel/convolve.hpp):
 // products accumulate from zero with the outer-dimension taps outside and
-// dim-0 taps inside.  Two outputs share one packed f32x2 instruction where
-// their operands form aligned register pairs; packed multiply and add round
-// each lane separately, so the exact mode stays bit-identical.
+// dim-0 taps inside.  The 2-D kernel runs one scalar FMA per tap and output
+// (a form that paired taps into packed f32x2 FMAs issued more instructions,
+// for the register-pair moves of odd-aligned windows, and was measured
+// slower).  The separable kernel's passes share one packed f32x2 instruction
+// between two outputs whose operands form aligned register pairs; packed
+// multiply and add round each lane separately, so the exact mode stays
+// bit-identical.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -40,10 +44,12 @@ using tc::smem_u32;
 
 constexpr int TILE = 64;
 constexpr int THREADS = 256;
-// tile buffers per CTA (one computed, the rest in flight): three for the 2-D
-// kernel, whose registers already hold it at two CTAs per SM; two for the
-// separable kernel, whose shared temp image would otherwise cost a CTA per SM
-constexpr int NST_2D = 3;
+// tile buffers per CTA (one computed, the rest in flight): two for the 2-D
+// kernel (its scalar-FMA form needs few registers, so shared memory sets the
+// CTAs per SM: five at two 21 KB buffers, each CTA's next tile loading during
+// a whole tile of compute); two for the separable kernel, whose shared temp
+// image would otherwise cost a CTA per SM
+constexpr int NST_2D = 2;
 constexpr int NST_SEP = 2;
 // separable temp-image pitch (floats): 17 16-byte words, odd for the same reason
 constexpr int SEP_TP = TILE + 4;
@@ -227,6 +233,11 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
         for (int i = 0; i < NST - 1; ++i)
             if (tile + i * (int)gridDim.x < tg.ntiles) issue(tile + i * (int)gridDim.x, i);
     const int tx = tid & 15, ty = tid >> 4;
+    // the taps stay in registers from tile to tile and are reloaded only when
+    // a tile's filter differs from the previous one (consecutive tiles of a
+    // CTA mostly belong to one image)
+    long long cur_filt = -1;
+    float wr[F0 * F1];
     for (int k = 0; tile < tg.ntiles; tile += gridDim.x, ++k) {
         const int buf = k % NST;
         const int ahead = tile + (NST - 1) * (int)gridDim.x;
@@ -235,12 +246,15 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
         const int ttx = tr.tx, tty = tr.ty;
         const long long out_off = tr.out;
         // taps go to registers before the wait, overlapping the tile load
-        const float *w = static_cast<const float *>(p.filt) + tr.filt;
-        float wr[F0 * F1];
+        if (tr.filt != cur_filt) {
+            const float *w = static_cast<const float *>(p.filt) + tr.filt;
 #pragma unroll
-        for (int fj = 0; fj < F1; ++fj)
+            for (int fj = 0; fj < F1; ++fj)
 #pragma unroll
-            for (int fi = 0; fi < F0; ++fi) wr[fj * F0 + fi] = __ldg(w + fi * p.fs[0] + fj * p.fs[1]);
+                for (int fi = 0; fi < F0; ++fi)
+                    wr[fj * F0 + fi] = __ldg(w + fi * p.fs[0] + fj * p.fs[1]);
+            cur_filt = tr.filt;
+        }
         if (!wait_tile(&full[buf], (k / NST) & 1)) break;
         const float *tile_f;
         if (sizeof(T) == 4) {
@@ -252,100 +266,34 @@ __global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constan
         }
 
         float acc[4][4];
-        if constexpr (!EXACT && sizeof(T) == 4) {
-            // Fused mode: taps u = 2m, 2m+1 of one output share a packed FMA
-            // (even taps accumulate in the low lane, odd taps in the high
-            // lane); the odd filter's last tap takes a scalar FMA into its own
-            // accumulator, so no lane ever reads a pixel outside the filter
-            // window and no accumulator pair is split.
-            constexpr int NP = F0 / 2;
-            static_assert(H::OFF + F0 + 2 < NW4 * 4, "packed window exceeds the loaded row");
-            f2 wp[F1][NP > 0 ? NP : 1];
+        // one scalar FMA (or, in the exact mode, a rounded product and sum) per
+        // tap and output; fused mode only changes the rounding
 #pragma unroll
-            for (int fj = 0; fj < F1; ++fj)
+        for (int a = 0; a < 4; ++a)
 #pragma unroll
-                for (int m = 0; m < NP; ++m)
-                    wp[fj][m] = pk(wr[fj * F0 + F0 - 1 - 2 * m], wr[fj * F0 + F0 - 2 - 2 * m]);
-            f2 acc2[4][4];
-            float acc1[4][4];  // the odd filter's last tap, kept apart (no pair moves)
+            for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
 #pragma unroll
-            for (int a = 0; a < 4; ++a)
+        for (int q = 3 + F1 - 1; q >= 0; --q) {
+            float v[NW4 * 4];
+            const float *row = tile_f + (4 * ty + q) * H::PF + 4 * tx;
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    acc2[a][c] = 0ull;
-                    acc1[a][c] = 0.0f;
-                }
-#pragma unroll
-            for (int q = 3 + F1 - 1; q >= 0; --q) {
-                float v[NW4 * 4];
-                const float *row = tile_f + (4 * ty + q) * H::PF + 4 * tx;
-#pragma unroll
-                for (int u = 0; u < NW4; ++u) {
-                    const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
-                    v[4 * u] = t4.x;
-                    v[4 * u + 1] = t4.y;
-                    v[4 * u + 2] = t4.z;
-                    v[4 * u + 3] = t4.w;
-                }
-                f2 ve[NW4 * 2], vo[NW4 * 2 - 1];
-#pragma unroll
-                for (int i = 0; i < NW4 * 2; ++i) ve[i] = pk(v[2 * i], v[2 * i + 1]);
-#pragma unroll
-                for (int i = 0; i < NW4 * 2 - 1; ++i) vo[i] = pk(v[2 * i + 1], v[2 * i + 2]);
-#pragma unroll
-                for (int rr = 0; rr < 4; ++rr) {
-                    const int fj = rr + F1 - 1 - q;
-                    if (fj >= 0 && fj < F1) {
-#pragma unroll
-                        for (int cc = 0; cc < 4; ++cc) {
-                            const int b0 = cc + H::OFF;  // window index of tap u = 0
-#pragma unroll
-                            for (int m = 0; m < NP; ++m) {
-                                const int j = b0 + 2 * m;
-                                const f2 in2 = (j & 1) ? vo[(j - 1) >> 1] : ve[j >> 1];
-                                acc2[rr][cc] = mac2<false>(acc2[rr][cc], in2, wp[fj][m]);
-                            }
-                            if (F0 & 1) acc1[rr][cc] = fmaf(v[b0 + F0 - 1], wr[fj * F0], acc1[rr][cc]);
-                        }
-                    }
-                }
+            for (int u = 0; u < NW4; ++u) {
+                const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
+                v[4 * u] = t4.x;
+                v[4 * u + 1] = t4.y;
+                v[4 * u + 2] = t4.z;
+                v[4 * u + 3] = t4.w;
             }
 #pragma unroll
-            for (int a = 0; a < 4; ++a)
+            for (int rr = 0; rr < 4; ++rr) {
+                const int fj = rr + F1 - 1 - q;
+                if (fj >= 0 && fj < F1) {
 #pragma unroll
-                for (int c = 0; c < 4; ++c) {
-                    float lo, hi;
-                    upk(acc2[a][c], lo, hi);
-                    acc[a][c] = (lo + hi) + acc1[a][c];
-                }
-        } else {
+                    for (int fi = 0; fi < F0; ++fi) {
+                        const float wv = wr[fj * F0 + fi];
 #pragma unroll
-            for (int a = 0; a < 4; ++a)
-#pragma unroll
-                for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
-#pragma unroll
-            for (int q = 3 + F1 - 1; q >= 0; --q) {
-                float v[NW4 * 4];
-                const float *row = tile_f + (4 * ty + q) * H::PF + 4 * tx;
-#pragma unroll
-                for (int u = 0; u < NW4; ++u) {
-                    const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
-                    v[4 * u] = t4.x;
-                    v[4 * u + 1] = t4.y;
-                    v[4 * u + 2] = t4.z;
-                    v[4 * u + 3] = t4.w;
-                }
-#pragma unroll
-                for (int rr = 0; rr < 4; ++rr) {
-                    const int fj = rr + F1 - 1 - q;
-                    if (fj >= 0 && fj < F1) {
-#pragma unroll
-                        for (int fi = 0; fi < F0; ++fi) {
-                            const float wv = wr[fj * F0 + fi];
-#pragma unroll
-                            for (int cc = 0; cc < 4; ++cc)
-                                acc[rr][cc] = mac<EXACT>(acc[rr][cc], v[cc + H::OFF + F0 - 1 - fi], wv);
-                        }
+                        for (int cc = 0; cc < 4; ++cc)
+                            acc[rr][cc] = mac<EXACT>(acc[rr][cc], v[cc + H::OFF + F0 - 1 - fi], wv);
                     }
                 }
             }

@@ -298,7 +298,11 @@ unsigned blocks_for(long long n, int per_block) {
 // scratch buffer released when it goes out of scope (stream-ordered)
 struct Scratch {
     void *p = nullptr;
-    explicit Scratch(size_t bytes) : p(bytes ? alloc_device(bytes) : nullptr) {}
+    explicit Scratch(size_t bytes) : p(bytes ? tagged(bytes) : nullptr) {}
+    static void *tagged(size_t bytes) {
+        MemTag tag("frequency-domain buffers");
+        return alloc_device(bytes);
+    }
     ~Scratch() {
         if (p) free_device(p);
     }

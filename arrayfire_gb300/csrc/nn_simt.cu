@@ -516,6 +516,7 @@ static void gather_run(const NNGeom &g, int mode, const T *A, long long SW, long
     using A_t = typename NNAcc<T>::type;
     if (g.fw * g.fh > MAX_TAPS) AFGB_THROW(AF_ERR_NOT_SUPPORTED, "filter has more than 1024 taps");
     const long long nw = g.fw * g.fh * g.C * g.K;
+    MemTag tag("weight operands");
     A_t *B = static_cast<A_t *>(alloc_device((size_t)nw * sizeof(A_t)));
     filter_relayout_kernel<T, A_t><<<grid_cap(nw, 256), 256, 0, stream()>>>(
         w, g.fw, g.fh, g.C, g.K, B, mode == 0 ? 0 : 1);
@@ -605,7 +606,11 @@ static void simt_wgrad_t(const NNGeom &g, const Array &grad, const Array &sig, A
     p.chunk = chunk;
     const long long total = p.rows * g.K;
     if (total == 0) return;
-    A_t *partial = static_cast<A_t *>(alloc_device((size_t)(splits * total) * sizeof(A_t)));
+    A_t *partial;
+    {
+        MemTag tag("split-K partial sums");
+        partial = static_cast<A_t *>(alloc_device((size_t)(splits * total) * sizeof(A_t)));
+    }
     p.partial = partial;
     size_t smem = (size_t)(WG_K * WG_M + WG_K * WG_N) * sizeof(A_t) + WG_M * (8 + 4 + 4);
     AFGB_CUDA(cudaFuncSetAttribute(wgrad_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -675,7 +680,11 @@ static void bias_t(const NNGeom &g, const Array &grad, Array &db) {
     const long long total = WoHo * g.N;
     const long long chunk = 16384;
     const int nchunks = (int)std::max(1LL, (total + chunk - 1) / chunk);
-    float *partial = static_cast<float *>(alloc_device((size_t)nchunks * g.K * sizeof(float)));
+    float *partial;
+    {
+        MemTag tag("split-K partial sums");
+        partial = static_cast<float *>(alloc_device((size_t)nchunks * g.K * sizeof(float)));
+    }
     dim3 grid1((unsigned)nchunks, (unsigned)g.K);
     bias_stage1_kernel<T><<<grid1, 256, 0, stream()>>>(grad.ptr<T>(), WoHo, g.K, g.N, chunk,
                                                         partial, nchunks);

@@ -810,7 +810,7 @@ struct WgradParams {
     const __nv_bfloat16 *g;  // [N][Ho][Wo][Kpad]
     float *partial;          // [splits][C*taps][K]
     int W, H, Cpad, C, N;
-    int Wo, Ho, Kpad, K;
+    int Wo, Ho, Kpad, K;  // Kpad: channels stored per pixel of G (a multiple of 64)
     int sx, sy, px, py, dx, dy, fw, fh;
     long long Q;        // cp.async path: Wo*Ho*N pixels; TMA path: pixel blocks
     long long chunk;    // pixels (cp.async) or pixel blocks (TMA) per split
@@ -907,14 +907,16 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
                 const uint32_t sb = smem_u32(b_stage + s * WG_B_BYTES);
                 const bool qv = q < q_end;
                 const uint32_t rowoff = (row >> 3) * 1024 + (row & 7) * 128;
-                // A: G row (128 k = two 64-wide MN atoms)
+                // A: G row (128 k = two 64-wide MN atoms); channels at or past
+                // the row's stored Kpad (a multiple of 64) read as zero
                 const __nv_bfloat16 *gsrc = p.g + q * p.Kpad + k0;
 #pragma unroll
                 for (int e = 0; e < 8; ++e) {
                     const int ch = half * 8 + e;  // 16-byte chunk along k
                     const int atom = ch >> 3, j = ch & 7;
+                    const bool cv = qv && k0 + 8 * ch < p.Kpad;
                     cp_async_16(sa + atom * 8192 + rowoff + ((j ^ (row & 7)) << 4),
-                                qv ? gsrc + 8 * ch : p.g, qv ? 16u : 0u);
+                                cv ? gsrc + 8 * ch : p.g, cv ? 16u : 0u);
                 }
                 // B: X rows at the shifted pixel for each (tap, channel chunk)
                 for (int grp = 0; grp < ng; ++grp) {
@@ -1038,7 +1040,7 @@ struct StripParams {
     const __nv_bfloat16 *g;  // [N][Ho][Wo][Kpad]
     float *partial;          // [splits][C*taps][K]
     int W, H, Cpad, C, N;
-    int Wo, Ho, Kpad, K;
+    int Wo, Ho, Kpad, K;  // Kpad: channels stored per pixel of G (a multiple of 64)
     int sy, px, py, dx, dy, fw, fh;
     int BX, BY, ntx, nty;
     int UB, nub;             // taps per tile along u, u-blocks per filter row
@@ -1609,8 +1611,12 @@ static CUtensorMap make_imap(const void *ptr, int Cpad, int W, int H, int N, int
 static int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
 static __nv_bfloat16 *to_nhwc(const float *src, int W, int H, int C, int N, int Cpad) {
-    __nv_bfloat16 *out =
-        static_cast<__nv_bfloat16 *>(alloc_device((size_t)W * H * N * Cpad * sizeof(__nv_bfloat16)));
+    __nv_bfloat16 *out;
+    {
+        MemTag tag("bf16 channels-last copies");
+        out = static_cast<__nv_bfloat16 *>(
+            alloc_device((size_t)W * H * N * Cpad * sizeof(__nv_bfloat16)));
+    }
     const long long P = (long long)W * H;
     if ((P & 3) == 0 && (reinterpret_cast<uintptr_t>(src) & 15) == 0) {
         const long long tiles_p = (P + CV_PIX - 1) / CV_PIX;
@@ -1680,6 +1686,7 @@ static NNGeom folded_geometry(const NNGeom &g) {
 
 static __nv_bfloat16 *fold_taps(const float *x, const NNGeom &g) {
     const long long npix = g.Wo * g.Ho * g.N;
+    MemTag tag("bf16 channels-last copies");
     __nv_bfloat16 *out = static_cast<__nv_bfloat16 *>(alloc_device((size_t)npix * 64 * 2));
     const unsigned blocks = (unsigned)std::max(1LL, std::min<long long>((npix + 255) / 256,
                                                                         num_sms() * 16LL));
@@ -1760,6 +1767,7 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     unsigned int *amax = nullptr;
     if (!fp8 && unfolded) {
         img = fold_taps(img_f32, *unfolded);
+        MemTag tag("weight operands");
         wt = alloc_device((size_t)OCpad * 64 * 2);
         const long long total = (long long)OCpad * 64;
         const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
@@ -1771,6 +1779,7 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     } else if (!fp8) {
         img = img_ready ? const_cast<__nv_bfloat16 *>(img_ready)
                         : to_nhwc(img_f32, SW, SH, SC, (int)g.N, SCpad);
+        MemTag tag("weight operands");
         wt = alloc_device((size_t)OCpad * taps * SCpad * 2);
         long long total = (long long)OCpad * taps * SCpad;
         unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
@@ -1781,6 +1790,7 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
         AFGB_POST_LAUNCH("weights_bf16_kernel");
     } else {
         const int K = (int)g.K;
+        MemTag tag("fp8 operands and scales");
         scales = static_cast<float *>(alloc_device((size_t)(2 * K + 1) * sizeof(float)));
         amax = static_cast<unsigned int *>(alloc_device(sizeof(unsigned int)));
         AFGB_CUDA(cudaMemsetAsync(amax, 0, sizeof(unsigned int), stream()));
@@ -1964,8 +1974,11 @@ static void run_strip_conv(const NNGeom &g, int mode, const __nv_bfloat16 *img, 
     const int SCpad = round_up(SC, 64);
     const int OCpad = round_up(DC, 64);
     const int taps = (int)(g.fw * g.fh);
-    __nv_bfloat16 *wt =
-        static_cast<__nv_bfloat16 *>(alloc_device((size_t)OCpad * taps * SCpad * 2));
+    __nv_bfloat16 *wt;
+    {
+        MemTag tag("weight operands");
+        wt = static_cast<__nv_bfloat16 *>(alloc_device((size_t)OCpad * taps * SCpad * 2));
+    }
     {
         const long long total = (long long)OCpad * taps * SCpad;
         const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
@@ -2132,7 +2145,7 @@ static bool run_wgrad_strip(const NNGeom &g, const __nv_bfloat16 *x, const __nv_
     p.fw = (int)g.fw;
     p.fh = (int)g.fh;
     p.nchunk = Cpad / 64;
-    p.n_k_tiles = Kpad / 128;
+    p.n_k_tiles = round_up((int)g.K, 128) / 128;  // past Kpad the G map reads zeros
     p.ntx = ((int)g.Wo + p.BX - 1) / p.BX;
     p.nty = ((int)g.Ho + p.BY - 1) / p.BY;
     p.Q = (long long)p.ntx * p.nty * g.N;
@@ -2146,7 +2159,11 @@ static bool run_wgrad_strip(const NNGeom &g, const __nv_bfloat16 *x, const __nv_
     splits = (p.Q + chunk - 1) / chunk;
     p.chunk = chunk;
     const long long rows = g.C * g.fw * g.fh;
-    float *partial = static_cast<float *>(alloc_device((size_t)(splits * rows * g.K) * sizeof(float)));
+    float *partial;
+    {
+        MemTag tag("split-K partial sums");
+        partial = static_cast<float *>(alloc_device((size_t)(splits * rows * g.K) * sizeof(float)));
+    }
     p.partial = partial;
     const size_t smem = 1024 + (size_t)p.nst * p.stage_bytes + sizeof(StripSmem) + 64;
     {
@@ -2164,7 +2181,8 @@ static bool run_wgrad_strip(const NNGeom &g, const __nv_bfloat16 *x, const __nv_
 }
 
 // filter gradient from the incoming gradient already in bf16 NHWC, its
-// channels padded to Kpad (a multiple of 128)
+// channels padded to Kpad (a multiple of 64; the 128-row k tiles read the
+// channels past it as zeros)
 static void filter_grad_from(const NNGeom &g0, const __nv_bfloat16 *gg, int Kpad, const Array &sig,
                              Array &dw) {
     // folded taps: the signal operand is the folded image and the problem is
@@ -2221,7 +2239,7 @@ static void filter_grad_from(const NNGeom &g0, const __nv_bfloat16 *gg, int Kpad
         }
     }
     p.groups_per_tile = best;
-    p.n_k_tiles = Kpad / 128;
+    p.n_k_tiles = round_up((int)g.K, 128) / 128;  // past Kpad the G loads read zeros
     // 64-pixel rectangles by TMA; the signal map walks every s-th pixel
     // (traversal strides up to 8); otherwise the cp.async row gather
     int rbx = 0, rby = 0;
@@ -2254,7 +2272,11 @@ static void filter_grad_from(const NNGeom &g0, const __nv_bfloat16 *gg, int Kpad
     splits = (units + chunk - 1) / chunk;
     p.chunk = chunk;
     const long long rows = g.C * g.fw * g.fh;
-    float *partial = static_cast<float *>(alloc_device((size_t)(splits * rows * g.K) * sizeof(float)));
+    float *partial;
+    {
+        MemTag tag("split-K partial sums");
+        partial = static_cast<float *>(alloc_device((size_t)(splits * rows * g.K) * sizeof(float)));
+    }
     p.partial = partial;
     const size_t smem = 1024 + WG_STAGES * (WG_A_BYTES + WG_B_BYTES) + sizeof(Smem) + 64;
     {
@@ -2281,21 +2303,20 @@ static void filter_grad_from(const NNGeom &g0, const __nv_bfloat16 *gg, int Kpad
 
 bool tc_filter_grad(const NNGeom &g, const Array &grad, const Array &sig, Array &dw) {
     if (grad.type != f32) return false;
-    const int Kpad = round_up((int)g.K, 128);
+    const int Kpad = round_up((int)g.K, 64);
     __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kpad);
     filter_grad_from(g, gg, Kpad, sig, dw);
     free_device(gg);
     return true;
 }
 
-// data and filter gradients sharing one bf16 copy of the incoming gradient;
-// false (nothing done) when the two would want different channel paddings
-// (K mod 128 in 1..64) or the data-gradient kernel does not cover the shape
+// data and filter gradients sharing one bf16 copy of the incoming gradient
+// (channels padded to 64); false (nothing done) when the data-gradient kernel
+// does not cover the shape
 bool tc_data_filter_grads(const NNGeom &g, const Array &grad, const Array &sig, const Array &filt,
                           Array &dx, Array &dw) {
     if (grad.type != f32 || !gather_fits(g, 1)) return false;
-    const int Kpad = round_up((int)g.K, 128);
-    if (Kpad != round_up((int)g.K, 64)) return false;
+    const int Kpad = round_up((int)g.K, 64);
     __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kpad);
     if (strip_conv_fits(g, 1))
         run_strip_conv(g, 1, gg, filt.ptr<float>(), dx.ptr<float>(), nullptr);

@@ -679,6 +679,7 @@ def run_cnn(af, args) -> dict:
         loss, grads, rfl = cnn_step(x0, ws, CNN_GEOMS, precision=prec, recompute=True)
         torch.cuda.synchronize()
         lib_peak = af.device_mem_peak()
+        breakdown = af.device_mem_peak_breakdown()
         torch_peak = torch.cuda.max_memory_allocated() - base
         errs = [float(torch.linalg.vector_norm(g.double() - r) / torch.linalg.vector_norm(r))
                 for g, r in zip(grads, ref)]
@@ -697,7 +698,9 @@ def run_cnn(af, args) -> dict:
         ms = tot / k
         out[prec] = {"ms_per_step": round(ms, 3), "TFLOP/s": round(useful / (ms / 1e3) / 1e12, 2),
                      "recompute_gflop": round(rfl / 1e9, 2),
-                     "peak_library_bytes": int(lib_peak), "peak_torch_harness_bytes": int(torch_peak),
+                     "peak_library_bytes": int(lib_peak),
+                     "peak_library_breakdown": breakdown,
+                     "peak_torch_harness_bytes": int(torch_peak),
                      "filter_grad_rel_err_vs_fp64": [float(f"{e:.3e}") for e in errs]}
     out["bf16_speedup_over_fp32"] = round(out["fp32"]["ms_per_step"] / out["bf16"]["ms_per_step"], 2)
     return out

@@ -335,6 +335,10 @@ AFGB_API af_err af_device_gc(void);
 /* Peak of lock_bytes since load or the last reset (reset != 0 restarts it at
  * the current value).  No counterpart in the reference. */
 AFGB_API af_err afgb_device_mem_peak(size_t *peak_bytes, int reset);
+/* What the bytes at that peak held, as "purpose=bytes" lines (arrays,
+ * bf16 channels-last copies, weight operands, split-K partial sums, ...),
+ * written to buf (len bytes, NUL-terminated, truncated if short). */
+AFGB_API af_err afgb_device_mem_peak_breakdown(char *buf, size_t len);
 
 /* Fault injection for tests: the n-th device allocation from now fails with
  * AF_ERR_NO_MEM (n <= 0 disables).  Host-side only. */

@@ -61,9 +61,13 @@ def assert_same(got, ref, what=""):
 
 
 def _fused_ok(oracle, out, s, f, rank, expand):
-    ref = oracle.convolve(s, f, C.F32, rank, expand)
+    """max over outputs of |out - ref| / sum|s*f| (all flattened in the
+    same column-major order, so no broadcasting between shapes)."""
+    ref = oracle.convolve(s, f, C.F32, rank, expand).ravel(order="F")
     bound = oracle.convolve(np.abs(s.astype(np.float64)), np.abs(f.astype(np.float64)), C.F64,
-                            rank, expand)
+                            rank, expand).ravel(order="F")
+    out = np.asarray(out).ravel(order="F")
+    assert out.size == ref.size
     err = np.abs(out.astype(np.float64) - ref)
     return float((err / (bound + 1e-30)).max())
 
@@ -230,18 +234,21 @@ def test_sep15_f32_64x2048sq(af, oracle):
     # |sep - ref| <= 1e-6 * (|cf| (x) |rf|) * |s|, the separable sum of |terms|
     bound = oracle.convolve2_sep(np.abs(sb.astype(np.float64)), np.abs(cf.astype(np.float64)),
                                  np.abs(rf.astype(np.float64)), C.F64, False)
-    got = np.asfortranarray(fused[9].cpu().numpy().T)
+    got = np.asfortranarray(fused[9].cpu().numpy().T).ravel(order="F")
+    ref, bound = ref.ravel(order="F"), bound.ravel(order="F")
     assert float((np.abs(got - ref) / (bound + 1e-30)).max()) <= 1e-6
 
 
 @pytest.mark.parametrize("expand", [False, True], ids=["default", "expand"])
 def test_sep_tma_many_tiles_per_cta(af, oracle, expand):
-    """32 images of 512x512 with 7 + 15 taps: 2048 tiles over the
-    two-stage ring of each CTA; every output bit for bit."""
+    """32 images of 512x512 with 15 + 15 taps (7 + 7 in EXPAND mode; the TMA
+    kernel takes equal lengths): 2048 tiles over the two-stage ring of each
+    CTA; every output bit for bit."""
     g = C.rng(2222)
     s = np.asfortranarray(g.random((512, 512, 32), dtype=np.float32))
-    cf = g.standard_normal(7).astype(np.float32)
-    rf = g.standard_normal(15).astype(np.float32)
+    taps = 7 if expand else 15
+    cf = g.standard_normal(taps).astype(np.float32)
+    rf = g.standard_normal(taps).astype(np.float32)
     S = af.Array.from_numpy(s)
     CF, RF = af.Array.from_numpy(cf), af.Array.from_numpy(rf)
     mode = af.AF_CONV_EXPAND if expand else af.AF_CONV_DEFAULT
