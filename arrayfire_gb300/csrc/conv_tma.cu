@@ -199,7 +199,7 @@ __device__ __forceinline__ void widen_tile(const T *tb, float *ft) {
 // 2-D direct convolution, F0 x F1 filter, 64x64 tile, 4x4 outputs per thread
 // ===========================================================================
 template <typename T, int F0, int F1, bool EXACT, bool EXPAND>
-__global__ void __launch_bounds__(THREADS) conv2_tma_kernel(const __grid_constant__ CUtensorMap smap,
+__global__ void __launch_bounds__(THREADS, 3) conv2_tma_kernel(const __grid_constant__ CUtensorMap smap,
                                                             const DirectParams p,
                                                             const TileGrid tg) {
     using H = Halo<T, F0, F1, EXPAND>;
@@ -738,21 +738,28 @@ __global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ 
     __syncthreads();  // barriers initialised before anyone waits on them
 
     int k = 0;
+    // filter taps of the tile's volume (SAME batches: one filter per volume),
+    // kept in registers and reloaded only when the volume's filter changes
+    long long cur_filt = -1;
+    float wr[27];
     for (int t = blockIdx.x; t < t3.ntiles; t += gridDim.x, ++k) {
         const int buf = k & 1;
         if (threadIdx.x == 0 && t + (int)gridDim.x < t3.ntiles) issue(t + gridDim.x, buf ^ 1);
         long long i0, j0, k0, b;
         decode(t, i0, j0, k0, b);
-        // filter taps for this batch (SAME batches: one filter per volume)
-        const float *w = static_cast<const float *>(p.filt) + b * p.filt_step[3];
-        float wr[27];
+        const long long foff = b * p.filt_step[3];
+        if (foff != cur_filt) {
+            const float *w = static_cast<const float *>(p.filt) + foff;
 #pragma unroll
-        for (int fk = 0; fk < 3; ++fk)
+            for (int fk = 0; fk < 3; ++fk)
 #pragma unroll
-            for (int fj = 0; fj < 3; ++fj)
+                for (int fj = 0; fj < 3; ++fj)
 #pragma unroll
-                for (int fi = 0; fi < 3; ++fi)
-                    wr[(fk * 3 + fj) * 3 + fi] = __ldg(w + fi * p.fs[0] + fj * p.fs[1] + fk * p.fs[2]);
+                    for (int fi = 0; fi < 3; ++fi)
+                        wr[(fk * 3 + fj) * 3 + fi] =
+                            __ldg(w + fi * p.fs[0] + fj * p.fs[1] + fk * p.fs[2]);
+            cur_filt = foff;
+        }
         if (!wait_tile(&bar[buf], (k >> 1) & 1)) break;
         const float *tile = reinterpret_cast<const float *>(sm3 + buf * C3_BUF);
         const int tx = threadIdx.x & 15;

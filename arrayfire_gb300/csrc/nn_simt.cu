@@ -371,26 +371,45 @@ __global__ void __launch_bounds__(WG_THREADS) wgrad_kernel(WgradParams<T> p) {
     }
 }
 
-// Neumaier-compensated sum over splits in fixed order, then the reference's
-// flip into dW (fw,fh,C,K): R[c + C*tap][k] -> dW[fw-1-u, fh-1-v, c, k]
+__device__ __forceinline__ float abs_of(float v) { return fabsf(v); }
+__device__ __forceinline__ double abs_of(double v) { return fabs(v); }
+
+// s + v into the running sum s with its Neumaier compensation comp
+template <typename A>
+__device__ __forceinline__ void neumaier_add(A &s, A &comp, A v) {
+    const A tsum = s + v;
+    if (abs_of(s) >= abs_of(v)) comp += (s - tsum) + v;
+    else comp += (v - tsum) + s;
+    s = tsum;
+}
+
+// Split-K partial sums -> the filter gradient with the reference's flip into
+// dW (fw,fh,C,K): R[c + C*tap][k] -> dW[fw-1-u, fh-1-v, c, k].  One thread
+// per output sums the splits in split order with Neumaier compensation; the
+// loads of eight splits are issued before any of them is summed, so their
+// latencies overlap.  The order is fixed, so results are bit-reproducible.
 template <typename T, typename A>
-__global__ void wgrad_reduce_kernel(const A *partial, int splits, long long rows, long long K,
-                                    long long C, long long fw, long long fh, T *dw) {
-    long long total = rows * K;
+__global__ void __launch_bounds__(256) wgrad_reduce_kernel(const A *partial, int splits,
+                                                           long long rows, long long K,
+                                                           long long C, long long fw,
+                                                           long long fh, T *dw) {
+    const long long total = rows * K;
     for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
          t += (long long)gridDim.x * blockDim.x) {
         A s = 0, comp = 0;
-        for (int z = 0; z < splits; ++z) {
-            A v = partial[(long long)z * total + t];
-            A tsum = s + v;
-            if (fabs((double)s) >= fabs((double)v)) comp += (s - tsum) + v;
-            else comp += (v - tsum) + s;
-            s = tsum;
+        int z = 0;
+        for (; z + 8 <= splits; z += 8) {
+            A v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) v[i] = partial[(long long)(z + i) * total + t];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) neumaier_add(s, comp, v[i]);
         }
-        A res = s + comp;
-        long long r = t / K, k = t % K;
-        long long c = r % C, tap = r / C;
-        long long u = tap % fw, v = tap / fw;
+        for (; z < splits; ++z) neumaier_add(s, comp, partial[(long long)z * total + t]);
+        const A res = s + comp;
+        const long long r = t / K, k = t % K;
+        const long long c = r % C, tap = r / C;
+        const long long u = tap % fw, v = tap / fw;
         dw[(fw - 1 - u) + fw * ((fh - 1 - v) + fh * (c + C * k))] = st_conv<T, A>(res);
     }
 }

@@ -70,6 +70,8 @@ struct GatherParams {
     int DW, DH, DC;
     int mode;  // 0 forward, 1 data gradient
     int tma_store;  // epilogue writes by TMA through the output map (unit-stride outputs)
+    int a_rows;     // weight rows loaded per stage: 128, or 64 when the output has at most 64
+                    // channels (the upper half of each weight tile is zero, set once)
     int sx, sy, px, py, dx, dy, fw;
     int nchunk;       // SCpad / 64
     int n_och_tiles;  // ceil(DC / 128)
@@ -205,6 +207,17 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
     if (warp == 9 && lane == 0) {
         prefetch_tmap(&wmap);
         if (TMA_B) prefetch_tmap(&xmap);
+    }
+    if (p.a_rows < BM) {
+        // rows a_rows..127 of every weight tile are zero padding: written once
+        // here, never loaded (the tensor core reads them through the async proxy)
+        const int half_bytes = (BM - p.a_rows) * 128;
+        for (int i = threadIdx.x; i < STAGES * half_bytes / 16; i += blockDim.x) {
+            const int st = i / (half_bytes / 16), off = i - st * (half_bytes / 16);
+            *reinterpret_cast<uint4 *>(a_stage + st * A_BYTES + p.a_rows * 128 + off * 16) =
+                make_uint4(0u, 0u, 0u, 0u);
+        }
+        fence_proxy_async_smem();
     }
     tc_fence_before();
     __syncthreads();
@@ -343,9 +356,12 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         // one 64-byte row per channel, 16-byte chunks swizzled by
                         // (row >> 1) & 3 (the output map's 64-byte swizzle: conflict-
                         // free 128-bit stores); one lane stores the 32x16 block by TMA
+                        // (two alternating staging buffers were measured no faster: the
+                        // forward is not bound by this wait)
+                        float *sbuf = stg;
                         if (lane == 0) bulk_wait_read();  // the last store has read the buffer
                         __syncwarp();
-                        unsigned char *row = reinterpret_cast<unsigned char *>(stg) + lane * 64;
+                        unsigned char *row = reinterpret_cast<unsigned char *>(sbuf) + lane * 64;
 #pragma unroll
                         for (int e = 0; e < 4; ++e)
                             *reinterpret_cast<float4 *>(row + ((e ^ ((lane >> 1) & 3)) << 4)) =
@@ -354,7 +370,7 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                         fence_proxy_async_smem();
                         __syncwarp();
                         if (lane == 0) {
-                            tma_store_4d(&omap, smem_u32(stg), ti.x0 + (e0 % p.BX), ti.y0 + e0 / p.BX,
+                            tma_store_4d(&omap, smem_u32(sbuf), ti.x0 + (e0 % p.BX), ti.y0 + e0 / p.BX,
                                          ti.och0 + 32 * q, ti.n);
                             bulk_commit();
                         }
@@ -502,7 +518,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                             break;
                         }
                         const int u = p.tap_u[tq], v = p.tap_v[tq];
-                        mbar_arrive_expect_tx(&sm->full[s], TMA_B ? A_BYTES + B_BYTES : A_BYTES);
+                        mbar_arrive_expect_tx(&sm->full[s], (uint32_t)(p.a_rows * 128) +
+                                                                (TMA_B ? B_BYTES : 0));
                         tma_load_2d(smem_u32(a_stage + s * A_BYTES), &wmap, &sm->full[s],
                                     (u + p.fw * v) * p.SCpad + cchunk * (FP8 ? 128 : 64), ti.och0);
                         if (TMA_B)
@@ -1913,7 +1930,9 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
                         CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
             p.tma_store = 1;
     }
-    CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad, esize);
+    // at most 64 output channels: only the real half of each weight tile is loaded
+    p.a_rows = (OCpad == BM && DC <= 64) ? 64 : BM;
+    CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad, esize, p.a_rows);
     const size_t smem = gather_smem();
     if (ntile > 0) {
         const int grid = std::min(ntile, num_sms());
@@ -2114,7 +2133,9 @@ bool tc_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &
 // the strip kernel (stride 1 along x); false when its shape limits do not hold
 static bool run_wgrad_strip(const NNGeom &g, const __nv_bfloat16 *x, const __nv_bfloat16 *gg,
                             int Cpad, int Kpad, const NNGeom &g0, float *dw) {
-    if (g.sx != 1 || g.sy > 8 || g.fw * g.fh > 64) return false;
+    // one-tap-wide filters give the strip kernel an N of only 64; the tile
+    // kernel groups up to four 64-channel groups into one N=256 MMA instead
+    if (g.sx != 1 || g.sy > 8 || g.fw * g.fh > 64 || g.fw < 2) return false;
     StripParams p;
     std::memset(&p, 0, sizeof(p));
     if (!pick_rect((int)g.Wo, (int)g.Ho, WG_KP, 16, p.BX, p.BY)) return false;

@@ -20,6 +20,7 @@ Host dispatch logic restated here (same decisions as the library):
 from __future__ import annotations
 
 import ctypes
+import math
 import os
 import subprocess
 from pathlib import Path
@@ -370,6 +371,119 @@ def sobel(img: np.ndarray, dtype: int, which: str = "port"):
         dx = ((SW + SE) - (NW + NE)) + two * (S - N)
         dy = ((NE + SE) - (NW + SW)) + two * (E - W)
     return np.asfortranarray(dx.astype(ot)), np.asfortranarray(dy.astype(ot))
+
+
+# ---------------------------------------------------------------------------
+# af_harris (src/api/c/harris.cpp:42-95 -> src/backend/cpu/harris.cpp:28-144)
+# ---------------------------------------------------------------------------
+def harris_filter_len(sigma: float, block_size: int) -> int:
+    """src/api/c/harris.cpp:47-50: block_size, else floor(6*sigma) made odd
+    (6.f * sigma in float)."""
+    if block_size:
+        return int(block_size)
+    fl = int(math.floor(float(np.float32(6.0) * np.float32(sigma))))
+    return fl - 1 if fl % 2 == 0 else fl
+
+
+def harris_window(filter_len: int, sigma: float, dtype: int) -> np.ndarray:
+    """The window of src/backend/cpu/harris.cpp:38-47: a box of 1/filter_len
+    when sigma < 0.5, else gaussian1D (src/backend/cpu/utility.hpp:35-49:
+    each tap evaluated in double, stored in T, summed in T in order, divided
+    in T)."""
+    T = NP_OF[dtype]
+    if np.float32(sigma) < np.float32(0.5):
+        return np.full(filter_len, T(1) / T(filter_len), dtype=T)
+    s = float(np.float32(sigma))
+    taps = np.zeros(filter_len, dtype=T)
+    total = T(0)
+    for i in range(filter_len):
+        x = i - (filter_len - 1) // 2
+        el = T(1.0 / math.sqrt(2 * math.pi * s * s) * math.exp(-((x * x) / (2 * (s * s)))))
+        taps[i] = el
+        total = T(total + el)
+    return (taps / total).astype(T)
+
+
+def harris(img: np.ndarray, dtype: int, max_corners: int, min_response: float, sigma: float,
+           block_size: int, k_thr: float, which: str = "port"):
+    """af_harris on a 2-D f32/f64 image: returns (x, y, score) float32 vectors
+    (x along dim1, y along dim0), in the reference's order.
+
+    Port of src/backend/cpu/harris.cpp:28-144 with the kernels of
+    src/backend/cpu/kernel/gradient.hpp:18-80 (central differences, one-sided
+    at the edges) and src/backend/cpu/kernel/harris.hpp:18-118 (products,
+    responses det - k*tr^2 on [border, d - border), strict 8-neighbour maxima
+    on [border+1, d - border - 1) in scan order, at most 20% of the pixels
+    kept); the window is the separable convolve2 of this oracle; with
+    max_corners > 0 and more corners found, a stable descending sort by score
+    keeps the first max_corners."""
+    a = as_af(img, NP_OF[dtype])
+    d0, d1 = a.shape[0], a.shape[1]
+    T = NP_OF[dtype]
+    fl = harris_filter_len(sigma, block_size)
+    if which == "ref":
+        cap = max(int(np.float32(d0 * d1) * np.float32(0.2)), 1)
+        xo = np.zeros(cap, np.float32)
+        yo = np.zeros(cap, np.float32)
+        ro = np.zeros(cap, np.float32)
+        n = lib("ref").ref_harris(ctypes.c_int(dtype), a.ctypes.data_as(_P), ctypes.c_longlong(d0),
+                                  ctypes.c_longlong(d1), ctypes.c_uint(max_corners),
+                                  ctypes.c_float(min_response), ctypes.c_float(sigma),
+                                  ctypes.c_uint(fl), ctypes.c_float(k_thr), xo.ctypes.data_as(_P),
+                                  yo.ctypes.data_as(_P), ro.ctypes.data_as(_P),
+                                  ctypes.c_longlong(cap))
+        if n < 0:
+            raise RuntimeError(f"ref_harris failed ({n})")
+        return xo[:n].copy(), yo[:n].copy(), ro[:n].copy()
+    x = a[:, :, 0, 0]
+    border = fl // 2 + 1
+    r = border + 1
+    empty = (np.zeros(0, np.float32),) * 3
+    if d0 <= 2 * r or d1 <= 2 * r:
+        return empty
+    # gradient(iy, ix, in): grad0 along dim0 is iy, grad1 along dim1 is ix
+    iy = np.empty_like(x)
+    ix = np.empty_like(x)
+    half = T(0.5)
+    iy[1:-1, :] = half * (x[2:, :] - x[:-2, :])
+    iy[0, :] = x[1, :] - x[0, :]
+    iy[-1, :] = x[-1, :] - x[-2, :]
+    ix[:, 1:-1] = half * (x[:, 2:] - x[:, :-2])
+    ix[:, 0] = x[:, 1] - x[:, 0]
+    ix[:, -1] = x[:, -1] - x[:, -2]
+    win = harris_window(fl, sigma, dtype)
+    ixx = convolve2_sep(np.asfortranarray(ix * ix), win, win, dtype, False)[:, :, 0, 0]
+    ixy = convolve2_sep(np.asfortranarray(ix * iy), win, win, dtype, False)[:, :, 0, 0]
+    iyy = convolve2_sep(np.asfortranarray(iy * iy), win, win, dtype, False)[:, :, 0, 0]
+    k = T(np.float32(k_thr))
+    resp = np.zeros((d0, d1), T)
+    sl = (slice(border, d0 - border), slice(border, d1 - border))
+    tr = ixx[sl] + iyy[sl]
+    det = ixx[sl] * iyy[sl] - ixy[sl] * ixy[sl]
+    resp[sl] = det - k * (tr * tr)
+    v = resp[r:d0 - r, r:d1 - r]
+    mx = None
+    for dy in (-1, 0, 1):
+        for dx in (-1, 0, 1):
+            if dy == 0 and dx == 0:
+                continue
+            nb = resp[r + dy:d0 - r + dy, r + dx:d1 - r + dx]
+            mx = nb if mx is None else np.maximum(mx, nb)
+    min_r = 0 if max_corners > 0 else int(np.float32(min_response))
+    keep = (v > mx) & (v >= T(np.float32(min_r)))
+    idx = np.flatnonzero(keep.ravel(order="F"))
+    h = d0 - 2 * r
+    ys = (idx % h + r).astype(np.float32)
+    xs = (idx // h + r).astype(np.float32)
+    sc = v.ravel(order="F")[idx].astype(np.float32)
+    corner_lim = int(np.float32(d0 * d1) * np.float32(0.2))
+    found = idx.size
+    ys, xs, sc = ys[:corner_lim], xs[:corner_lim], sc[:corner_lim]
+    out_n = min(found, max_corners if max_corners > 0 else corner_lim)
+    if max_corners > 0 and found > out_n:
+        order = np.argsort(-sc, kind="stable")[:out_n]
+        return xs[order], ys[order], sc[order]
+    return xs[:out_n], ys[:out_n], sc[:out_n]
 
 
 # ---------------------------------------------------------------------------

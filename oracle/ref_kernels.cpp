@@ -21,12 +21,25 @@
  *   ref_sobel            -> kernel::derivative<Ti, To, isDX> for dx and dy
  *                           (src/backend/cpu/kernel/sobel.hpp:19-75), every
  *                           af_sobel_operator type
+ *   ref_harris_f32/_f64  -> the corner pipeline of src/backend/cpu/harris.cpp:
+ *                           gaussian1D / box window (cpu/utility.hpp:35-49),
+ *                           kernel::gradient (cpu/kernel/gradient.hpp),
+ *                           kernel::second_order_deriv, kernel::convolve2 (the
+ *                           separable window), kernel::harris_responses,
+ *                           kernel::non_maximal (cpu/kernel/harris.hpp), and the
+ *                           stable descending sort + keep_corners of the
+ *                           max_corners > 0 case (cpu/kernel/sort_by_key_impl.hpp)
  */
 #include <kernel/convolve.hpp>
+#include <kernel/gradient.hpp>
+#include <kernel/harris.hpp>
 #include <kernel/sobel.hpp>
+#include <kernel/sort_helper.hpp>
+#include <utility.hpp>
 #include <kernel/unwrap.hpp>
 #include <kernel/wrap.hpp>
 
+#include <algorithm>
 #include <complex>
 #include <utility>
 #include <cstring>
@@ -246,4 +259,87 @@ int ref_wrap_any(int dtype, void *out, const long long *odims, const void *in,
     return 0;
 }
 
+}  // extern "C"
+
+namespace {
+// the steps of arrayfire::cpu::harris (src/backend/cpu/harris.cpp:28-144),
+// each a reference kernel; returns the number of corners written
+template <typename T>
+int harris_any(const T *in, long long d0, long long d1, unsigned max_corners, float min_response,
+               float sigma, unsigned filter_len, float k_thr, float *xo, float *yo, float *ro,
+               long long cap) {
+    const dim4 id(d0, d1, 1, 1), st(1, d0, d0 * d1, d0 * d1);
+    const long long n = d0 * d1;
+    std::vector<T> filt(filter_len);
+    if (sigma < 0.5f) {
+        for (unsigned i = 0; i < filter_len; i++) filt[i] = static_cast<T>(1) / (filter_len);
+    } else {
+        arrayfire::cpu::gaussian1D<T>(filt.data(), static_cast<int>(filter_len), sigma);
+    }
+    const unsigned border_len = filter_len / 2 + 1;
+    std::vector<T> ix(n), iy(n), ixx(n), ixy(n), iyy(n), tmp(n);
+    CParam<T> cin(in, id, st);
+    K::gradient<T>(Param<T>(iy.data(), id, st), Param<T>(ix.data(), id, st), cin);
+    K::second_order_deriv<T>(Param<T>(ixx.data(), id, st), Param<T>(ixy.data(), id, st),
+                             Param<T>(iyy.data(), id, st), (unsigned)n,
+                             CParam<T>(ix.data(), id, st), CParam<T>(iy.data(), id, st));
+    const dim4 fd(filter_len, 1, 1, 1), fs(1, filter_len, filter_len, filter_len);
+    CParam<T> cf(filt.data(), fd, fs);
+    for (std::vector<T> *a : {&ixx, &ixy, &iyy}) {
+        std::vector<T> t2(n), out(n);
+        K::convolve2<T, T, false>(Param<T>(out.data(), id, st), CParam<T>(a->data(), id, st), cf,
+                                  cf, Param<T>(t2.data(), id, st));
+        *a = out;
+    }
+    std::vector<T> resp(n, T(0));
+    K::harris_responses<T>(Param<T>(resp.data(), dim4(n, 1, 1, 1), dim4(1, n, n, n)),
+                           (unsigned)d0, (unsigned)d1, CParam<T>(ixx.data(), id, st),
+                           CParam<T>(ixy.data(), id, st), CParam<T>(iyy.data(), id, st), k_thr,
+                           border_len);
+    const unsigned corner_lim = (unsigned)(n * 0.2f);
+    std::vector<float> xc(corner_lim + 1), yc(corner_lim + 1), rc(corner_lim + 1);
+    const unsigned min_r = (max_corners > 0) ? 0U : static_cast<unsigned>(min_response);
+    unsigned found = 0;
+    const dim4 cd(corner_lim, 1, 1, 1), cs(1, corner_lim, corner_lim, corner_lim);
+    K::non_maximal<T>(Param<float>(xc.data(), cd, cs), Param<float>(yc.data(), cd, cs),
+                      Param<float>(rc.data(), cd, cs), &found, (unsigned)d0, (unsigned)d1,
+                      CParam<T>(resp.data(), dim4(n, 1, 1, 1), dim4(1, n, n, n)), (float)min_r,
+                      border_len, corner_lim);
+    const unsigned out_n = std::min(found, (max_corners > 0) ? max_corners : corner_lim);
+    if ((long long)out_n > cap) return -1;
+    if (max_corners > 0 && found > out_n) {
+        // sort_index(respCorners, descending): a stable sort of (value, index)
+        const unsigned m = std::min(found, corner_lim);
+        // with the reference's comparator (cpu/kernel/sort_by_key_impl.hpp:58-63)
+        std::vector<K::IndexPair<float, unsigned>> kv(m);
+        for (unsigned i = 0; i < m; ++i) kv[i] = std::make_tuple(rc[i], i);
+        std::stable_sort(kv.begin(), kv.end(), K::IPCompare<float, unsigned, false>());
+        for (unsigned f = 0; f < out_n; ++f) {
+            xo[f] = xc[std::get<1>(kv[f])];
+            yo[f] = yc[std::get<1>(kv[f])];
+            ro[f] = std::get<0>(kv[f]);
+        }
+    } else {
+        for (unsigned f = 0; f < out_n; ++f) {
+            xo[f] = xc[f];
+            yo[f] = yc[f];
+            ro[f] = rc[f];
+        }
+    }
+    return (int)out_n;
+}
+}  // namespace
+
+extern "C" {
+int ref_harris(int dtype, const void *in, long long d0, long long d1, unsigned max_corners,
+               float min_response, float sigma, unsigned filter_len, float k_thr, float *xo,
+               float *yo, float *ro, long long cap) {
+    if (dtype == 0)
+        return harris_any<float>(static_cast<const float *>(in), d0, d1, max_corners, min_response,
+                                 sigma, filter_len, k_thr, xo, yo, ro, cap);
+    if (dtype == 2)
+        return harris_any<double>(static_cast<const double *>(in), d0, d1, max_corners,
+                                  min_response, sigma, filter_len, k_thr, xo, yo, ro, cap);
+    return -2;
+}
 }  // extern "C"
