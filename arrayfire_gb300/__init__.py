@@ -369,6 +369,72 @@ def sobel_operator(image: Array, ker_size: int = 3):
     return Array(dx.value), Array(dy.value)
 
 
+class Features:
+    """An af_features object (include/af/features.h): the count and five f32
+    arrays, owned by the object; released with it."""
+
+    def __init__(self, handle: int):
+        self.handle = handle
+
+    def __del__(self):
+        h, self.handle = getattr(self, "handle", None), None
+        if h:
+            try:
+                lib().af_release_features(h)
+            except Exception:
+                pass
+
+    def num(self) -> int:
+        n = ctypes.c_longlong()
+        _check(lib().af_get_features_num(ctypes.byref(n), self.handle))
+        return n.value
+
+    def array(self, fn) -> Array:
+        """One of the object's arrays, retained (an Array of its own)."""
+        a, r = af_array(), af_array()
+        _check(fn(ctypes.byref(a), self.handle))
+        _check(lib().af_retain_array(ctypes.byref(r), a))
+        return Array(r.value)
+
+    def _get(self, fn) -> np.ndarray:
+        return self.array(fn).to_numpy().ravel(order="F")
+
+    def x(self) -> np.ndarray:
+        return self._get(lib().af_get_features_xpos)
+
+    def y(self) -> np.ndarray:
+        return self._get(lib().af_get_features_ypos)
+
+    def score(self) -> np.ndarray:
+        return self._get(lib().af_get_features_score)
+
+    def orientation(self) -> np.ndarray:
+        return self._get(lib().af_get_features_orientation)
+
+    def size(self) -> np.ndarray:
+        return self._get(lib().af_get_features_size)
+
+
+def harris(image: Array, max_corners: int = 500, min_response: float = 1e5, sigma: float = 1.0,
+           block_size: int = 0, k_thr: float = 0.04) -> Features:
+    """af_harris (include/af/vision.h:402; defaults of af::harris)."""
+    out = ctypes.c_void_p()
+    _check(lib().af_harris(ctypes.byref(out), image.handle, max_corners, min_response, sigma,
+                           block_size, k_thr))
+    return Features(out.value)
+
+
+AF_CANNY_THRESHOLD_MANUAL, AF_CANNY_THRESHOLD_AUTO_OTSU = 0, 1
+
+
+def canny(image: Array, threshold_type: int = AF_CANNY_THRESHOLD_MANUAL,
+          low_threshold_ratio: float = 0.1, high_threshold_ratio: float = 0.2,
+          sobel_window: int = 3, is_fast: bool = False) -> Array:
+    """af_canny (include/af/image.h:1682; defaults of af::canny)."""
+    return _out_call(lib().af_canny, image.handle, threshold_type, low_threshold_ratio,
+                     high_threshold_ratio, sobel_window, is_fast)
+
+
 def unwrap(signal: Array, wx: int, wy: int, sx: int, sy: int, px: int = 0, py: int = 0,
            is_column: bool = True) -> Array:
     """af_unwrap: wx x wy patches at strides (sx, sy), zero padding (px, py)."""

@@ -56,6 +56,19 @@ SIGNATURES = [
     ("af_dog", af_err, [ctypes.POINTER(af_array), af_array, ctypes.c_int, ctypes.c_int]),
     ("af_sobel_operator", af_err, [ctypes.POINTER(af_array), ctypes.POINTER(af_array), af_array,
                                    ctypes.c_uint]),
+    ("af_harris", af_err, [ctypes.POINTER(_P), af_array, ctypes.c_uint, ctypes.c_float,
+                           ctypes.c_float, ctypes.c_uint, ctypes.c_float]),
+    ("af_create_features", af_err, [ctypes.POINTER(_P), dim_t]),
+    ("af_retain_features", af_err, [ctypes.POINTER(_P), _P]),
+    ("af_get_features_num", af_err, [ctypes.POINTER(dim_t), _P]),
+    ("af_get_features_xpos", af_err, [ctypes.POINTER(af_array), _P]),
+    ("af_get_features_ypos", af_err, [ctypes.POINTER(af_array), _P]),
+    ("af_get_features_score", af_err, [ctypes.POINTER(af_array), _P]),
+    ("af_get_features_orientation", af_err, [ctypes.POINTER(af_array), _P]),
+    ("af_get_features_size", af_err, [ctypes.POINTER(af_array), _P]),
+    ("af_release_features", af_err, [_P]),
+    ("af_canny", af_err, [ctypes.POINTER(af_array), af_array, ctypes.c_int, ctypes.c_float,
+                          ctypes.c_float, ctypes.c_uint, ctypes.c_bool]),
     ("af_unwrap", af_err, [ctypes.POINTER(af_array), af_array] + [dim_t] * 6 + [ctypes.c_bool]),
     ("af_wrap", af_err, [ctypes.POINTER(af_array), af_array] + [dim_t] * 8 + [ctypes.c_bool]),
     ("af_wrap_v2", af_err, [ctypes.POINTER(af_array), af_array] + [dim_t] * 8 + [ctypes.c_bool]),

@@ -31,6 +31,8 @@ SOURCES = [
     "unwrap_wrap.cu",
     "fft_conv.cu",
     "image_ops.cu",
+    "harris.cu",
+    "canny.cu",
 ]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -3,6 +3,8 @@
 // dispatch (src/api/c/convolve.cpp), routed to this library's sm_103a
 // kernels.  No CPU fallback: every path below launches device code.
 #include <algorithm>
+#include <array>
+#include <cmath>
 #include <cstring>
 #include <string>
 
@@ -427,6 +429,28 @@ static void wrap_impl(af_array *out, const af_array in, dim_t ox, dim_t oy, dim_
 
 }  // namespace afgb
 
+namespace afgb {
+namespace {
+struct FeaturesObj {
+    dim_t n = 0;
+    af_array x = nullptr, y = nullptr, score = nullptr, orientation = nullptr, size = nullptr;
+    std::array<af_array *, 5> slots() { return {&x, &y, &score, &orientation, &size}; }
+};
+
+FeaturesObj *get_features(af_features f) {
+    if (f == nullptr) AFGB_THROW(AF_ERR_ARG, "null af_features handle");
+    return static_cast<FeaturesObj *>(f);
+}
+
+void release_features_arrays(FeaturesObj *f) {
+    for (af_array *slot : f->slots()) {
+        if (*slot) af_release_array(*slot);
+        *slot = nullptr;
+    }
+}
+}  // namespace
+}  // namespace afgb
+
 using namespace afgb;
 
 extern "C" {
@@ -675,6 +699,144 @@ af_err af_wrap_v2(af_array *out, const af_array in, const dim_t ox, const dim_t 
     AFGB_TRY
     AFGB_ARG_ASSERT(0, out != nullptr);
     wrap_impl(out, in, ox, oy, wx, wy, sx, sy, px, py, is_column, *out == nullptr);
+    AFGB_CATCHALL
+}
+
+// ---- af_features (src/api/c/features.cpp:15-127): five f32 arrays and a
+// count; the getters hand out the object's own handles (not retained)
+af_err af_create_features(af_features *feat, dim_t num) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, feat != nullptr);
+    AFGB_ARG_ASSERT(1, num >= 0);
+    auto *f = new FeaturesObj();
+    f->n = num;
+    if (num > 0) {
+        const dim_t d[4] = {num, 1, 1, 1};
+        try {
+            for (af_array *slot : f->slots()) {
+                Array a = *create_array(f32, d);
+                *slot = make_handle(&a);
+            }
+        } catch (...) {
+            release_features_arrays(f);
+            delete f;
+            throw;
+        }
+    }
+    *feat = static_cast<af_features>(f);
+    AFGB_CATCHALL
+}
+
+af_err af_release_features(af_features feat) {
+    AFGB_TRY
+    FeaturesObj *f = get_features(feat);
+    release_features_arrays(f);
+    delete f;
+    AFGB_CATCHALL
+}
+
+af_err af_retain_features(af_features *out, const af_features feat) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    FeaturesObj *f = get_features(feat);
+    auto *o = new FeaturesObj();
+    o->n = f->n;
+    auto src = f->slots(), dst = o->slots();
+    for (size_t i = 0; i < src.size(); ++i) {
+        if (*src[i] == nullptr) continue;
+        const af_err e = af_retain_array(dst[i], *src[i]);
+        if (e != AF_SUCCESS) {
+            release_features_arrays(o);
+            delete o;
+            return e;
+        }
+    }
+    *out = static_cast<af_features>(o);
+    AFGB_CATCHALL
+}
+
+af_err af_get_features_num(dim_t *num, const af_features feat) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, num != nullptr);
+    *num = get_features(feat)->n;
+    AFGB_CATCHALL
+}
+
+#define AFGB_FEATURES_GETTER(NAME, FIELD)                      \
+    af_err NAME(af_array *out, const af_features feat) {       \
+        AFGB_TRY                                               \
+        AFGB_ARG_ASSERT(0, out != nullptr);                    \
+        *out = get_features(feat)->FIELD;                      \
+        AFGB_CATCHALL                                          \
+    }
+AFGB_FEATURES_GETTER(af_get_features_xpos, x)
+AFGB_FEATURES_GETTER(af_get_features_ypos, y)
+AFGB_FEATURES_GETTER(af_get_features_score, score)
+AFGB_FEATURES_GETTER(af_get_features_orientation, orientation)
+AFGB_FEATURES_GETTER(af_get_features_size, size)
+#undef AFGB_FEATURES_GETTER
+
+// af_harris (src/api/c/harris.cpp:42-95): window length block_size, else
+// floor(6 sigma) made odd; the reference's checks in its order; f32 and f64
+af_err af_harris(af_features *out, const af_array in, const unsigned max_corners,
+                 const float min_response, const float sigma, const unsigned block_size,
+                 const float k_thr) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    Array *a = get_array(in);
+    unsigned filter_len =
+        (block_size == 0) ? static_cast<unsigned>(std::floor(6.f * sigma)) : block_size;
+    if (block_size == 0 && filter_len % 2 == 0) filter_len--;
+    const unsigned edge = (block_size > 0) ? block_size / 2 : filter_len / 2;
+    AFGB_DIM_ASSERT(1, (a->ndims() == 2));
+    AFGB_ARG_ASSERT(1, (a->dims[0] >= (dim_t)(2 * edge + 1) ||
+                        a->dims[1] >= (dim_t)(2 * edge + 1)));
+    AFGB_ARG_ASSERT(3, (max_corners > 0) || (min_response > 0.0f));
+    AFGB_ARG_ASSERT(7, (k_thr >= 0.01f));
+    AFGB_ARG_ASSERT(4, (block_size > 2) || (sigma >= 0.5f && sigma <= 5.f));
+    AFGB_ARG_ASSERT(5, (block_size <= 32));
+    if (a->type != f32 && a->type != f64) AFGB_TYPE_ERROR(1, a->type);
+    HarrisOut r;
+    harris_corners(*a, max_corners, min_response, sigma, filter_len, k_thr, r);
+    if (r.n == 0) {
+        // the reference's empty result: x, y, score of dims (0,0,0,0),
+        // orientation and size of dims (0,1,1,1)
+        const dim_t e0[4] = {0, 0, 0, 0}, e1[4] = {0, 1, 1, 1};
+        r.x = *create_array(f32, e0);
+        r.y = *create_array(f32, e0);
+        r.score = *create_array(f32, e0);
+        r.orientation = *create_array(f32, e1);
+        r.size = *create_array(f32, e1);
+    }
+    auto *f = new FeaturesObj();
+    f->n = r.n;
+    f->x = make_handle(&r.x);
+    f->y = make_handle(&r.y);
+    f->score = make_handle(&r.score);
+    f->orientation = make_handle(&r.orientation);
+    f->size = make_handle(&r.size);
+    *out = static_cast<af_features>(f);
+    AFGB_CATCHALL
+}
+
+// af_canny (src/api/c/canny.cpp:232-285): the reference's checks in its
+// order; any threshold type but AUTO_OTSU is manual; b8 result
+af_err af_canny(af_array *out, const af_array in, const af_canny_threshold threshold_type,
+                const float low_threshold_ratio, const float high_threshold_ratio,
+                const unsigned sobel_window, const bool is_fast) {
+    AFGB_TRY
+    AFGB_ARG_ASSERT(0, out != nullptr);
+    Array *a = get_array(in);
+    AFGB_DIM_ASSERT(2, (a->ndims() >= 2));
+    AFGB_DIM_ASSERT(2, (a->dims[0] >= 5 && a->dims[1] >= 5));
+    AFGB_ARG_ASSERT(5, (sobel_window == 3));
+    switch (a->type) {
+        case f32: case f64: case s32: case u32: case s16: case u16: case s8: case u8: break;
+        default: AFGB_TYPE_ERROR(1, a->type);
+    }
+    Array r = canny_edges(*a, threshold_type == AF_CANNY_THRESHOLD_AUTO_OTSU, low_threshold_ratio,
+                          high_threshold_ratio, is_fast);
+    *out = make_handle(&r);
     AFGB_CATCHALL
 }
 

@@ -147,6 +147,13 @@ unsigned int tc_take_error();
 void check_device_errors();
 int device();
 bool exact_fp();
+// while one lives, exact_fp() is true on this thread (for callers whose
+// results feed discrete decisions, e.g. the corner detector's window sums,
+// which must round like the reference whatever the global setting)
+struct ExactScope {
+    ExactScope();
+    ~ExactScope();
+};
 int num_sms();
 void count_launch(unsigned n = 1);
 

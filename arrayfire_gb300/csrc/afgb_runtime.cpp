@@ -172,7 +172,12 @@ void check_device_errors() {
                                        std::to_string(w) + "); its results are invalid");
     }
 }
-bool exact_fp() { return g_exact.load() != 0; }
+namespace {
+thread_local int t_exact_depth = 0;
+}
+bool exact_fp() { return t_exact_depth > 0 || g_exact.load() != 0; }
+ExactScope::ExactScope() { ++t_exact_depth; }
+ExactScope::~ExactScope() { --t_exact_depth; }
 void count_launch(unsigned n) { g_launches += n; }
 
 // ---------------------------------------------------------------- memory

@@ -56,6 +56,17 @@ __device__ __forceinline__ float to_acc(uint32_t v, float) { return __uint2float
 __device__ __forceinline__ float to_acc(long long v, float) { return __ll2float_rn(v); }
 __device__ __forceinline__ float to_acc(unsigned long long v, float) { return __ull2float_rn(v); }
 
+// separately rounded arithmetic for floating types, plain for integers
+template <typename T> __device__ __forceinline__ T r_add(T a, T b) { return a + b; }
+template <typename T> __device__ __forceinline__ T r_sub(T a, T b) { return a - b; }
+template <typename T> __device__ __forceinline__ T r_mul(T a, T b) { return a * b; }
+template <> __device__ __forceinline__ float r_add(float a, float b) { return __fadd_rn(a, b); }
+template <> __device__ __forceinline__ float r_sub(float a, float b) { return __fsub_rn(a, b); }
+template <> __device__ __forceinline__ float r_mul(float a, float b) { return __fmul_rn(a, b); }
+template <> __device__ __forceinline__ double r_add(double a, double b) { return __dadd_rn(a, b); }
+template <> __device__ __forceinline__ double r_sub(double a, double b) { return __dsub_rn(a, b); }
+template <> __device__ __forceinline__ double r_mul(double a, double b) { return __dmul_rn(a, b); }
+
 // ---- accumulate one product: acc + fl(s*f), either exactly in the
 // reference's order (separate rounding of product and sum) or fused.
 template <bool EXACT>

@@ -43,6 +43,20 @@ Array gaussian_kernel(int rows, int cols, double sigma_r, double sigma_c);
 Array dog(const Array &in, int radius1, int radius2);
 void sobel_3x3(const Array &img, Array &dx, Array &dy);
 
+// af_harris (harris.cu): the corners of a 2-D f32/f64 image as dense f32
+// vectors of n elements -- x along dim1, y along dim0, score, orientation 0,
+// size 1 -- in the reference's order (src/backend/cpu/harris.cpp:28-144)
+struct HarrisOut {
+    long long n = 0;
+    Array x, y, score, orientation, size;
+};
+void harris_corners(const Array &img, unsigned max_corners, float min_response, float sigma,
+                    unsigned filter_len, float k_thr, HarrisOut &out);
+
+// af_canny (canny.cu): the 0/1 (b8) edge map of each 2-D slice, threshold
+// ratios manual or Otsu, L1 or L2 gradient magnitude (src/api/c/canny.cpp)
+Array canny_edges(const Array &img, bool otsu, float t1, float t2, bool is_fast);
+
 // out = T( s * (c * r) ) element-wise: the scalar-filter shortcut of
 // af_convolve2_sep (src/api/c/convolve.cpp:57-68).
 void launch_sep_scalar(const Array &sig, const Array &cfilt, const Array &rfilt, Array &out);

@@ -64,17 +64,6 @@ __global__ void gaussian_kernel_kernel(float *out, int rows, int cols, float rc,
     for (long long t = threadIdx.x; t < n; t += blockDim.x) out[t] = __fdiv_rn(out[t], norm);
 }
 
-// separately rounded arithmetic for floating types, plain for integers
-template <typename T> __device__ __forceinline__ T r_add(T a, T b) { return a + b; }
-template <typename T> __device__ __forceinline__ T r_sub(T a, T b) { return a - b; }
-template <typename T> __device__ __forceinline__ T r_mul(T a, T b) { return a * b; }
-template <> __device__ __forceinline__ float r_add(float a, float b) { return __fadd_rn(a, b); }
-template <> __device__ __forceinline__ float r_sub(float a, float b) { return __fsub_rn(a, b); }
-template <> __device__ __forceinline__ float r_mul(float a, float b) { return __fmul_rn(a, b); }
-template <> __device__ __forceinline__ double r_add(double a, double b) { return __dadd_rn(a, b); }
-template <> __device__ __forceinline__ double r_sub(double a, double b) { return __dsub_rn(a, b); }
-template <> __device__ __forceinline__ double r_mul(double a, double b) { return __dmul_rn(a, b); }
-
 // reflect-101 index |end - |end - idx|| (sobel.hpp:26-28); a size-1 dim
 // reflects onto its only element
 __device__ __forceinline__ long long reflect101(long long idx, long long end) {

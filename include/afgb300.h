@@ -34,6 +34,7 @@ extern "C" {
 
 typedef long long dim_t;  /* include/af/defines.h:50 (64-bit dim_t) */
 typedef void *af_array;   /* include/af/defines.h:243 */
+typedef void *af_features; /* include/af/features.h:13 */
 
 /* include/af/defines.h:75-202 — numeric values identical */
 typedef enum {
@@ -182,6 +183,58 @@ AFGB_API af_err af_dog(af_array *out, const af_array in, const int radius1, cons
  * with reflect-101 borders; ker_size must be 3. */
 AFGB_API af_err af_sobel_operator(af_array *dx, af_array *dy, const af_array img,
                                   const unsigned ker_size);
+
+/* ---- corner detection on the separable window (af_harris) and the
+ * af_features object it returns ------------------------------------------ */
+
+/* include/af/vision.h:402 (src/api/c/harris.cpp:42-95, CPU backend
+ * src/backend/cpu/harris.cpp:28-144): Harris corners of a 2-D f32/f64 image.
+ * Window length block_size, else floor(6 sigma) made odd: a box when
+ * sigma < 0.5, else a Gaussian.  Responses det - k_thr tr^2, strict
+ * 8-neighbour maxima of at least (unsigned)min_response (0 when
+ * max_corners > 0) in column-major scan order, at most 20% of the pixels;
+ * with max_corners > 0 the max_corners strongest (stable descending sort).
+ * Feature x is the dim1 index, y the dim0 index; orientation 0, size 1.
+ * Checks: 2-D input; d0 or d1 >= the window; max_corners > 0 or
+ * min_response > 0; k_thr >= 0.01; block_size > 2 or sigma in [0.5, 5];
+ * block_size <= 32. */
+AFGB_API af_err af_harris(af_features *out, const af_array in, const unsigned max_corners,
+                          const float min_response, const float sigma,
+                          const unsigned block_size, const float k_thr);
+/* include/af/features.h:92-154 (src/api/c/features.cpp:15-127): num > 0 gives
+ * five uninitialised f32 arrays of num elements; the getters return the
+ * object's own handles (not retained; released with the object). */
+AFGB_API af_err af_create_features(af_features *feat, dim_t num);
+AFGB_API af_err af_retain_features(af_features *out, const af_features feat);
+AFGB_API af_err af_get_features_num(dim_t *num, const af_features feat);
+AFGB_API af_err af_get_features_xpos(af_array *out, const af_features feat);
+AFGB_API af_err af_get_features_ypos(af_array *out, const af_features feat);
+AFGB_API af_err af_get_features_score(af_array *score, const af_features feat);
+AFGB_API af_err af_get_features_orientation(af_array *orientation, const af_features feat);
+AFGB_API af_err af_get_features_size(af_array *size, const af_features feat);
+AFGB_API af_err af_release_features(af_features feat);
+
+/* include/af/defines.h:486-489 */
+typedef enum {
+    AF_CANNY_THRESHOLD_MANUAL = 0,
+    AF_CANNY_THRESHOLD_AUTO_OTSU = 1
+} af_canny_threshold;
+
+/* include/af/image.h:1682 (src/api/c/canny.cpp:232-285, CPU kernels
+ * src/backend/cpu/kernel/canny.hpp): the b8 edge map (0/1) of each 2-D slice
+ * (stacked along dim2): the image in float smoothed by the reference's 5-tap
+ * separable filter, 3x3 Sobel derivatives, |gx| + |gy| (is_fast) or
+ * sqrt(gx^2 + gy^2), non-maximum suppression, thresholds -- manual: ratios of
+ * (s - min) / (max - min); AUTO_OTSU: the Otsu split T2 of a floor(max)-bin
+ * histogram per slice and T1 = low_threshold_ratio * T2 -- and hysteresis.
+ * Checks: at least 2-D, d0 and d1 >= 5, sobel_window == 3; f32, f64, s32,
+ * u32, s16, u16, s8, u8.  AUTO_OTSU with a gradient maximum below 2 returns
+ * AF_ERR_NOT_SUPPORTED (the reference's histogram then indexes outside its
+ * arrays). */
+AFGB_API af_err af_canny(af_array *out, const af_array in,
+                         const af_canny_threshold threshold_type,
+                         const float low_threshold_ratio, const float high_threshold_ratio,
+                         const unsigned sobel_window, const bool is_fast);
 
 /* ---- patch extraction and accumulation (the NN path's unwrap / wrap as
  * public calls; dilation 1) ----------------------------------------------- */

@@ -487,6 +487,167 @@ def harris(img: np.ndarray, dtype: int, max_corners: int, min_response: float, s
 
 
 # ---------------------------------------------------------------------------
+# af_canny (src/api/c/canny.cpp:196-285; CPU kernels src/backend/cpu/kernel/canny.hpp)
+# ---------------------------------------------------------------------------
+CANNY_TYPES = (F32, F64, S32, U32, S16, U16, S8, U8)
+CANNY_TAPS = np.array([-0.11021, -0.23691, -0.30576, -0.23691, -0.11021], np.float32)
+
+
+def canny_nms(mag, gx, gy):
+    """kernel::nonMaxSuppression (src/backend/cpu/kernel/canny.hpp:18-116) on
+    (d0, d1) float32 planes: interior pixels only; the magnitude interpolated
+    along the gradient, each operation rounded separately."""
+    d0, d1 = mag.shape
+    out = np.zeros_like(mag)
+    if d0 < 3 or d1 < 3:
+        return out
+    c = mag[1:-1, 1:-1]
+    se, nw = mag[2:, 2:], mag[:-2, :-2]        # offset +d0+1, -d0-1
+    ea, we = mag[2:, 1:-1], mag[:-2, 1:-1]     # offset +1, -1
+    ne, sw = mag[2:, :-2], mag[:-2, 2:]        # offset -d0+1, +d0-1
+    no, so = mag[1:-1, :-2], mag[1:-1, 2:]     # offset -d0, +d0
+    dx, dy = gx[1:-1, 1:-1], gy[1:-1, 1:-1]
+    with np.errstate(all="ignore"):
+        px, py = dx >= 0, dy >= 0
+        g1 = (dx - dy) >= 0          # dx >= 0, dy >= 0
+        g2 = (dx + dy) >= 0          # mixed signs
+        g4 = (-dx + dy) >= 0         # dx < 0, dy < 0
+        q1 = px & py
+        q2 = px & ~py
+        q3 = ~px & py
+        q4 = ~px & ~py
+        a1 = np.select([q1, q2, q3, q4], [np.where(g1, ea, so), np.where(g2, ea, no),
+                                          np.where(g2, so, we), np.where(g4, we, no)])
+        a2 = np.select([q1, q2, q3, q4], [np.where(g1, we, no), np.where(g2, we, so),
+                                          np.where(g2, no, ea), np.where(g4, ea, so)])
+        b1 = np.select([q1, q2, q3, q4], [se, ne, sw, nw])
+        b2 = np.select([q1, q2, q3, q4], [nw, sw, ne, se])
+        al = np.select([q1, q2, q3, q4], [np.where(g1, dy / dx, dx / dy),
+                                          np.where(g2, -dy / dx, dx / -dy),
+                                          np.where(g2, -dx / dy, dy / -dx),
+                                          np.where(g4, dy / dx, dx / dy)]).astype(np.float32)
+        one = np.float32(1.0)
+        m1 = (one - al) * a1 + al * b1
+        m2 = (one - al) * a2 + al * b2
+        keep = (c != 0) & (c > m1) & (c > m2)
+    out[1:-1, 1:-1] = np.where(keep, c, np.float32(0))
+    return out
+
+
+def canny_hysteresis(strong, weak):
+    """kernel::edgeTrackingHysteresis (src/backend/cpu/kernel/canny.hpp:148-182)
+    on one (d0, d1) slice: seeds are strong pixels at linear indices
+    [d0+1, d0 + (d0-1)(d1-1)] (the reference's scan, whose index advances one
+    less than a column per column); from each, weak pixels are followed
+    through the 8 linear-offset neighbours (t +- 1, t +- d0, t +- d0 +- 1).
+    Neighbours outside the slice, which the reference would read out of
+    bounds, are skipped."""
+    from collections import deque
+    d0, d1 = strong.shape
+    n = d0 * d1
+    s = strong.ravel(order="F") > 0
+    w = weak.ravel(order="F") > 0
+    out = np.zeros(n, np.int8)
+    lo, hi = d0 + 1, d0 + (d0 - 1) * (d1 - 1)
+    offs = (-d0 - 1, -d0, -d0 + 1, -1, 1, d0 - 1, d0, d0 + 1)
+    for t in np.flatnonzero(s[lo:hi + 1]) + lo:
+        if out[t] == 1:
+            continue
+        out[t] = 1
+        q = deque([int(t)])
+        while q:
+            u = q.popleft()
+            for o in offs:
+                v = u + o
+                if 0 <= v < n and w[v] and out[v] != 1:
+                    out[v] = 1
+                    q.append(v)
+    return out.reshape((d0, d1), order="F")
+
+
+def canny(img: np.ndarray, dtype: int, otsu: bool, t1: float, t2: float, is_fast: bool,
+          which: str = "port") -> np.ndarray:
+    """af_canny, sobel window 3, on 2-D slices stacked along dim2: returns an
+    int8 (d0, d1, d2) array of 0/1 edges.
+
+    Port of cannyHelper (src/api/c/canny.cpp:205-230): the image cast to
+    float, the 5-tap separable smoothing (this oracle's convolve2_sep), the
+    Sobel derivatives (this oracle's sobel), |gx| + |gy| or
+    sqrt(gx^2 + gy^2), non-maximum suppression, then computeCandidates
+    (canny.cpp:153-190): manual thresholds on (s - min) / (max - min), or the
+    Otsu threshold of a (max)-bin histogram per slice (otsuThreshold,
+    canny.cpp:81-141, every float operation in its order), and hysteresis."""
+    a = as_af(img, NP_OF[dtype])
+    d = _dims4(a)
+    if which == "ref":
+        out = np.zeros(d, np.int8, order="F")
+        rc = lib("ref").ref_canny(ctypes.c_int(dtype), a.ctypes.data_as(_P), _ll(d),
+                                  ctypes.c_int(1 if otsu else 0), ctypes.c_float(t1),
+                                  ctypes.c_float(t2), ctypes.c_int(1 if is_fast else 0),
+                                  out.ctypes.data_as(_P))
+        if rc != 0:
+            raise RuntimeError(f"ref_canny failed ({rc})")
+        return out[:, :, :, 0]
+    x = np.asfortranarray(a.astype(np.float32))
+    smt = convolve2_sep(x, CANNY_TAPS, CANNY_TAPS, F32, False)
+    gx, gy = sobel(smt, F32)
+    if is_fast:
+        mag = np.abs(gx) + np.abs(gy)
+    else:
+        mag = np.sqrt(gx * gx + gy * gy)
+    d0, d1, d2 = d[0], d[1], d[2]
+    sup = np.zeros((d0, d1, d2), np.float32, order="F")
+    for z in range(d2):
+        sup[:, :, z] = canny_nms(mag[:, :, z, 0], gx[:, :, z, 0], gy[:, :, z, 0])
+    max_v = np.float32(sup.max())
+    if otsu:
+        nb = int(max_v)
+        if nb < 2:
+            raise ValueError("the Otsu threshold needs at least two bins")
+        step = np.float32(float(max_v) / float(np.float32(nb)))
+        total = np.float32(d0 * d1)
+        weak = np.zeros_like(sup, dtype=bool)
+        strong = np.zeros_like(sup, dtype=bool)
+        for z in range(d2):
+            v = sup[:, :, z].ravel(order="F")
+            with np.errstate(all="ignore"):
+                bins = np.clip(((v - np.float32(0)) / step).astype(np.int64), 0, nb - 1)
+            hist = np.bincount(bins, minlength=nb)
+            freqs = hist.astype(np.float32) / total
+            cum = np.add.accumulate(freqs, dtype=np.float32)
+            prod = np.arange(nb, dtype=np.float32) * freqs
+            cprod = np.add.accumulate(prod, dtype=np.float32)
+            ws = cprod[-1]
+            best, loc = np.float32(0), 0
+            with np.errstate(all="ignore"):
+                qL = cum[:-1]
+                qH = np.float32(1) - qL
+                muL = cprod[:-1] / qL
+                muH = (ws - cprod[:-1]) / qH
+                diff = muL - muH
+                sig = (diff * diff) * (cum[:-1] * (np.float32(1) - cum[:-1]))
+            for b in range(nb - 1):  # ireduce<af_max_t>: first maximum, NaN skipped
+                if b == 0:
+                    best = np.float32(-np.inf) if np.isnan(sig[0]) else sig[0]
+                elif sig[b] > best:
+                    best, loc = sig[b], b
+            T2 = np.float32(loc)
+            T1 = T2 * np.float32(t1)
+            weak[:, :, z] = (sup[:, :, z] >= T1) & (sup[:, :, z] < T2)
+            strong[:, :, z] = sup[:, :, z] >= T2
+    else:
+        min_v = np.float32(sup.min())
+        with np.errstate(all="ignore"):
+            g = (sup - min_v) / np.float32(max_v - min_v)
+        weak = (g >= np.float32(t1)) & (g < np.float32(t2))
+        strong = g >= np.float32(t2)
+    out = np.zeros((d0, d1, d2), np.int8, order="F")
+    for z in range(d2):
+        out[:, :, z] = canny_hysteresis(strong[:, :, z], weak[:, :, z])
+    return out
+
+
+# ---------------------------------------------------------------------------
 # af_unwrap / af_wrap (public form: dilation 1, is_column, every type)
 # ---------------------------------------------------------------------------
 def patch_grid(W, H, wx, wy, sx, sy, px, py):

@@ -29,9 +29,23 @@
  *                           kernel::non_maximal (cpu/kernel/harris.hpp), and the
  *                           stable descending sort + keep_corners of the
  *                           max_corners > 0 case (cpu/kernel/sort_by_key_impl.hpp)
+ *   ref_canny            -> the edge pipeline of src/api/c/canny.cpp:205-230:
+ *                           the 5-tap separable smoothing (kernel::convolve2),
+ *                           kernel::derivative (Sobel), the gradient magnitude,
+ *                           kernel::nonMaxSuppression, the manual or Otsu
+ *                           thresholds (kernel::histogram; the array
+ *                           arithmetic of canny.cpp:85-190 restated as loops in
+ *                           its order), kernel::edgeTrackingHysteresis
+ *                           (cpu/kernel/canny.hpp)
  */
+#include <kernel/canny.hpp>
 #include <kernel/convolve.hpp>
 #include <kernel/gradient.hpp>
+// kernel/histogram.hpp names dim4 unqualified, as its own includer
+// (src/backend/cpu/histogram.cpp) arranges
+#include <af/dim4.hpp>
+using af::dim4;
+#include <kernel/histogram.hpp>
 #include <kernel/harris.hpp>
 #include <kernel/sobel.hpp>
 #include <kernel/sort_helper.hpp>
@@ -40,6 +54,8 @@
 #include <kernel/wrap.hpp>
 
 #include <algorithm>
+#include <cmath>
+#include <limits>
 #include <complex>
 #include <utility>
 #include <cstring>
@@ -341,5 +357,125 @@ int ref_harris(int dtype, const void *in, long long d0, long long d1, unsigned m
         return harris_any<double>(static_cast<const double *>(in), d0, d1, max_corners,
                                   min_response, sigma, filter_len, k_thr, xo, yo, ro, cap);
     return -2;
+}
+}  // extern "C"
+
+namespace {
+// the array operations of src/api/c/canny.cpp around the reference's CPU
+// kernels, on one or more 2-D slices stacked along dim2 (dims[3] == 1)
+template <typename T>
+int canny_any(const T *in, const long long *dims, int otsu, float t1, float t2, int isf,
+              char *out) {
+    const long long d0 = dims[0], d1 = dims[1], d2 = dims[2];
+    if (dims[3] != 1) return -3;
+    const long long n = d0 * d1 * d2;
+    const dim4 id(d0, d1, d2, 1), st(1, d0, d0 * d1, d0 * d1 * d2);
+    std::vector<float> x(n), t(n), smt(n), gx(n), gy(n), mag(n), sup(n, 0.f);
+    for (long long i = 0; i < n; ++i) x[i] = static_cast<float>(in[i]);  // cast<float, T>
+    static const float v[5] = {-0.11021f, -0.23691f, -0.30576f, -0.23691f, -0.11021f};
+    CParam<float> cf(v, dim4(5, 1, 1, 1), dim4(1, 5, 5, 5));
+    CParam<float> rf(v, dim4(1, 5, 1, 1), dim4(1, 1, 5, 5));
+    K::convolve2<float, float, false>(Param<float>(smt.data(), id, st),
+                                      CParam<float>(x.data(), id, st), cf, rf,
+                                      Param<float>(t.data(), id, st));
+    K::derivative<float, float, true>(Param<float>(gx.data(), id, st),
+                                      CParam<float>(smt.data(), id, st));
+    K::derivative<float, float, false>(Param<float>(gy.data(), id, st),
+                                       CParam<float>(smt.data(), id, st));
+    for (long long i = 0; i < n; ++i) {  // gradientMagnitude (canny.cpp:66-79)
+        if (isf) {
+            mag[i] = std::abs(gx[i]) + std::abs(gy[i]);
+        } else {
+            const float a = gx[i] * gx[i], b = gy[i] * gy[i];
+            const float sg = a + b;
+            mag[i] = std::sqrt(sg);
+        }
+    }
+    K::nonMaxSuppression<float>(Param<float>(sup.data(), id, st),
+                                CParam<float>(mag.data(), id, st),
+                                CParam<float>(gx.data(), id, st), CParam<float>(gy.data(), id, st));
+    // computeCandidates (canny.cpp:153-190)
+    float maxVal = -std::numeric_limits<float>::infinity();
+    for (long long i = 0; i < n; ++i) maxVal = std::max(sup[i], maxVal);
+    std::vector<char> strong(n), weak(n);
+    if (otsu) {
+        const unsigned NB = static_cast<unsigned>(maxVal);
+        if (NB < 2) return -4;  // the reference's Otsu loop needs two bins
+        std::vector<unsigned> hist((size_t)NB * d2, 0u);
+        K::histogram<float, true>(
+            Param<unsigned>(hist.data(), dim4(NB, 1, d2, 1), dim4(1, NB, NB, NB * d2)),
+            CParam<float>(sup.data(), id, st), NB, 0.0, maxVal);
+        const float total = static_cast<float>(d0 * d1);
+        for (long long z = 0; z < d2; ++z) {
+            const unsigned *h = hist.data() + z * NB;
+            std::vector<float> freqs(NB), cum(NB), prod(NB), cprod(NB), qlqh(NB);
+            float c = 0.f, cp = 0.f, ws = 0.f;
+            for (unsigned b = 0; b < NB; ++b) {
+                freqs[b] = static_cast<float>(h[b]) / total;
+                c = freqs[b] + c;  // scan: in + running
+                cum[b] = c;
+                qlqh[b] = cum[b] * (1.0f - cum[b]);
+                prod[b] = static_cast<float>(b) * freqs[b];
+                cp = prod[b] + cp;
+                cprod[b] = cp;
+                ws = prod[b] + ws;  // reduce: in + running
+            }
+            float best = 0.f;
+            unsigned loc = 0;
+            for (unsigned b = 0; b + 1 < NB; ++b) {
+                const float qL = cum[b];
+                const float qH = 1.0f - qL;
+                const float muL = cprod[b] / qL;
+                const float muH = (ws - cprod[b]) / qH;
+                const float diff = muL - muH;
+                const float sigma = (diff * diff) * qlqh[b];
+                // ireduce<af_max_t> (cpu/kernel/ireduce.hpp:47-63)
+                if (b == 0) {
+                    best = std::isnan(sigma) ? -std::numeric_limits<float>::infinity() : sigma;
+                    loc = 0;
+                } else if (sigma > best) {
+                    best = sigma;
+                    loc = b;
+                }
+            }
+            const float T2 = static_cast<float>(loc);
+            const float T1 = T2 * t1;
+            for (long long i = z * d0 * d1; i < (z + 1) * d0 * d1; ++i) {
+                weak[i] = (sup[i] >= T1) && (sup[i] < T2);
+                strong[i] = sup[i] >= T2;
+            }
+        }
+    } else {
+        float minVal = std::numeric_limits<float>::infinity();
+        for (long long i = 0; i < n; ++i) minVal = std::min(sup[i], minVal);
+        const float denom = maxVal - minVal;
+        for (long long i = 0; i < n; ++i) {
+            const float g = (sup[i] - minVal) / denom;
+            weak[i] = (g >= t1) && (g < t2);
+            strong[i] = g >= t2;
+        }
+    }
+    std::fill(out, out + n, (char)0);
+    K::edgeTrackingHysteresis<char>(Param<char>(out, id, st), CParam<char>(strong.data(), id, st),
+                                    CParam<char>(weak.data(), id, st));
+    return 0;
+}
+}  // namespace
+
+extern "C" {
+// af_canny: dtype numbering of include/af/defines.h; out holds 0/1 bytes
+int ref_canny(int dtype, const void *in, const long long *dims, int otsu, float t1, float t2,
+              int isf, char *out) {
+    switch (dtype) {
+        case 0: return canny_any<float>(static_cast<const float *>(in), dims, otsu, t1, t2, isf, out);
+        case 2: return canny_any<double>(static_cast<const double *>(in), dims, otsu, t1, t2, isf, out);
+        case 5: return canny_any<int>(static_cast<const int *>(in), dims, otsu, t1, t2, isf, out);
+        case 6: return canny_any<unsigned>(static_cast<const unsigned *>(in), dims, otsu, t1, t2, isf, out);
+        case 10: return canny_any<short>(static_cast<const short *>(in), dims, otsu, t1, t2, isf, out);
+        case 11: return canny_any<unsigned short>(static_cast<const unsigned short *>(in), dims, otsu, t1, t2, isf, out);
+        case 13: return canny_any<signed char>(static_cast<const signed char *>(in), dims, otsu, t1, t2, isf, out);
+        case 7: return canny_any<unsigned char>(static_cast<const unsigned char *>(in), dims, otsu, t1, t2, isf, out);
+        default: return -2;
+    }
 }
 }  // extern "C"

@@ -314,3 +314,94 @@ def sobel_input(dt: int, shape, seed: int) -> np.ndarray:
     if dt in (F32, F64):
         x = (x * 10).astype(x.dtype)
     return np.asfortranarray(x)
+
+
+# ---------------------------------------------------------------------------
+# af_harris: (id, dtype, (d0, d1), max_corners, min_response, sigma,
+# block_size, k_thr, image kind, seed).  "blocks" are bright rectangles on
+# a dark ground plus faint noise, scaled to [0, 255]; "tiles" repeat one
+# random 12x12 tile exactly, so many corners tie on score (the sort's
+# stability decides their order); "noise" is smoothed random texture.
+# ---------------------------------------------------------------------------
+def harris_cases():
+    base = [
+        ("mc500_default", (64, 48), 500, 1e5, 1.0, 0, 0.04, "blocks"),
+        ("mc20_sorted", (100, 80), 20, 0.0, 1.0, 0, 0.04, "blocks"),
+        ("minresp_sigma2", (97, 131), 0, 1000.0, 2.0, 0, 0.06, "blocks"),
+        ("box5_sorted", (64, 64), 10, 0.0, 0.3, 5, 0.04, "blocks"),
+        ("block7_gauss", (120, 90), 0, 50.0, 1.5, 7, 0.05, "blocks"),
+        ("sigma5_len29", (160, 150), 10, 0.0, 5.0, 0, 0.04, "noise"),
+        ("block32_box", (180, 140), 0, 10.0, 0.2, 32, 0.04, "noise"),
+        ("ties_sorted", (120, 96), 25, 0.0, 1.0, 0, 0.04, "tiles"),
+        ("ties_all", (96, 120), 0, 1.0, 1.0, 3, 0.04, "tiles"),
+        ("one_interior_px", (9, 9), 10, 0.0, 1.0, 0, 0.04, "noise"),
+        ("too_narrow", (8, 40), 10, 0.0, 1.0, 0, 0.04, "noise"),
+        ("noise_many", (257, 190), 0, 0.5, 1.0, 0, 0.04, "noise"),
+    ]
+    out = []
+    seed = 40000
+    for name, shape, mc, mr, sg, bs, k, kind in base:
+        for dt in (F32, F64):
+            seed += 1
+            out.append((f"harris_{name}_{DT_NAME[dt]}", dt, shape, mc, mr, sg, bs, k, kind, seed))
+    return out
+
+
+def harris_image(dt: int, shape, kind: str, seed: int) -> np.ndarray:
+    g = rng(seed)
+    d0, d1 = shape
+    if kind == "tiles":
+        tile = g.random((12, 12)) * 255.0
+        a = np.tile(tile, (d0 // 12 + 1, d1 // 12 + 1))[:d0, :d1]
+    elif kind == "noise":
+        a = g.random((d0 + 4, d1 + 4))
+        a = (a[:-4, :-4] + a[2:-2, 2:-2] + a[4:, 4:] + a[4:, :-4]) * 64.0
+    else:
+        y, x = np.mgrid[0:d0, 0:d1]
+        a = np.zeros((d0, d1))
+        for _ in range(20):
+            cy, cx = g.uniform(0, d0), g.uniform(0, d1)
+            w = g.uniform(3, 12)
+            a += ((np.abs(y - cy) < w) & (np.abs(x - cx) < w * 1.3)) * g.uniform(0.3, 1.0)
+        a = a * 200.0 + 5.0 * g.standard_normal((d0, d1))
+    return np.asfortranarray(a.astype(NP_OF[dt]))
+
+
+# ---------------------------------------------------------------------------
+# af_canny: (id, dtype, dims, otsu, low ratio, high ratio, is_fast, image
+# kind, seed).  Images as for Harris; integer types get the image clipped to
+# their range.  "wide" shapes (d1 > d0 + 3) exercise the reference's seed
+# scan, which stops before the last columns.
+# ---------------------------------------------------------------------------
+CANNY_TYPES = (F32, F64, S32, U32, S16, U16, S8, U8)
+
+
+def canny_cases():
+    base = [
+        ("manual_l2", (64, 48), False, 0.1, 0.3, False, "blocks"),
+        ("otsu_l2", (100, 80), True, 0.4, 0.0, False, "blocks"),
+        ("manual_l1_wide", (97, 131), False, 0.05, 0.2, True, "noise"),
+        ("otsu_l1_tiles", (120, 90), True, 0.3, 0.0, True, "tiles"),
+        ("manual_batch3", (60, 60, 3), False, 0.1, 0.25, False, "blocks"),
+        ("manual_very_wide", (40, 150), False, 0.08, 0.3, False, "blocks"),
+        ("otsu_batch2", (70, 64, 2), True, 0.5, 0.0, False, "blocks"),
+        ("smallest_5x5", (5, 5), False, 0.1, 0.2, False, "noise"),
+    ]
+    out = []
+    seed = 50000
+    for name, shape, otsu, t1, t2, isf, kind in base:
+        for dt in CANNY_TYPES:
+            seed += 1
+            out.append((f"canny_{name}_{DT_NAME[dt]}", dt, shape, otsu, t1, t2, isf, kind, seed))
+    return out
+
+
+def canny_image(dt: int, shape, kind: str, seed: int) -> np.ndarray:
+    planes = [harris_image(F64, shape[:2], kind, seed + 1000 * z)
+              for z in range(shape[2] if len(shape) > 2 else 1)]
+    a = np.stack(planes, axis=2) if len(planes) > 1 else planes[0]
+    if dt == S8:
+        a = np.clip(a * 0.5, -128, 127)
+    elif dt not in (F32, F64):
+        a = np.clip(a, 0, 255)
+    return np.asfortranarray(a.astype(NP_OF[dt]))

@@ -16,6 +16,11 @@ Writes, next to this file:
                image, for every tests/golden/cases.py:patch_cases case;
   image.json   SHA-256 of the reference's Sobel derivatives (dx, dy) for every
                tests/golden/cases.py:sobel_cases case;
+  harris.json  the count and SHA-256 of x, y and score of the reference's
+               Harris corners for every tests/golden/cases.py:harris_cases
+               case (its CPU kernels composed as its CPU backend does);
+  canny.json   the edge count and SHA-256 of the reference's Canny edge map
+               for every tests/golden/cases.py:canny_cases case;
   nn.npz       FP64 NN forward / data-gradient / filter-gradient outputs for
                NN_CASES, each cross-checked against the reference's own
                unwrap + GEMM (forward, filter gradient) and wrap_dilated
@@ -87,6 +92,39 @@ def images() -> None:
         gold[cid] = {"dx": digest(rx), "dy": digest(ry)}
     (HERE / "image.json").write_text(json.dumps(gold, indent=0, sort_keys=True))
     print(f"image {len(gold)}")
+
+
+def harris() -> None:
+    """af_harris corners (count, x, y, score) from the reference's CPU
+    kernels composed as src/backend/cpu/harris.cpp does, with the numpy port
+    asserted bit-identical on every case."""
+    gold = {}
+    for cid, dt, shape, mc, mr, sg, bs, k, kind, seed in C.harris_cases():
+        img = C.harris_image(dt, shape, kind, seed)
+        ref = O.harris(img, dt, mc, mr, sg, bs, k, which="ref")
+        port = O.harris(img, dt, mc, mr, sg, bs, k, which="port")
+        if any(a.tobytes() != b.tobytes() for a, b in zip(ref, port)):
+            raise SystemExit(f"port differs from reference on {cid}")
+        gold[cid] = {"n": int(ref[0].size), "x": digest(ref[0]), "y": digest(ref[1]),
+                     "score": digest(ref[2])}
+    (HERE / "harris.json").write_text(json.dumps(gold, indent=0, sort_keys=True))
+    print(f"harris {len(gold)}")
+
+
+def canny() -> None:
+    """af_canny edge maps from the reference's CPU kernels composed as
+    src/api/c/canny.cpp does, with the numpy port asserted bit-identical on
+    every case."""
+    gold = {}
+    for cid, dt, shape, otsu, t1, t2, isf, kind, seed in C.canny_cases():
+        img = C.canny_image(dt, shape, kind, seed)
+        ref = O.canny(img, dt, otsu, t1, t2, isf, which="ref")
+        port = O.canny(img, dt, otsu, t1, t2, isf)
+        if ref.tobytes(order="F") != port.tobytes(order="F"):
+            raise SystemExit(f"port differs from reference on {cid}")
+        gold[cid] = {"edges": int(ref.sum()), "digest": digest(ref)}
+    (HERE / "canny.json").write_text(json.dumps(gold, indent=0, sort_keys=True))
+    print(f"canny {len(gold)}")
 
 
 def main() -> None:
@@ -170,7 +208,7 @@ def main() -> None:
 
 
 if __name__ == "__main__":
-    parts = {"patches": patches, "images": images}
+    parts = {"patches": patches, "images": images, "harris": harris, "canny": canny}
     if sys.argv[1:] and all(a in parts for a in sys.argv[1:]):
         if O.build_ref() is None:
             raise SystemExit("reference source tree not found; golden vectors need it")
@@ -180,3 +218,5 @@ if __name__ == "__main__":
         main()
         patches()
         images()
+        harris()
+        canny()
