@@ -523,6 +523,7 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
         res["nn_workloads"] = run_nn_workloads(af, O, args, flush)
     if not args.no_secondary:
         res["secondary"] = run_direct_workloads(af, O, peaks, args)
+        res["image_callers"] = run_image_callers(af, O, args)
         res["cnn4"] = run_cnn(af, args)
     return res
 
@@ -970,6 +971,76 @@ def run_direct_workloads(af, O, peaks, args) -> dict:
 # ---------------------------------------------------------------------------
 # CPU baseline: the reference's algorithm on the host cores
 # ---------------------------------------------------------------------------
+def _blocks_image(shape, seed, dtype=np.float32) -> np.ndarray:
+    """Bright rectangles on a dark ground plus faint noise, in [0, ~255]."""
+    g = np.random.Generator(np.random.Philox(seed))
+    d0, d1 = shape
+    a = np.zeros((d0, d1), np.float32)
+    for _ in range(400):
+        cy, cx = g.uniform(0, d0), g.uniform(0, d1)
+        w = g.uniform(4, 40)
+        a[max(0, int(cy - w)):int(cy + w), max(0, int(cx - 1.3 * w)):int(cx + 1.3 * w)] += \
+            np.float32(g.uniform(0.3, 1.0))
+    a = a * 200.0 + 5.0 * g.standard_normal((d0, d1), dtype=np.float32)
+    if dtype == np.uint8:
+        a = np.clip(a, 0, 255)
+    return np.asfortranarray(a.astype(dtype))
+
+
+def run_image_callers(af, O, args) -> dict:
+    """af_harris and af_canny on 2048 x 2048 images through the C ABI: ms per
+    call with the image resident on the device (each call reads its corner
+    count or gradient range back to the host, as the reference does),
+    megapixels per second, the result checked bit for bit against the oracle,
+    and the oracle port's time on the same image on one host thread."""
+    import torch
+
+    flush = make_flush()
+    steps = max(3, min(args.steps, 10))
+    out = {}
+    cases = [
+        ("harris_2048x2048_f32_max500", np.float32, O.F32,
+         lambda A: af.harris(A, 500, 1e5, 1.0, 0, 0.04),
+         lambda img: O.harris(img, O.F32, 500, 1e5, 1.0, 0, 0.04)),
+        ("harris_2048x2048_f32_minresp", np.float32, O.F32,
+         lambda A: af.harris(A, 0, 1e6, 1.0, 0, 0.04),
+         lambda img: O.harris(img, O.F32, 0, 1e6, 1.0, 0, 0.04)),
+        ("canny_2048x2048_f32_manual", np.float32, O.F32,
+         lambda A: af.canny(A, 0, 0.1, 0.3, 3, False),
+         lambda img: O.canny(img, O.F32, False, 0.1, 0.3, False)),
+        ("canny_2048x2048_u8_otsu", np.uint8, O.U8,
+         lambda A: af.canny(A, 1, 0.4, 0.0, 3, False),
+         lambda img: O.canny(img, O.U8, True, 0.4, 0.0, False)),
+    ]
+    for name, npt, dt, call, oracle_call in cases:
+        img = _blocks_image((2048, 2048), 61, npt)
+        A = af.Array.from_numpy(img)
+        times = _timed(lambda: call(A), steps, 3, flush)
+        ms = float(np.median(times))
+        res = call(A)
+        t0 = time.perf_counter()
+        want = oracle_call(img)
+        cpu_s = time.perf_counter() - t0
+        if name.startswith("harris"):
+            got = (res.x(), res.y(), res.score())
+            same = all(a.tobytes() == b.tobytes() for a, b in zip(got, want))
+            extra = {"corners": int(got[0].size)}
+        else:
+            got = res.to_numpy().reshape(img.shape, order="F").astype(np.int8)
+            same = got.tobytes(order="F") == np.asarray(want)[:, :, 0].tobytes(order="F")
+            extra = {"edge_pixels": int(got.sum())}
+        mpx = img.size / 1e6
+        out[name] = {"ms": round(ms, 4), "Mpixel/s": round(mpx / (ms / 1e3), 1),
+                     "bit_exact_vs_oracle": bool(same), **extra,
+                     "cpu_baseline": {"value": round(mpx / cpu_s, 2), "unit": "Mpixel/s",
+                                      "cores": 1, "kind": "port",
+                                      "sample": "the same 2048x2048 image, oracle port (numpy "
+                                                "and the C separable port)"}}
+        del res, A
+        torch.cuda.synchronize()
+    return out
+
+
 def cpu_nn_steps(steps: int, warmup: int, seconds_budget: float) -> dict:
     """Forward + both gradients of the headline workload, full 32-image
     steps, timed on the host: oracle unwrap/wrap (C restatement of the
@@ -1041,6 +1112,11 @@ def run_only(args) -> None:
     s = NN_SHAPE
     st, pd, dl = s["stride"], s["pad"], s["dil"]
     g = np.random.Generator(np.random.Philox(1234))
+    if args.only == "image_callers":
+        import oracle as O
+
+        print(json.dumps(run_image_callers(af, O, args)))
+        return
     if args.only == "cnn":
         from arrayfire_gb300.autograd import cnn_step
 
@@ -1157,7 +1233,7 @@ def main() -> None:
     ap.add_argument("--only", default=None,
                     choices=["fwd", "dgrad", "wgrad", "step", "sep_f32", "sep_u8", "same7", "conv3",
                              "conv3_expand", "conv1", "cnn", "unwrap", "wrap", "unwrap_rows",
-                             "wrap_rows"],
+                             "wrap_rows", "image_callers"],
                     help="run one operation of the workload --steps times after --warmup "
                          "(for profiler captures); prints its timing, not the bench line")
     args = ap.parse_args()
