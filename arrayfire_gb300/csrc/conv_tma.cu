@@ -738,26 +738,25 @@ __global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ 
     __syncthreads();  // barriers initialised before anyone waits on them
 
     int k = 0;
-    // filter taps of the tile's volume (SAME batches: one filter per volume),
-    // kept in registers and reloaded only when the volume's filter changes
+    // filter taps of the tile's volume (SAME batches: one filter per volume)
+    // in shared memory, rewritten only when the volume's filter changes; the
+    // reads are broadcasts.  (Taps held in registers through __ldg were
+    // re-fetched from global memory at every use by the compiled code.)
+    __shared__ float wsm[27];
     long long cur_filt = -1;
-    float wr[27];
     for (int t = blockIdx.x; t < t3.ntiles; t += gridDim.x, ++k) {
         const int buf = k & 1;
         if (threadIdx.x == 0 && t + (int)gridDim.x < t3.ntiles) issue(t + gridDim.x, buf ^ 1);
         long long i0, j0, k0, b;
         decode(t, i0, j0, k0, b);
         const long long foff = b * p.filt_step[3];
-        if (foff != cur_filt) {
-            const float *w = static_cast<const float *>(p.filt) + foff;
-#pragma unroll
-            for (int fk = 0; fk < 3; ++fk)
-#pragma unroll
-                for (int fj = 0; fj < 3; ++fj)
-#pragma unroll
-                    for (int fi = 0; fi < 3; ++fi)
-                        wr[(fk * 3 + fj) * 3 + fi] =
-                            __ldg(w + fi * p.fs[0] + fj * p.fs[1] + fk * p.fs[2]);
+        if (foff != cur_filt) {  // the same for the whole CTA: the barrier is uniform
+            if (threadIdx.x < 27) {
+                const int fi = threadIdx.x % 3, fj = (threadIdx.x / 3) % 3, fk = threadIdx.x / 9;
+                wsm[threadIdx.x] = __ldg(static_cast<const float *>(p.filt) + foff + fi * p.fs[0] +
+                                         fj * p.fs[1] + fk * p.fs[2]);
+            }
+            __syncthreads();  // the previous tile's reads ended at its closing barrier
             cur_filt = foff;
         }
         if (!wait_tile(&bar[buf], (k >> 1) & 1)) break;
@@ -790,7 +789,7 @@ __global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ 
                     if (fk >= 0 && fk < 3) {
 #pragma unroll
                         for (int fi = 0; fi < 3; ++fi) {
-                            const float wv = wr[(fk * 3 + fj) * 3 + fi];
+                            const float wv = wsm[(fk * 3 + fj) * 3 + fi];
 #pragma unroll
                             for (int cc = 0; cc < 4; ++cc)
                                 acc[rz][cc] = mac<EXACT>(acc[rz][cc], v[OFF + cc + 2 - fi], wv);

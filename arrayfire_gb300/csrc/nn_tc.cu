@@ -571,7 +571,13 @@ constexpr int SC_NA = 2;                    // strip-set buffers
 constexpr int SC_B_AREA = 64 * 1024;        // weight-tile ring
 constexpr int SC_MAXN = 128;
 constexpr int SC_MAXNB = 8;
-constexpr int SC_THREADS = 320;             // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+// warp 0 TMA; warps 1 and 10 issue the MMAs of output rows 0 and 1; warps
+// 2-9 epilogue.  One issuing thread needs 75-100 cycles per MMA (waits,
+// fences, descriptor arithmetic), more than an N<=128 MMA takes (48-64
+// cycles); two issuers, each with its own accumulator, keep the tensor pipe
+// busy (measured by microbenchmark).
+constexpr int SC_THREADS = 352;
+constexpr int SC_MMA_WARP1 = 10;
 
 struct StripConvParams {
     float *dst;          // ArrayFire layout (DW, DH, DC, N)
@@ -592,7 +598,7 @@ struct StripConvSmem {
     uint64_t a_full[SC_NA], a_empty[SC_NA];
     uint64_t b_full[SC_MAXNB], b_empty[SC_MAXNB];
     uint64_t tmem_full[2], tmem_empty[2];
-    uint64_t final_bar;
+    uint64_t final_bar[SC_R];
     uint32_t tmem_base;
     int abort;
 };
@@ -613,19 +619,21 @@ __global__ void __launch_bounds__(SC_THREADS, 1)
     const int tiles_per_img = p.nseg * p.nrg;
 
     if (threadIdx.x == 0) {
+        // the empty and tmem_full barriers complete when both issuers'
+        // MMAs have read the stage / written the accumulator
         for (int i = 0; i < SC_NA; ++i) {
             mbar_init(&sm->a_full[i], 1);
-            mbar_init(&sm->a_empty[i], 1);
+            mbar_init(&sm->a_empty[i], SC_R);
         }
         for (int i = 0; i < p.nb; ++i) {
             mbar_init(&sm->b_full[i], 1);
-            mbar_init(&sm->b_empty[i], 1);
+            mbar_init(&sm->b_empty[i], SC_R);
         }
         for (int i = 0; i < 2; ++i) {
-            mbar_init(&sm->tmem_full[i], 1);
+            mbar_init(&sm->tmem_full[i], SC_R);
             mbar_init(&sm->tmem_empty[i], 256);
         }
-        mbar_init(&sm->final_bar, 1);
+        for (int r = 0; r < SC_R; ++r) mbar_init(&sm->final_bar[r], 1);
         sm->abort = 0;
         fence_barrier_init();
     }
@@ -681,10 +689,11 @@ __global__ void __launch_bounds__(SC_THREADS, 1)
             }
         }
         __syncwarp();
-    } else if (warp == 1) {
-        // ---------------- MMA issuer: descriptors are precomputed bases plus
-        // 16-byte-unit offsets; stage indices and phases advance without
-        // division
+    } else if (warp == 1 || warp == SC_MMA_WARP1) {
+        // ---------------- MMA issuers, one per output row r: descriptors are
+        // precomputed bases plus 16-byte-unit offsets; stage indices and
+        // phases advance without division
+        const int r = warp == 1 ? 0 : 1;
         if (lane == 0) {
             const uint32_t idesc = idesc_bf16(128, (uint32_t)p.nmma, 0, 0);
             const uint64_t a0 = smem_desc(smem_u32(a_area), 16, 1024);
@@ -698,7 +707,7 @@ __global__ void __launch_bounds__(SC_THREADS, 1)
                 const int acc = acc_it & 1;
                 if (!mbar_wait(&sm->tmem_empty[acc], ((acc_it >> 1) & 1) ^ 1, abort, 4u)) break;
                 tc_fence_after();
-                const uint32_t d0 = tmem_base + (uint32_t)(acc * SC_R * p.nmma);
+                const uint32_t d0 = tmem_base + (uint32_t)((acc * SC_R + r) * p.nmma);
                 for (int ch = 0; ch < p.nchunk && !stop; ++ch) {
                     if (!mbar_wait(&sm->a_full[a], aph, abort, 8u)) {
                         stop = true;
@@ -711,15 +720,12 @@ __global__ void __launch_bounds__(SC_THREADS, 1)
                             break;
                         }
                         tc_fence_after();
-                        const uint64_t ad = a0 + aoff + p.a_off[t];
+                        const uint64_t ad = a0 + aoff + p.a_off[t] + (uint32_t)(r * p.strip16);
                         const uint64_t bd = b0 + boff;
 #pragma unroll
-                        for (int r = 0; r < SC_R; ++r)
-#pragma unroll
-                            for (int k = 0; k < 4; ++k)
-                                mma_f16(d0 + (uint32_t)(r * p.nmma),
-                                        ad + (uint32_t)(r * p.strip16 + 2 * k),
-                                        bd + (uint32_t)(2 * k), idesc, (ch | t | k) != 0);
+                        for (int k = 0; k < 4; ++k)
+                            mma_f16(d0, ad + (uint32_t)(2 * k), bd + (uint32_t)(2 * k), idesc,
+                                    (ch | t | k) != 0);
                         mma_commit(&sm->b_empty[b]);
                         issued = true;
                         if (++b == p.nb) {
@@ -745,9 +751,9 @@ __global__ void __launch_bounds__(SC_THREADS, 1)
                 ++acc_it;
             }
             if (issued) {
-                mma_commit(&sm->final_bar);
+                mma_commit(&sm->final_bar[r]);
                 unsigned n = 0;
-                while (!mbar_try_wait(&sm->final_bar, 0) && ++n < kSpinLimit) {
+                while (!mbar_try_wait(&sm->final_bar[r], 0) && ++n < kSpinLimit) {
                 }
             }
         }
