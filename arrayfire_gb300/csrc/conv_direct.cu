@@ -859,7 +859,16 @@ constexpr int C1P_MAXF = 129;
 constexpr int C1P_GROUPS = (16 * 255 + 8 * ((C1P_MAXF + 2) / 8) + 24 + 15) / 16;
 constexpr int C1P_STAGE = C1P_GROUPS * 20;                        // floats
 constexpr int C1P_WMAX = 8 * ((C1P_MAXF + 2) / 8 + 1);            // padded taps
-constexpr size_t C1P_SMEM = (size_t)C1P_NST * C1P_STAGE * 4 + (size_t)C1P_WMAX * 4;
+// taps staged with each tile (reversed and zero-padded for its `mis`)
+constexpr size_t C1P_SMEM = (size_t)C1P_NST * C1P_STAGE * 4 + (size_t)C1P_NST * C1P_WMAX * 4;
+
+// one tap into shared memory, or zero when bytes == 0
+__device__ __forceinline__ void c1p_copy4(float *dst, const float *src, int bytes) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(
+                     (unsigned)__cvta_generic_to_shared(dst)),
+                 "l"(src), "r"(bytes)
+                 : "memory");
+}
 
 __device__ __forceinline__ void c1p_copy16(float *dst, const float *src, int bytes) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(
@@ -927,7 +936,7 @@ template <bool EXACT>
 __global__ void __launch_bounds__(C1P_THREADS, 3)
     conv1_pipe_kernel(const DirectParams p, long long ntx, long long ntiles) {
     extern __shared__ __align__(16) float c1p_smem[];
-    float *wbuf = c1p_smem + C1P_NST * C1P_STAGE;
+    float *wring = c1p_smem + C1P_NST * C1P_STAGE;  // C1P_NST x C1P_WMAX staged taps
     const int F = (int)p.fd[0];
     const long long len = p.sd[0], od = p.od[0];
     const long long c0 = p.expand ? 0 : F / 2;
@@ -978,6 +987,18 @@ __global__ void __launch_bounds__(C1P_THREADS, 3)
             }
             c1p_copy16(st + (c >> 2) * 20 + (c & 3) * 4, src, bytes);
         }
+        // the tile's taps, reversed from W_hi = F - 1 + mis and zero outside
+        // [0, F), arrive with the same copy group: no global load waits at
+        // the barrier that opens the tile
+        const int whi = F - 1 + t.mis;
+        const int nw = 8 * (whi / 8 + 1);
+        float *wb = wring + buf * C1P_WMAX;
+        const float *fp = filt + t.bo.filt;
+        for (int kk = tid; kk < nw; kk += C1P_THREADS) {
+            const int wi = whi - kk;
+            const bool in = wi >= 0 && wi < F;
+            c1p_copy4(wb + kk, in ? fp + (long long)wi * p.fs[0] : fp, in ? 4 : 0);
+        }
     };
 
 #pragma unroll 1
@@ -1000,12 +1021,8 @@ __global__ void __launch_bounds__(C1P_THREADS, 3)
         const Tile t = tinfo[buf];
         const int whi = F - 1 + t.mis;
         const int M = whi / 8 + 1;
-        for (int kk = tid; kk < 8 * M; kk += C1P_THREADS) {
-            const int wi = whi - kk;
-            const float w = (wi >= 0 && wi < F) ? filt[t.bo.filt + wi * p.fs[0]] : 0.0f;
-            wbuf[kk] = w;
-        }
-        __syncthreads();
+        const float *wbuf = wring + buf * C1P_WMAX;
+        __syncthreads();  // every thread's copies of this stage have landed
         float *st = c1p_smem + buf * C1P_STAGE;
         if (t.lo < 0) {  // staged elements before the signal start read as zero
             const int nz = (int)min(-t.lo, (long long)C1P_STAGE);

@@ -198,8 +198,12 @@ __device__ __forceinline__ void widen_tile(const T *tb, float *ft) {
 // ===========================================================================
 // 2-D direct convolution, F0 x F1 filter, 64x64 tile, 4x4 outputs per thread
 // ===========================================================================
+// Filters above 5x5 keep all their taps in registers at two CTAs per SM
+// (112 registers at 7x7); under a three-CTA cap (85) the 7x7 taps do not fit
+// and are fetched again inside the tap loop.
 template <typename T, int F0, int F1, bool EXACT, bool EXPAND>
-__global__ void __launch_bounds__(THREADS, 3) conv2_tma_kernel(const __grid_constant__ CUtensorMap smap,
+__global__ void __launch_bounds__(THREADS, (F0 * F1 > 25) ? 2 : 3)
+    conv2_tma_kernel(const __grid_constant__ CUtensorMap smap,
                                                             const DirectParams p,
                                                             const TileGrid tg) {
     using H = Halo<T, F0, F1, EXPAND>;
@@ -692,6 +696,10 @@ constexpr int C3_PF = 76;              // box width: an odd number of 16-byte wo
 constexpr int C3_TH = C3_BY + 2, C3_TD = C3_BZ + 2;
 constexpr int C3_BYTES = C3_PF * C3_TH * C3_TD * 4;
 constexpr int C3_BUF = (C3_BYTES + 1023) / 1024 * 1024;  // TMA destinations stay 1024-aligned
+// input boxes per CTA: the one computed and the next in flight, three CTAs
+// per SM (three boxes at two CTAs per SM measured slower: 0.050 against
+// 0.047 ms on 256^3)
+constexpr int C3_NB = 2;
 
 struct Conv3Tma {
     FastDiv ntx, nty, nz;    // tiles along x, y, z
@@ -709,7 +717,7 @@ __global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ 
     extern __shared__ __align__(1024) unsigned char sm3_raw[];
     unsigned char *sm3 = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(sm3_raw) + 1023) & ~uintptr_t(1023));
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sm3 + 2 * C3_BUF);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm3 + C3_NB * C3_BUF);
 
     // tile t -> (x tile, y tile, z tile, batch)
     auto decode = [&](int t, long long &i0, long long &j0, long long &k0, long long &b) {
@@ -730,10 +738,12 @@ __global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ 
                         (int)(j0 + C0 - 2), (int)(k0 + C0 - 2), (int)(b * t3.vstep));
     };
     if (threadIdx.x == 0) {
-        tc::mbar_init(&bar[0], 1);
-        tc::mbar_init(&bar[1], 1);
+        for (int i = 0; i < C3_NB; ++i) tc::mbar_init(&bar[i], 1);
         tc::fence_barrier_init();
-        if ((int)blockIdx.x < t3.ntiles) issue(blockIdx.x, 0);
+        for (int i = 0; i < C3_NB - 1; ++i) {
+            const long long t = blockIdx.x + (long long)i * gridDim.x;
+            if (t < t3.ntiles) issue((int)t, i);
+        }
     }
     __syncthreads();  // barriers initialised before anyone waits on them
 
@@ -745,8 +755,10 @@ __global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ 
     __shared__ float wsm[27];
     long long cur_filt = -1;
     for (int t = blockIdx.x; t < t3.ntiles; t += gridDim.x, ++k) {
-        const int buf = k & 1;
-        if (threadIdx.x == 0 && t + (int)gridDim.x < t3.ntiles) issue(t + gridDim.x, buf ^ 1);
+        const int buf = k % C3_NB;
+        // the buffer of the previous tile, released by its closing barrier
+        const long long ahead = t + (long long)(C3_NB - 1) * gridDim.x;
+        if (threadIdx.x == 0 && ahead < t3.ntiles) issue((int)ahead, (k + C3_NB - 1) % C3_NB);
         long long i0, j0, k0, b;
         decode(t, i0, j0, k0, b);
         const long long foff = b * p.filt_step[3];
@@ -759,7 +771,18 @@ __global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ 
             __syncthreads();  // the previous tile's reads ended at its closing barrier
             cur_filt = foff;
         }
-        if (!wait_tile(&bar[buf], (k >> 1) & 1)) break;
+        if (!wait_tile(&bar[buf], (k / C3_NB) & 1)) {
+            // a box that never landed: give the later boxes this CTA issued
+            // a bounded chance to land before the CTA exits
+            if (threadIdx.x == 0)
+                for (int j = k + 1; j < k + C3_NB; ++j) {
+                    if (blockIdx.x + (long long)j * gridDim.x >= t3.ntiles) break;
+                    unsigned n = 0;
+                    while (!mbar_try_wait(&bar[j % C3_NB], (j / C3_NB) & 1) && ++n < (1u << 16)) {
+                    }
+                }
+            break;
+        }
         const float *tile = reinterpret_cast<const float *>(sm3 + buf * C3_BUF);
         const int tx = threadIdx.x & 15;
         const int ty = (threadIdx.x >> 4) & 7;
@@ -1086,7 +1109,7 @@ bool tma_convolve3(const DirectParams &p, bool exact) {
            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return false;
-    const size_t smem = 1024 + 2 * C3_BUF + 16;
+    const size_t smem = 1024 + C3_NB * C3_BUF + 8 * C3_NB;
 #define AFGB_C3(E, X)                                                                           \
     do {                                                                                        \
         AFGB_CUDA(cudaFuncSetAttribute(conv3_tma_kernel<E, X>,                                  \
