@@ -30,6 +30,7 @@ SOURCES = [
     "nn_tc.cu",
     "unwrap_wrap.cu",
     "fft_conv.cu",
+    "fft_own.cu",
     "image_ops.cu",
     "harris.cu",
     "canny.cu",

@@ -49,6 +49,7 @@
 #include "afgb_internal.hpp"
 #include "conv_common.cuh"
 #include "conv_direct.hpp"
+#include "fft_own.hpp"
 
 namespace afgb {
 
@@ -398,16 +399,68 @@ void crop_to(const V *buf, Array &out, const FftGeom &g, bool expand, const dim_
     }
 }
 
+// This library's transforms (fft_own.cu) serve every size whose lengths are
+// 2^a 3^b and fit one block's shared memory, the sizes good_size picks by
+// default; cuFFT serves the others (AFGB_FFT_RADICES with factors 5 or 7,
+// or lengths above about 12800), or every size with AFGB_FFT_IMPL=cufft.
+bool use_own_fft(const FftGeom &g, bool real, size_t csize) {
+    static const bool force_cufft = [] {
+        const char *e = std::getenv("AFGB_FFT_IMPL");
+        return e && std::string(e) == "cufft";
+    }();
+    if (force_cufft) return false;
+    for (int k = 0; k < g.rank; ++k)
+        if (!fft_own_len_ok(g.n[k], real && k == 0, csize)) return false;
+    return true;
+}
+
+// the rank-r transform of `b` slices over the axes above 0, in place on the
+// (n0c, n1, n2, b) spectrum (n0c = n0/2+1 for real data, n0 for complex)
+template <typename C>
+void own_axes(C *spec, const FftGeom &g, long long n0c, long long b, bool inverse) {
+    if (!inverse) {
+        if (g.rank >= 2) fft_axis<C>(spec, g.n[1], n0c, g.n[2] * b, false);
+        if (g.rank >= 3) fft_axis<C>(spec, g.n[2], n0c * g.n[1], b, false);
+    } else {
+        if (g.rank >= 3) fft_axis<C>(spec, g.n[2], n0c * g.n[1], b, true);
+        if (g.rank >= 2) fft_axis<C>(spec, g.n[1], n0c, g.n[2] * b, true);
+    }
+}
+
+template <typename R, typename C>
+void own_forward_real(const R *in, C *spec, const FftGeom &g, long long b) {
+    fft_real_forward<R, C>(in, spec, g.n[0], g.n[1] * g.n[2] * b);
+    own_axes<C>(spec, g, g.n[0] / 2 + 1, b, false);
+}
+
+template <typename R, typename C>
+void own_inverse_real(C *spec, R *out, const FftGeom &g, long long b) {
+    own_axes<C>(spec, g, g.n[0] / 2 + 1, b, true);
+    fft_real_inverse<R, C>(spec, out, g.n[0], g.n[1] * g.n[2] * b);
+}
+
+template <typename C>
+void own_complex(C *spec, const FftGeom &g, long long b, bool inverse) {
+    if (!inverse) fft_axis<C>(spec, g.n[0], 1, g.n[1] * g.n[2] * b, false);
+    own_axes<C>(spec, g, g.n[0], b, inverse);
+    if (inverse) fft_axis<C>(spec, g.n[0], 1, g.n[1] * g.n[2] * b, true);
+}
+
 // real data: R2C / C2R (float or double working type R, spectrum C)
 template <typename R, typename C>
 void run_real(const Array &s, const Array &f, Array &out, const FftGeom &g, bool expand, int mode,
               cufftType fwd, cufftType inv) {
-    CufftApi &api = cufft();
+    const bool own_fft = use_own_fft(g, true, sizeof(C));
     Scratch sreal(sizeof(R) * g.nreal * g.sb), freal(sizeof(R) * g.nreal * g.fb);
     Scratch sspec(sizeof(C) * g.ncplx * g.sb), fspec(sizeof(C) * g.ncplx * g.fb);
     pad_into<R>(s, sreal.as<R>(), g, g.sb);
     pad_into<R>(f, freal.as<R>(), g, g.fb);
     const int nf[3] = {(int)g.n[0], (int)g.n[1], (int)g.n[2]};
+    if (own_fft) {
+        own_forward_real<R, C>(sreal.as<R>(), sspec.as<C>(), g, g.sb);
+        own_forward_real<R, C>(freal.as<R>(), fspec.as<C>(), g, g.fb);
+    } else {
+    CufftApi &api = cufft();
     cufftHandle ps = get_plan(g.rank, nf, (int)g.sb, fwd, g.epoch);
     cufftHandle pf = get_plan(g.rank, nf, (int)g.fb, fwd, g.epoch);
     cufft_check(api.set_stream(ps, stream()), "set stream");
@@ -421,6 +474,7 @@ void run_real(const Array &s, const Array &f, Array &out, const FftGeom &g, bool
         cufft_check(api.d2z(pf, freal.as<cufftDoubleReal>(), fspec.as<cufftDoubleComplex>()),
                     "D2Z");
     }
+    }
     // product in place where one side's slices are the output's (NONE, LHS,
     // SAME: the signal's; RHS: the filter's), else (DIFF) in new buffers
     const bool s_is_out = g.ob == g.sb && std::equal(g.bm.sd, g.bm.sd + g.bm.nbd, g.bm.od);
@@ -432,6 +486,10 @@ void run_real(const Array &s, const Array &f, Array &out, const FftGeom &g, bool
     C *P = s_is_out ? sspec.as<C>() : (f_is_out ? fspec.as<C>() : pspec.as<C>());
     R *oreal = s_is_out ? sreal.as<R>() : (f_is_out ? freal.as<R>() : obuf.as<R>());
     multiply<C>(sspec.as<C>(), fspec.as<C>(), P, g);
+    if (own_fft) {
+        own_inverse_real<R, C>(P, oreal, g, g.ob);
+    } else {
+    CufftApi &api = cufft();
     cufftHandle po = get_plan(g.rank, nf, (int)g.ob, inv, g.epoch);
     cufft_check(api.set_stream(po, stream()), "set stream");
     if constexpr (std::is_same<R, float>::value)
@@ -441,6 +499,7 @@ void run_real(const Array &s, const Array &f, Array &out, const FftGeom &g, bool
         cufft_check(api.z2d(po, reinterpret_cast<cufftDoubleComplex *>(P),
                             reinterpret_cast<cufftDoubleReal *>(oreal)),
                     "Z2D");
+    }
     if (mode == CROP_ROUND) crop_to<R, CROP_ROUND>(oreal, out, g, expand, f.dims);
     else if (mode == CROP_TRUNC) crop_to<R, CROP_TRUNC>(oreal, out, g, expand, f.dims);
     else crop_to<R, CROP_PLAIN>(oreal, out, g, expand, f.dims);
@@ -450,11 +509,26 @@ void run_real(const Array &s, const Array &f, Array &out, const FftGeom &g, bool
 template <typename C>
 void run_complex(const Array &s, const Array &f, Array &out, const FftGeom &g, bool expand,
                  int mode, cufftType type) {
-    CufftApi &api = cufft();
+    const bool own = use_own_fft(g, false, sizeof(C));
     Scratch sspec(sizeof(C) * g.ncplx * g.sb), fspec(sizeof(C) * g.ncplx * g.fb);
     pad_into<C>(s, sspec.as<C>(), g, g.sb);
     pad_into<C>(f, fspec.as<C>(), g, g.fb);
     const int nf[3] = {(int)g.n[0], (int)g.n[1], (int)g.n[2]};
+    if (own) {
+        own_complex<C>(sspec.as<C>(), g, g.sb, false);
+        own_complex<C>(fspec.as<C>(), g, g.fb, false);
+        const bool s_is_out = g.ob == g.sb && std::equal(g.bm.sd, g.bm.sd + g.bm.nbd, g.bm.od);
+        const bool f_is_out =
+            !s_is_out && g.ob == g.fb && std::equal(g.bm.fd, g.bm.fd + g.bm.nbd, g.bm.od);
+        Scratch pspec(s_is_out || f_is_out ? 0 : sizeof(C) * g.ncplx * g.ob);
+        C *P = s_is_out ? sspec.as<C>() : (f_is_out ? fspec.as<C>() : pspec.as<C>());
+        multiply<C>(sspec.as<C>(), fspec.as<C>(), P, g);
+        own_complex<C>(P, g, g.ob, true);
+        if (mode == CROP_TRUNC) crop_to<C, CROP_TRUNC>(P, out, g, expand, f.dims);
+        else crop_to<C, CROP_PLAIN>(P, out, g, expand, f.dims);
+        return;
+    }
+    CufftApi &api = cufft();
     cufftHandle ps = get_plan(g.rank, nf, (int)g.sb, type, g.epoch);
     cufftHandle pf = get_plan(g.rank, nf, (int)g.fb, type, g.epoch);
     cufft_check(api.set_stream(ps, stream()), "set stream");

@@ -180,3 +180,68 @@ def test_fft_plan_cache_eviction(af, oracle):
             got = af.fft_convolve1(af.Array.from_numpy(s), af.Array.from_numpy(f)).to_numpy()
             ref = oracle.fft_convolve(s, f, C.F32, 1, False)
             assert np.abs(got - ref).max() <= 1e-5 * bound(s, f, 1, False, oracle)
+
+
+def _launches(af, names, fn):
+    import ctypes
+
+    L = af.lib()
+    L.afgb_kernel_timing(1)
+    try:
+        r = fn()
+        af.sync()
+        counts = {}
+        for name in names:
+            c, ms = ctypes.c_ulonglong(), ctypes.c_double()
+            L.afgb_kernel_time(name.encode(), ctypes.byref(c), ctypes.byref(ms))
+            counts[name] = c.value
+    finally:
+        L.afgb_kernel_timing(0)
+    return counts, r
+
+
+OWN = ("fft_r2c_rows_kernel", "fft_c2r_rows_kernel", "fft_axis_kernel")
+
+
+@pytest.mark.parametrize("dt,rank,sd,fd", [
+    (C.F32, 1, (3000, 4), (77,)), (C.F64, 1, (513,), (40, 3)),
+    (C.F32, 2, (300, 250, 2), (31, 17)), (C.F64, 2, (97, 130), (9, 9, 2)),
+    (C.F32, 3, (40, 33, 20), (5, 4, 3)), (C.C32, 2, (120, 90), (11, 11)),
+    (C.C64, 3, (20, 18, 10, 2), (3, 3, 3)), (C.S32, 2, (200, 150), (15, 15))],
+    ids=lambda v: str(v).replace(" ", ""))
+def test_own_transforms_serve_2a3b_sizes(af, oracle, dt, rank, sd, fd):
+    """The padded lengths are 2^a 3^b, so this library's Stockham transforms
+    run (no cuFFT): the real-row kernels for real data, the axis kernel for
+    every other axis and for complex data; results within the rounding bound
+    of the FP64 oracle (integers bit for bit)."""
+    s = values(dt, sd, 70 + rank)
+    if dt in (C.C32, C.C64):
+        f = C.make_signal(dt, fd, 71 + rank)
+    elif dt in (C.F32, C.F64):
+        f = C.make_filter(dt, fd, 71 + rank, rank)
+    else:
+        f = np.asfortranarray(np.ones(fd, np.float32))
+    counts, got = _launches(af, OWN, lambda: run_fft(af, s, f, dt, rank, True))
+    real = dt not in (C.C32, C.C64)
+    if real:
+        assert counts["fft_r2c_rows_kernel"] > 0 and counts["fft_c2r_rows_kernel"] > 0
+    if rank > 1 or not real:
+        assert counts["fft_axis_kernel"] > 0
+    ref = oracle.fft_convolve(s, f, dt, rank, True)
+    if dt in (C.F32, C.F64, C.C32, C.C64):
+        eps = 1e-5 if dt in (C.F32, C.C32) else 1e-13
+        assert np.abs(got.astype(np.complex128) - ref).max() <= eps * bound(s, f, rank, True, oracle)
+    else:
+        np.testing.assert_array_equal(got, ref)
+
+
+def test_cufft_serves_lengths_above_the_shared_memory_plan(af, oracle):
+    """A 1-D length whose half does not fit one block's shared memory
+    (36864 = 2^12 * 9 here) goes to cuFFT, with the same results."""
+    g = np.random.Generator(np.random.Philox(9))
+    s = np.asfortranarray(g.random(32768, dtype=np.float32))
+    f = np.asfortranarray(g.random(4095, dtype=np.float32))
+    counts, got = _launches(af, OWN, lambda: run_fft(af, s, f, C.F32, 1, False))
+    assert counts["fft_r2c_rows_kernel"] == 0
+    ref = oracle.fft_convolve(s, f, C.F32, 1, False)
+    assert np.abs(got - ref).max() <= 2e-6 * float(np.abs(ref).max()) + 1e-6
