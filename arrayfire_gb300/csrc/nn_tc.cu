@@ -58,6 +58,18 @@ constexpr int MAX_T = 256;
 constexpr int NUM_THREADS = 320;      // warps 0-3 gather, 4-7 epilogue, 8 MMA, 9 TMA
 constexpr int EP_PITCH = 20;          // epilogue staging row pitch (floats): 16 pixels + 4
 constexpr int EP_WARPS = 8;           // epilogue warps of the TMA path (two per TMEM quadrant)
+// Column groups (stride 1, filters at most three taps high): the taps of one
+// filter column read the same pixel columns one row apart, so they share one
+// TMA box BY + 2 rows high; tap v's operand is the view (oy_v - oy_min) * BX
+// pixel rows into it (an MMA operand may start at any 128-byte row).  Three
+// taps per stage, one box load instead of three: the L2-to-shared traffic of
+// the pixel operand drops from 9 to 3.75 boxes per tile and chunk.
+constexpr int CG_STAGES = 2;
+constexpr int CG_GT = 3;                                 // taps per group at most
+constexpr int CG_BX = 32, CG_BY = 8;                      // 256-pixel rectangles
+constexpr int CG_BOX_BYTES = CG_BX * (CG_BY + 2) * 128;  // 40 KB
+constexpr int CG_STAGE_A = CG_GT * A_BYTES;              // 48 KB
+constexpr int MAX_G = 16;
 constexpr int EP_SLOT = 768;          // floats of staging per warp: 3 KB, 1024-byte aligned slots
 
 struct GatherParams {
@@ -83,6 +95,12 @@ struct GatherParams {
     int phase_tap_begin[MAX_PH + 1];
     short tap_u[MAX_T], tap_v[MAX_T];
     short tap_ox[MAX_T], tap_oy[MAX_T];  // operand offset of each tap (TMA path)
+    // column groups (cg != 0): group g holds taps cg_begin[g] .. cg_begin[g+1]-1
+    // of the one phase, its box at (cg_ox[g], cg_oymin[g]); the j-th tap's
+    // view starts cg_view[g * CG_GT + j] pixel rows into the box
+    int cg, cg_ngroups, cg_box_bytes;
+    short cg_begin[MAX_G + 1], cg_ox[MAX_G], cg_oymin[MAX_G];
+    short cg_view[MAX_G * CG_GT];
 };
 
 struct Smem {
@@ -171,19 +189,25 @@ __device__ __forceinline__ void tap_offsets(const GatherParams &p, const TileInf
     }
 }
 
-// FP8: e4m3 operands, 128 channels per 128-byte row, kind::f8f6f4 MMA
-template <bool TMA_B, bool FP8>
+// FP8: e4m3 operands, 128 channels per 128-byte row, kind::f8f6f4 MMA;
+// CG: column groups (stride-1 TMA path, bf16)
+template <bool TMA_B, bool FP8, bool CG = false>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
     gather_conv_kernel(const __grid_constant__ GatherParams p,
                        const __grid_constant__ CUtensorMap wmap,
                        const __grid_constant__ CUtensorMap xmap,
                        const __grid_constant__ CUtensorMap omap) {
+    static_assert(!CG || (TMA_B && !FP8), "column groups: TMA path, bf16");
+    static_assert(CG_STAGES * (CG_STAGE_A + CG_BOX_BYTES) <= STAGES * (A_BYTES + B_BYTES),
+                  "column-group stages fit the stage area");
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    unsigned char *a_stage = base;                     // STAGES x 16 KB
-    unsigned char *b_stage = base + STAGES * A_BYTES;  // STAGES x 32 KB
-    float *ep_stage = reinterpret_cast<float *>(b_stage + STAGES * B_BYTES);  // 8 x 32 x 20
+    // STAGES x 16 KB weight tiles then STAGES x 32 KB pixel tiles; column
+    // groups: CG_STAGES x 3 x 16 KB weight tiles then CG_STAGES x 40 KB boxes
+    unsigned char *a_stage = base;
+    unsigned char *b_stage = base + (CG ? CG_STAGES * CG_STAGE_A : STAGES * A_BYTES);
+    float *ep_stage = reinterpret_cast<float *>(base + STAGES * (A_BYTES + B_BYTES));  // 8 x 32 x 20
     Smem *sm = reinterpret_cast<Smem *>(ep_stage + EP_WARPS * EP_SLOT);
     volatile int *abort = &sm->abort;
 
@@ -212,7 +236,8 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
         // rows a_rows..127 of every weight tile are zero padding: written once
         // here, never loaded (the tensor core reads them through the async proxy)
         const int half_bytes = (BM - p.a_rows) * 128;
-        for (int i = threadIdx.x; i < STAGES * half_bytes / 16; i += blockDim.x) {
+        const int nslots = CG ? CG_STAGES * CG_GT : STAGES;  // weight tiles, A_BYTES apart
+        for (int i = threadIdx.x; i < nslots * half_bytes / 16; i += blockDim.x) {
             const int st = i / (half_bytes / 16), off = i - st * (half_bytes / 16);
             *reinterpret_cast<uint4 *>(a_stage + st * A_BYTES + p.a_rows * 128 + off * 16) =
                 make_uint4(0u, 0u, 0u, 0u);
@@ -463,8 +488,43 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 if (!mbar_wait(&sm->tmem_empty[b], ((acc_it >> 1) & 1) ^ 1, abort, 4u)) break;
                 tc_fence_after();
                 const uint32_t d_tmem = tmem_base + (uint32_t)(b * BN);
-                const int iters = p.nchunk * ti.ntaps;
                 bool ok = true;
+                if constexpr (CG) {
+                    // one stage per (channel chunk, filter column): the
+                    // column's taps, each against its view of the box
+                    bool first = true;
+                    for (int cchunk = 0; cchunk < p.nchunk && ok; ++cchunk) {
+                        for (int g = 0; g < p.cg_ngroups; ++g, ++it) {
+                            const int s = it % CG_STAGES;
+                            if (!mbar_wait(&sm->full[s], (it / CG_STAGES) & 1, abort, 8u)) {
+                                ok = false;
+                                break;
+                            }
+                            tc_fence_after();
+                            const int nt = p.cg_begin[g + 1] - p.cg_begin[g];
+                            for (int j = 0; j < nt; ++j) {
+                                const uint64_t as =
+                                    a0 + (uint32_t)((s * CG_STAGE_A + j * A_BYTES) >> 4);
+                                const uint64_t bs =
+                                    b0 + (uint32_t)((s * CG_BOX_BYTES) >> 4) +
+                                    (uint32_t)(p.cg_view[g * CG_GT + j] * 8);  // rows of 128 B
+#pragma unroll
+                                for (int k = 0; k < 4; ++k) {
+                                    mma_f16(d_tmem, as + (uint32_t)(2 * k), bs + (uint32_t)(2 * k),
+                                            idesc, first ? (k != 0) : 1);
+                                }
+                                first = false;
+                            }
+                            mma_commit(&sm->empty[s]);
+                            issued = true;
+                        }
+                    }
+                    if (!ok) break;
+                    mma_commit(&sm->tmem_full[b]);
+                    ++acc_it;
+                    continue;
+                }
+                const int iters = p.nchunk * ti.ntaps;
                 for (int kb = 0; kb < iters; ++kb, ++it) {
                     const int s = it % STAGES;
                     if (!mbar_wait(&sm->full[s], (it / STAGES) & 1, abort, 8u)) {
@@ -510,6 +570,30 @@ __global__ void __launch_bounds__(NUM_THREADS, 1)
                 const int bx0 = p.mode == 0 ? ti.x0 * p.sx : ti.x0;
                 const int by0 = p.mode == 0 ? ti.y0 * p.sy : ti.y0;
                 bool stop = false;
+                if constexpr (CG) {
+                    for (int cchunk = 0; cchunk < p.nchunk && !stop; ++cchunk) {
+                        for (int g = 0; g < p.cg_ngroups; ++g, ++it) {
+                            const int s = it % CG_STAGES;
+                            if (!mbar_wait(&sm->empty[s], ((it / CG_STAGES) & 1) ^ 1, abort, 16u)) {
+                                stop = true;
+                                break;
+                            }
+                            const int t0 = p.cg_begin[g], nt = p.cg_begin[g + 1] - t0;
+                            mbar_arrive_expect_tx(&sm->full[s], (uint32_t)p.cg_box_bytes +
+                                                                    (uint32_t)(nt * p.a_rows * 128));
+                            tma_load_4d(smem_u32(b_stage + s * CG_BOX_BYTES), &xmap, &sm->full[s],
+                                        cchunk * 64, bx0 + p.cg_ox[g], by0 + p.cg_oymin[g], ti.n);
+                            for (int j = 0; j < nt; ++j) {
+                                const int u = p.tap_u[t0 + j], v = p.tap_v[t0 + j];
+                                tma_load_2d(smem_u32(a_stage + s * CG_STAGE_A + j * A_BYTES), &wmap,
+                                            &sm->full[s], (u + p.fw * v) * p.SCpad + cchunk * 64,
+                                            ti.och0);
+                            }
+                        }
+                    }
+                    if (stop) break;
+                    continue;
+                }
                 for (int cchunk = 0; cchunk < p.nchunk && !stop; ++cchunk) {
                     for (int tq = ti.tap_begin; tq < ti.tap_begin + ti.ntaps; ++tq, ++it) {
                         const int s = it % STAGES;
@@ -1880,6 +1964,15 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     p.n_och_tiles = OCpad / 128;
     p.nphx = mode == 0 ? 1 : (int)g.sx;
     p.nphase = mode == 0 ? 1 : (int)(g.sx * g.sy);
+    // column groups: stride 1, bf16, two or three taps per filter column
+    // within a two-row span, images at least one rectangle wide
+    const int cg_span = (int)((g.fh - 1) * g.dy);
+    const bool cg = tma_b && !fp8 && !unfolded && g.sx == 1 && g.sy == 1 && g.fh >= 2 &&
+                    g.fh <= CG_GT && cg_span <= 2 && g.fw <= MAX_G && MX0 >= CG_BX;
+    if (cg) {
+        rbx = CG_BX;
+        rby = CG_BY;
+    }
     if (tma_b) {
         p.BX = rbx;
         p.BY = rby;
@@ -1916,9 +2009,33 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
     }
     p.phase_tap_begin[p.nphase] = ntap;
     p.phase_tile_begin[p.nphase] = ntile;
+    if (cg) {
+        // the one phase's taps again, filter column by filter column
+        p.cg = 1;
+        p.cg_ngroups = (int)g.fw;
+        p.cg_box_bytes = CG_BX * (CG_BY + cg_span) * 128;
+        int t = 0;
+        for (int u = 0; u < g.fw; ++u) {
+            p.cg_begin[u] = (short)t;
+            const int ox = (int)(mode == 0 ? u * g.dx - g.px : g.px - u * g.dx);
+            const int oymin = (int)(mode == 0 ? -g.py : g.py - (g.fh - 1) * g.dy);
+            p.cg_ox[u] = (short)ox;
+            p.cg_oymin[u] = (short)oymin;
+            for (int v = 0; v < g.fh; ++v, ++t) {
+                const int oy = (int)(mode == 0 ? v * g.dy - g.py : g.py - v * g.dy);
+                p.tap_u[t] = (short)u;
+                p.tap_v[t] = (short)v;
+                p.tap_ox[t] = (short)ox;
+                p.tap_oy[t] = (short)oy;
+                p.cg_view[u * CG_GT + v] = (short)((oy - oymin) * CG_BX);
+            }
+        }
+        p.cg_begin[g.fw] = (short)t;
+    }
     CUtensorMap xmap;
     std::memset(&xmap, 0, sizeof(xmap));
-    if (tma_b) xmap = make_imap(img, SCpad, SW, SH, (int)g.N, p.BX, p.BY, esize, tsx, tsy);
+    if (cg) xmap = make_imap(img, SCpad, SW, SH, (int)g.N, CG_BX, CG_BY + cg_span, esize, 1, 1);
+    else if (tma_b) xmap = make_imap(img, SCpad, SW, SH, (int)g.N, p.BX, p.BY, esize, tsx, tsy);
     p.total_tiles = ntile;
 
     // epilogue by TMA stores for unit-stride outputs with 16-byte rows
@@ -1949,7 +2066,12 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
         gather_conv_kernel<TB, F8><<<grid, NUM_THREADS, smem, stream()>>>(p, wmap, xmap, omap);  \
     } while (0)
-        if (tma_b && fp8) AFGB_LAUNCH_GATHER(true, true);
+        if (cg) {
+            AFGB_CUDA(cudaFuncSetAttribute(gather_conv_kernel<true, false, true>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+            gather_conv_kernel<true, false, true><<<grid, NUM_THREADS, smem, stream()>>>(p, wmap, xmap,
+                                                                                         omap);
+        } else if (tma_b && fp8) AFGB_LAUNCH_GATHER(true, true);
         else if (tma_b) AFGB_LAUNCH_GATHER(true, false);
         else if (fp8) AFGB_LAUNCH_GATHER(false, true);
         else AFGB_LAUNCH_GATHER(false, false);

@@ -1293,7 +1293,8 @@ def main() -> None:
         "kernel_launches_per_step": res["kernel_launches_per_step"],
         "fp32_path": res["fp32_path"], "cudnn": res.get("cudnn"),
         "nn_workloads": res.get("nn_workloads"),
-        "secondary": res.get("secondary"), "cnn4": res.get("cnn4"), "peaks": peaks,
+        "secondary": res.get("secondary"), "image_callers": res.get("image_callers"),
+        "cnn4": res.get("cnn4"), "peaks": peaks,
     }
     print(json.dumps(line))
 
