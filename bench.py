@@ -418,6 +418,54 @@ def ours_split(af, s, prec, steps, flush, seed) -> dict:
 # ---------------------------------------------------------------------------
 # our implementation
 # ---------------------------------------------------------------------------
+def bind_to_gpu_numa(dev: int) -> dict:
+    """Runs this process on the host CPUs attached to the GPU (read from the
+    PCI device's local_cpulist), so the pinned host buffers the e2e leg
+    allocates afterwards are placed on the GPU's side of the host link.  A
+    process-local affinity only; nothing on the machine is changed."""
+    import torch
+
+    try:
+        pr = torch.cuda.get_device_properties(dev)
+        bus = "%04x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        text = open(f"/sys/bus/pci/devices/{bus}/local_cpulist").read().strip()
+        cpus = set()
+        for part in text.split(","):
+            if "-" in part:
+                a, b = part.split("-")
+                cpus.update(range(int(a), int(b) + 1))
+            elif part:
+                cpus.add(int(part))
+        allowed = os.sched_getaffinity(0)
+        use = cpus & allowed
+        if use and use != allowed:
+            os.sched_setaffinity(0, use)
+        return {"pci": bus, "local_cpus": text, "cpus_used": len(use or allowed)}
+    except Exception as e:  # no sysfs entry (or no affinity support): leave it
+        return {"unbound": str(e)[:120]}
+
+
+def link_bandwidth(nbytes: int) -> dict:
+    """One pinned host->device and one device->host copy of nbytes (GB/s)."""
+    import torch
+
+    h = torch.empty(nbytes // 4, dtype=torch.float32).pin_memory()
+    d = torch.empty(nbytes // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    for name, fn in (("h2d", lambda: d.copy_(h, non_blocking=True)),
+                     ("d2h", lambda: h.copy_(d, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record()
+        fn()
+        b.record()
+        b.synchronize()
+        out[name + "_GBs"] = round(nbytes / (a.elapsed_time(b) / 1e3) / 1e9, 1)
+    return out
+
+
 def run_ours(args, peaks, rank: int, world: int) -> dict:
     import torch
 
@@ -425,6 +473,7 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
 
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
+    numa = bind_to_gpu_numa(dev)
     af.set_stream(torch.cuda.current_stream())
     L = af.lib()
     L.afgb_kernel_timing(0)
@@ -495,6 +544,7 @@ def run_ours(args, peaks, rank: int, world: int) -> dict:
 
     # e2e through the C ABI with pinned host buffers
     e2e = run_e2e(af, X, Wt, Gd, prec, args)
+    e2e["host"] = {**numa, **link_bandwidth(e2e["h2d_bytes_per_step"])}
 
     # the plain FP32 CUDA-core path on the same workload (the >= 5x target's
     # denominator), fewer steps
