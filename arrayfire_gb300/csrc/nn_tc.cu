@@ -902,6 +902,343 @@ __global__ void __launch_bounds__(SC_THREADS, 1)
 }
 
 // ===========================================================================
+// stride-1 forward and data gradient by source rows (the row kernel)
+// ===========================================================================
+// Pixels on M, (filter row, output channel) on N.  A CTA owns one group of
+// 64 output channels (ncg groups; the CTAs of a band's groups run side by
+// side and share its source rows through L2) and walks bands of output rows
+// (one image, one 128-pixel segment) source row by source row.  For source row r and each 64-channel
+// chunk the producer loads one strip of SL = 128 + (fw-1)*dx pixels; tap
+// column u's A operand (128 pixels x 64 channels, K-major, 128-byte swizzle)
+// is the view ox(u) - ox_min pixel rows into it.  Tap column u's B operand
+// stacks its FH filter rows' weights along N (FH blocks of 64 output
+// channels), so one MMA of N = FH*64 per K step gives source row r's
+// contribution to FH output rows: block j to output row r - oy_max + j.
+// Each source row accumulates into a fresh TMEM buffer (two, alternating);
+// MMAs that accumulate into regions overlapping the previous MMA's at another
+// column offset drain the tensor pipe (measured: about 800 cycles per shift),
+// while alternating disjoint regions run at the full rate.  The epilogue
+// keeps FH - 1 partial output rows per pixel in registers: source row r
+// completes output row r - oy_max (partial + block 0), the others shift by
+// one row, and the band's last FH - 1 rows are stored after its last source
+// row.  Each source pixel is loaded once per band and chunk, every MMA is
+// full width (no padded M rows), and the weights stay in shared memory for
+// the whole kernel.
+constexpr int RC_THREADS = 320;  // warp 0 TMA, warp 1 MMA, warps 2-9 epilogue
+constexpr int RC_STRIP = SC_STRIP;
+constexpr int RC_DC = 64;        // output channels per block and CTA (zero rows past DC)
+constexpr int RC_MAXCG = 4;      // channel groups: at most 256 output channels
+constexpr int RC_MAXNS = 8;
+constexpr int RC_MAXCH = 16;
+constexpr int RC_MAXTAP = 48;
+
+struct RowConvParams {
+    float *dst;          // ArrayFire layout (DW, DH, DC, N)
+    const float *bias;   // forward: per-output-channel bias, or 0
+    int relu;
+    int SW, SH, N;
+    int DW, DH, DC;
+    int fw, nchunk;
+    int ox_min, oy_min, oy_max;
+    int SL;               // strip pixels
+    int nseg, ns;         // 128-pixel segments, strip buffers
+    int ncg;              // 64-channel output groups (CTA b serves group b % ncg)
+    long long rows;       // N * nseg * DH output rows
+    int wcol[RC_MAXTAP];  // weight-map column of tap column u, block j (chunk 0), at u*FH + j
+    uint32_t a_view[16];  // tap column u's A view offset in 16-byte units
+};
+
+struct RowConvSmem {
+    uint64_t w_full[RC_MAXCH];
+    uint64_t s_full[RC_MAXNS], s_empty[RC_MAXNS];
+    uint64_t buf_full[2], buf_free[2];
+    uint64_t final_bar;
+    uint32_t tmem_base;
+    int abort;
+    float bias[RC_DC];  // forward: the group's bias per output channel (zero past DC or without one)
+};
+
+struct RowBand {
+    int n, seg, y0, y1, rs, re;  // output rows [y0, y1), source rows rs..re
+};
+
+// next band of this CTA's output rows [pos, end), flattened over (image,
+// segment, row); every role walks the same sequence
+__device__ __forceinline__ bool row_next_band(const RowConvParams &p, long long &pos,
+                                               long long end, RowBand &b) {
+    if (pos >= end) return false;
+    const long long col = pos / p.DH;
+    b.y0 = (int)(pos - col * p.DH);
+    b.y1 = (int)min((long long)p.DH, (long long)b.y0 + (end - pos));
+    b.n = (int)(col / p.nseg);
+    b.seg = (int)(col - (long long)b.n * p.nseg);
+    b.rs = max(b.y0 + p.oy_min, 0);
+    b.re = min(b.y1 - 1 + p.oy_max, p.SH - 1);
+    pos += b.y1 - b.y0;
+    return true;
+}
+
+template <int FH>
+__global__ void __launch_bounds__(RC_THREADS, 1)
+    row_conv_kernel(const __grid_constant__ RowConvParams p,
+                     const __grid_constant__ CUtensorMap wmap,
+                     const __grid_constant__ CUtensorMap smap) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char *base = reinterpret_cast<unsigned char *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    constexpr uint32_t kBlk = RC_DC * 128;      // one block: 64 rows of 128 bytes
+    constexpr uint32_t kTile = kBlk * FH;       // tap column u, one chunk
+    const uint32_t wchunk_bytes = kTile * (uint32_t)p.fw;
+    unsigned char *w_area = base;  // [chunk][u][j] blocks of 8 KB
+    unsigned char *s_area = base + (size_t)p.nchunk * wchunk_bytes;
+    RowConvSmem *sm = reinterpret_cast<RowConvSmem *>(s_area + (size_t)p.ns * RC_STRIP);
+    volatile int *abort = &sm->abort;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int cg = (int)(blockIdx.x % (unsigned)p.ncg);
+    const long long nbands = gridDim.x / p.ncg, band = blockIdx.x / p.ncg;
+    const long long r_begin = p.rows * band / nbands;
+    const long long r_end = p.rows * (band + 1) / nbands;
+    const int och0 = cg * RC_DC;
+
+    if (threadIdx.x == 0) {
+        for (int c = 0; c < p.nchunk; ++c) mbar_init(&sm->w_full[c], 1);
+        for (int i = 0; i < p.ns; ++i) {
+            mbar_init(&sm->s_full[i], 1);
+            mbar_init(&sm->s_empty[i], 1);
+        }
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(&sm->buf_full[i], 1);
+            mbar_init(&sm->buf_free[i], 256);
+        }
+        mbar_init(&sm->final_bar, 1);
+        sm->abort = 0;
+        fence_barrier_init();
+    }
+    if (threadIdx.x < RC_DC) {
+        const int c = och0 + (int)threadIdx.x;
+        sm->bias[threadIdx.x] = (p.bias && c < p.DC) ? p.bias[c] : 0.0f;
+    }
+    if (warp == 1) tmem_alloc(&sm->tmem_base, 512);
+    if (warp == 0 && lane == 0) {
+        prefetch_tmap(&wmap);
+        prefetch_tmap(&smap);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem_base = sm->tmem_base;
+
+    if (warp == 0) {
+        // ---------------- TMA producer: the weights once, then strips
+        if (lane == 0 && r_begin < r_end) {
+            for (int c = 0; c < p.nchunk; ++c) {
+                mbar_arrive_expect_tx(&sm->w_full[c], wchunk_bytes);
+                for (int t = 0; t < p.fw * FH; ++t)
+                    tma_load_2d(smem_u32(w_area + c * wchunk_bytes + t * kBlk), &wmap, &sm->w_full[c],
+                                p.wcol[t] + c * 64, och0);
+            }
+            int s = 0;
+            uint32_t ph = 1, nload = 0;
+            bool stop = false;
+            long long pos = r_begin;
+            RowBand b;
+            while (!stop && row_next_band(p, pos, r_end, b)) {
+                const int xs = b.seg * 128 + p.ox_min;
+                for (int r = b.rs; r <= b.re && !stop; ++r) {
+                    for (int c = 0; c < p.nchunk; ++c) {
+                        if (!mbar_wait(&sm->s_empty[s], ph, abort, 1u)) {
+                            stop = true;
+                            break;
+                        }
+                        mbar_arrive_expect_tx(&sm->s_full[s], (uint32_t)p.SL * 128u);
+                        tma_load_4d(smem_u32(s_area + s * RC_STRIP), &smap, &sm->s_full[s], c * 64, xs,
+                                    r, b.n);
+                        ++nload;
+                        if (++s == p.ns) {
+                            s = 0;
+                            ph ^= 1u;
+                        }
+                    }
+                }
+            }
+            if (stop) {
+                // the CTA is unwinding: let this thread's copies land before exit
+                // (bounded), the weights and the last ns strips
+                const unsigned limit = g_spin_limit;
+                for (int c = 0; c < p.nchunk; ++c) {
+                    unsigned n = 0;
+                    while (!mbar_try_wait(&sm->w_full[c], 0) && ++n < limit) {
+                    }
+                }
+                for (uint32_t l = nload > (uint32_t)p.ns ? nload - p.ns : 0; l < nload; ++l) {
+                    unsigned n = 0;
+                    while (!mbar_try_wait(&sm->s_full[l % p.ns], (l / p.ns) & 1u) && ++n < limit) {
+                    }
+                }
+            }
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ---------------- MMA issuer: one N = FH*64 MMA per K step into the
+        // source row's buffer; descriptors are bases plus 16-byte-unit offsets
+        if (lane == 0) {
+            const uint64_t a0 = smem_desc(smem_u32(s_area), 16, 1024);
+            const uint64_t b0 = smem_desc(smem_u32(w_area), 16, 1024);
+            const uint32_t tile16 = kTile >> 4, wchunk16 = wchunk_bytes >> 4;
+            const uint32_t strip16 = (uint32_t)RC_STRIP >> 4;
+            constexpr uint32_t idesc = idesc_bf16(128, FH * RC_DC, 0, 0);
+            int s = 0;
+            uint32_t sph = 0, soff = 0, it = 0;
+            bool wready = false, issued = false, stop = false;
+            long long pos = r_begin;
+            RowBand b;
+            while (!stop && row_next_band(p, pos, r_end, b)) {
+                for (int r = b.rs; r <= b.re; ++r, ++it) {
+                    const uint32_t bf = it & 1u, use = it >> 1;
+                    if (!mbar_wait(&sm->buf_free[bf], (use & 1u) ^ 1u, abort, 4u)) {
+                        stop = true;
+                        break;
+                    }
+                    tc_fence_after();
+                    const uint32_t d = tmem_base + bf * 256u;
+                    for (int c = 0; c < p.nchunk; ++c) {
+                        if (!wready && !mbar_wait(&sm->w_full[c], 0, abort, 2u)) {
+                            stop = true;
+                            break;
+                        }
+                        if (!mbar_wait(&sm->s_full[s], sph, abort, 8u)) {
+                            stop = true;
+                            break;
+                        }
+                        tc_fence_after();
+                        const uint64_t as = a0 + soff;
+                        const uint64_t bc = b0 + (uint32_t)c * wchunk16;
+                        for (int u = 0; u < p.fw; ++u) {
+                            const uint64_t au = as + p.a_view[u];
+                            const uint64_t bu = bc + (uint32_t)u * tile16;
+#pragma unroll
+                            for (int k = 0; k < 4; ++k)
+                                mma_f16(d, au + (uint32_t)(2 * k), bu + (uint32_t)(2 * k), idesc,
+                                        (c | u | k) != 0);
+                        }
+                        mma_commit(&sm->s_empty[s]);
+                        issued = true;
+                        if (++s == p.ns) {
+                            s = 0;
+                            soff = 0;
+                            sph ^= 1u;
+                        } else {
+                            soff += strip16;
+                        }
+                    }
+                    if (stop) break;
+                    wready = true;
+                    mma_commit(&sm->buf_full[bf]);
+                }
+            }
+            if (issued) {
+                mma_commit(&sm->final_bar);
+                unsigned n = 0;
+                while (!mbar_try_wait(&sm->final_bar, 0) && ++n < kSpinLimit) {
+                }
+            }
+        }
+        __syncwarp();
+    } else {
+        // ---------------- epilogue: warp w reads TMEM lanes 32*(w % 4) .., i.e.
+        // pixel seg*128 + 32*(w % 4) + lane, and channels 32*half .. +31 of
+        // each block (output channels och0 + ..); partial output rows P[i]
+        // (output row r - oy_max + 1 + i after source row r) stay in registers
+        const int qd = warp & 3, half = (warp - 2) >> 2;
+        const int cbase = 32 * half;
+        const long long plane = (long long)p.DW * p.DH;
+        const int nc = min(32, p.DC - och0 - cbase);  // this warp's real channels (may be <= 0)
+        const bool act = p.bias != nullptr || p.relu;
+        auto finish = [&](float v, int c) {
+            if (act) {
+                v += sm->bias[c];
+                if (p.relu && v < 0.0f) v = 0.0f;
+            }
+            return v;
+        };
+        uint32_t it = 0;
+        bool stop = false;
+        long long pos = r_begin;
+        RowBand b;
+        while (!stop && row_next_band(p, pos, r_end, b)) {
+            const int x = b.seg * 128 + 32 * qd + lane;
+            const bool xok = x < p.DW;
+            // channel cbase of this band's image at pixel x, row 0
+            float *img = p.dst + ((long long)b.n * p.DC + och0 + cbase) * plane + x;
+            float P[FH > 1 ? FH - 1 : 1][32];
+#pragma unroll
+            for (int i = 0; i < (FH > 1 ? FH - 1 : 1); ++i)
+#pragma unroll
+                for (int e = 0; e < 32; ++e) P[i][e] = 0.0f;
+            for (int r = b.rs; r <= b.re; ++r, ++it) {
+                const uint32_t bf = it & 1u, use = it >> 1;
+                if (!mbar_wait(&sm->buf_full[bf], use & 1u, abort, 32u)) {
+                    stop = true;
+                    break;
+                }
+                tc_fence_after();
+                const uint32_t taddr = tmem_base + bf * 256u + (uint32_t)cbase + ((uint32_t)(32 * qd) << 16);
+                const int y = r - p.oy_max;
+                const bool yok = xok && y >= b.y0 && y < b.y1;
+                float *q = img + (long long)y * p.DW;  // advances one channel plane per value
+#pragma unroll
+                for (int g = 0; g < 2; ++g) {
+                    uint32_t v[FH][16];
+#pragma unroll
+                    for (int j = 0; j < FH; ++j) tmem_ld16(taddr + (uint32_t)(j * RC_DC + 16 * g), v[j]);
+                    tmem_ld_wait();
+#pragma unroll
+                    for (int e = 0; e < 16; ++e) {
+                        const int ci = 16 * g + e;
+                        float o;
+                        if constexpr (FH == 1) {
+                            o = __uint_as_float(v[0][e]);
+                        } else {
+                            o = P[0][ci] + __uint_as_float(v[0][e]);
+#pragma unroll
+                            for (int i = 0; i + 2 < FH; ++i) P[i][ci] = P[i + 1][ci] + __uint_as_float(v[i + 1][e]);
+                            P[FH - 2][ci] = __uint_as_float(v[FH - 1][e]);
+                        }
+                        if (yok && ci < nc) *q = finish(o, cbase + ci);
+                        q += plane;
+                    }
+                }
+                tc_fence_before();
+                mbar_arrive(&sm->buf_free[bf]);
+            }
+            if (stop) break;
+            if constexpr (FH > 1) {
+                // the band's last rows: their remaining source rows lie past the image
+                // or outside the band
+#pragma unroll
+                for (int i = 0; i < FH - 1; ++i) {
+                    const int y = b.re - p.oy_max + 1 + i;
+                    if (!xok || y < b.y0 || y >= b.y1) continue;
+                    float *q = img + (long long)y * p.DW;
+#pragma unroll
+                    for (int ci = 0; ci < 32; ++ci) {
+                        if (ci < nc) *q = finish(P[i][ci], cbase + ci);
+                        q += plane;
+                    }
+                }
+            }
+        }
+    }
+
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        tc_fence_after();
+        tmem_dealloc(tmem_base, 512);
+    }
+}
+
+// ===========================================================================
 // filter gradient kernel
 // ===========================================================================
 constexpr int WG_STAGES = 4;
@@ -2093,12 +2430,10 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
 // a quarter of the MMA rows.  The gather kernel is measured faster on the
 // shapes both cover, so the strip kernel runs only when AFGB_NN_KERNEL=strip
 // selects it (its parity tests run that way).
+static int nn_kernel_choice();
+
 static bool strip_conv_fits(const NNGeom &g, int mode) {
-    static const int wanted = [] {
-        const char *e = std::getenv("AFGB_NN_KERNEL");
-        return e && std::strcmp(e, "strip") == 0 ? 1 : 0;
-    }();
-    if (!wanted) return false;
+    if (nn_kernel_choice() != 2) return false;
     if (g.sx != 1 || g.sy != 1 || g.fw * g.fh > MAX_T) return false;
     const long long DW = mode == 0 ? g.Wo : g.W, DC = mode == 0 ? g.K : g.C;
     if (DC > SC_MAXN || DW < 96) return false;
@@ -2191,6 +2526,149 @@ static void run_strip_conv(const NNGeom &g, int mode, const __nv_bfloat16 *img, 
     free_device(wt);
 }
 
+// Which stride-1 kernel serves a bf16 forward or data gradient: the row
+// kernel where its limits hold, unless AFGB_NN_KERNEL names "gather" or
+// "strip" (read once per process; the parity tests of the other kernels run
+// that way).
+static int nn_kernel_choice() {
+    static const int v = [] {
+        const char *e = std::getenv("AFGB_NN_KERNEL");
+        if (e && std::strcmp(e, "gather") == 0) return 1;
+        if (e && std::strcmp(e, "strip") == 0) return 2;
+        return 0;
+    }();
+    return v;
+}
+
+static size_t smem_optin() {
+    static const size_t v = [] {
+        int s = 0;
+        AFGB_CUDA(cudaDeviceGetAttribute(&s, cudaDevAttrMaxSharedMemoryPerBlockOptin, device()));
+        return (size_t)s;
+    }();
+    return v;
+}
+
+// The row kernel's plan for g (mode 0 forward, 1 data gradient); false when
+// its limits do not hold: unit strides and unit vertical dilation, filters at
+// most three rows high, at most 256 output channels, rows long enough that
+// 128-pixel segments waste at most a quarter of the MMA rows, strips of at
+// most RC_STRIP / 128 pixels, every output row reached by some source row
+// (py <= fh - 1), and the weights plus two strips within one CTA's shared
+// memory.
+static bool row_conv_plan(const NNGeom &g, int mode, RowConvParams &p, size_t &smem) {
+    if (nn_kernel_choice() != 0) return false;
+    if (g.sx != 1 || g.sy != 1 || g.dy != 1) return false;
+    if (g.fh > 3 || g.fw > 16 || g.fw * g.fh > RC_MAXTAP || g.py > g.fh - 1) return false;
+    const long long SW = mode == 0 ? g.W : g.Wo, SH = mode == 0 ? g.H : g.Ho;
+    const long long DW = mode == 0 ? g.Wo : g.W, DH = mode == 0 ? g.Ho : g.H;
+    const long long SC = mode == 0 ? g.C : g.K, DC = mode == 0 ? g.K : g.C;
+    if (DW < 96 || DC > RC_DC * RC_MAXCG || SW >= (1 << 24) || SH >= (1 << 24) || g.N >= (1 << 24))
+        return false;
+    const long long nseg = (DW + 127) / 128;
+    if ((nseg * 128 - DW) * 4 > nseg * 128) return false;
+    if ((g.fw - 1) * g.dx > RC_STRIP / 128 - 128) return false;
+    const int SCpad = round_up((int)SC, 64);
+    const int nchunk = SCpad / 64;
+    if (nchunk > RC_MAXCH) return false;
+    const size_t wbytes = (size_t)nchunk * g.fw * g.fh * RC_DC * 128;
+    const size_t fixed = 1024 + wbytes + sizeof(RowConvSmem) + 64;
+    if (fixed + 2 * (size_t)RC_STRIP > smem_optin()) return false;
+    std::memset(&p, 0, sizeof(p));
+    p.ns = (int)std::min<size_t>(RC_MAXNS, (smem_optin() - fixed) / RC_STRIP);
+    smem = fixed + (size_t)p.ns * RC_STRIP;
+    p.SW = (int)SW;
+    p.SH = (int)SH;
+    p.N = (int)g.N;
+    p.DW = (int)DW;
+    p.DH = (int)DH;
+    p.DC = (int)DC;
+    p.fw = (int)g.fw;
+    p.nchunk = nchunk;
+    p.nseg = (int)nseg;
+    p.ncg = (int)((DC + RC_DC - 1) / RC_DC);
+    p.rows = g.N * nseg * DH;
+    // source offsets of an output pixel: forward (u*dx - px, v - py), data
+    // gradient (px - u*dx, py - v); block j of a tap column holds filter row
+    // v_j, the one whose offset is oy_max - j
+    int oxmin = 1 << 30, oxmax = -(1 << 30);
+    for (int u = 0; u < g.fw; ++u) {
+        const int ox = mode == 0 ? u * (int)g.dx - (int)g.px : (int)g.px - u * (int)g.dx;
+        oxmin = std::min(oxmin, ox);
+        oxmax = std::max(oxmax, ox);
+    }
+    p.ox_min = oxmin;
+    p.SL = 128 + (oxmax - oxmin);
+    p.oy_min = mode == 0 ? -(int)g.py : (int)g.py - (int)(g.fh - 1);
+    p.oy_max = p.oy_min + (int)(g.fh - 1);
+    for (int u = 0; u < g.fw; ++u) {
+        const int ox = mode == 0 ? u * (int)g.dx - (int)g.px : (int)g.px - u * (int)g.dx;
+        p.a_view[u] = (uint32_t)(((ox - oxmin) * 128) >> 4);
+        for (int j = 0; j < g.fh; ++j) {
+            const int v = mode == 0 ? (int)(g.fh - 1) - j : j;
+            p.wcol[u * g.fh + j] = (u + (int)g.fw * v) * SCpad;
+        }
+    }
+    return true;
+}
+
+// Stride-1 forward (mode 0) or data gradient (mode 1) by the row kernel from
+// the source already in bf16 NHWC with channels padded to 64; false (nothing
+// launched) when row_conv_plan rejects the shape.
+static bool run_row_conv(const NNGeom &g, int mode, const __nv_bfloat16 *img, const float *w_f32,
+                          float *dst, const NNEpilogue *ep) {
+    RowConvParams p;
+    size_t smem = 0;
+    if (!row_conv_plan(g, mode, p, smem)) return false;
+    const int SC = mode == 0 ? (int)g.C : (int)g.K;
+    const int DC = p.DC;
+    const int SCpad = round_up(SC, 64);
+    const int OCpad = round_up(DC, 64);
+    const int taps = (int)(g.fw * g.fh);
+    __nv_bfloat16 *wt;
+    {
+        MemTag tag("weight operands");
+        wt = static_cast<__nv_bfloat16 *>(alloc_device((size_t)OCpad * taps * SCpad * 2));
+    }
+    {
+        const long long total = (long long)OCpad * taps * SCpad;
+        const unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
+        weights_bf16_kernel<<<blocks, 256, 0, stream()>>>(w_f32, (int)g.fw, (int)g.fh, (int)g.C,
+                                                          (int)g.K, mode, OCpad, SCpad, wt);
+        count_launch();
+        AFGB_POST_LAUNCH("weights_bf16_kernel");
+    }
+    p.dst = dst;
+    if (ep && mode == 0) {
+        p.bias = ep->bias;
+        p.relu = ep->relu;
+    }
+    CUtensorMap wmap = make_wmap(wt, OCpad, (long long)taps * SCpad, 2, RC_DC);
+    CUtensorMap smap = make_imap(img, SCpad, p.SW, p.SH, (int)g.N, p.SL, 1);
+    if (p.rows > 0) {
+        // bands of at least 8 rows (each band loads fh - 1 extra source rows),
+        // one CTA per band and channel group
+        const long long nbands = std::max(1LL, std::min<long long>(num_sms() / p.ncg, p.rows / 8));
+        const int grid = (int)(nbands * p.ncg);
+        KernelTimer kt(mode == 0 ? "tc_fwd_kernel" : "tc_dgrad_kernel");
+        KernelTimer kr("tc_row_kernel");  // which stride-1 kernel ran, for the tests
+#define AFGB_LAUNCH_ROW(FH)                                                                  \
+    do {                                                                                     \
+        AFGB_CUDA(cudaFuncSetAttribute(row_conv_kernel<FH>,                                 \
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)); \
+        row_conv_kernel<FH><<<grid, RC_THREADS, smem, stream()>>>(p, wmap, smap);           \
+    } while (0)
+        if (g.fh == 1) AFGB_LAUNCH_ROW(1);
+        else if (g.fh == 2) AFGB_LAUNCH_ROW(2);
+        else AFGB_LAUNCH_ROW(3);
+#undef AFGB_LAUNCH_ROW
+        count_launch();
+        AFGB_POST_LAUNCH("row_conv_kernel");
+    }
+    free_device(wt);
+    return true;
+}
+
 // the gather kernel's limits: phases and taps fit the parameter block,
 // 32-bit pixel coordinates
 static bool gather_fits(const NNGeom &g, int mode) {
@@ -2236,21 +2714,26 @@ bool tc_forward(const NNGeom &g, const Array &sig, const Array &filt, Array &out
     bool owned = false;
     const __nv_bfloat16 *x = signal_nhwc(sig, (int)g.W, (int)g.H, (int)g.C, (int)g.N,
                                          round_up((int)g.C, 64), owned);
-    if (strip_conv_fits(g, 0))
+    if (run_row_conv(g, 0, x, filt.ptr<float>(), out.ptr<float>(), ep)) {
+    } else if (strip_conv_fits(g, 0)) {
         run_strip_conv(g, 0, x, filt.ptr<float>(), out.ptr<float>(), ep);
-    else
+    } else {
         run_gather(g, 0, nullptr, filt.ptr<float>(), out.ptr<float>(), false, nullptr, nullptr, x,
                    ep);
+    }
     if (owned) free_device(const_cast<__nv_bfloat16 *>(x));
     return true;
 }
 
 bool tc_data_grad(const NNGeom &g, const Array &grad, const Array &filt, Array &dx) {
     if (grad.type != f32 || !gather_fits(g, 1)) return false;
-    if (strip_conv_fits(g, 1)) {
+    RowConvParams rp;
+    size_t rsm = 0;
+    if (row_conv_plan(g, 1, rp, rsm) || strip_conv_fits(g, 1)) {
         const int Kp = round_up((int)g.K, 64);
         __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kp);
-        run_strip_conv(g, 1, gg, filt.ptr<float>(), dx.ptr<float>(), nullptr);
+        if (!run_row_conv(g, 1, gg, filt.ptr<float>(), dx.ptr<float>(), nullptr))
+            run_strip_conv(g, 1, gg, filt.ptr<float>(), dx.ptr<float>(), nullptr);
         free_device(gg);
         return true;
     }
@@ -2467,10 +2950,12 @@ bool tc_data_filter_grads(const NNGeom &g, const Array &grad, const Array &sig, 
     if (grad.type != f32 || !gather_fits(g, 1)) return false;
     const int Kpad = round_up((int)g.K, 64);
     __nv_bfloat16 *gg = to_nhwc(grad.ptr<float>(), (int)g.Wo, (int)g.Ho, (int)g.K, (int)g.N, Kpad);
-    if (strip_conv_fits(g, 1))
+    if (run_row_conv(g, 1, gg, filt.ptr<float>(), dx.ptr<float>(), nullptr)) {
+    } else if (strip_conv_fits(g, 1)) {
         run_strip_conv(g, 1, gg, filt.ptr<float>(), dx.ptr<float>(), nullptr);
-    else
+    } else {
         run_gather(g, 1, nullptr, filt.ptr<float>(), dx.ptr<float>(), false, nullptr, nullptr, gg);
+    }
     filter_grad_from(g, gg, Kpad, sig, dw);
     free_device(gg);
     return true;
