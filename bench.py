@@ -65,7 +65,7 @@ NN_OTHER = {
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) per launch of each
 # tensor-core kernel on NN_SHAPE, from one ncu capture of `bench.py --only
 # fwd|dgrad|wgrad` (ncu cannot run inside the timed bench)
-NCU_TRAFFIC = {"tc_fwd_kernel": 67.30e6 + 212.86e6, "tc_dgrad_kernel": 134.60e6 + 90.88e6,
+NCU_TRAFFIC = {"tc_fwd_kernel": 69.68e6 + 207.37e6, "tc_dgrad_kernel": 143.89e6 + 85.84e6,
                "tc_wgrad_kernel": 206.02e6 + 18.06e6}
 MAIN_KERNELS = ("simt_fwd_kernel", "simt_dgrad_kernel", "simt_wgrad_kernel", "tc_fwd_kernel",
                 "tc_fwd_fp8_kernel", "tc_dgrad_kernel", "tc_wgrad_kernel", "tc_convert_kernel",
