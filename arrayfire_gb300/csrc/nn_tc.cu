@@ -1465,11 +1465,17 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
 // ===========================================================================
 // filter gradient, stride 1 along x: one signal strip per filter row
 // ===========================================================================
-// A stage is a rectangle of 64 output pixels (BY rows of BX).  For each of
-// its rows the producer loads one strip of BX + (nu-1)*dx signal pixels
-// (64 channels each), and the nu taps u0..u0+nu-1 of filter row v read it at
-// row offsets u*dx: nine shifted 8 KB tiles become three ~8.5 KB strips for
-// a 3x3 filter.  One MMA per K step covers the row's taps: B (MN-major) has
+// A stage is a rectangle of KP = 64 or 128 output pixels (BY rows of BX).  For
+// each of its rows the producer loads one strip of BX + (nu-1)*dx signal
+// pixels (64 channels each), and the nu taps u0..u0+nu-1 of filter row v read
+// it at row offsets u*dx: nine shifted tiles become three strips for a 3x3
+// filter.  The SM's copy engine completes about one TMA copy per 400 cycles
+// whatever its size up to 18 KB (measured: 8 KB copies move 21 bytes per
+// cycle, 16 KB copies 42), so a stage of 128 pixels, two 16 KB
+// incoming-gradient boxes and one ~17 KB strip, feeds twice the MMA work of a
+// 64-pixel stage for the same three copies.  (Tiles of two filter rows
+// sharing the incoming-gradient operand were measured slower: 0.078 against
+// 0.066 ms on 128x128x64x32.)  One MMA per K step covers the row's taps: B (MN-major) has
 // one 64-channel N atom per tap, the atoms dx rows apart (LBO = dx * 128
 // bytes, overlapping), each starting inside the strip at any 128-byte row;
 // the 128-byte
@@ -1490,6 +1496,7 @@ struct StripParams {
     int UB, nub;             // taps per tile along u, u-blocks per filter row
     int nchunk, n_k_tiles;
     int SL, strip_bytes, stage_bytes, nst;
+    int KP, a_bytes;         // pixels per stage (MMA K: 64 or 128), incoming-gradient bytes per stage
     long long Q, chunk;      // pixel blocks, blocks per split
 };
 
@@ -1547,7 +1554,7 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            const uint32_t bytes = WG_A_BYTES + (uint32_t)(p.BY * p.SL * 128);
+            const uint32_t bytes = (uint32_t)p.a_bytes + (uint32_t)(p.BY * p.SL * 128);
             // consecutive pixel blocks: (tx, ty, n) advance without division
             int tx = (int)(q_begin % p.ntx);
             const long long r0 = q_begin / p.ntx;
@@ -1561,9 +1568,9 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
                 mbar_arrive_expect_tx(&sm->full[s], bytes);
                 const uint32_t sa = smem_u32(stage);
                 tma_load_4d(sa, &gmap, &sm->full[s], k0, x0, y0, n);
-                tma_load_4d(sa + 8192, &gmap, &sm->full[s], k0 + 64, x0, y0, n);
+                tma_load_4d(sa + p.KP * 128, &gmap, &sm->full[s], k0 + 64, x0, y0, n);
                 for (int j = 0; j < p.BY; ++j)
-                    tma_load_4d(sa + WG_A_BYTES + j * p.strip_bytes, &smap, &sm->full[s], cchunk * 64,
+                    tma_load_4d(sa + p.a_bytes + j * p.strip_bytes, &smap, &sm->full[s], cchunk * 64,
                                 x0 - p.px + u0 * p.dx, (y0 + j) * p.sy - p.py + v * p.dy, n);
                 if (++s == p.nst) {
                     s = 0;
@@ -1588,11 +1595,12 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
             // one MMA per K step covers all nu taps: B's N atoms (64 channels
             // each) are the tap-shifted views of the strip, dx rows apart
             const uint32_t idesc = idesc_bf16(128, (uint32_t)(64 * nu), 1, 1);
-            const uint64_t a0 = smem_desc(smem_u32(base), 8192, 1024);
-            const uint64_t b0 = smem_desc(smem_u32(base) + WG_A_BYTES, (uint32_t)p.dx * 128u, 1024);
-            uint32_t bk[WG_KP / 16];  // per K step: strip 16k/BX, row 16k%BX
+            const uint64_t a0 = smem_desc(smem_u32(base), (uint32_t)p.KP * 128u, 1024);
+            const uint64_t b0 = smem_desc(smem_u32(base) + (uint32_t)p.a_bytes, (uint32_t)p.dx * 128u, 1024);
+            const int ksteps = p.KP / 16;
+            uint32_t bk[8];  // per K step: strip 16k/BX, row 16k%BX
 #pragma unroll
-            for (int k = 0; k < WG_KP / 16; ++k)
+            for (int k = 0; k < 8; ++k)
                 bk[k] = (uint32_t)(((16 * k) / p.BX) * p.strip_bytes + ((16 * k) % p.BX) * 128) >> 4;
             const uint32_t stage_step = (uint32_t)p.stage_bytes >> 4;
             uint32_t soff = 0, phase = 0;
@@ -1601,10 +1609,10 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
                 if (!mbar_wait(&sm->full[s], phase, abort, 64u)) break;
                 tc_fence_after();
 #pragma unroll
-                for (int k = 0; k < WG_KP / 16; ++k) {
-                    mma_f16(tmem_base, a0 + soff + (uint32_t)k * 128u, b0 + soff + bk[k], idesc,
-                            (st | k) != 0);
-                }
+                for (int k = 0; k < 8; ++k)
+                    if (k < ksteps)
+                        mma_f16(tmem_base, a0 + soff + (uint32_t)k * 128u, b0 + soff + bk[k], idesc,
+                                (st | k) != 0);
                 mma_commit(&sm->empty[s]);
                 if (++s == p.nst) {
                     s = 0;
@@ -1617,9 +1625,17 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
             mma_commit(&sm->tmem_full);
         }
         __syncwarp();
-        // epilogue: warps 4-7 (TMEM lanes 32*(warp-4) ...); waits for the
-        // MMAs even when aborting, so TMEM is never freed under them
-        const int q = warp - 4;
+    }
+    // ---------------- epilogue, all eight warps (warp w reads TMEM lanes
+    // 32*(w % 4) .., i.e. k = k0 + 32*(w % 4) + lane, and takes every other
+    // tap); waits for the MMAs even when aborting, so TMEM is never freed
+    // under them.  The partial sums of one tap are 64 rows (c) of K floats:
+    // with K a multiple of 4 they go through the now idle stage area, one
+    // 32 KB tile [c][128 k] per tap, conflict-free shared stores, then bulk
+    // copies (one per tap when K is 128, else one per row);
+    // otherwise each thread stores its k column directly.
+    {
+        const int q = warp & 3, h = warp >> 2;
         bool have = false;
         if (nstages > 0) {
             have = mbar_wait_sleep(&sm->tmem_full, 0);
@@ -1632,23 +1648,69 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
         const int k = k0 + 32 * q + lane;
         const long long rows = (long long)p.C * p.fw * p.fh;
         float *out = p.partial + (long long)blockIdx.y * rows * p.K;
-        for (int cc = 0; cc < nu * 4; ++cc) {
-            uint32_t r[16];
-            if (have) {
-                tmem_ld16(tmem_base + cc * 16 + ((uint32_t)(32 * q) << 16), r);
-                tmem_ld_wait();
-            } else {
-#pragma unroll
-                for (int e = 0; e < 16; ++e) r[e] = 0u;
+        const int ntap = nu;
+        const int nrow = min(64, p.C - cchunk * 64);  // real c rows of a tap tile
+        const int kcnt = min(128, p.K - k0);          // real k of a row
+        const bool staged = (p.K & 3) == 0;
+        const int slots = max(1, (p.nst * p.stage_bytes) / (64 * 128 * 4));
+        auto tap_of = [&](int i) { return (u0 + i) + p.fw * v; };  // the tile's i-th tap
+        for (int r0 = 0; r0 < ntap; r0 += slots) {
+            const int rn = min(slots, ntap - r0);
+            if (staged && r0 > 0) {
+                if (threadIdx.x == 0) bulk_wait_read();  // the last round's copies have read the slots
+                __syncthreads();
             }
-            if (k >= p.K || *abort) continue;
-            const int tap = (u0 + cc / 4) + p.fw * v;
+            for (int i = r0 + h; i < r0 + rn; i += 2) {
+                uint32_t v[4][16];
+                if (have) {
 #pragma unroll
-            for (int e = 0; e < 16; ++e) {
-                const int c = cchunk * 64 + (cc & 3) * 16 + e;
-                if (c < p.C) out[((long long)c + (long long)p.C * tap) * p.K + k] = __uint_as_float(r[e]);
+                    for (int g = 0; g < 4; ++g)
+                        tmem_ld16(tmem_base + (uint32_t)(i * 64 + 16 * g) + ((uint32_t)(32 * q) << 16), v[g]);
+                    tmem_ld_wait();
+                } else {
+#pragma unroll
+                    for (int g = 0; g < 4; ++g)
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) v[g][e] = 0u;
+                }
+                if (*abort) continue;
+                if (staged) {
+                    float *tile = reinterpret_cast<float *>(base) + (size_t)(i - r0) * (64 * 128);
+#pragma unroll
+                    for (int g = 0; g < 4; ++g)
+#pragma unroll
+                        for (int e = 0; e < 16; ++e)
+                            tile[(16 * g + e) * 128 + 32 * q + lane] = __uint_as_float(v[g][e]);
+                } else if (k < p.K) {
+                    const int tap = tap_of(i);
+#pragma unroll
+                    for (int g = 0; g < 4; ++g)
+#pragma unroll
+                        for (int e = 0; e < 16; ++e) {
+                            const int c = cchunk * 64 + 16 * g + e;
+                            if (c < p.C) out[((long long)c + (long long)p.C * tap) * p.K + k] = __uint_as_float(v[g][e]);
+                        }
+                }
+            }
+            if (!staged) continue;
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (threadIdx.x == 0 && !*abort) {
+                for (int i = r0; i < r0 + rn; ++i) {
+                    const uint32_t src = smem_u32(base) + (uint32_t)((i - r0) * 64 * 128 * 4);
+                    float *dst = out + ((long long)p.C * tap_of(i) + cchunk * 64) * p.K + k0;
+                    if (p.K == 128) {  // whole rows of 128 k: the tile is contiguous in the partials
+                        bulk_store(dst, src, (uint32_t)(nrow * 128 * 4));
+                    } else {
+                        for (int c = 0; c < nrow; ++c)
+                            bulk_store(dst + (long long)c * p.K, src + (uint32_t)(c * 128 * 4),
+                                       (uint32_t)(kcnt * 4));
+                    }
+                }
+                bulk_commit();
             }
         }
+        if (staged && threadIdx.x == 0) bulk_wait_all();  // copies done before the CTA exits
     }
     tc_fence_before();
     __syncthreads();
@@ -2749,13 +2811,21 @@ static bool run_wgrad_strip(const NNGeom &g, const __nv_bfloat16 *x, const __nv_
     if (g.sx != 1 || g.sy > 8 || g.fw * g.fh > 64 || g.fw < 2) return false;
     StripParams p;
     std::memset(&p, 0, sizeof(p));
-    if (!pick_rect((int)g.Wo, (int)g.Ho, WG_KP, 16, p.BX, p.BY)) return false;
+    // stages of 128 pixels where the rows allow: every TMA copy costs about
+    // 400 cycles of the SM's copy engine whatever its size (measured, up to
+    // 18 KB), so fewer, larger copies per MMA cycle
+    p.KP = 128;
+    if (!pick_rect((int)g.Wo, (int)g.Ho, 128, 64, p.BX, p.BY)) {
+        p.KP = 64;
+        if (!pick_rect((int)g.Wo, (int)g.Ho, 64, 16, p.BX, p.BY)) return false;
+    }
+    p.a_bytes = 2 * p.KP * 128;
     p.nub = (int)((g.fw + 3) / 4);
     p.UB = (int)((g.fw + p.nub - 1) / p.nub);
     p.SL = p.BX + (p.UB - 1) * (int)g.dx;
     if (p.SL > 256) return false;
     p.strip_bytes = (p.SL * 128 + 1023) / 1024 * 1024;
-    p.stage_bytes = WG_A_BYTES + p.BY * p.strip_bytes;
+    p.stage_bytes = p.a_bytes + p.BY * p.strip_bytes;
     p.nst = std::min(WS_MAXST, WS_SMEM / p.stage_bytes);
     if (p.nst < 2) return false;
     p.x = x;

@@ -139,6 +139,13 @@ __device__ __forceinline__ void tma_store_4d(const CUtensorMap *map, uint32_t sr
         "r"(src), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
         : "memory");
 }
+// shared -> global contiguous copy (bulk async group): both addresses 16-byte
+// aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_store(void *gdst, uint32_t ssrc, uint32_t bytes) {
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(ssrc),
+                 "r"(bytes)
+                 : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 // the shared sources of this thread's committed bulk stores may be reused
 __device__ __forceinline__ void bulk_wait_read() {
