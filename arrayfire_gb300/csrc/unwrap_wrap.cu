@@ -470,6 +470,86 @@ __global__ void __launch_bounds__(WT_THREADS) wrap_tiled_kernel(const T *__restr
     }
 }
 
+// af_wrap, column layout, stride 1 and WX x WY windows (3 x 3: the NN
+// im2col geometry): a tile is TY output rows across the whole image width.
+// The patches of the window rows covering it are one contiguous run of the
+// patch matrix (nwy rows x nx windows x WX*WY elements, one 16-byte phase),
+// staged with 16-byte asynchronous copies; then each thread sums its pixels'
+// elements from shared memory, window rows ascending and windows along x
+// ascending (the reference's order, as the tiled kernel sums them), with
+// fixed offsets for interior pixels.  Consecutive pixels read elements
+// WX*WY - 1 apart (8 for 3 x 3: eight lanes per bank group), and about 30
+// instructions per pixel replace the tiled kernel's 470.
+constexpr int WS1_THREADS = 256;
+
+template <typename T, int WX, int WY>
+__global__ void __launch_bounds__(WS1_THREADS) wrap_s1_kernel(const T *__restrict__ in,
+                                                              T *__restrict__ out, PatchGeom g,
+                                                              PatchDivs f, int TY, int tiles_y) {
+    constexpr int WSZ = WX * WY;
+    constexpr int VEC = vec_of<T>();
+    extern __shared__ __align__(16) unsigned char wrap_smem[];
+    T *sm = reinterpret_cast<T *>(wrap_smem);
+    const int nx = (int)g.nx, ny = (int)g.ny, W = (int)g.W, H = (int)g.H;
+    const int px = (int)g.px, py = (int)g.py;
+    const long long np = g.nx * g.ny;
+    const int ty = (int)(blockIdx.x % (unsigned)tiles_y);
+    const long long s = blockIdx.x / (unsigned)tiles_y;
+    const int y0 = ty * TY, y1 = min(y0 + TY, H) - 1;
+    const int wy_lo = max(0, y0 + py - WY + 1), wy_hi = min(ny - 1, y1 + py);
+    const long long gstart = (long long)WSZ * ((long long)nx * wy_lo + np * s);
+    const int phase = (int)(gstart & (VEC - 1));
+    if (wy_hi >= wy_lo) {
+        const int run = WSZ * nx * (wy_hi - wy_lo + 1);
+        const T *src = in + (gstart - phase);
+        const int nchunks = (phase + run + VEC - 1) / VEC;
+        for (int c = threadIdx.x; c < nchunks; c += WS1_THREADS) {
+            const int e0 = c * VEC - phase;
+            if (e0 >= 0 && e0 + VEC <= run) {
+                stage16(sm + c * VEC, src + c * VEC);
+            } else {
+#pragma unroll
+                for (int j = 0; j < VEC; ++j)
+                    if (e0 + j >= 0 && e0 + j < run) sm[c * VEC + j] = src[c * VEC + j];
+            }
+        }
+    }
+    stage_wait();
+    __syncthreads();
+    const T *run0 = sm + phase;  // element e of the staged run
+    const long long z = s % g.d2, w = s / g.d2;
+    T *oslice = out + z * g.os[2] + w * g.os[3];
+    const int npix = (y1 - y0 + 1) * W;
+    const int rstep = nx * WSZ - WX;  // next window row: tap row - 1
+    for (int q = threadIdx.x; q < npix; q += WS1_THREADS) {
+        const int ly = (int)fdiv((uint32_t)q, f.W), x = q - ly * W, y = y0 + ly;
+        const int ax = x + px, ay = y + py;
+        const int cx_lo = max(0, ax - WX + 1), cx_hi = min(nx - 1, ax);
+        const int cy_lo = max(0, ay - WY + 1), cy_hi = min(ny - 1, ay);
+        T *op = oslice + x * g.os[0] + y * g.os[1];
+        T acc = g.zero_init ? pzero<T>() : *op;
+        // element of window (cx_lo, cy_lo) at tap (ax - cx_lo, ay - cy_lo)
+        const T *p0 = run0 + ((cy_lo - wy_lo) * nx + cx_lo) * WSZ + (ax - cx_lo) + WX * (ay - cy_lo);
+        if (cx_hi - cx_lo == WX - 1 && cy_hi - cy_lo == WY - 1) {
+            T v[WSZ];
+#pragma unroll
+            for (int r = 0; r < WY; ++r)
+#pragma unroll
+                for (int j = 0; j < WX; ++j) v[r * WX + j] = p0[r * rstep + j * (WSZ - 1)];
+#pragma unroll
+            for (int e = 0; e < WSZ; ++e) acc = padd<T>(acc, v[e]);
+        } else {
+            const int nr = cy_hi - cy_lo + 1, nc = cx_hi - cx_lo + 1;
+#pragma unroll
+            for (int r = 0; r < WY; ++r)
+#pragma unroll
+                for (int j = 0; j < WX; ++j)
+                    if (r < nr && j < nc) acc = padd<T>(acc, p0[r * rstep + j * (WSZ - 1)]);
+        }
+        *op = acc;
+    }
+}
+
 // af_wrap, row layout: one thread per pixel of a 32 x 8 tile, reading the
 // patch elements straight from global memory -- for a given tap consecutive
 // windows are consecutive elements, so a warp's reads coalesce when sx = 1 --
@@ -616,6 +696,25 @@ static bool wrap_tiled_plan(const PatchGeom &g, size_t esize, const void *in, Wr
     return true;
 }
 
+// the stride-1 3 x 3 column-layout kernel: rows of tiles up to 16 deep whose
+// staged run fits 48 KB (four blocks per SM), 32-bit offsets
+static bool wrap_s1_plan(const PatchGeom &g, size_t esize, const void *in, int &TY, int &tiles_y,
+                         size_t &smem) {
+    if (!g.is_column || g.sx != 1 || g.sy != 1 || g.wx != 3 || g.wy != 3) return false;
+    if (((uintptr_t)in % 16) != 0 || g.W <= 0 || g.H <= 0 || g.nx <= 0 || g.ny <= 0) return false;
+    if (g.W >= (1 << 24) || g.H >= (1 << 24) || std::llabs(g.px) > 2 || std::llabs(g.py) > 2) return false;
+    const long long row_bytes = 9 * g.nx * (long long)esize;
+    const long long budget = 48 * 1024 - 16;
+    TY = (int)std::min<long long>(16, budget / row_bytes - 2);
+    if (TY < 1) return false;
+    TY = (int)std::min<long long>(TY, g.H);
+    tiles_y = (int)((g.H + TY - 1) / TY);
+    if ((long long)tiles_y * g.slices > 0x7fffffffll) return false;
+    if ((long long)(TY + 2) * g.W >= (1 << 30)) return false;
+    smem = (size_t)((TY + 2) * row_bytes + 16);
+    return true;
+}
+
 template <typename T>
 static void launch_wrap(const Array &in, Array &out, const PatchGeom &g) {
     const long long total = g.W * g.H * g.slices;
@@ -623,6 +722,20 @@ static void launch_wrap(const Array &in, Array &out, const PatchGeom &g) {
     WrapTile wt;
     size_t smem = 0;
     const PatchDivs f = patch_divs(g);
+    int TY = 0, tiles_y = 0;
+    if (wrap_s1_plan(g, sizeof(T), in.data(), TY, tiles_y, smem)) {
+        const unsigned blocks = (unsigned)((long long)tiles_y * g.slices);
+        AFGB_CUDA(cudaFuncSetAttribute(wrap_s1_kernel<T, 3, 3>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        {
+            KernelTimer kt("wrap_s1_kernel");
+            wrap_s1_kernel<T, 3, 3><<<blocks, WS1_THREADS, smem, stream()>>>(in.ptr<T>(), out.ptr<T>(),
+                                                                              g, f, TY, tiles_y);
+        }
+        count_launch();
+        AFGB_POST_LAUNCH("wrap_s1_kernel");
+        return;
+    }
     if (wrap_tiled_plan(g, sizeof(T), in.data(), wt, smem)) {
         const unsigned blocks = (unsigned)((long long)wt.tiles_x * wt.tiles_y * g.slices);
         if (g.is_column) {

@@ -60,7 +60,10 @@ def test_kernels_launch(af):
     a = af.Array.from_numpy(np.ones((16, 16), np.float32))
     n, U = _ran(af, "unwrap_rows_kernel", lambda: af.unwrap(a, 3, 3, 1, 1, 1, 1))
     assert n == 1
-    n, _ = _ran(af, "wrap_tiled_kernel", lambda: af.wrap(U, 16, 16, 3, 3, 1, 1, 1, 1))
+    n, _ = _ran(af, "wrap_s1_kernel", lambda: af.wrap(U, 16, 16, 3, 3, 1, 1, 1, 1))
+    assert n == 1
+    U2 = af.unwrap(a, 3, 3, 2, 2, 1, 1)
+    n, _ = _ran(af, "wrap_tiled_kernel", lambda: af.wrap(U2, 16, 16, 3, 3, 2, 2, 1, 1))
     assert n == 1
     R = af.unwrap(a, 3, 3, 1, 1, 1, 1, False)
     n, _ = _ran(af, "wrap_rows_kernel", lambda: af.wrap(R, 16, 16, 3, 3, 1, 1, 1, 1, False))
@@ -243,3 +246,32 @@ def test_patch_units_and_tiles_match_oracle(af, oracle, dt, col, shape, geo):
     W = af.wrap(af.Array.from_numpy(pm, dt), shape[0], shape[1], wx, wy, sx, sy, px, py, col)
     ref_w = oracle.wrap_patches(pm, shape[0], shape[1], wx, wy, sx, sy, px, py, col)
     assert W.to_numpy().tobytes(order="F") == ref_w.tobytes(order="F")
+
+
+WRAP_S1 = [
+    # (W, H, d2, d3), pad, dtype: several row tiles, ragged widths, every pad the kernel takes
+    ((131, 77, 3, 2), 1, C.F32),
+    ((128, 40, 2, 1), 0, C.F64),
+    ((97, 35, 2, 2), 2, C.S16),
+    ((64, 64, 1, 3), 1, C.C32),
+]
+
+
+@pytest.mark.parametrize("case", WRAP_S1, ids=lambda c: f"{c[0][0]}x{c[0][1]}p{c[1]}_{C.DT_NAME[c[2]]}")
+def test_wrap_s1_kernel_matches_oracle(af, oracle, case):
+    """The stride-1 3x3 column-layout wrap (row tiles staged as one contiguous
+    run) against the oracle, bit for bit, over several row tiles per slice; and
+    wrap_v2 adding into an existing output."""
+    (W, H, d2, d3), pad, dt = case
+    nx, ny = W + 2 * pad - 2, H + 2 * pad - 2
+    pm = C.patch_values(dt, (9, nx * ny, d2, d3), 7700 + W)
+    P = af.Array.from_numpy(pm)
+    n, out = _ran(af, "wrap_s1_kernel", lambda: af.wrap(P, W, H, 3, 3, 1, 1, pad, pad))
+    assert n == 1
+    want = oracle.wrap_patches(pm, W, H, 3, 3, 1, 1, pad, pad)
+    assert digest(out.to_numpy()) == digest(want)
+    base_np = C.patch_values(dt, (W, H, d2, d3), 7800 + W)
+    base = af.Array.from_numpy(base_np)
+    af.wrap_v2(base, P, W, H, 3, 3, 1, 1, pad, pad)
+    want2 = oracle.wrap_patches(pm, W, H, 3, 3, 1, 1, pad, pad, out=base_np)
+    assert digest(base.to_numpy()) == digest(want2)
