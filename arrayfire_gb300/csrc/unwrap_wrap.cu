@@ -470,22 +470,23 @@ __global__ void __launch_bounds__(WT_THREADS) wrap_tiled_kernel(const T *__restr
     }
 }
 
-// af_wrap, column layout, stride 1 and WX x WY windows (3 x 3: the NN
-// im2col geometry): a tile is TY output rows across the whole image width.
-// The patches of the window rows covering it are one contiguous run of the
-// patch matrix (nwy rows x nx windows x WX*WY elements, one 16-byte phase),
-// staged with 16-byte asynchronous copies; then each thread sums its pixels'
-// elements from shared memory, window rows ascending and windows along x
-// ascending (the reference's order, as the tiled kernel sums them), with
-// fixed offsets for interior pixels.  Consecutive pixels read elements
-// WX*WY - 1 apart (8 for 3 x 3: eight lanes per bank group), and about 30
-// instructions per pixel replace the tiled kernel's 470.
+// af_wrap, stride 1 and WX x WY windows (3 x 3: the NN im2col geometry): a
+// tile is TY output rows across the whole image width.  The patches of the
+// window rows covering it are contiguous in the patch matrix: one run of
+// nwy rows x nx windows x WX*WY elements in the column layout, one run of
+// nwy x nx windows per tap plane in the row layout.  The block stages the
+// run(s) with 16-byte asynchronous copies (each run keeps its global 16-byte
+// phase); then each thread sums its pixels' elements from shared memory,
+// window rows ascending and windows along x ascending (the reference's
+// order, as the tiled kernel sums them), with fixed offsets for interior
+// pixels.  About 30 instructions per pixel replace the tiled kernel's 470.
 constexpr int WS1_THREADS = 256;
 
-template <typename T, int WX, int WY>
+template <typename T, int WX, int WY, bool COL>
 __global__ void __launch_bounds__(WS1_THREADS) wrap_s1_kernel(const T *__restrict__ in,
                                                               T *__restrict__ out, PatchGeom g,
-                                                              PatchDivs f, int TY, int tiles_y) {
+                                                              PatchDivs f, int TY, int tiles_y,
+                                                              int pitch) {
     constexpr int WSZ = WX * WY;
     constexpr int VEC = vec_of<T>();
     extern __shared__ __align__(16) unsigned char wrap_smem[];
@@ -497,54 +498,95 @@ __global__ void __launch_bounds__(WS1_THREADS) wrap_s1_kernel(const T *__restric
     const long long s = blockIdx.x / (unsigned)tiles_y;
     const int y0 = ty * TY, y1 = min(y0 + TY, H) - 1;
     const int wy_lo = max(0, y0 + py - WY + 1), wy_hi = min(ny - 1, y1 + py);
-    const long long gstart = (long long)WSZ * ((long long)nx * wy_lo + np * s);
-    const int phase = (int)(gstart & (VEC - 1));
-    if (wy_hi >= wy_lo) {
-        const int run = WSZ * nx * (wy_hi - wy_lo + 1);
-        const T *src = in + (gstart - phase);
-        const int nchunks = (phase + run + VEC - 1) / VEC;
-        for (int c = threadIdx.x; c < nchunks; c += WS1_THREADS) {
-            const int e0 = c * VEC - phase;
-            if (e0 >= 0 && e0 + VEC <= run) {
-                stage16(sm + c * VEC, src + c * VEC);
-            } else {
+    const int nwy = max(0, wy_hi - wy_lo + 1);
+    // run q (COL: the one run; ROW: tap plane q) starts at global element
+    // gs(q) and is staged at sm + q * pitch, its phase first
+    auto gs = [&](int q) {
+        return COL ? (long long)WSZ * ((long long)nx * wy_lo + np * s)
+                   : np * ((long long)q + WSZ * s) + (long long)nx * wy_lo;
+    };
+    constexpr int NRUN = COL ? 1 : WSZ;
+    const int run = (COL ? WSZ : 1) * nx * nwy;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (nwy > 0) {
+        for (int q = COL ? 0 : warp; q < NRUN; q += (COL ? 1 : WS1_THREADS / 32)) {
+            const long long g0 = gs(q);
+            const int phase = (int)(g0 & (VEC - 1));
+            const T *src = in + (g0 - phase);
+            T *dst = sm + q * pitch;
+            const int nchunks = (phase + run + VEC - 1) / VEC;
+            const int t0 = COL ? threadIdx.x : lane, tstep = COL ? WS1_THREADS : 32;
+            for (int c = t0; c < nchunks; c += tstep) {
+                const int e0 = c * VEC - phase;
+                if (e0 >= 0 && e0 + VEC <= run) {
+                    stage16(dst + c * VEC, src + c * VEC);
+                } else {
 #pragma unroll
-                for (int j = 0; j < VEC; ++j)
-                    if (e0 + j >= 0 && e0 + j < run) sm[c * VEC + j] = src[c * VEC + j];
+                    for (int j = 0; j < VEC; ++j)
+                        if (e0 + j >= 0 && e0 + j < run) dst[c * VEC + j] = src[c * VEC + j];
+                }
             }
         }
     }
     stage_wait();
     __syncthreads();
-    const T *run0 = sm + phase;  // element e of the staged run
     const long long z = s % g.d2, w = s / g.d2;
     T *oslice = out + z * g.os[2] + w * g.os[3];
     const int npix = (y1 - y0 + 1) * W;
-    const int rstep = nx * WSZ - WX;  // next window row: tap row - 1
-    for (int q = threadIdx.x; q < npix; q += WS1_THREADS) {
-        const int ly = (int)fdiv((uint32_t)q, f.W), x = q - ly * W, y = y0 + ly;
+    int pb[COL ? 1 : WSZ];  // row layout: tap plane k's staged window 0
+#pragma unroll
+    for (int k = 0; k < (COL ? 1 : WSZ); ++k) pb[k] = k * pitch + (int)(gs(k) & (VEC - 1));
+    for (int qp = threadIdx.x; qp < npix; qp += WS1_THREADS) {
+        const int ly = (int)fdiv((uint32_t)qp, f.W), x = qp - ly * W, y = y0 + ly;
         const int ax = x + px, ay = y + py;
         const int cx_lo = max(0, ax - WX + 1), cx_hi = min(nx - 1, ax);
         const int cy_lo = max(0, ay - WY + 1), cy_hi = min(ny - 1, ay);
         T *op = oslice + x * g.os[0] + y * g.os[1];
         T acc = g.zero_init ? pzero<T>() : *op;
-        // element of window (cx_lo, cy_lo) at tap (ax - cx_lo, ay - cy_lo)
-        const T *p0 = run0 + ((cy_lo - wy_lo) * nx + cx_lo) * WSZ + (ax - cx_lo) + WX * (ay - cy_lo);
-        if (cx_hi - cx_lo == WX - 1 && cy_hi - cy_lo == WY - 1) {
-            T v[WSZ];
+        const int nr = cy_hi - cy_lo + 1, nc = cx_hi - cx_lo + 1;
+        const bool full = nr == WY && nc == WX;
+        if (COL) {
+            // element of window (cx_lo, cy_lo) at tap (ax - cx_lo, ay - cy_lo);
+            // next window along x: + WSZ - 1, next window row: + nx*WSZ - WX
+            const T *p0 = sm + (int)(gs(0) & (VEC - 1)) + ((cy_lo - wy_lo) * nx + cx_lo) * WSZ +
+                          (ax - cx_lo) + WX * (ay - cy_lo);
+            const int rstep = nx * WSZ - WX;
+            if (full) {
+                T v[WSZ];
 #pragma unroll
-            for (int r = 0; r < WY; ++r)
+                for (int r = 0; r < WY; ++r)
 #pragma unroll
-                for (int j = 0; j < WX; ++j) v[r * WX + j] = p0[r * rstep + j * (WSZ - 1)];
+                    for (int j = 0; j < WX; ++j) v[r * WX + j] = p0[r * rstep + j * (WSZ - 1)];
 #pragma unroll
-            for (int e = 0; e < WSZ; ++e) acc = padd<T>(acc, v[e]);
+                for (int e = 0; e < WSZ; ++e) acc = padd<T>(acc, v[e]);
+            } else {
+#pragma unroll
+                for (int r = 0; r < WY; ++r)
+#pragma unroll
+                    for (int j = 0; j < WX; ++j)
+                        if (r < nr && j < nc) acc = padd<T>(acc, p0[r * rstep + j * (WSZ - 1)]);
+            }
         } else {
-            const int nr = cy_hi - cy_lo + 1, nc = cx_hi - cx_lo + 1;
+            // window (cx_lo + j, cy_lo + r) holds the pixel at tap
+            // (ax - cx_lo - j, ay - cy_lo - r), in that tap's plane
+            const int wbase = (cy_lo - wy_lo) * nx + cx_lo;
+            if (full) {  // interior: tap (WX-1-j, WY-1-r) of window (cx_lo + j, cy_lo + r)
+                T v[WSZ];
 #pragma unroll
-            for (int r = 0; r < WY; ++r)
+                for (int r = 0; r < WY; ++r)
 #pragma unroll
-                for (int j = 0; j < WX; ++j)
-                    if (r < nr && j < nc) acc = padd<T>(acc, p0[r * rstep + j * (WSZ - 1)]);
+                    for (int j = 0; j < WX; ++j)
+                        v[r * WX + j] = sm[pb[(WX - 1 - j) + WX * (WY - 1 - r)] + wbase + r * nx + j];
+#pragma unroll
+                for (int e = 0; e < WSZ; ++e) acc = padd<T>(acc, v[e]);
+            } else {
+                const int k0 = (ax - cx_lo) + WX * (ay - cy_lo);
+                for (int r = 0; r < nr; ++r)
+                    for (int j = 0; j < nc; ++j) {
+                        const int k = k0 - j - WX * r;
+                        acc = padd<T>(acc, sm[k * pitch + (int)(gs(k) & (VEC - 1)) + wbase + r * nx + j]);
+                    }
+            }
         }
         *op = acc;
     }
@@ -696,22 +738,26 @@ static bool wrap_tiled_plan(const PatchGeom &g, size_t esize, const void *in, Wr
     return true;
 }
 
-// the stride-1 3 x 3 column-layout kernel: rows of tiles up to 16 deep whose
-// staged run fits 48 KB (four blocks per SM), 32-bit offsets
+// the stride-1 3 x 3 kernel: row tiles up to 16 deep whose staged runs fit
+// 48 KB (four blocks per SM), 32-bit offsets; `pitch` is the staged run pitch
+// (elements, room for the phase) of the row layout's tap planes
 static bool wrap_s1_plan(const PatchGeom &g, size_t esize, const void *in, int &TY, int &tiles_y,
-                         size_t &smem) {
-    if (!g.is_column || g.sx != 1 || g.sy != 1 || g.wx != 3 || g.wy != 3) return false;
+                         int &pitch, size_t &smem) {
+    if (g.sx != 1 || g.sy != 1 || g.wx != 3 || g.wy != 3) return false;
     if (((uintptr_t)in % 16) != 0 || g.W <= 0 || g.H <= 0 || g.nx <= 0 || g.ny <= 0) return false;
     if (g.W >= (1 << 24) || g.H >= (1 << 24) || std::llabs(g.px) > 2 || std::llabs(g.py) > 2) return false;
+    const long long vec = esize >= 16 ? 1 : 16 / (long long)esize;
     const long long row_bytes = 9 * g.nx * (long long)esize;
-    const long long budget = 48 * 1024 - 16;
+    const long long budget = 48 * 1024 - 16 - 9 * 2 * vec * (long long)esize;
     TY = (int)std::min<long long>(16, budget / row_bytes - 2);
     if (TY < 1) return false;
     TY = (int)std::min<long long>(TY, g.H);
     tiles_y = (int)((g.H + TY - 1) / TY);
     if ((long long)tiles_y * g.slices > 0x7fffffffll) return false;
     if ((long long)(TY + 2) * g.W >= (1 << 30)) return false;
-    smem = (size_t)((TY + 2) * row_bytes + 16);
+    const long long plane = (TY + 2) * g.nx;  // a tap plane's staged windows
+    pitch = (int)((plane + 2 * vec - 1) / vec * vec);
+    smem = g.is_column ? (size_t)((TY + 2) * row_bytes + 16) : (size_t)(9 * pitch) * esize;
     return true;
 }
 
@@ -722,15 +768,15 @@ static void launch_wrap(const Array &in, Array &out, const PatchGeom &g) {
     WrapTile wt;
     size_t smem = 0;
     const PatchDivs f = patch_divs(g);
-    int TY = 0, tiles_y = 0;
-    if (wrap_s1_plan(g, sizeof(T), in.data(), TY, tiles_y, smem)) {
+    int TY = 0, tiles_y = 0, pitch = 0;
+    if (wrap_s1_plan(g, sizeof(T), in.data(), TY, tiles_y, pitch, smem)) {
         const unsigned blocks = (unsigned)((long long)tiles_y * g.slices);
-        AFGB_CUDA(cudaFuncSetAttribute(wrap_s1_kernel<T, 3, 3>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        auto k = g.is_column ? wrap_s1_kernel<T, 3, 3, true> : wrap_s1_kernel<T, 3, 3, false>;
+        AFGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         {
             KernelTimer kt("wrap_s1_kernel");
-            wrap_s1_kernel<T, 3, 3><<<blocks, WS1_THREADS, smem, stream()>>>(in.ptr<T>(), out.ptr<T>(),
-                                                                              g, f, TY, tiles_y);
+            k<<<blocks, WS1_THREADS, smem, stream()>>>(in.ptr<T>(), out.ptr<T>(), g, f, TY, tiles_y,
+                                                       pitch);
         }
         count_launch();
         AFGB_POST_LAUNCH("wrap_s1_kernel");

@@ -66,7 +66,10 @@ def test_kernels_launch(af):
     n, _ = _ran(af, "wrap_tiled_kernel", lambda: af.wrap(U2, 16, 16, 3, 3, 2, 2, 1, 1))
     assert n == 1
     R = af.unwrap(a, 3, 3, 1, 1, 1, 1, False)
-    n, _ = _ran(af, "wrap_rows_kernel", lambda: af.wrap(R, 16, 16, 3, 3, 1, 1, 1, 1, False))
+    n, _ = _ran(af, "wrap_s1_kernel", lambda: af.wrap(R, 16, 16, 3, 3, 1, 1, 1, 1, False))
+    assert n == 1
+    R2 = af.unwrap(a, 3, 3, 2, 2, 1, 1, False)
+    n, _ = _ran(af, "wrap_rows_kernel", lambda: af.wrap(R2, 16, 16, 3, 3, 2, 2, 1, 1, False))
     assert n == 1
     # windows too large to stage: the untiled kernels
     big = af.Array.from_numpy(np.ones((80, 70), np.complex128))
@@ -257,21 +260,24 @@ WRAP_S1 = [
 ]
 
 
+@pytest.mark.parametrize("col", [True, False], ids=["col", "row"])
 @pytest.mark.parametrize("case", WRAP_S1, ids=lambda c: f"{c[0][0]}x{c[0][1]}p{c[1]}_{C.DT_NAME[c[2]]}")
-def test_wrap_s1_kernel_matches_oracle(af, oracle, case):
-    """The stride-1 3x3 column-layout wrap (row tiles staged as one contiguous
-    run) against the oracle, bit for bit, over several row tiles per slice; and
+def test_wrap_s1_kernel_matches_oracle(af, oracle, case, col):
+    """The stride-1 3x3 wrap (row tiles staged as contiguous runs of the patch
+    matrix: one in the column layout, one per tap plane in the row layout)
+    against the oracle, bit for bit, over several row tiles per slice; and
     wrap_v2 adding into an existing output."""
     (W, H, d2, d3), pad, dt = case
     nx, ny = W + 2 * pad - 2, H + 2 * pad - 2
-    pm = C.patch_values(dt, (9, nx * ny, d2, d3), 7700 + W)
+    shape = (9, nx * ny, d2, d3) if col else (nx * ny, 9, d2, d3)
+    pm = C.patch_values(dt, shape, 7700 + W)
     P = af.Array.from_numpy(pm)
-    n, out = _ran(af, "wrap_s1_kernel", lambda: af.wrap(P, W, H, 3, 3, 1, 1, pad, pad))
+    n, out = _ran(af, "wrap_s1_kernel", lambda: af.wrap(P, W, H, 3, 3, 1, 1, pad, pad, col))
     assert n == 1
-    want = oracle.wrap_patches(pm, W, H, 3, 3, 1, 1, pad, pad)
+    want = oracle.wrap_patches(pm, W, H, 3, 3, 1, 1, pad, pad, col)
     assert digest(out.to_numpy()) == digest(want)
     base_np = C.patch_values(dt, (W, H, d2, d3), 7800 + W)
     base = af.Array.from_numpy(base_np)
-    af.wrap_v2(base, P, W, H, 3, 3, 1, 1, pad, pad)
-    want2 = oracle.wrap_patches(pm, W, H, 3, 3, 1, 1, pad, pad, out=base_np)
+    af.wrap_v2(base, P, W, H, 3, 3, 1, 1, pad, pad, col)
+    want2 = oracle.wrap_patches(pm, W, H, 3, 3, 1, 1, pad, pad, col, out=base_np)
     assert digest(base.to_numpy()) == digest(want2)
