@@ -479,8 +479,9 @@ __global__ void __launch_bounds__(WT_THREADS) wrap_tiled_kernel(const T *__restr
 // phase); then each thread sums its pixels' elements from shared memory,
 // window rows ascending and windows along x ascending (the reference's
 // order, as the tiled kernel sums them), with fixed offsets for interior
-// pixels.  About 30 instructions per pixel replace the tiled kernel's 470.
-constexpr int WS1_THREADS = 256;
+// pixels: about 180 instructions per pixel instead of the tiled kernel's 470.
+// 8 warps (column layout) or 9 (row layout: one warp per tap plane's run)
+constexpr int WS1_THREADS = 288;
 
 template <typename T, int WX, int WY, bool COL>
 __global__ void __launch_bounds__(WS1_THREADS) wrap_s1_kernel(const T *__restrict__ in,
@@ -509,13 +510,13 @@ __global__ void __launch_bounds__(WS1_THREADS) wrap_s1_kernel(const T *__restric
     const int run = (COL ? WSZ : 1) * nx * nwy;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (nwy > 0) {
-        for (int q = COL ? 0 : warp; q < NRUN; q += (COL ? 1 : WS1_THREADS / 32)) {
+        for (int q = COL ? 0 : warp; q < NRUN; q += (COL ? NRUN : (int)(blockDim.x >> 5))) {
             const long long g0 = gs(q);
             const int phase = (int)(g0 & (VEC - 1));
             const T *src = in + (g0 - phase);
             T *dst = sm + q * pitch;
             const int nchunks = (phase + run + VEC - 1) / VEC;
-            const int t0 = COL ? threadIdx.x : lane, tstep = COL ? WS1_THREADS : 32;
+            const int t0 = COL ? threadIdx.x : lane, tstep = COL ? (int)blockDim.x : 32;
             for (int c = t0; c < nchunks; c += tstep) {
                 const int e0 = c * VEC - phase;
                 if (e0 >= 0 && e0 + VEC <= run) {
@@ -536,7 +537,7 @@ __global__ void __launch_bounds__(WS1_THREADS) wrap_s1_kernel(const T *__restric
     int pb[COL ? 1 : WSZ];  // row layout: tap plane k's staged window 0
 #pragma unroll
     for (int k = 0; k < (COL ? 1 : WSZ); ++k) pb[k] = k * pitch + (int)(gs(k) & (VEC - 1));
-    for (int qp = threadIdx.x; qp < npix; qp += WS1_THREADS) {
+    for (int qp = threadIdx.x; qp < npix; qp += blockDim.x) {
         const int ly = (int)fdiv((uint32_t)qp, f.W), x = qp - ly * W, y = y0 + ly;
         const int ax = x + px, ay = y + py;
         const int cx_lo = max(0, ax - WX + 1), cx_hi = min(nx - 1, ax);
@@ -775,8 +776,8 @@ static void launch_wrap(const Array &in, Array &out, const PatchGeom &g) {
         AFGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         {
             KernelTimer kt("wrap_s1_kernel");
-            k<<<blocks, WS1_THREADS, smem, stream()>>>(in.ptr<T>(), out.ptr<T>(), g, f, TY, tiles_y,
-                                                       pitch);
+            k<<<blocks, g.is_column ? 256 : WS1_THREADS, smem, stream()>>>(in.ptr<T>(), out.ptr<T>(),
+                                                                             g, f, TY, tiles_y, pitch);
         }
         count_launch();
         AFGB_POST_LAUNCH("wrap_s1_kernel");

@@ -1023,7 +1023,7 @@ def run_direct_workloads(af, O, peaks, args) -> dict:
             img_bytes, par_slices=list(range(nthreads)))
         return {**err_vs(res.to_numpy()[..., 0:1], ref), "cpu_baseline": cpu}
     measure("wrap_3x3_f32_128x128x64x32", lambda: af.wrap(U, 128, 128, 3, 3, 1, 1, 1, 1),
-            ni * 4 * 10, ("wrap_tiled_kernel", "wrap_kernel"), chk_wrap)
+            ni * 4 * 10, ("wrap_s1_kernel", "wrap_tiled_kernel", "wrap_kernel"), chk_wrap)
     del U, u0
     # the same with is_column = false (patch elements along dim 1)
     measure("unwrap_rows_3x3_f32_128x128x64x32",
@@ -1039,7 +1039,7 @@ def run_direct_workloads(af, O, peaks, args) -> dict:
         return {**err_vs(res.to_numpy()[..., 0:1], ref), "cpu_baseline": cpu}
     measure("wrap_rows_3x3_f32_128x128x64x32",
             lambda: af.wrap(R, 128, 128, 3, 3, 1, 1, 1, 1, False), ni * 4 * 10,
-            ("wrap_rows_kernel", "wrap_kernel"), chk_wrap_rows)
+            ("wrap_s1_kernel", "wrap_rows_kernel", "wrap_kernel"), chk_wrap_rows)
     return out
 
 
