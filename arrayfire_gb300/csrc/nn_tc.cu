@@ -1242,11 +1242,9 @@ __global__ void __launch_bounds__(RC_THREADS, 1)
 // filter gradient kernel
 // ===========================================================================
 constexpr int WG_STAGES = 4;
-constexpr int WG_KP = 64;                      // pixels per stage (MMA K)
-constexpr int WG_A_BYTES = 128 * WG_KP * 2;    // G^T tile: 128 k x 64 pixels, 16 KB
-constexpr int WG_B_GROUP = 64 * WG_KP * 2;     // one 64-channel group x 64 pixels, 8 KB
+constexpr int WG_KP = 64;                      // pixels per stage (MMA K) of the cp.async path
+constexpr int WG_B_GROUP = 64 * WG_KP * 2;     // cp.async path: one 64-channel group x 64 pixels
 constexpr int WG_MAXG = 4;
-constexpr int WG_B_BYTES = WG_B_GROUP * WG_MAXG;  // 32 KB
 constexpr int WG_THREADS = 256;  // warps 0-3 producers (warp 0 TMA), 4-7 epilogue, MMA in warp 4
 
 struct WgradParams {
@@ -1261,7 +1259,13 @@ struct WgradParams {
     int ngroups_total;  // taps * (Cpad/64)
     int groups_per_tile;
     int n_k_tiles;
-    int BX, BY, ntx, nty;  // 64-pixel rectangles (TMA path)
+    int BX, BY, ntx, nty;  // KP-pixel rectangles (TMA path)
+    // stage geometry: KP pixels per stage (64, or 128 on the TMA path: the
+    // SM's copy engine costs about 400 cycles per copy whatever its size, so
+    // 16 KB boxes feed twice the MMA work of 8 KB ones), nst stages, the
+    // incoming-gradient tile (a_bytes) and one 64-channel signal group
+    // (b_group) per stage
+    int KP, nst, a_bytes, b_group;
 };
 
 template <bool TMA>
@@ -1271,9 +1275,10 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     unsigned char *base = reinterpret_cast<unsigned char *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int b_bytes = WG_MAXG * p.b_group;
     unsigned char *a_stage = base;
-    unsigned char *b_stage = base + WG_STAGES * WG_A_BYTES;
-    Smem *sm = reinterpret_cast<Smem *>(b_stage + WG_STAGES * WG_B_BYTES);
+    unsigned char *b_stage = base + p.nst * p.a_bytes;
+    Smem *sm = reinterpret_cast<Smem *>(b_stage + p.nst * b_bytes);
     volatile int *abort = &sm->abort;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -1284,12 +1289,12 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
     const int ng = min(p.groups_per_tile, p.ngroups_total - g0);
     const long long q_begin = (long long)blockIdx.y * p.chunk;
     const long long q_end = min(p.Q, q_begin + p.chunk);
-    const int nstages = TMA ? (int)(q_end - q_begin) : (int)((q_end - q_begin + WG_KP - 1) / WG_KP);
+    const int nstages = TMA ? (int)(q_end - q_begin) : (int)((q_end - q_begin + p.KP - 1) / p.KP);
     const int ncols = 64 * ng;
     const int nchunk = p.Cpad / 64;
 
     if (threadIdx.x == 0) {
-        for (int s = 0; s < WG_STAGES; ++s) {
+        for (int s = 0; s < p.nst; ++s) {
             mbar_init(&sm->full[s], TMA ? 1 : 128);
             mbar_init(&sm->empty[s], 1);
         }
@@ -1310,10 +1315,10 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
     if (warp < 4) {
         if (TMA) {
             if (warp == 0 && lane == 0) {
-                const uint32_t bytes = WG_A_BYTES + WG_B_GROUP * ng;
+                const uint32_t bytes = (uint32_t)(p.a_bytes + p.b_group * ng);
                 for (int st = 0; st < nstages && !*abort; ++st) {
-                    const int s = st % WG_STAGES;
-                    if (!mbar_wait(&sm->empty[s], ((st / WG_STAGES) & 1) ^ 1, abort, 32u)) break;
+                    const int s = st % p.nst;
+                    if (!mbar_wait(&sm->empty[s], ((st / p.nst) & 1) ^ 1, abort, 32u)) break;
                     long long blk = q_begin + st;
                     const int tx = (int)(blk % p.ntx);
                     blk /= p.ntx;
@@ -1321,15 +1326,15 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
                     const int n = (int)(blk / p.nty);
                     const int x0 = tx * p.BX, y0 = ty * p.BY;
                     mbar_arrive_expect_tx(&sm->full[s], bytes);
-                    const uint32_t sa = smem_u32(a_stage + s * WG_A_BYTES);
-                    const uint32_t sb = smem_u32(b_stage + s * WG_B_BYTES);
+                    const uint32_t sa = smem_u32(a_stage + s * p.a_bytes);
+                    const uint32_t sb = smem_u32(b_stage + s * b_bytes);
                     tma_load_4d(sa, &gmap, &sm->full[s], k0, x0, y0, n);
-                    tma_load_4d(sa + 8192, &gmap, &sm->full[s], k0 + 64, x0, y0, n);
+                    tma_load_4d(sa + p.KP * 128, &gmap, &sm->full[s], k0 + 64, x0, y0, n);
                     for (int grp = 0; grp < ng; ++grp) {
                         const int gi = g0 + grp;
                         const int tap = gi / nchunk, cchunk = gi - tap * nchunk;
                         const int u = tap % p.fw, v = tap / p.fw;
-                        tma_load_4d(sb + grp * WG_B_GROUP, &xmap, &sm->full[s], cchunk * 64,
+                        tma_load_4d(sb + grp * p.b_group, &xmap, &sm->full[s], cchunk * 64,
                                     x0 * p.sx - p.px + u * p.dx, y0 * p.sy - p.py + v * p.dy, n);
                     }
                 }
@@ -1345,10 +1350,10 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
             int Y = (int)(rest % p.Ho), n = (int)(rest / p.Ho);
             uint32_t it = 0;
             for (int st = 0; st < nstages && !*abort; ++st, ++it) {
-                const int s = it % WG_STAGES;
-                if (!mbar_wait(&sm->empty[s], ((it / WG_STAGES) & 1) ^ 1, abort, 32u)) break;
-                const uint32_t sa = smem_u32(a_stage + s * WG_A_BYTES);
-                const uint32_t sb = smem_u32(b_stage + s * WG_B_BYTES);
+                const int s = it % p.nst;
+                if (!mbar_wait(&sm->empty[s], ((it / p.nst) & 1) ^ 1, abort, 32u)) break;
+                const uint32_t sa = smem_u32(a_stage + s * p.a_bytes);
+                const uint32_t sb = smem_u32(b_stage + s * b_bytes);
                 const bool qv = q < q_end;
                 const uint32_t rowoff = (row >> 3) * 1024 + (row & 7) * 128;
                 // A: G row (128 k = two 64-wide MN atoms); channels at or past
@@ -1382,7 +1387,7 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
                 if (it >= LAG) {
                     cp_async_wait<LAG>();
                     fence_proxy_async_smem();
-                    mbar_arrive(&sm->full[(it - LAG) % WG_STAGES]);
+                    mbar_arrive(&sm->full[(it - LAG) % p.nst]);
                 }
                 q += WG_KP;
                 X += WG_KP;
@@ -1397,22 +1402,26 @@ __global__ void __launch_bounds__(WG_THREADS, 1)
             cp_async_wait_all();
             fence_proxy_async_smem();
             for (uint32_t k = (it >= LAG ? it - LAG : 0); k < it; ++k)
-                mbar_arrive(&sm->full[k % WG_STAGES]);
+                mbar_arrive(&sm->full[k % p.nst]);
         }
     } else {
         if (warp == 4 && lane == 0) {
-            // MMA: M = 128 (k), N = 64*ng, both operands MN-major
+            // MMA: M = 128 (k), N = 64*ng, both operands MN-major; the k atoms
+            // and the signal groups are KP*128 bytes apart
             const uint32_t idesc = idesc_bf16(128, (uint32_t)ncols, 1, 1);
+            const uint32_t lbo = (uint32_t)p.KP * 128u;
+            const int ksteps = p.KP / 16;
             for (int st = 0; st < nstages; ++st) {
-                const int s = st % WG_STAGES;
-                if (!mbar_wait(&sm->full[s], (st / WG_STAGES) & 1, abort, 64u)) break;
+                const int s = st % p.nst;
+                if (!mbar_wait(&sm->full[s], (st / p.nst) & 1, abort, 64u)) break;
                 tc_fence_after();
-                const uint32_t sa = smem_u32(a_stage + s * WG_A_BYTES);
-                const uint32_t sb = smem_u32(b_stage + s * WG_B_BYTES);
+                const uint32_t sa = smem_u32(a_stage + s * p.a_bytes);
+                const uint32_t sb = smem_u32(b_stage + s * b_bytes);
 #pragma unroll
-                for (int k = 0; k < WG_KP / 16; ++k) {
-                    const uint64_t ad = smem_desc(sa + k * 2048, 8192, 1024);
-                    const uint64_t bd = smem_desc(sb + k * 2048, 8192, 1024);
+                for (int k = 0; k < 8; ++k) {
+                    if (k >= ksteps) break;
+                    const uint64_t ad = smem_desc(sa + k * 2048, lbo, 1024);
+                    const uint64_t bd = smem_desc(sb + k * 2048, lbo, 1024);
                     mma_f16(tmem_base, ad, bd, idesc, (st | k) != 0);
                 }
                 mma_commit(&sm->empty[s]);
@@ -2945,17 +2954,28 @@ static void filter_grad_from(const NNGeom &g0, const __nv_bfloat16 *gg, int Kpad
     }
     p.groups_per_tile = best;
     p.n_k_tiles = round_up((int)g.K, 128) / 128;  // past Kpad the G loads read zeros
-    // 64-pixel rectangles by TMA; the signal map walks every s-th pixel
-    // (traversal strides up to 8); otherwise the cp.async row gather
+    // 128- (else 64-) pixel rectangles by TMA, two (four) stages; the signal
+    // map walks every s-th pixel (traversal strides up to 8); otherwise the
+    // cp.async row gather of 64-pixel stages
     int rbx = 0, rby = 0;
-    const bool tma = g.sx <= 8 && g.sy <= 8 &&
-                     pick_rect((int)g.Wo, (int)g.Ho, WG_KP, 8, rbx, rby, (int)g.sx, (int)g.sy);
+    p.KP = 128;
+    bool tma = g.sx <= 8 && g.sy <= 8 &&
+               pick_rect((int)g.Wo, (int)g.Ho, 128, 8, rbx, rby, (int)g.sx, (int)g.sy);
+    if (!tma) {
+        p.KP = WG_KP;
+        tma = g.sx <= 8 && g.sy <= 8 &&
+              pick_rect((int)g.Wo, (int)g.Ho, WG_KP, 8, rbx, rby, (int)g.sx, (int)g.sy);
+    }
+    p.nst = p.KP == 128 ? 2 : WG_STAGES;
+    p.a_bytes = 2 * p.KP * 128;
+    p.b_group = p.KP * 128;
     CUtensorMap gmap, xmap;
     std::memset(&gmap, 0, sizeof(gmap));
     std::memset(&xmap, 0, sizeof(xmap));
     long long units;  // pixel blocks (TMA) or pixels (cp.async)
     if (tma) {
-        pick_rect((int)g.Wo, (int)g.Ho, WG_KP, 8, p.BX, p.BY, (int)g.sx, (int)g.sy);
+        p.BX = rbx;
+        p.BY = rby;
         p.ntx = ((int)g.Wo + p.BX - 1) / p.BX;
         p.nty = ((int)g.Ho + p.BY - 1) / p.BY;
         units = (long long)p.ntx * p.nty * g.N;
@@ -2966,7 +2986,10 @@ static void filter_grad_from(const NNGeom &g0, const __nv_bfloat16 *gg, int Kpad
     }
     p.Q = units;
     const long long ntiles = (long long)p.n_k_tiles * ((p.ngroups_total + best - 1) / best);
-    const long long target = (long long)num_sms() * 2;
+    // one wave of CTAs (two waves were measured slower: 0.106 against 0.087 ms
+    // on 56x56x256x64 with a 1x1 filter, 0.076 against 0.053 ms on the 5x5
+    // stride-2 backward shape)
+    const long long target = (long long)num_sms();
     long long splits = std::max(1LL, target / std::max(1LL, ntiles));
     long long chunk = (units + splits - 1) / splits;
     if (tma) {
@@ -2983,7 +3006,7 @@ static void filter_grad_from(const NNGeom &g0, const __nv_bfloat16 *gg, int Kpad
         partial = static_cast<float *>(alloc_device((size_t)(splits * rows * g.K) * sizeof(float)));
     }
     p.partial = partial;
-    const size_t smem = 1024 + WG_STAGES * (WG_A_BYTES + WG_B_BYTES) + sizeof(Smem) + 64;
+    const size_t smem = 1024 + (size_t)p.nst * (p.a_bytes + WG_MAXG * p.b_group) + sizeof(Smem) + 64;
     {
         KernelTimer kt("tc_wgrad_kernel");
         if (tma) {
