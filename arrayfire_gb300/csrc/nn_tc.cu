@@ -2007,6 +2007,70 @@ __device__ __forceinline__ unsigned char to_e4m3(float v) {
 }
 
 // f32 ArrayFire (W,H,C,N) -> e4m3 [N][H][W][Cpad] of x / act_scale
+// f32 ArrayFire planes (W*H pixels with 16-byte aligned rows, as the flat
+// bf16 converter takes them) -> e4m3 [N][H][W][Cpad] scaled by 1/act_scale:
+// one block converts CV_PIX pixels x 64 channels.  Phase 1: an item is four
+// channels x four pixels (four float4 loads along the pixels), packed into
+// one 32-bit word of four e4m3 channels per pixel, into a tile of 16 words per
+// pixel whose word index is XOR-swizzled by the pixel; phase 2: 16-byte
+// stores of 16 channels of one pixel.  Rounding and saturation are those of
+// the per-element converter, so the bytes are the same.
+__global__ void __launch_bounds__(256) to_nhwc_flat_e4m3_kernel(const float *__restrict__ in,
+                                                                long long P, int C, int Cpad,
+                                                                long long tiles_p, long long ntiles,
+                                                                const float *act_scale,
+                                                                unsigned char *__restrict__ out) {
+    __shared__ __align__(16) uint32_t tile[CV_PIX * 16];
+    const int t = threadIdx.x;
+    const int nck = Cpad / 64;
+    const float inv = 1.0f / *act_scale;
+    for (long long bt = blockIdx.x; bt < ntiles; bt += gridDim.x) {
+        const long long ck = bt % nck;
+        const long long r = bt / nck;
+        const long long pt = r % tiles_p;
+        const long long n = r / tiles_p;
+        const long long p0 = pt * CV_PIX;
+        const int c0 = (int)ck * 64;
+        // phase 1: item = (c4 in 0..15, p4 in 0..CV_PIX/4-1)
+        for (int item = t; item < 16 * (CV_PIX / 4); item += 256) {
+            const int c4 = item & 15, p4 = item >> 4;
+            const long long px = p0 + 4 * p4;
+            float4 v[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int c = c0 + 4 * c4 + i;
+                v[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (px < P && c < C) v[i] = __ldg(reinterpret_cast<const float4 *>(in + (n * C + c) * P + px));
+            }
+            const float a[4][4] = {{v[0].x, v[0].y, v[0].z, v[0].w}, {v[1].x, v[1].y, v[1].z, v[1].w},
+                                   {v[2].x, v[2].y, v[2].z, v[2].w}, {v[3].x, v[3].y, v[3].z, v[3].w}};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {  // pixel 4*p4 + j: channels 4*c4 .. +3
+                const int pl = 4 * p4 + j;
+                const uint32_t w = (uint32_t)to_e4m3(a[0][j] * inv) | ((uint32_t)to_e4m3(a[1][j] * inv) << 8) |
+                                   ((uint32_t)to_e4m3(a[2][j] * inv) << 16) |
+                                   ((uint32_t)to_e4m3(a[3][j] * inv) << 24);
+                tile[pl * 16 + (c4 ^ (pl & 15))] = w;
+            }
+        }
+        __syncthreads();
+        // phase 2: item = (pixel, 16-byte chunk j in 0..3)
+        for (int item = t; item < CV_PIX * 4; item += 256) {
+            const int pl = item >> 2, j = item & 3;
+            const long long px = p0 + pl;
+            if (px < P) {
+                uint4 w;
+                w.x = tile[pl * 16 + ((4 * j + 0) ^ (pl & 15))];
+                w.y = tile[pl * 16 + ((4 * j + 1) ^ (pl & 15))];
+                w.z = tile[pl * 16 + ((4 * j + 2) ^ (pl & 15))];
+                w.w = tile[pl * 16 + ((4 * j + 3) ^ (pl & 15))];
+                *reinterpret_cast<uint4 *>(out + (n * P + px) * Cpad + c0 + 16 * j) = w;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void __launch_bounds__(256) to_nhwc_e4m3_kernel(const float *__restrict__ in, int W,
                                                            int H, int C, int N, int Cpad,
                                                            const float *act_scale,
@@ -2326,14 +2390,29 @@ static void run_gather(const NNGeom &g, int mode, const float *img_f32, const fl
         count_launch();
         AFGB_POST_LAUNCH("combine_scale_kernel");
         img = alloc_device((size_t)SW * SH * g.N * SCpad);
-        dim3 cgrid((unsigned)((SW + 63) / 64), (unsigned)(SH * g.N), (unsigned)(SCpad / 64));
-        {
-            KernelTimer kt("tc_convert_kernel");
-            to_nhwc_e4m3_kernel<<<cgrid, 256, 0, stream()>>>(img_f32, SW, SH, SC, (int)g.N, SCpad,
-                                                             scales, static_cast<unsigned char *>(img));
+        const long long P = (long long)SW * SH;
+        if ((P & 3) == 0 && (reinterpret_cast<uintptr_t>(img_f32) & 15) == 0) {
+            const long long tiles_p = (P + CV_PIX - 1) / CV_PIX;
+            const long long ntiles = tiles_p * g.N * (SCpad / 64);
+            const unsigned grid = (unsigned)std::min<long long>(ntiles, (long long)num_sms() * 8);
+            {
+                KernelTimer kt("tc_convert_kernel");
+                to_nhwc_flat_e4m3_kernel<<<grid, 256, 0, stream()>>>(img_f32, P, SC, SCpad, tiles_p,
+                                                                     ntiles, scales,
+                                                                     static_cast<unsigned char *>(img));
+            }
+            count_launch();
+            AFGB_POST_LAUNCH("to_nhwc_flat_e4m3_kernel");
+        } else {
+            dim3 cgrid((unsigned)((SW + 63) / 64), (unsigned)(SH * g.N), (unsigned)(SCpad / 64));
+            {
+                KernelTimer kt("tc_convert_kernel");
+                to_nhwc_e4m3_kernel<<<cgrid, 256, 0, stream()>>>(img_f32, SW, SH, SC, (int)g.N, SCpad,
+                                                                 scales, static_cast<unsigned char *>(img));
+            }
+            count_launch();
+            AFGB_POST_LAUNCH("to_nhwc_e4m3_kernel");
         }
-        count_launch();
-        AFGB_POST_LAUNCH("to_nhwc_e4m3_kernel");
         wt = alloc_device((size_t)OCpad * taps * SCpad);
         long long total = (long long)OCpad * taps * SCpad;
         unsigned blocks = (unsigned)std::min<long long>((total + 255) / 256, num_sms() * 8LL);
