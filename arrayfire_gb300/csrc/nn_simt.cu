@@ -86,13 +86,22 @@ struct GatherParams {
     int mode;  // 0 forward, 1 data gradient
 };
 
-constexpr int GB_M = 128, GB_N = 128, GB_K = 8, GB_THREADS = 256;
+constexpr int GB_K = 8, GB_THREADS = 256;
 
-template <typename T>
+// Tiles of TM pixels x TN output channels (128 x 128, or 256 x 64 when the
+// output has at most 64 channels, which would leave half of a 128-wide tile
+// empty), 8 x 8 accumulators per thread, the K loop in steps of GB_K
+// channels of one tap with double-buffered shared tiles and one step of
+// register prefetch.  The tap and channel step advance incrementally.
+template <typename T, int TM, int TN>
 __global__ void __launch_bounds__(GB_THREADS) igemm_gather_kernel(GatherParams<T> p) {
+    static_assert(TM * TN == 64 * GB_THREADS && TM % 32 == 0 && TN % 32 == 0, "tile shape");
     using A_t = typename NNAcc<T>::type;
-    __shared__ __align__(16) A_t As[2][GB_K][GB_M];
-    __shared__ __align__(16) A_t Bs[2][GB_K][GB_N];
+    constexpr int HM = TM / 2, HN = TN / 2;
+    constexpr int NA = TM / 32, ASTEP = GB_THREADS / TM;  // A loads per thread, their channel step
+    constexpr int NB = TN / 32, BSTEP = GB_THREADS / TN;
+    __shared__ __align__(16) A_t As[2][GB_K][TM];
+    __shared__ __align__(16) A_t Bs[2][GB_K][TN];
     __shared__ short tap_u[MAX_TAPS], tap_v[MAX_TAPS];
     __shared__ int s_ntaps;
 
@@ -104,9 +113,9 @@ __global__ void __launch_bounds__(GB_THREADS) igemm_gather_kernel(GatherParams<T
     const long long MY = p.mode ? (p.DH - ry + p.sy - 1) / p.sy : p.DH;
     if (MX <= 0 || MY <= 0) return;
     const long long Mp = MX * MY * p.N;
-    const long long m0 = (long long)blockIdx.x * GB_M;
+    const long long m0 = (long long)blockIdx.x * TM;
     if (m0 >= Mp) return;
-    const long long n0 = (long long)blockIdx.y * GB_N;
+    const long long n0 = (long long)blockIdx.y * TN;
 
     if (tid == 0) {
         int cnt = 0;
@@ -126,9 +135,9 @@ __global__ void __launch_bounds__(GB_THREADS) igemm_gather_kernel(GatherParams<T
     const long long nch = (p.SC + GB_K - 1) / GB_K;
     const long long iters = (long long)ntaps * nch;
 
-    // A-load role: one pixel, four channel slots
-    const int am = tid & (GB_M - 1);
-    const int akk = tid >> 7;
+    // A-load role: one pixel, NA channel slots ASTEP apart
+    const int am = tid % TM;
+    const int akk = tid / TM;
     const long long mA = m0 + am;
     const bool mvalid = mA < Mp;
     long long AX = 0, AY = 0, An = 0;
@@ -140,15 +149,15 @@ __global__ void __launch_bounds__(GB_THREADS) igemm_gather_kernel(GatherParams<T
     const long long SWH = p.SW * p.SH;
     const T *Abase = p.A + An * SWH * p.SC;
     // B-load role
-    const int bn = tid & (GB_N - 1);
-    const int bkk = tid >> 7;
+    const int bn = tid % TN;
+    const int bkk = tid / TN;
     const bool nvalid = (n0 + bn) < p.NC;
 
-    A_t ra[4], rb[4];
-    auto load_tile = [&](long long it) {
-        const int t = (int)(it / nch);
-        const long long c0 = (it - (long long)t * nch) * GB_K;
-        const int u = tap_u[t], v = tap_v[t];
+    A_t ra[NA], rb[NB];
+    int lt = 0;        // tap of the next load
+    long long lc0 = 0; // its first channel
+    auto load_tile = [&]() {
+        const int u = tap_u[lt], v = tap_v[lt];
         long long xs, ys;
         if (p.mode == 0) {
             xs = AX * p.sx + (long long)u * p.dx - p.px;
@@ -161,22 +170,29 @@ __global__ void __launch_bounds__(GB_THREADS) igemm_gather_kernel(GatherParams<T
         const T *src = Abase + xs + p.SW * ys;
         const long long tapidx = u + (long long)p.fw * v;
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            const long long c = c0 + akk + 2 * j;
+        for (int j = 0; j < NA; ++j) {
+            const long long c = lc0 + akk + ASTEP * j;
             ra[j] = (ok && c < p.SC) ? ld_acc<A_t, T>(src + c * SWH) : (A_t)0;
-            const long long cb = c0 + bkk + 2 * j;
+        }
+#pragma unroll
+        for (int j = 0; j < NB; ++j) {
+            const long long cb = lc0 + bkk + BSTEP * j;
             rb[j] = (nvalid && cb < p.SC) ? p.B[(tapidx * p.SC + cb) * p.NC + n0 + bn] : (A_t)0;
+        }
+        lc0 += GB_K;
+        if (lc0 >= p.SC) {
+            lc0 = 0;
+            ++lt;
         }
     };
     auto store_tile = [&](int buf) {
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            As[buf][akk + 2 * j][am] = ra[j];
-            Bs[buf][bkk + 2 * j][bn] = rb[j];
-        }
+        for (int j = 0; j < NA; ++j) As[buf][akk + ASTEP * j][am] = ra[j];
+#pragma unroll
+        for (int j = 0; j < NB; ++j) Bs[buf][bkk + BSTEP * j][bn] = rb[j];
     };
 
-    const int tm = tid & 15, tn = tid >> 4;
+    const int tm = tid % (TM / 8), tn = tid / (TM / 8);
     A_t acc[8][8];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
@@ -184,21 +200,21 @@ __global__ void __launch_bounds__(GB_THREADS) igemm_gather_kernel(GatherParams<T
         for (int j = 0; j < 8; ++j) acc[i][j] = (A_t)0;
 
     if (iters > 0) {
-        load_tile(0);
+        load_tile();
         store_tile(0);
         __syncthreads();
         int cur = 0;
         for (long long it = 0; it < iters; ++it) {
-            if (it + 1 < iters) load_tile(it + 1);
+            if (it + 1 < iters) load_tile();
 #pragma unroll
             for (int kk = 0; kk < GB_K; ++kk) {
                 A_t a[8], b[8];
 #pragma unroll
                 for (int i = 0; i < 4; ++i) {
                     a[i] = As[cur][kk][4 * tm + i];
-                    a[4 + i] = As[cur][kk][64 + 4 * tm + i];
+                    a[4 + i] = As[cur][kk][HM + 4 * tm + i];
                     b[i] = Bs[cur][kk][4 * tn + i];
-                    b[4 + i] = Bs[cur][kk][64 + 4 * tn + i];
+                    b[4 + i] = Bs[cur][kk][HN + 4 * tn + i];
                 }
 #pragma unroll
                 for (int i = 0; i < 8; ++i)
@@ -214,14 +230,14 @@ __global__ void __launch_bounds__(GB_THREADS) igemm_gather_kernel(GatherParams<T
     const int aox = p.mode ? p.sx : 1, aoy = p.mode ? p.sy : 1;
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        const long long m = m0 + (i < 4 ? 4 * tm + i : 64 + 4 * tm + i - 4);
+        const long long m = m0 + (i < 4 ? 4 * tm + i : HM + 4 * tm + i - 4);
         if (m >= Mp) continue;
         const long long X = m % MX, Y = (m / MX) % MY, n = m / (MX * MY);
         const long long dxp = rx + aox * X, dyp = ry + aoy * Y;
         T *dst = p.D + dxp + p.DW * (dyp + p.DH * p.NC * n);
 #pragma unroll
         for (int j = 0; j < 8; ++j) {
-            const long long nc = n0 + (j < 4 ? 4 * tn + j : 64 + 4 * tn + j - 4);
+            const long long nc = n0 + (j < 4 ? 4 * tn + j : HN + 4 * tn + j - 4);
             if (nc < p.NC) dst[p.DW * p.DH * nc] = st_conv<T, A_t>(acc[i][j]);
         }
     }
@@ -244,14 +260,18 @@ struct WgradParams {
 };
 
 constexpr int WG_M = 128, WG_N = 128, WG_K = 32, WG_THREADS = 256;
+// shared tile pitch: a warp stores one row of 32 pixels (lanes) at stride
+// WG_P, so a pitch of 128 would put all 32 lanes on one bank; 132 keeps the
+// compute loop's 16-byte reads aligned and spreads the stores over 8 banks
+constexpr int WG_P = WG_M + 4;
 
 template <typename T>
 __global__ void __launch_bounds__(WG_THREADS) wgrad_kernel(WgradParams<T> p) {
     using A_t = typename NNAcc<T>::type;
     extern __shared__ __align__(16) unsigned char wg_smem[];
-    A_t *As = reinterpret_cast<A_t *>(wg_smem);       // [WG_K][WG_M]
-    A_t *Bs = As + WG_K * WG_M;                         // [WG_K][WG_N]
-    long long *row_off = reinterpret_cast<long long *>(Bs + WG_K * WG_N);
+    A_t *As = reinterpret_cast<A_t *>(wg_smem);       // [WG_K][WG_P]
+    A_t *Bs = As + WG_K * WG_P;                         // [WG_K][WG_P]
+    long long *row_off = reinterpret_cast<long long *>(Bs + WG_K * WG_P);
     int *row_x = reinterpret_cast<int *>(row_off + WG_M);
     int *row_y = row_x + WG_M;
 
@@ -319,8 +339,8 @@ __global__ void __launch_bounds__(WG_THREADS) wgrad_kernel(WgradParams<T> p) {
     auto store = [&]() {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
-            As[aq * WG_M + ar + 8 * j] = ra[j];
-            Bs[bq * WG_N + bk + 8 * j] = rb[j];
+            As[aq * WG_P + ar + 8 * j] = ra[j];
+            Bs[bq * WG_P + bk + 8 * j] = rb[j];
         }
     };
 
@@ -346,10 +366,10 @@ __global__ void __launch_bounds__(WG_THREADS) wgrad_kernel(WgradParams<T> p) {
             A_t a[8], b[8];
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                a[i] = As[kk * WG_M + 4 * tm + i];
-                a[4 + i] = As[kk * WG_M + 64 + 4 * tm + i];
-                b[i] = Bs[kk * WG_N + 4 * tn + i];
-                b[4 + i] = Bs[kk * WG_N + 64 + 4 * tn + i];
+                a[i] = As[kk * WG_P + 4 * tm + i];
+                a[4 + i] = As[kk * WG_P + 64 + 4 * tm + i];
+                b[i] = Bs[kk * WG_P + 4 * tn + i];
+                b[4 + i] = Bs[kk * WG_P + 64 + 4 * tn + i];
             }
 #pragma unroll
             for (int i = 0; i < 8; ++i)
@@ -572,10 +592,16 @@ static void gather_run(const NNGeom &g, int mode, const T *A, long long SW, long
         maxM = ((DW + g.sx - 1) / g.sx) * ((DH + g.sy - 1) / g.sy) * g.N;
         phases = (unsigned)(g.sx * g.sy);
     }
-    dim3 grid((unsigned)((maxM + GB_M - 1) / GB_M), (unsigned)((NC + GB_N - 1) / GB_N), phases);
+    // 256-pixel x 64-channel tiles when the output has at most 64 channels
+    const bool narrow = NC <= 64;
+    const long long TMl = narrow ? 256 : 128, TNl = narrow ? 64 : 128;
+    dim3 grid((unsigned)((maxM + TMl - 1) / TMl), (unsigned)((NC + TNl - 1) / TNl), phases);
     if (maxM > 0 && NC > 0) {
         KernelTimer kt(mode == 0 ? "simt_fwd_kernel" : "simt_dgrad_kernel");
-        igemm_gather_kernel<T><<<grid, GB_THREADS, 0, stream()>>>(p);
+        if (narrow)
+            igemm_gather_kernel<T, 256, 64><<<grid, GB_THREADS, 0, stream()>>>(p);
+        else
+            igemm_gather_kernel<T, 128, 128><<<grid, GB_THREADS, 0, stream()>>>(p);
         count_launch();
         AFGB_POST_LAUNCH("igemm_gather_kernel");
     }
@@ -631,7 +657,7 @@ static void simt_wgrad_t(const NNGeom &g, const Array &grad, const Array &sig, A
         partial = static_cast<A_t *>(alloc_device((size_t)(splits * total) * sizeof(A_t)));
     }
     p.partial = partial;
-    size_t smem = (size_t)(WG_K * WG_M + WG_K * WG_N) * sizeof(A_t) + WG_M * (8 + 4 + 4);
+    size_t smem = (size_t)(2 * WG_K * WG_P) * sizeof(A_t) + WG_M * (8 + 4 + 4);
     AFGB_CUDA(cudaFuncSetAttribute(wgrad_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
     if (p.Q > 0) {
@@ -810,7 +836,7 @@ static void filter_grad_noalloc(const NNGeom &g, const float *grad, const float 
     }
     p.chunk = chunk;
     p.partial = scratch;
-    const size_t smem = (size_t)(WG_K * WG_M + WG_K * WG_N) * sizeof(float) + WG_M * (8 + 4 + 4);
+    const size_t smem = (size_t)(2 * WG_K * WG_P) * sizeof(float) + WG_M * (8 + 4 + 4);
     AFGB_CUDA(cudaFuncSetAttribute(wgrad_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
     // p.Q > 0: the entry point rejects empty signals and output grids.  Every
