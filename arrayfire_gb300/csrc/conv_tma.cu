@@ -12,18 +12,17 @@
 //
 // Arithmetic is the reference's (src/backend/cpu/kernel/convolve.hpp):
 // products accumulate from zero with the outer-dimension taps outside and
-// dim-0 taps inside.  The 2-D kernel runs one scalar FMA per tap and output
-// (a form that paired taps into packed f32x2 FMAs issued more instructions,
-// for the register-pair moves of odd-aligned windows, and was measured
-// slower).  The separable kernel's passes share one packed f32x2 instruction
-// between two outputs whose operands form aligned register pairs; packed
-// multiply and add round each lane separately, so the exact mode stays
-// bit-identical.
+// dim-0 taps inside.  Both kernels run one scalar FMA (exact mode: a rounded
+// product and sum) per tap and output.  Packed f32x2 FMAs occupy the FMA pipe
+// for two cycles, so they raise no FMA throughput on this part; their
+// register-pair moves for odd-aligned windows cost issue slots, and both
+// kernels measured slower with them.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <type_traits>
@@ -62,7 +61,19 @@ struct TileGrid {
     FastDiv b1, b2;       // batch extents of dims 2 and 3 (2-D kernel)
     int ntiles;
     int zstep[4];         // slice index step per batch coordinate (2-D kernel)
+    FastDiv run;          // consecutive tiles per CTA and round (2-D kernel)
 };
+// tile of a CTA's k-th step in the 2-D kernel: rounds of `run` consecutive
+// tiles per CTA (CTA c takes tiles c*run .. c*run + run-1 of each round of
+// gridDim.x * run).  Consecutive tiles of a CTA then mostly share one image
+// and its filter, and the CTAs running together still cover neighbouring
+// tiles, whose shared halo rows meet in L2.  Increasing in k, so a CTA is
+// done at its first tile past the end.
+__device__ __forceinline__ int run_tile(int k, const FastDiv &run) {
+    const int r = (int)fdiv((uint32_t)k, run);
+    const int n = (int)run.d;
+    return (r * (int)gridDim.x + (int)blockIdx.x) * n + (k - r * n);
+}
 struct TileRec {
     int tx, ty, z;
     long long out, filt;  // element offsets of the tile's output slice and filter
@@ -82,33 +93,6 @@ __device__ __forceinline__ TileRec decode_tile(int t, const TileGrid &tg, const 
     tr.filt = (long long)b1 * filt_step[1] + (long long)b2 * filt_step[2] +
               (long long)b3 * filt_step[3];
     return tr;
-}
-
-// ---------------------------------------------------------------- f32x2
-typedef unsigned long long f2;
-__device__ __forceinline__ f2 pk(float a, float b) {
-    f2 r;
-    asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a), "f"(b));
-    return r;
-}
-__device__ __forceinline__ void upk(f2 r, float &a, float &b) {
-    asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
-}
-// acc + a*b on both lanes.  The exact mode rounds the product and the sum
-// separately in each lane with __fmul_rn/__fadd_rn, which the compiler never
-// contracts (a packed mul.rn/add.rn pair may be fused into one FMA).
-template <bool EXACT>
-__device__ __forceinline__ f2 mac2(f2 acc, f2 a, f2 b) {
-    if (EXACT) {
-        float a0, a1, b0, b1, c0, c1;
-        upk(a, a0, a1);
-        upk(b, b0, b1);
-        upk(acc, c0, c1);
-        return pk(__fadd_rn(c0, __fmul_rn(a0, b0)), __fadd_rn(c1, __fmul_rn(a1, b1)));
-    }
-    f2 d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(acc));
-    return d;
 }
 
 __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap *map, uint64_t *bar,
@@ -142,8 +126,9 @@ template <typename T> __device__ __forceinline__ float to_f(T v) { return (float
 
 
 
-// geometry of a haloed tile for an F0 x F1 filter (shared by both kernels)
-template <typename T, int F0, int F1, bool EXPAND>
+// geometry of a haloed tile for an F0 x F1 filter, TW outputs wide (shared by
+// both kernels)
+template <typename T, int F0, int F1, bool EXPAND, int TW = TILE>
 struct Halo {
     static constexpr int ES = sizeof(T);
     static constexpr int A = 16 / ES;                 // TMA x alignment (elements)
@@ -158,10 +143,10 @@ struct Halo {
     // float tile pitch: covers the right halo; an odd number of 16-byte
     // words, so eight rows at the same column fall in eight different bank
     // groups (a conflict-free 128-bit access by eight lanes on eight rows)
-    static constexpr int PF0 = (LF + TILE + C0 + 3) / 4 * 4;
+    static constexpr int PF0 = (LF + TW + C0 + 3) / 4 * 4;
     static constexpr int PF = (PF0 / 4) % 2 ? PF0 : PF0 + 4;
     // TMA box width (elements); f32 loads straight into the float layout
-    static constexpr int BW = ES == 4 ? PF : (LT + TILE + C0 + A - 1) / A * A;
+    static constexpr int BW = ES == 4 ? PF : (LT + TW + C0 + A - 1) / A * A;
     static constexpr int TBYTES = BH * BW * ES;
     static constexpr int TB_ALIGNED = (TBYTES + 127) / 128 * 128;
     static constexpr int FT_BYTES = ES == 4 ? 0 : (BH * PF * 4 + 127) / 128 * 128;
@@ -196,20 +181,34 @@ __device__ __forceinline__ void widen_tile(const T *tb, float *ft) {
 }
 
 // ===========================================================================
-// 2-D direct convolution, F0 x F1 filter, 64x64 tile, 4x4 outputs per thread
+// 2-D direct convolution, F0 x F1 filter, 64 x (64 CG) tile, 4 x 4 CG outputs
+// per thread
 // ===========================================================================
-// Filters above 5x5 keep all their taps in registers at two CTAs per SM
-// (112 registers at 7x7); under a three-CTA cap (85) the 7x7 taps do not fit
-// and are fetched again inside the tap loop.
+// Filters above 5x5 keep all their taps in registers at two CTAs per SM; under
+// a three-CTA cap (85 registers) the 7x7 taps do not fit and are fetched again
+// inside the tap loop.  They also take two 64-column groups per tile (CG = 2:
+// a 128 x 64 tile, each thread 4 rows of columns 4 tx.. and 64 + 4 tx..): the
+// per-tile work outside the FMAs (tile decode, waits, barrier, stores' address
+// arithmetic) then spreads over twice the outputs, which matters where the
+// FMAs alone already fill most issue slots (49 per output at 7x7).
+template <typename T, int F0, int F1, bool EXACT> struct Conv2Shape {
+    // the exact mode's separate products and sums leave room for one group
+    static constexpr int CG = (!EXACT && F0 * F1 > 25) ? 2 : 1;
+};
+template <typename T, int F0, int F1, bool EXACT, bool EXPAND>
+using Conv2Halo = Halo<T, F0, F1, EXPAND, TILE * Conv2Shape<T, F0, F1, EXACT>::CG>;
+
 template <typename T, int F0, int F1, bool EXACT, bool EXPAND>
 __global__ void __launch_bounds__(THREADS, (F0 * F1 > 25) ? 2 : 3)
     conv2_tma_kernel(const __grid_constant__ CUtensorMap smap,
                                                             const DirectParams p,
                                                             const TileGrid tg) {
-    using H = Halo<T, F0, F1, EXPAND>;
+    using H = Conv2Halo<T, F0, F1, EXACT, EXPAND>;
+    constexpr int CG = Conv2Shape<T, F0, F1, EXACT>::CG;
+    constexpr int TWX = TILE * CG;
     constexpr int NST = NST_2D;
     constexpr int NW4 = (H::OFF + 4 + F0 - 1 + 3) / 4;
-    static_assert(60 + 4 * NW4 <= H::PF, "window exceeds the tile pitch");
+    static_assert(TILE * (CG - 1) + 60 + 4 * NW4 <= H::PF, "window exceeds the tile pitch");
     extern __shared__ __align__(128) unsigned char sm[];
     auto tb = [&](int i) { return reinterpret_cast<T *>(sm + i * H::TB_ALIGNED); };
     float *ft = reinterpret_cast<float *>(sm + NST * H::TB_ALIGNED);
@@ -228,23 +227,26 @@ __global__ void __launch_bounds__(THREADS, (F0 * F1 > 25) ? 2 : 3)
         const TileRec tr = decode_tile(t, tg, p.out_step, p.filt_step);
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         mbar_arrive_expect_tx(&full[buf], H::TBYTES);
-        tma_load_3d(smem_u32(tb(buf)), &smap, &full[buf], tr.tx * TILE - H::LT,
+        tma_load_3d(smem_u32(tb(buf)), &smap, &full[buf], tr.tx * TWX - H::LT,
                     tr.ty * TILE - H::LY, tr.z);
     };
 
-    int tile = blockIdx.x;
     if (tid == 0)
-        for (int i = 0; i < NST - 1; ++i)
-            if (tile + i * (int)gridDim.x < tg.ntiles) issue(tile + i * (int)gridDim.x, i);
+        for (int i = 0; i < NST - 1; ++i) {
+            const int t = run_tile(i, tg.run);
+            if (t < tg.ntiles) issue(t, i);
+        }
     const int tx = tid & 15, ty = tid >> 4;
     // the taps stay in registers from tile to tile and are reloaded only when
     // a tile's filter differs from the previous one (consecutive tiles of a
     // CTA mostly belong to one image)
     long long cur_filt = -1;
     float wr[F0 * F1];
-    for (int k = 0; tile < tg.ntiles; tile += gridDim.x, ++k) {
+    for (int k = 0;; ++k) {
+        const int tile = run_tile(k, tg.run);
+        if (tile >= tg.ntiles) break;
         const int buf = k % NST;
-        const int ahead = tile + (NST - 1) * (int)gridDim.x;
+        const int ahead = run_tile(k + NST - 1, tg.run);
         if (tid == 0 && ahead < tg.ntiles) issue(ahead, (k + NST - 1) % NST);
         const TileRec tr = decode_tile(tile, tg, p.out_step, p.filt_step);
         const int ttx = tr.tx, tty = tr.ty;
@@ -269,63 +271,73 @@ __global__ void __launch_bounds__(THREADS, (F0 * F1 > 25) ? 2 : 3)
             tile_f = ft;
         }
 
-        float acc[4][4];
+        float acc[CG][4][4];
         // one scalar FMA (or, in the exact mode, a rounded product and sum) per
         // tap and output; fused mode only changes the rounding
 #pragma unroll
-        for (int a = 0; a < 4; ++a)
+        for (int g = 0; g < CG; ++g)
 #pragma unroll
-            for (int c = 0; c < 4; ++c) acc[a][c] = 0.0f;
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int c = 0; c < 4; ++c) acc[g][a][c] = 0.0f;
 #pragma unroll
         for (int q = 3 + F1 - 1; q >= 0; --q) {
-            float v[NW4 * 4];
-            const float *row = tile_f + (4 * ty + q) * H::PF + 4 * tx;
 #pragma unroll
-            for (int u = 0; u < NW4; ++u) {
-                const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
-                v[4 * u] = t4.x;
-                v[4 * u + 1] = t4.y;
-                v[4 * u + 2] = t4.z;
-                v[4 * u + 3] = t4.w;
-            }
+            for (int g = 0; g < CG; ++g) {
+                float v[NW4 * 4];
+                const float *row = tile_f + (4 * ty + q) * H::PF + TILE * g + 4 * tx;
 #pragma unroll
-            for (int rr = 0; rr < 4; ++rr) {
-                const int fj = rr + F1 - 1 - q;
-                if (fj >= 0 && fj < F1) {
+                for (int u = 0; u < NW4; ++u) {
+                    const float4 t4 = *reinterpret_cast<const float4 *>(row + 4 * u);
+                    v[4 * u] = t4.x;
+                    v[4 * u + 1] = t4.y;
+                    v[4 * u + 2] = t4.z;
+                    v[4 * u + 3] = t4.w;
+                }
 #pragma unroll
-                    for (int fi = 0; fi < F0; ++fi) {
-                        const float wv = wr[fj * F0 + fi];
+                for (int rr = 0; rr < 4; ++rr) {
+                    const int fj = rr + F1 - 1 - q;
+                    if (fj >= 0 && fj < F1) {
 #pragma unroll
-                        for (int cc = 0; cc < 4; ++cc)
-                            acc[rr][cc] = mac<EXACT>(acc[rr][cc], v[cc + H::OFF + F0 - 1 - fi], wv);
+                        for (int fi = 0; fi < F0; ++fi) {
+                            const float wv = wr[fj * F0 + fi];
+#pragma unroll
+                            for (int cc = 0; cc < 4; ++cc)
+                                acc[g][rr][cc] =
+                                    mac<EXACT>(acc[g][rr][cc], v[cc + H::OFF + F0 - 1 - fi], wv);
+                        }
                     }
                 }
             }
         }
         T *out = static_cast<T *>(p.out) + out_off;
-        const long long x = (long long)ttx * TILE + 4 * tx;
-        const bool vec = (x + 3 < p.od[0]) && ((p.os[1] & 3) == 0) &&
-                         ((reinterpret_cast<uintptr_t>(out) % (4 * sizeof(T))) == 0);
+        const bool row_vec = ((p.os[1] & 3) == 0) &&
+                             ((reinterpret_cast<uintptr_t>(out) % (4 * sizeof(T))) == 0);
 #pragma unroll
-        for (int rr = 0; rr < 4; ++rr) {
-            const long long y = (long long)tty * TILE + 4 * ty + rr;
-            if (y >= p.od[1] || x >= p.od[0]) continue;
-            T *dst = out + y * p.os[1] + x;
-            if (vec) {
-                if constexpr (sizeof(T) == 4) {
-                    *reinterpret_cast<float4 *>(dst) =
-                        make_float4(acc[rr][0], acc[rr][1], acc[rr][2], acc[rr][3]);
+        for (int g = 0; g < CG; ++g) {
+            const long long x = (long long)ttx * TWX + TILE * g + 4 * tx;
+            const bool vec = row_vec && (x + 3 < p.od[0]);
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                const long long y = (long long)tty * TILE + 4 * ty + rr;
+                if (y >= p.od[1] || x >= p.od[0]) continue;
+                T *dst = out + y * p.os[1] + x;
+                if (vec) {
+                    if constexpr (sizeof(T) == 4) {
+                        *reinterpret_cast<float4 *>(dst) =
+                            make_float4(acc[g][rr][0], acc[g][rr][1], acc[g][rr][2], acc[g][rr][3]);
+                    } else {
+                        const uint32_t w4 = (uint32_t)(uint8_t)from_acc<T>(acc[g][rr][0]) |
+                                            ((uint32_t)(uint8_t)from_acc<T>(acc[g][rr][1]) << 8) |
+                                            ((uint32_t)(uint8_t)from_acc<T>(acc[g][rr][2]) << 16) |
+                                            ((uint32_t)(uint8_t)from_acc<T>(acc[g][rr][3]) << 24);
+                        *reinterpret_cast<uint32_t *>(dst) = w4;
+                    }
                 } else {
-                    const uint32_t w4 = (uint32_t)(uint8_t)from_acc<T>(acc[rr][0]) |
-                                        ((uint32_t)(uint8_t)from_acc<T>(acc[rr][1]) << 8) |
-                                        ((uint32_t)(uint8_t)from_acc<T>(acc[rr][2]) << 16) |
-                                        ((uint32_t)(uint8_t)from_acc<T>(acc[rr][3]) << 24);
-                    *reinterpret_cast<uint32_t *>(dst) = w4;
-                }
-            } else {
 #pragma unroll
-                for (int cc = 0; cc < 4; ++cc)
-                    if (x + cc < p.od[0]) dst[cc] = from_acc_any(acc[rr][cc], T{});
+                    for (int cc = 0; cc < 4; ++cc)
+                        if (x + cc < p.od[0]) dst[cc] = from_acc_any(acc[g][rr][cc], T{});
+                }
             }
         }
         __syncthreads();  // this buffer is reloaded at the next iteration's issue
@@ -374,11 +386,11 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
     if (tid < CFL) ctap[tid] = sep_tap<T>(p.cf[tid]);
     if (tid < RFL) rtap[tid] = sep_tap<T>(p.rf[tid]);
     __syncthreads();
-    f2 c2[CFL], r2[RFL];
+    float cr[CFL], rr_[RFL];
 #pragma unroll
-    for (int f = 0; f < CFL; ++f) c2[f] = pk(ctap[f], ctap[f]);
+    for (int f = 0; f < CFL; ++f) cr[f] = ctap[f];
 #pragma unroll
-    for (int f = 0; f < RFL; ++f) r2[f] = pk(rtap[f], rtap[f]);
+    for (int f = 0; f < RFL; ++f) rr_[f] = rtap[f];
 
     auto issue = [&](int t, int buf) {
         const uint32_t r = fdiv((uint32_t)t, tg.tx);
@@ -421,7 +433,9 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
             const int row = (it >> 6) * 8 + (it & 7), g = (it >> 3) & 7;
             if (row >= H::BH) continue;
             const long long gy = y_top + row;
-            f2 a2[4] = {0ull, 0ull, 0ull, 0ull};
+            float a[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) a[e] = 0.0f;
             if (gy >= 0 && gy < p.sd1) {
                 float v[NWP * 4];
                 const float *src = tile_f + row * H::PF + 8 * g;
@@ -433,28 +447,13 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
                     v[4 * u + 2] = t4.z;
                     v[4 * u + 3] = t4.w;
                 }
-                // aligned pairs (v0,v1),(v2,v3).. and shifted pairs (v1,v2),(v3,v4)..
-                f2 ve[NWP * 2], vo[NWP * 2 - 1];
-#pragma unroll
-                for (int i = 0; i < NWP * 2; ++i) ve[i] = pk(v[2 * i], v[2 * i + 1]);
-#pragma unroll
-                for (int i = 0; i < NWP * 2 - 1; ++i) vo[i] = pk(v[2 * i + 1], v[2 * i + 2]);
 #pragma unroll
                 for (int f = 0; f < CFL; ++f) {
-                    constexpr int dummy = 0;
-                    (void)dummy;
                     const int j0 = H::OFF + CFL - 1 - f;  // window index of output 0
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const int j = j0 + 2 * e;
-                        const f2 in2 = (j & 1) ? vo[(j - 1) >> 1] : ve[j >> 1];
-                        a2[e] = mac2<EXACT>(a2[e], in2, c2[f]);
-                    }
+                    for (int e = 0; e < 8; ++e) a[e] = mac<EXACT>(a[e], v[j0 + e], cr[f]);
                 }
             }
-            float a[8];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) upk(a2[e], a[2 * e], a[2 * e + 1]);
 #pragma unroll
             for (int e = 0; e < 8; ++e) a[e] = sep_round<T>(a[e]);
             float *trow = temp + row * SEP_TP + 8 * g;
@@ -464,19 +463,21 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
         __syncthreads();
         // pass 2: out[x][y] = IN( sum_g temp[y + RFL-1-g][x] * r[g] ), 4x4 per thread
         const int tx = tid & 15, ty = tid >> 4;
-        f2 acc[4][2];
+        float acc[4][4];
 #pragma unroll
-        for (int rr = 0; rr < 4; ++rr) acc[rr][0] = acc[rr][1] = 0ull;
+        for (int rr = 0; rr < 4; ++rr)
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) acc[rr][cc] = 0.0f;
 #pragma unroll
         for (int q = 3 + RFL - 1; q >= 0; --q) {
             const float4 t4 = *reinterpret_cast<const float4 *>(temp + (4 * ty + q) * SEP_TP + 4 * tx);
-            const f2 lo = pk(t4.x, t4.y), hi = pk(t4.z, t4.w);
+            const float tv[4] = {t4.x, t4.y, t4.z, t4.w};
 #pragma unroll
             for (int rr = 0; rr < 4; ++rr) {
                 const int g = rr + RFL - 1 - q;
                 if (g >= 0 && g < RFL) {
-                    acc[rr][0] = mac2<EXACT>(acc[rr][0], lo, r2[g]);
-                    acc[rr][1] = mac2<EXACT>(acc[rr][1], hi, r2[g]);
+#pragma unroll
+                    for (int cc = 0; cc < 4; ++cc) acc[rr][cc] = mac<EXACT>(acc[rr][cc], tv[cc], rr_[g]);
                 }
             }
         }
@@ -488,9 +489,7 @@ __global__ void __launch_bounds__(THREADS) sep_tma_kernel(const __grid_constant_
         for (int rr = 0; rr < 4; ++rr) {
             const long long y = (long long)tty * TILE + 4 * ty + rr;
             if (y >= p.od1 || x >= p.od0) continue;
-            float o[4];
-            upk(acc[rr][0], o[0], o[1]);
-            upk(acc[rr][1], o[2], o[3]);
+            const float *o = acc[rr];
             T *dst = out + y * p.od0 + x;
             if (vec) {
                 if constexpr (sizeof(T) == 4) {
@@ -897,10 +896,12 @@ static int persistent_grid(K kernel, size_t smem, long long ntiles) {
     return (int)std::max(1LL, std::min<long long>(ntiles, (long long)num_sms() * per_sm));
 }
 
-// tile grid of a launch; false when a count exceeds the 31-bit decoder
+// tile grid of a launch; false when a count exceeds the decoder's range
+// (tile indices, and the 2-D kernel's run order past the last tile, stay
+// below 2^31)
 static bool make_grid(TileGrid &tg, long long tiles_x, long long tiles_y, long long nbatch,
                       long long b1 = 1, long long b2 = 1) {
-    const long long lim = 1LL << 31;
+    const long long lim = 1LL << 30;
     if (tiles_x < 1 || tiles_y < 1 || b1 < 1 || b2 < 1) return false;
     if (tiles_x * tiles_y * nbatch >= lim || b1 >= lim || b2 >= lim) return false;
     std::memset(&tg, 0, sizeof(tg));
@@ -909,15 +910,36 @@ static bool make_grid(TileGrid &tg, long long tiles_x, long long tiles_y, long l
     tg.b1 = make_fastdiv((uint32_t)b1);
     tg.b2 = make_fastdiv((uint32_t)b2);
     tg.ntiles = (int)(tiles_x * tiles_y * nbatch);
+    tg.run = make_fastdiv(1);
     return true;
+}
+
+// run length of the 2-D kernel's tile order: the longest of 8, 4, 2 whose
+// last, partial round costs at most 3 % more steps on the busiest CTA than
+// single tiles do (AFGB_TILE_RUN overrides, for tests)
+static int tile_run(long long ntiles, int grid) {
+    static const int forced = [] {
+        const char *e = std::getenv("AFGB_TILE_RUN");
+        const int v = e ? std::atoi(e) : 0;
+        return v >= 1 && v <= 64 ? v : 0;
+    }();
+    if (forced) return forced;
+    const long long g = std::max(1, grid);
+    const long long base = (ntiles + g - 1) / g;
+    for (int r = 8; r > 1; r /= 2) {
+        const long long steps = (ntiles + g * r - 1) / (g * r) * r;
+        if (steps * 100 <= base * 103) return r;
+    }
+    return 1;
 }
 
 template <typename T, int F0, int F1, bool EXACT, bool EXPAND>
 static bool run_conv2(const DirectParams &p) {
-    using H = Halo<T, F0, F1, EXPAND>;
+    using H = Conv2Halo<T, F0, F1, EXACT, EXPAND>;
+    constexpr int TWX = TILE * Conv2Shape<T, F0, F1, EXACT>::CG;
     const long long slice = p.sd[0] * p.sd[1];
     const long long slices = p.sd[2] * p.sd[3];
-    const long long tx = (p.od[0] + TILE - 1) / TILE, ty = (p.od[1] + TILE - 1) / TILE;
+    const long long tx = (p.od[0] + TWX - 1) / TWX, ty = (p.od[1] + TILE - 1) / TILE;
     TileGrid tg;
     if (!make_grid(tg, tx, ty, p.nbatch, p.batch[1], p.batch[2])) return false;
     // slice index of a batch coordinate: the signal is dense, so each batch
@@ -934,6 +956,7 @@ static bool run_conv2(const DirectParams &p) {
     auto kfn = conv2_tma_kernel<T, F0, F1, EXACT, EXPAND>;
     AFGB_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const int grid = persistent_grid(kfn, smem, tg.ntiles);
+    tg.run = make_fastdiv((uint32_t)tile_run(tg.ntiles, grid));
     {
         KernelTimer kt("conv2_tma_kernel");
         kfn<<<grid, THREADS, smem, stream()>>>(m, p, tg);

@@ -205,6 +205,60 @@ def test_conv2_tma_many_tiles_per_cta(af, oracle, fsz, expand, kind):
     assert_same(out.to_numpy(), oracle.convolve(s, f, C.F32, 2, expand))
 
 
+RUN_CHILD = r"""
+import json, sys
+import numpy as np
+sys.path.insert(0, sys.argv[1]); sys.path.insert(0, sys.argv[1] + "/tests/golden")
+import torch
+import arrayfire_gb300 as af
+import oracle as O
+import cases as C
+O.build_port()
+af.lib(); torch.cuda.init(); af.set_stream(torch.cuda.current_stream())
+res = {}
+for i, (name, fsz, kind, expand, dt) in enumerate(json.loads(sys.argv[2])):
+    code = C.U8 if dt == "u8" else C.F32
+    nb = 12
+    s = C.make_signal(code, (520, 200, nb), 910 + i)
+    f = C.make_filter(code, (fsz, fsz) + ((nb,) if kind == "same" else ()), 930 + i, 2)
+    S = af.Array.from_numpy(s, code)
+    F = af.Array.from_numpy(f)
+    mode = af.AF_CONV_EXPAND if expand else af.AF_CONV_DEFAULT
+    af.set_exact_fp(True)
+    out = af.convolve2(S, F, mode, af.AF_CONV_SPATIAL).to_numpy()
+    af.set_exact_fp(False)
+    ref = O.convolve(s, f, code, 2, expand)
+    res[name] = bool(out.tobytes() == ref.tobytes())
+print(json.dumps(res))
+"""
+
+
+@pytest.mark.parametrize("run_len", [3, 8])
+def test_conv2_tma_tile_runs_in_child_process(run_len):
+    """The 2-D kernel's tile order with a forced run length (AFGB_TILE_RUN, in
+    a child process): each CTA takes `run_len` consecutive tiles per round,
+    so runs cross image boundaries (a filter change inside a run, SAME batch
+    of 12 distinct filters), the last round is partial and most CTAs get no
+    tile of it.  Every output bit for bit in the exact mode, f32 and u8,
+    for the 128-wide (7x7) and 64-wide (3x3, 5x5) tiles."""
+    import json
+    import os
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parents[1]
+    cases = [["f32_7x7_same", 7, "same", False, "f32"], ["f32_7x7_lhs_expand", 7, "lhs", True, "f32"],
+             ["f32_5x5_same_expand", 5, "same", True, "f32"], ["f32_3x3_same", 3, "same", False, "f32"],
+             ["u8_7x7_same", 7, "same", False, "u8"], ["u8_3x3_lhs", 3, "lhs", False, "u8"]]
+    env = dict(os.environ, AFGB_TILE_RUN=str(run_len))
+    r = subprocess.run([sys.executable, "-c", RUN_CHILD, str(root), json.dumps(cases)],
+                       capture_output=True, text=True, env=env, timeout=600)
+    assert r.returncode == 0, r.stderr[-3000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    assert res == {c[0]: True for c in cases}, res
+
+
 def test_sep15_f32_64x2048sq(af, oracle):
     """The fused separable kernel on 64 images of 2048x2048 (15 + 15 taps):
     three slices bit for bit in the exact mode, one in the fused mode."""
