@@ -837,9 +837,10 @@ __global__ void __launch_bounds__(256) conv1_tile_kernel(DirectParams p, long lo
 // ---- 1-D, f32, unit-stride signal and output rows: persistent blocks walk
 // tiles of C1P_T outputs through a C1P_NST-stage ring filled by 16-byte
 // cp.async copies (zero-filled outside the signal).  Thread t owns outputs
-// 16t .. 16t+15 of a tile and slides a register window over the input: the
-// taps run in chunks of eight, each chunk loading 24 inputs with six 128-bit
-// shared loads for 128 multiply-adds.
+// 32t .. 32t+31 of a tile and slides a register window over the input: the
+// taps run in chunks of eight, each chunk loading 40 inputs with ten 128-bit
+// shared loads for 256 multiply-adds (with 16 outputs per thread, half of
+// the instructions were not FMAs).
 //
 // The copy grid is aligned to the absolute address, so a tile's staged span
 // starts `mis` (0..3) elements before its first needed input.  Chunk k of
@@ -847,20 +848,25 @@ __global__ void __launch_bounds__(256) conv1_tile_kernel(DirectParams p, long lo
 // W_hi = F - 1 + mis, which makes every thread's window start on a 16-byte
 // boundary; k outside [mis, W_hi] is no tap and is skipped (never multiplied
 // by zero, so an inf or NaN next to the window cannot leak in).
-// Shared layout: 16-float groups at a pitch of 20 floats, so eight lanes
-// reading 128 bits at the same offset of consecutive groups hit eight
-// different bank quads.
-constexpr int C1P_T = 4096;
-constexpr int C1P_THREADS = 256;
-constexpr int C1P_NST = 3;
+// Shared layout: 32-float groups at a pitch of 36 floats (nine 16-byte
+// words), so eight lanes reading 128 bits at the same offset of consecutive
+// groups hit eight different bank quads.
+constexpr int C1P_OPT = 32;   // outputs per thread
+constexpr int C1P_THREADS = 128;
+constexpr int C1P_T = C1P_OPT * C1P_THREADS;
+constexpr int C1P_NST = 2;
+static_assert(C1P_NST >= 2, "the ring issues the next tile after the barrier that frees its stage");
 constexpr int C1P_MAXF = 129;
+constexpr int C1P_GP = 36;    // group pitch (floats)
 // the last thread's window of the last chunk ends at element
-// 16*255 + 8*(M-1) + 23 with M <= (C1P_MAXF + 2) / 8 + 1
-constexpr int C1P_GROUPS = (16 * 255 + 8 * ((C1P_MAXF + 2) / 8) + 24 + 15) / 16;
-constexpr int C1P_STAGE = C1P_GROUPS * 20;                        // floats
+// 32*127 + 8*(M-1) + 39 with M <= (C1P_MAXF + 2) / 8 + 1
+constexpr int C1P_GROUPS = (C1P_OPT * (C1P_THREADS - 1) + 8 * ((C1P_MAXF + 2) / 8) + 40 + 31) / 32;
+constexpr int C1P_STAGE = C1P_GROUPS * C1P_GP;                    // floats
 constexpr int C1P_WMAX = 8 * ((C1P_MAXF + 2) / 8 + 1);            // padded taps
 // taps staged with each tile (reversed and zero-padded for its `mis`)
 constexpr size_t C1P_SMEM = (size_t)C1P_NST * C1P_STAGE * 4 + (size_t)C1P_NST * C1P_WMAX * 4;
+// staged element e of a tile (e >= 0)
+__device__ __forceinline__ int c1p_at(int e) { return (e >> 5) * C1P_GP + (e & 31); }
 
 // one tap into shared memory, or zero when bytes == 0
 __device__ __forceinline__ void c1p_copy4(float *dst, const float *src, int bytes) {
@@ -877,17 +883,16 @@ __device__ __forceinline__ void c1p_copy16(float *dst, const float *src, int byt
                  : "memory");
 }
 
-// one chunk of eight taps for the 16 outputs of a thread.  gb points at the
-// thread's group for this chunk pair; ODD selects the second chunk of the
-// pair (window starting 8 floats into the group).  wk holds the chunk's
-// eight taps; k0 is the chunk's first padded tap index and [klo, khi] the
-// real taps.
-template <bool ODD>
-__device__ __forceinline__ void c1p_window(float (&win)[24], const float *gb) {
+// one chunk of eight taps for the 32 outputs of a thread.  gb points at the
+// thread's first group for this chunk; PH (0..3) is the chunk's window
+// start within it, 8 PH floats.  wk holds the chunk's eight taps; k0 is the
+// chunk's first padded tap index and [klo, khi] the real taps.
+template <int PH>
+__device__ __forceinline__ void c1p_window(float (&win)[40], const float *gb) {
 #pragma unroll
-    for (int q = 0; q < 6; ++q) {
-        const int x = ODD ? q + 2 : q;
-        const float4 v = *reinterpret_cast<const float4 *>(gb + (x >> 2) * 20 + (x & 3) * 4);
+    for (int q = 0; q < 10; ++q) {
+        const int o = 8 * PH + 4 * q;
+        const float4 v = *reinterpret_cast<const float4 *>(gb + (o >> 5) * C1P_GP + (o & 31));
         win[4 * q] = v.x;
         win[4 * q + 1] = v.y;
         win[4 * q + 2] = v.z;
@@ -896,13 +901,12 @@ __device__ __forceinline__ void c1p_window(float (&win)[24], const float *gb) {
 }
 
 // fused mode: one fused multiply-add per tap and output from the register
-// window (packing output pairs into f32x2 FMAs needs a register-pair move
-// per misaligned window pair, which cost more issue slots than it saved)
-template <bool ODD, bool FULL>
-__device__ __forceinline__ void c1p_chunk_fused(float (&acc)[16], const float *gb, const float *wk,
+// window
+template <int PH, bool FULL>
+__device__ __forceinline__ void c1p_chunk_fused(float (&acc)[C1P_OPT], const float *gb, const float *wk,
                                                 int k0, int klo, int khi) {
-    float win[24];
-    c1p_window<ODD>(win, gb);
+    float win[40];
+    c1p_window<PH>(win, gb);
     const float4 wa = *reinterpret_cast<const float4 *>(wk);
     const float4 wb = *reinterpret_cast<const float4 *>(wk + 4);
     const float w[8] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
@@ -910,30 +914,57 @@ __device__ __forceinline__ void c1p_chunk_fused(float (&acc)[16], const float *g
     for (int r = 0; r < 8; ++r) {
         if (FULL || (k0 + r >= klo && k0 + r <= khi)) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc[j] = __fmaf_rn(win[j + r], w[r], acc[j]);
+            for (int j = 0; j < C1P_OPT; ++j) acc[j] = __fmaf_rn(win[j + r], w[r], acc[j]);
         }
     }
 }
 
 // exact mode: taps in ascending wi, i.e. descending k, each product and sum
 // rounded separately
-template <bool ODD, bool FULL>
-__device__ __forceinline__ void c1p_chunk_exact(float (&acc)[16], const float *gb, const float *wk,
+template <int PH, bool FULL>
+__device__ __forceinline__ void c1p_chunk_exact(float (&acc)[C1P_OPT], const float *gb, const float *wk,
                                                 int k0, int klo, int khi) {
-    float win[24];
-    c1p_window<ODD>(win, gb);
+    float win[40];
+    c1p_window<PH>(win, gb);
 #pragma unroll
     for (int r = 7; r >= 0; --r) {
         if (FULL || (k0 + r >= klo && k0 + r <= khi)) {
             const float w = wk[r];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) acc[j] = mac<true>(acc[j], win[j + r], w);
+            for (int j = 0; j < C1P_OPT; ++j) acc[j] = mac<true>(acc[j], win[j + r], w);
         }
     }
 }
 
+// chunk m of a thread's window, dispatched on its phase and on whether all
+// eight of its taps are real
 template <bool EXACT>
-__global__ void __launch_bounds__(C1P_THREADS, 3)
+__device__ __forceinline__ void c1p_chunk(float (&acc)[C1P_OPT], const float *st, const float *wbuf,
+                                          int m, int mis, int whi) {
+    const float *gb = st + (threadIdx.x + (m >> 2)) * C1P_GP;
+    const float *wk = wbuf + 8 * m;
+    const bool full = 8 * m >= mis && 8 * m + 7 <= whi;
+#define C1P_CASE(PH)                                                                          \
+    case PH:                                                                                  \
+        if (EXACT) {                                                                          \
+            if (full) c1p_chunk_exact<PH, true>(acc, gb, wk, 8 * m, mis, whi);                \
+            else c1p_chunk_exact<PH, false>(acc, gb, wk, 8 * m, mis, whi);                    \
+        } else {                                                                              \
+            if (full) c1p_chunk_fused<PH, true>(acc, gb, wk, 8 * m, mis, whi);                \
+            else c1p_chunk_fused<PH, false>(acc, gb, wk, 8 * m, mis, whi);                    \
+        }                                                                                     \
+        break;
+    switch (m & 3) {
+        C1P_CASE(0)
+        C1P_CASE(1)
+        C1P_CASE(2)
+        C1P_CASE(3)
+    }
+#undef C1P_CASE
+}
+
+template <bool EXACT>
+__global__ void __launch_bounds__(C1P_THREADS, 4)
     conv1_pipe_kernel(const DirectParams p, long long ntx, long long ntiles) {
     extern __shared__ __align__(16) float c1p_smem[];
     float *wring = c1p_smem + C1P_NST * C1P_STAGE;  // C1P_NST x C1P_WMAX staged taps
@@ -985,7 +1016,7 @@ __global__ void __launch_bounds__(C1P_THREADS, 3)
                 bytes = (int)min(4LL, len - ci) * 4;
                 src = sp + ci;  // up to 3 elements before the slice: zeroed after landing
             }
-            c1p_copy16(st + (c >> 2) * 20 + (c & 3) * 4, src, bytes);
+            c1p_copy16(st + c1p_at(4 * c), src, bytes);
         }
         // the tile's taps, reversed from W_hi = F - 1 + mis and zero outside
         // [0, F), arrive with the same copy group: no global load waits at
@@ -1007,75 +1038,55 @@ __global__ void __launch_bounds__(C1P_THREADS, 3)
         if (t < ntiles) issue(t, i);
         asm volatile("cp.async.commit_group;" ::: "memory");
     }
-    __syncthreads();  // the prologue's tile records
     long long k = 0;
 #pragma unroll 1
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++k) {
         const int buf = (int)(k % C1P_NST);
+        // this thread's copies of this tile have landed (the later tiles'
+        // groups may still be in flight); after the barrier every thread's
+        // have, and every thread is done with the previous tile, whose
+        // stage and record the next issue overwrites: one barrier per tile
+        asm volatile("cp.async.wait_group %0;" ::"n"(C1P_NST - 2) : "memory");
+        __syncthreads();
         const long long ahead = tile + (long long)(C1P_NST - 1) * gridDim.x;
         if (ahead < ntiles) issue(ahead, (int)((k + C1P_NST - 1) % C1P_NST));
         asm volatile("cp.async.commit_group;" ::: "memory");
-        asm volatile("cp.async.wait_group %0;" ::"n"(C1P_NST - 1) : "memory");
-        // tinfo[buf] was written when this tile was issued, at least one
-        // barrier ago (the prologue's, or an earlier iteration's last)
+        // tinfo[buf] was written when this tile was issued, before this
+        // iteration's barrier
         const Tile t = tinfo[buf];
         const int whi = F - 1 + t.mis;
         const int M = whi / 8 + 1;
         const float *wbuf = wring + buf * C1P_WMAX;
-        __syncthreads();  // every thread's copies of this stage have landed
         float *st = c1p_smem + buf * C1P_STAGE;
         if (t.lo < 0) {  // staged elements before the signal start read as zero
-            const int nz = (int)min(-t.lo, (long long)C1P_STAGE);
-            for (int e = tid; e < nz; e += C1P_THREADS) st[(e >> 4) * 20 + (e & 15)] = 0.0f;
+            const int nz = (int)min(-t.lo, (long long)C1P_GROUPS * 32);
+            for (int e = tid; e < nz; e += C1P_THREADS) st[c1p_at(e)] = 0.0f;
             __syncthreads();
         }
-        const long long i0 = t.x0 + 16LL * tid;
-        float res[16];
+        const long long i0 = t.x0 + (long long)C1P_OPT * tid;
+        float res[C1P_OPT];
+#pragma unroll
+        for (int j = 0; j < C1P_OPT; ++j) res[j] = 0.0f;
         if (EXACT) {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) res[j] = 0.0f;
 #pragma unroll 1
-            for (int m = M - 1; m >= 0; --m) {
-                const float *gb = st + (tid + (m >> 1)) * 20;
-                const bool full = 8 * m >= t.mis && 8 * m + 7 <= whi;
-                if (m & 1) {
-                    if (full) c1p_chunk_exact<true, true>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
-                    else c1p_chunk_exact<true, false>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
-                } else {
-                    if (full) c1p_chunk_exact<false, true>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
-                    else c1p_chunk_exact<false, false>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
-                }
-            }
+            for (int m = M - 1; m >= 0; --m) c1p_chunk<true>(res, st, wbuf, m, t.mis, whi);
         } else {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) res[j] = 0.0f;
 #pragma unroll 1
-            for (int m = 0; m < M; ++m) {
-                const float *gb = st + (tid + (m >> 1)) * 20;
-                const bool full = 8 * m >= t.mis && 8 * m + 7 <= whi;
-                if (m & 1) {
-                    if (full) c1p_chunk_fused<true, true>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
-                    else c1p_chunk_fused<true, false>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
-                } else {
-                    if (full) c1p_chunk_fused<false, true>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
-                    else c1p_chunk_fused<false, false>(res, gb, wbuf + 8 * m, 8 * m, t.mis, whi);
-                }
-            }
+            for (int m = 0; m < M; ++m) c1p_chunk<false>(res, st, wbuf, m, t.mis, whi);
         }
         if (i0 < od) {
             float *op = out + t.bo.out + i0;
-            if (i0 + 15 < od && (reinterpret_cast<uintptr_t>(op) & 15) == 0) {
+            if (i0 + C1P_OPT - 1 < od && (reinterpret_cast<uintptr_t>(op) & 15) == 0) {
 #pragma unroll
-                for (int q = 0; q < 4; ++q)
+                for (int q = 0; q < C1P_OPT / 4; ++q)
                     reinterpret_cast<float4 *>(op)[q] =
                         make_float4(res[4 * q], res[4 * q + 1], res[4 * q + 2], res[4 * q + 3]);
             } else {
 #pragma unroll
-                for (int j = 0; j < 16; ++j)
+                for (int j = 0; j < C1P_OPT; ++j)
                     if (i0 + j < od) op[j] = res[j];
             }
         }
-        __syncthreads();  // this stage and the taps are rewritten next
     }
     asm volatile("cp.async.wait_all;" ::: "memory");
 }
