@@ -1,10 +1,12 @@
 // TMA-staged direct convolutions (2-D filters and the fused separable pair)
 // for dense, 16-byte-aligned f32 and 8-bit images.
 //
-// Each CTA is persistent: it walks 64x64 output tiles with a stride of the
-// grid, and one thread keeps the next tile's haloed input window in flight
-// with a 3-D TMA box load (x, y, image) while the CTA computes the current
-// one.  The TMA fills coordinates outside the image with zeros, which is the
+// Each CTA is persistent: it walks output tiles (64 rows of 64 outputs, or
+// of 128 for 7x7 filters) in an order shared by the grid (the separable
+// kernel strides by the grid; the 2-D kernel takes runs of consecutive tiles
+// per round), and one thread keeps the next tile's haloed input window in
+// flight with a 3-D TMA box load (x, y, image) while the CTA computes the
+// current one.  The TMA fills coordinates outside the image with zeros, which is the
 // convolution's zero padding, so no thread computes an address or a bounds
 // check for the input.  The box's x origin is rounded down to the 16-byte
 // TMA alignment; the compute loops absorb that shift with compile-time
