@@ -940,7 +940,7 @@ def run_direct_workloads(af, O, peaks, args) -> dict:
             lambda: af.convolve2(S, F7, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL),
             n * 8 + f7.size * 4, ("conv2_tma_kernel", "conv2_tile_kernel"), chk7)
     # ---- a 31x31 filter: AUTO takes the frequency-domain route (the whole
-    # pipeline is timed: pads, cuFFT transforms, spectrum product, crop)
+    # pipeline is timed: pads, the library's transforms, spectrum product, crop)
     f31 = g.standard_normal((31, 31))
     f31 = np.asfortranarray((f31 / f31.sum()).astype(np.float32))
     F31 = af.Array.from_numpy(f31)
@@ -960,7 +960,7 @@ def run_direct_workloads(af, O, peaks, args) -> dict:
     # 2*31*31 flops per output
     e = out["fft31x31_f32_64x2048x2048"]
     e["equivalent_direct_TFLOP/s"] = round(2 * 31 * 31 * n / (e["ms"] / 1e3) / 1e12, 1)
-    e["bound"] = "cuFFT transforms (multi-pass), not one HBM pass"
+    e["bound"] = "the library's mixed-radix transforms (multi-pass), not one HBM pass"
     del S, xs
     # ---- 256^3 volume, 3x3x3
     v = torch.rand(256, 256, 256, device="cuda")
