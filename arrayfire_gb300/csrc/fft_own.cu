@@ -16,9 +16,14 @@
 // radix r reads x[j + q n/r] (q < r), multiplies by the twiddles
 // w^(q k), k = j mod Ns, does the radix-r butterfly and writes
 // y[(j - k) r + k + q Ns] (Ns = product of the earlier radices), then the
-// buffers swap.  Twiddles come from a table e^{-2 pi i j / L} computed in
-// double on the host.  Transforms are unnormalised (forward e^{-...},
-// inverse e^{+...}), as the convolution's output pass divides by the size.
+// buffers swap.  Twiddles come from per-stage tables computed in double on
+// the host: stage s holds w^(q k) = e^{-2 pi i q k / (R Ns)} at
+// [(q - 1) Ns + k], so the lanes of a warp (consecutive k) read consecutive
+// entries (a single table e^{-2 pi i j / L} read at q k L / (R Ns) put the
+// lanes of the late stages up to 16 entries apart, 16-way bank conflicts);
+// the stages' tables add up to L - 1 entries.  Transforms are unnormalised
+// (forward e^{-...}, inverse e^{+...}), as the convolution's output pass
+// divides by the size.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -160,7 +165,6 @@ __device__ __forceinline__ void fft_stage(const C *__restrict__ x, C *__restrict
                                           int npen, int Ns, const FftDiv &mdiv,
                                           const FftDiv &nsdiv, const C *__restrict__ tw) {
     const int m = n / R;
-    const int tstep = n / (Ns * R);
     for (int idx = threadIdx.x; idx < npen * m; idx += blockDim.x) {
         const int pen = fft_div(idx, mdiv), j = idx - pen * m;
         const int k = j - fft_div(j, nsdiv) * Ns;
@@ -169,10 +173,9 @@ __device__ __forceinline__ void fft_stage(const C *__restrict__ x, C *__restrict
 #pragma unroll
         for (int q = 0; q < R; ++q) v[q] = x[sp(xi + q * m)];
         if (Ns > 1) {
-            const int step = k * tstep;
 #pragma unroll
             for (int q = 1; q < R; ++q) {
-                const C w = tw[q * step];
+                const C w = tw[(q - 1) * Ns + k];
                 v[q] = cmulc(v[q], INV ? cconj(w) : w);
             }
         }
@@ -192,8 +195,8 @@ __device__ C *smem_fft(C *x, C *y, int n, int npen, const FftPlan &pl, const C *
     for (int s = 0; s < pl.nst; ++s) {
         const int r = pl.rad[s];
 #define AFGB_FFT_STAGE(RR)                                                                        \
-    (inverse ? fft_stage<C, RR, true>(x, y, n, npen, Ns, pl.mdiv[s], pl.nsdiv[s], tw)           \
-             : fft_stage<C, RR, false>(x, y, n, npen, Ns, pl.mdiv[s], pl.nsdiv[s], tw))
+    (inverse ? fft_stage<C, RR, true>(x, y, n, npen, Ns, pl.mdiv[s], pl.nsdiv[s], tw + pl.twoff[s]) \
+             : fft_stage<C, RR, false>(x, y, n, npen, Ns, pl.mdiv[s], pl.nsdiv[s], tw + pl.twoff[s]))
         switch (r) {
             case 8: AFGB_FFT_STAGE(8); break;
             case 9: AFGB_FFT_STAGE(9); break;
@@ -332,12 +335,48 @@ FftPlan make_plan(long long n) {
         m /= 3;
     }
     unsigned ns = 1;
+    int off = 0;
     for (int s = 0; s < pl.nst; ++s) {
         pl.mdiv[s] = make_div((unsigned)(n / pl.rad[s]));
         pl.nsdiv[s] = make_div(ns);
+        pl.twoff[s] = off;
+        if (ns > 1) off += (pl.rad[s] - 1) * (int)ns;
         ns *= (unsigned)pl.rad[s];
     }
     return pl;
+}
+
+// the per-stage twiddle tables of make_plan(L)'s stages, in double on the
+// host, kept per length and type; L entries (the stages use L - 1)
+std::mutex g_stw_mu;
+std::map<std::tuple<int, long long, int>, void *> g_stw;
+
+template <typename C>
+const C *stage_twiddles(long long L) {
+    using S = typename ScalarT<C>::type;
+    const auto key = std::make_tuple(device(), L, (int)sizeof(C));
+    std::lock_guard<std::mutex> lk(g_stw_mu);
+    auto it = g_stw.find(key);
+    if (it != g_stw.end()) return static_cast<const C *>(it->second);
+    const FftPlan pl = make_plan(L);
+    std::vector<C> h((size_t)L, C{(S)0, (S)0});
+    const double pi = 3.14159265358979323846264338327950288;
+    long long ns = 1;
+    for (int s = 0; s < pl.nst; ++s) {
+        const int R = pl.rad[s];
+        if (ns > 1)
+            for (int q = 1; q < R; ++q)
+                for (long long k = 0; k < ns; ++k) {
+                    const double a = -2.0 * pi * (double)(q * k) / (double)(R * ns);
+                    h[(size_t)(pl.twoff[s] + (q - 1) * ns + k)] = C{(S)std::cos(a), (S)std::sin(a)};
+                }
+        ns *= R;
+    }
+    void *d = nullptr;
+    AFGB_CUDA(cudaMalloc(&d, (size_t)L * sizeof(C)));  // held for the process
+    AFGB_CUDA(cudaMemcpy(d, h.data(), (size_t)L * sizeof(C), cudaMemcpyHostToDevice));
+    g_stw[key] = d;
+    return static_cast<const C *>(d);
 }
 
 // e^{-2 pi i j / L}, j < L, in double on the host, kept per length and type
@@ -400,7 +439,7 @@ void fft_real_forward(const R *in, C *out, long long n0, long long rows) {
     const size_t smem = (2 * (size_t)fft_padded(P * h) + h) * sizeof(C);
     auto k = fft_r2c_rows_kernel<R, C>;
     AFGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const C *twh = twiddles<C>(h), *twn = twiddles<C>(n0);
+    const C *twh = stage_twiddles<C>(h), *twn = twiddles<C>(n0);
     {
         KernelTimer kt("fft_r2c_rows_kernel");
         k<<<fft_grid((rows + P - 1) / P), fft_threads((long long)P * h), smem, stream()>>>(
@@ -419,7 +458,7 @@ void fft_real_inverse(const C *in, R *out, long long n0, long long rows) {
     const size_t smem = (2 * (size_t)fft_padded(P * h) + h) * sizeof(C);
     auto k = fft_c2r_rows_kernel<R, C>;
     AFGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    const C *twh = twiddles<C>(h), *twn = twiddles<C>(n0);
+    const C *twh = stage_twiddles<C>(h), *twn = twiddles<C>(n0);
     {
         KernelTimer kt("fft_c2r_rows_kernel");
         k<<<fft_grid((rows + P - 1) / P), fft_threads((long long)P * h), smem, stream()>>>(
@@ -447,7 +486,7 @@ void fft_axis(C *data, long long n, long long inner, long long outer, bool inver
     auto k = fft_axis_kernel<C>;
     AFGB_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     const long long units = outer * ((inner + P - 1) / P);
-    const C *tw = twiddles<C>(n);
+    const C *tw = stage_twiddles<C>(n);
     {
         KernelTimer kt("fft_axis_kernel");
         k<<<fft_grid(units), fft_threads(n * P), smem, stream()>>>(data, (int)n, inner, outer, P,

@@ -14,6 +14,7 @@ struct FftPlan {
     int rad[32];         // radices (8, 4, 2, 9, 3) in stage order
     FftDiv mdiv[32];     // n / radix of each stage
     FftDiv nsdiv[32];    // product of the earlier radices of each stage
+    int twoff[32];       // offset of each stage's twiddles in the plan's table
 };
 
 // whether a length runs on these kernels: 2^a 3^b (an even real row length
