@@ -668,20 +668,37 @@ def run_e2e(af, X, Wt, Gd, prec, args) -> dict:
         af._check(L.af_create_array(ctypes.byref(out), ctypes.c_void_p(t.data_ptr()), 4, d, af.f32))
         return af.Array(out.value)
 
+    calls = {}  # host time per call (each call blocks: the copies and the work it waits for)
+
+    def tick(name, t0):
+        t1 = time.perf_counter()
+        calls[name] = calls.get(name, 0.0) + (t1 - t0) * 1e3
+        return t1
+
     def step():
+        t = time.perf_counter()
         Xa = mk(pin["x"], X.shape)
+        t = tick("create_signal", t)
         Wa = mk(pin["w"], Wt.shape)
+        t = tick("create_filter", t)
         y = af.convolve2_nn(Xa, Wa, st, pd, dl, precision=prec)
+        t = tick("forward_call", t)
         af._check(L.af_get_data_ptr(ctypes.c_void_p(y_host.data_ptr()), y.handle))
+        t = tick("get_output", t)
         if grads:
             Ga = mk(pin["g"], Gd.shape)
+            t = tick("create_incoming_gradient", t)
             dx, dw, _ = af.convolve2_gradients_nn(Ga, Xa, Wa, st, pd, dl, precision=prec)
+            t = tick("gradients_call", t)
             af._check(L.af_get_data_ptr(ctypes.c_void_p(dx_host.data_ptr()), dx.handle))
+            t = tick("get_data_gradient", t)
             af._check(L.af_get_data_ptr(ctypes.c_void_p(dw_host.data_ptr()), dw.handle))
+            tick("get_filter_gradient", t)
 
     for _ in range(max(1, args.warmup)):
         step()
     torch.cuda.synchronize()
+    calls.clear()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         step()
@@ -691,7 +708,8 @@ def run_e2e(af, X, Wt, Gd, prec, args) -> dict:
     d2h = (y_host.numel() + ((dx_host.numel() + dw_host.numel()) if grads else 0)) * 4
     return {"value": (3 if grads else 1) * nn_flops() * args.steps / dt / 1e12, "unit": "TFLOP/s",
             "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
-            "ms_per_step": dt * 1e3 / args.steps}
+            "ms_per_step": dt * 1e3 / args.steps,
+            "host_ms_per_call": {k: round(v / args.steps, 3) for k, v in calls.items()}}
 
 
 CNN_CHANNELS = [(3, 32), (32, 64), (64, 128), (128, 128)]
