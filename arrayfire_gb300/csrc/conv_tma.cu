@@ -828,6 +828,10 @@ __global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ 
             const bool vec_ok = (x + 3 < p.od[0]) && ((p.os[1] & 3) == 0) &&
                                 ((p.os[2] & 3) == 0) &&
                                 ((reinterpret_cast<uintptr_t>(out) & 15) == 0);
+            // even row pitches (EXPAND's 258-wide rows): two 8-byte stores
+            const bool vec2_ok = (x + 3 < p.od[0]) && ((p.os[1] & 1) == 0) &&
+                                 ((p.os[2] & 1) == 0) &&
+                                 ((reinterpret_cast<uintptr_t>(out) & 7) == 0);
 #pragma unroll
             for (int rz = 0; rz < 4; ++rz) {
                 const long long z = k0 + 4 * tz + rz;
@@ -836,6 +840,9 @@ __global__ void __launch_bounds__(256) conv3_tma_kernel(const __grid_constant__ 
                 if (vec_ok) {
                     *reinterpret_cast<float4 *>(dst) =
                         make_float4(acc[rz][0], acc[rz][1], acc[rz][2], acc[rz][3]);
+                } else if (vec2_ok) {
+                    reinterpret_cast<float2 *>(dst)[0] = make_float2(acc[rz][0], acc[rz][1]);
+                    reinterpret_cast<float2 *>(dst)[1] = make_float2(acc[rz][2], acc[rz][3]);
                 } else {
 #pragma unroll
                     for (int cc = 0; cc < 4; ++cc)
