@@ -315,14 +315,10 @@ __global__ void __launch_bounds__(THREADS, (F0 * F1 > 25) ? 2 : 3)
         T *out = static_cast<T *>(p.out) + out_off;
         const bool row_vec = ((p.os[1] & 3) == 0) &&
                              ((reinterpret_cast<uintptr_t>(out) % (4 * sizeof(T))) == 0);
-        // f32 rows of an even pitch (EXPAND's W + F0 - 1): two 8-byte stores
-        const bool row_vec2 = sizeof(T) == 4 && ((p.os[1] & 1) == 0) &&
-                              ((reinterpret_cast<uintptr_t>(out) & 7) == 0);
 #pragma unroll
         for (int g = 0; g < CG; ++g) {
             const long long x = (long long)ttx * TWX + TILE * g + 4 * tx;
             const bool vec = row_vec && (x + 3 < p.od[0]);
-            const bool vec2 = !vec && row_vec2 && (x + 3 < p.od[0]);
 #pragma unroll
             for (int rr = 0; rr < 4; ++rr) {
                 const long long y = (long long)tty * TILE + 4 * ty + rr;
@@ -339,10 +335,6 @@ __global__ void __launch_bounds__(THREADS, (F0 * F1 > 25) ? 2 : 3)
                                             ((uint32_t)(uint8_t)from_acc<T>(acc[g][rr][3]) << 24);
                         *reinterpret_cast<uint32_t *>(dst) = w4;
                     }
-                } else if (vec2) {
-                    float *d2 = reinterpret_cast<float *>(dst);
-                    reinterpret_cast<float2 *>(d2)[0] = make_float2(acc[g][rr][0], acc[g][rr][1]);
-                    reinterpret_cast<float2 *>(d2)[1] = make_float2(acc[g][rr][2], acc[g][rr][3]);
                 } else {
 #pragma unroll
                     for (int cc = 0; cc < 4; ++cc)
