@@ -24,15 +24,17 @@
 // measured faster than sizes with factors 5 and 7 as well), all on the
 // library's stream:
 //   pad      signal and filter -> zero-padded real (or complex) batches
-//   forward  cuFFT R2C / D2Z / C2C / Z2Z, batched over the slices
+//   forward  R2C / C2C transforms, batched over the slices
 //   multiply one kernel, broadcasting the batch dims per batch kind
-//   inverse  cuFFT C2R / Z2D / C2C / Z2Z over the output slices
+//   inverse  C2R / C2C transforms over the output slices
 //   crop     one kernel: window, 1/size scale, rounding, type conversion
-// The transforms are cuFFT's (loaded at first use with dlopen, so the
-// library still loads where cuFFT is absent; the FFT calls then fail with
-// AF_ERR_LOAD_LIB); padding, spectrum products and the output pass are this
-// file's kernels.  Results equal the reference's up to floating-point
-// rounding (the transform sizes and summation orders differ).
+// The transforms are this library's (fft_own.cu) for every 2^a 3^b size that
+// fits one block, the sizes picked by default; other sizes go to cuFFT,
+// loaded at first use with dlopen, so the library still loads where cuFFT is
+// absent (such calls then fail with AF_ERR_LOAD_LIB).  Padding, spectrum
+// products and the output pass are this file's kernels.  Results equal the
+// reference's up to floating-point rounding (the transform sizes and
+// summation orders differ).
 #include <cuda_runtime.h>
 #include <cufft.h>
 #include <dlfcn.h>
