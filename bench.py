@@ -1261,6 +1261,12 @@ def run_only(args) -> None:
             k1 = g.standard_normal(31)
             F1 = af.Array.from_numpy((k1 / k1.sum()).astype(np.float32))
             fn = lambda: af.convolve1(S1, F1, af.AF_CONV_DEFAULT, af.AF_CONV_SPATIAL)  # noqa: E731
+        elif args.only == "fft31":
+            xs = torch.rand(64, 2048, 2048, device="cuda")
+            S = af.Array.view_torch(xs)
+            k31 = g.standard_normal((31, 31))
+            F31 = af.Array.from_numpy(np.asfortranarray((k31 / k31.sum()).astype(np.float32)))
+            fn = lambda: af.convolve2(S, F31, af.AF_CONV_DEFAULT, af.AF_CONV_AUTO)  # noqa: E731
         elif args.only == "sep_u8":
             xu = torch.randint(0, 256, (64, 2048, 2048), dtype=torch.uint8, device="cuda")
             S = af.Array.view_torch(xu)
@@ -1324,7 +1330,7 @@ def main() -> None:
     ap.add_argument("--cpu-seconds", type=float, default=150.0,
                     help="time budget of the reference arm's full-batch CPU steps")
     ap.add_argument("--only", default=None,
-                    choices=["fwd", "dgrad", "wgrad", "step", "sep_f32", "sep_u8", "same7", "conv3",
+                    choices=["fwd", "dgrad", "wgrad", "step", "sep_f32", "sep_u8", "same7", "fft31", "conv3",
                              "conv3_expand", "conv1", "cnn", "unwrap", "wrap", "unwrap_rows",
                              "wrap_rows", "image_callers"],
                     help="run one operation of the workload --steps times after --warmup "
